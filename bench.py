@@ -1,0 +1,471 @@
+#!/usr/bin/env python3
+"""Benchmark of the per-step velocity path (tree, SLAE, shed, tree, epsilon/merge,
+convective, diffusive) on the 4M-vortex wake behind an inclined ellipse.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+GPU arm (default): one step = restore the initial vortex list (device to device) and run
+every hot-path call of one simulate() iteration through the C ABI on data resident in HBM;
+timed with CUDA events on the context's stream.  The headline `value` is the FP32-pairwise
+path; the plain FP64 path is timed on the same workload for the ratio the metric names,
+and both are checked against each other and against an FP64 direct sum.  `e2e` is the same
+step with host buffers: pinned host -> device copy of the inputs and device -> host copy
+of the results inside the timed region.  With N > 1 (torchrun) every rank runs an
+independent replica (different seed); value = all vortices / max time over ranks.
+
+Reference arm: the reference's CPU algorithm (the C restatement in oracle/, which mirrors
+the reference's per-leaf OpenMP structure) on the machine's host cores, each step a bounded
+sample of the same workload: the tree partition runs in full, the per-leaf phases on every
+`stride`-th leaf and are scaled by stride.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "vortex-steps/s @4M vortices: learned/FP32 vs plain FP64 GPU at ≤1e-5 rel err"
+L2_BYTES = 129 * 2**20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--n", type=int, default=4_000_000)
+    ap.add_argument("--m", type=int, default=4000)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--cpu-stride", type=int, default=32)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def workload(n, m, rank):
+    from vvflow_gb300 import workloads as W
+    return W.ellipse_wake(n, m, seed=3 + rank, angle_deg=10.0)
+
+
+# ---------------------------------------------------------------------------------------
+# clocks
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, bus_id=None):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if bus_id:
+            cmd += ["-i", bus_id]
+        try:
+            self.p = subprocess.Popen(cmd, stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(5)
+            except Exception:
+                self.p.kill()
+        self.f.flush()
+        rows = []
+        try:
+            for line in open(self.f.name):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        finally:
+            os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k] and "Not" not in r[5 + k]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------------------
+# GPU arm
+def hot_path(S, wl, mn, mx, times=None, ev=None):
+    """One simulate() iteration of the hot path (utils/vvflow/vvflow.cpp:214-255)."""
+    S.tree_build(wl.far_criteria, mn, mx)
+    S.slae()
+    S.tree_destroy()
+    S.vortex_shed()
+    S.tree_build(wl.far_criteria, mn, mx)
+    S.eps(True)
+    if ev is not None:
+        ev[0].record()
+    S.convective()
+    if ev is not None:
+        ev[1].record()
+    S.diffusive()
+    S.tree_destroy()
+
+
+def gpu_arm(args):
+    import torch
+
+    from vvflow_gb300 import build as B
+    from vvflow_gb300.vvgpu import VVGPU_FP32, VVGPU_FP64, GpuSpace
+
+    rank, world, local = dist_env()
+    B.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    wl = workload(args.n, args.m, rank)
+    mn, mx = wl.node_sizes()
+    N = wl.n
+
+    def make(prec):
+        S = GpuSpace(prec, device=local, reserve=N + 4 * wl.m)
+        S.set_stream(stream.cuda_stream)
+        S.set_params(wl.re, wl.dt, wl.inf_vx, wl.inf_vy, 0.0, 0.0)
+        for cx, cy in wl.bodies:
+            S.add_body(cx, cy)
+        return S
+
+    dx = torch.from_numpy(wl.x).to(dev)
+    dy = torch.from_numpy(wl.y).to(dev)
+    dg = torch.from_numpy(wl.g).to(dev)
+
+    def restore(S):
+        S.set_vortices_device(N, dx.data_ptr(), dy.data_ptr(), dg.data_ptr(), None)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def maxall(v):
+        if dist is None:
+            return v
+        t = torch.tensor([v], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- FP32-pairwise path (headline) -------------------------------------------------
+    S = make(VVGPU_FP32)
+    for _ in range(args.warmup):
+        restore(S)
+        hot_path(S, wl, mn, mx)
+    torch.cuda.synchronize()
+    st0 = S.stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    bus = None
+    try:
+        bus = torch.cuda.get_device_properties(local).pci_bus_id if hasattr(
+            torch.cuda.get_device_properties(local), "pci_bus_id") else None
+    except Exception:
+        bus = None
+    clk = Clocks(None)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record()
+    for k in range(args.steps):
+        restore(S)
+        hot_path(S, wl, mn, mx, ev=cev[k])
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms_max = maxall(ms)
+    st1 = S.stats()
+    conv_ms = float(np.mean([a.elapsed_time(b) for a, b in cev]))
+    launches = int(st1["launches"] - st0["launches"])
+    value = world * N / (ms_max / 1e3)
+
+    # phase split of one step (host-timed with synchronisation, for the record)
+    phases = {}
+    restore(S)
+    torch.cuda.synchronize()
+    for name, fn in (("tree_build", lambda: S.tree_build(wl.far_criteria, mn, mx)), ("slae", S.slae),
+                     ("destroy", S.tree_destroy), ("shed", S.vortex_shed),
+                     ("tree_build2", lambda: S.tree_build(wl.far_criteria, mn, mx)),
+                     ("eps_merge", lambda: S.eps(True)), ("convective", S.convective),
+                     ("diffusive", S.diffusive)):
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        phases[name] = round((time.perf_counter() - t0) * 1e3, 3)
+    stp = S.stats()
+    v32 = S.vortices()
+    S.tree_destroy()
+
+    # ---- e2e through the C ABI with host buffers ----------------------------------------
+    hx = torch.from_numpy(wl.x).pin_memory()
+    hy = torch.from_numpy(wl.y).pin_memory()
+    hg = torch.from_numpy(wl.g).pin_memory()
+    nout = N + 2 * wl.m
+    outs = {k: torch.empty(nout, dtype=torch.float64).pin_memory() for k in ("x", "y", "g", "ie", "vx", "vy")}
+    oorig = torch.empty(nout, dtype=torch.int64).pin_memory()
+    h2d = 3 * 8 * N
+    for _ in range(1):
+        S.set_vortices_from(N, hx.data_ptr(), hy.data_ptr(), hg.data_ptr())
+        hot_path(S, wl, mn, mx)
+    torch.cuda.synchronize()
+    barrier()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record()
+    for _ in range(args.steps):
+        S.set_vortices_from(N, hx.data_ptr(), hy.data_ptr(), hg.data_ptr())
+        hot_path(S, wl, mn, mx)
+        S.get_vortices_into(outs["x"].data_ptr(), outs["y"].data_ptr(), outs["g"].data_ptr(),
+                            outs["ie"].data_ptr(), outs["vx"].data_ptr(), outs["vy"].data_ptr(), oorig.data_ptr())
+    e3.record()
+    torch.cuda.synchronize()
+    barrier()
+    n_after = S.n
+    d2h = (6 * 8 + 8) * n_after
+    e2e_ms = maxall(e2.elapsed_time(e3) / args.steps)
+    S.close()
+
+    # ---- plain FP64 path and accuracy ---------------------------------------------------
+    fp64 = None
+    acc = {}
+    if args.fp64_steps > 0:
+        S64 = make(VVGPU_FP64)
+        restore(S64)
+        hot_path(S64, wl, mn, mx)  # warm-up (includes the one-off SLAE inversion)
+        torch.cuda.synchronize()
+        e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e4.record()
+        for _ in range(args.fp64_steps):
+            restore(S64)
+            hot_path(S64, wl, mn, mx)
+        e5.record()
+        torch.cuda.synchronize()
+        ms64 = maxall(e4.elapsed_time(e5) / args.fp64_steps)
+        # accuracy: the same single step in both precisions (same tree, eps, merges)
+        restore(S64)
+        S64.tree_build(wl.far_criteria, mn, mx); S64.slae(); S64.tree_destroy(); S64.vortex_shed()
+        S64.tree_build(wl.far_criteria, mn, mx); S64.eps(True); S64.convective()
+        c64 = S64.vortices()
+        S64.diffusive()
+        d64 = S64.vortices()
+        S64.tree_destroy()
+        S64.close()
+        S = make(VVGPU_FP32)
+        restore(S)
+        S.tree_build(wl.far_criteria, mn, mx); S.slae(); S.tree_destroy(); S.vortex_shed()
+        S.tree_build(wl.far_criteria, mn, mx); S.eps(True); S.convective()
+        c32 = S.vortices()
+        S.diffusive()
+        d32 = S.vortices()
+        S.tree_destroy()
+        S.close()
+        same_tree = bool(np.array_equal(c32["orig"], c64["orig"]) and np.array_equal(c32["inv_eps"], c64["inv_eps"]))
+
+        def rel(ax, ay, bx, by):
+            mag = np.hypot(bx, by)
+            err = np.hypot(ax - bx, ay - by)
+            live = mag > 0
+            floor = 1e-3 * math.sqrt(float(np.mean(mag[live] ** 2))) if live.any() else 1.0
+            return float(np.max(err / (mag + floor))), float(math.sqrt(np.mean(err ** 2)) / math.sqrt(np.mean(mag ** 2)))
+
+        cmax, crms = rel(c32["vx"], c32["vy"], c64["vx"], c64["vy"])
+        dmax, drms = rel(d32["vx"], d32["vy"], d64["vx"], d64["vy"])
+        acc = {"fp32_vs_fp64_convective_max": cmax, "fp32_vs_fp64_convective_rms": crms,
+               "fp32_vs_fp64_total_max": dmax, "fp32_vs_fp64_total_rms": drms,
+               "identical_tree_eps_merges": same_tree}
+        # tree approximation error of both paths against the FP64 direct sum (sampled)
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            oracle.build(False)
+            R = oracle.OracleSpace("port")
+            R.set_params(wl.re, wl.dt, wl.inf_vx, wl.inf_vy)
+            for cx, cy in wl.bodies:
+                R.add_body(cx, cy)
+            R.set_vortices(c64["x"], c64["y"], c64["g"], c64["inv_eps"])
+            rng = np.random.default_rng(7)
+            live = np.flatnonzero(c64["g"] != 0)
+            idx = rng.choice(live, size=min(256, len(live)), replace=False)
+            t0 = time.time()
+            ux, uy = R.direct_velocity(c64["x"][idx], c64["y"][idx])
+            acc["direct_sum_targets"] = int(len(idx))
+            acc["direct_sum_seconds"] = round(time.time() - t0, 2)
+            acc["fp64_tree_vs_direct_max"] = rel(c64["vx"][idx], c64["vy"][idx], ux, uy)[0]
+            acc["fp32_tree_vs_direct_max"] = rel(c32["vx"][idx], c32["vy"][idx], ux, uy)[0]
+            R.close()
+        except Exception as e:  # the direct-sum check is informative only
+            acc["direct_sum_error"] = str(e)[:200]
+        fp64 = {"value": world * N / (ms64 / 1e3), "ms_per_step": ms64, "steps": args.fp64_steps,
+                "fp32_speedup": ms64 / ms_max}
+
+    # ---- roofline of the dominant kernel (convective near field, FP32 pipe) ------------
+    flops = 12 * stp["near_pairs"] + 24 * stp["far_pairs"]
+    peak = measure_fp32_peak(torch, dev)
+    roof = {"bound": "fp32", "kernel": "k_conv32 (convective near field)",
+            "achieved": flops / (conv_ms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+            "frac": flops / (conv_ms / 1e3) / 1e12 / peak, "traffic": None,
+            "algorithmic_flops_per_launch": flops,
+            "near_pairs": stp["near_pairs"], "far_pairs": stp["far_pairs"],
+            "launch_ms": conv_ms,
+            "peak_source": "cuBLAS FP32 SGEMM (TF32 off) measured in this run"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample(wl, args.cpu_stride)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "vortex-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
+            "data": "synthetic (seeded Karman-like wake, x~U(0.5,80), y~N(0,(0.2+0.05x)^2))",
+            "config": {"workload": f"ellipse_wake_{N // 1_000_000}M", "vortices": N, "segments": wl.m,
+                       "body": "ellipse 0.5x0.25 at 10 deg", "far_criteria": wl.far_criteria,
+                       "pairwise": "fp32 local frames, compensated", "decisions": "fp64 bit-exact",
+                       "re": wl.re, "dt": wl.dt,
+                       "l2": "inputs larger than L2 (vortex SoA %.0f MB + tree, L2 129 MB)" % (N * 56 / 2**20),
+                       "parallelism": f"replicas x{world}"},
+            "fp64": fp64, "accuracy": acc, "phases_ms": phases,
+            "tree": {k: stp[k] for k in ("n_leaves", "n_nodes", "tree_depth", "near_runs", "merge_rounds",
+                                         "merged", "near_pairs", "far_pairs", "diff_candidates")},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * N / (e2e_ms / 1e3), "unit": "vortex-steps/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def measure_fp32_peak(torch, dev):
+    """FP32 FMA throughput as reached by cuBLAS SGEMM (TF32 disabled), best of 5."""
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, device=dev)
+        b = torch.randn(n, n, device=dev)
+        for _ in range(2):
+            a @ b
+        best = 1e9
+        for _ in range(5):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            a @ b
+            e.record()
+            torch.cuda.synchronize()
+            best = min(best, s.elapsed_time(e))
+        del a, b
+        return 2 * n ** 3 / (best / 1e3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
+
+
+# ---------------------------------------------------------------------------------------
+# CPU: the reference algorithm (C restatement) on the host cores
+def cpu_sample(wl, stride):
+    """Seconds per step of the reference's CPU algorithm, from a bounded sample: the tree
+    partition and centroids run in full (twice per step, as in simulate()), the per-leaf
+    phases (lists, epsilon/merge, convective, diffusive, SLAE right-hand side) on every
+    stride-th leaf, scaled by stride.  Returns the JSON object."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build(False)
+    mn, mx = wl.node_sizes()
+    R = oracle.OracleSpace("port")
+    R.load(wl)
+    R.set_sample(stride)
+    t = {}
+    t0 = time.perf_counter()
+    R.tree_build(wl.far_criteria, mn, mx)
+    tb = R.last_timings()
+    t1 = time.perf_counter()
+    R.slae_rhs_step()
+    t2 = time.perf_counter()
+    R.tree_destroy()
+    R.vortex_shed()
+    t3 = time.perf_counter()
+    R.tree_build(wl.far_criteria, mn, mx)
+    tb2 = R.last_timings()
+    t4 = time.perf_counter()
+    R.eps(True)
+    t5 = time.perf_counter()
+    R.convective()
+    t6 = time.perf_counter()
+    R.diffusive()
+    t7 = time.perf_counter()
+    R.tree_destroy()
+    R.close()
+    full = (tb["partition"] + tb["cmass"] + tb2["partition"] + tb2["cmass"]
+            + stride * (tb["lists"] + tb2["lists"]) + stride * (t2 - t1) + (t3 - t2)
+            + stride * ((t5 - t4) + (t6 - t5) + (t7 - t6)))
+    sampled = t7 - t0
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": wl.n / full, "unit": "vortex-steps/s", "cores": threads, "kind": "port",
+            "seconds_per_step": full, "sample_seconds": round(sampled, 2),
+            "sample": f"full {wl.n}-vortex workload; tree partition in full, per-leaf phases on every "
+                      f"{stride}th leaf scaled x{stride}",
+            "phases_s": {"partition_x2": tb["partition"] + tb2["partition"], "lists_x2": stride * (tb["lists"] + tb2["lists"]),
+                         "slae_rhs": stride * (t2 - t1), "eps": stride * (t5 - t4), "convective": stride * (t6 - t5),
+                         "diffusive": stride * (t7 - t6)}}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    wl = workload(args.n, args.m, 0)
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        pass
+    vals = []
+    last = None
+    for k in range(args.warmup + args.steps):
+        last = cpu_sample(wl, args.cpu_stride)
+        if k >= args.warmup:
+            vals.append(last["seconds_per_step"])
+    sps = float(np.median(vals))
+    line = {"metric": METRIC, "value": wl.n / sps, "unit": "vortex-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "impl": "reference",
+            "data": "synthetic (seeded Karman-like wake)",
+            "config": {"workload": f"ellipse_wake_{wl.n // 1_000_000}M", "vortices": wl.n, "segments": wl.m,
+                       "far_criteria": wl.far_criteria, "parallelism": "host cores"},
+            "cpu_baseline": {"value": wl.n / sps, "unit": "vortex-steps/s", "cores": last["cores"],
+                             "kind": "port", "sample": last["sample"]},
+            "e2e": {"value": wl.n / sps, "unit": "vortex-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,191 @@
+/*
+ * vvgpu.h -- C ABI of the GB300 implementation of libvvhd's per-step velocity path.
+ *
+ * One context = one Space (vortices + bodies) resident in device memory, one CUDA
+ * stream.  The calls replace the reference's hot-path classes one for one:
+ *
+ *   vvgpu_tree_build / vvgpu_tree_destroy  <- stree::build / stree::destroy
+ *                                             (libvvhd/headers/TSortedTree.hpp:74-75,
+ *                                              libvvhd/src/TSortedTree.cpp:232-265, 267-273)
+ *   vvgpu_eps                              <- MEpsilonFast::CalcEpsilonFast(bool merge),
+ *                                             MEpsilonFast::Merged()
+ *                                             (libvvhd/headers/MEpsilonFast.hpp:10-11,
+ *                                              libvvhd/src/MEpsilonFast.cpp:11-63)
+ *   vvgpu_convective                       <- MConvectiveFast::process_all_lists()
+ *                                             (libvvhd/headers/MConvectiveFast.hpp:16,
+ *                                              libvvhd/src/MConvectiveFast.cpp:36-114)
+ *   vvgpu_velocity_points                  <- MConvectiveFast::velocity(TVec p)
+ *                                             (libvvhd/headers/MConvectiveFast.hpp:17,
+ *                                              libvvhd/src/MConvectiveFast.cpp:20-34)
+ *   vvgpu_slae                             <- MConvectiveFast::calc_circulation(const void**)
+ *                                             (libvvhd/headers/MConvectiveFast.hpp:18-26,
+ *                                              libvvhd/src/MConvectiveFast.cpp:235-273)
+ *   vvgpu_diffusive                        <- MDiffusiveFast::process_vort_list()
+ *                                             (libvvhd/headers/MDiffusiveFast.hpp:10,
+ *                                              libvvhd/src/MDiffusiveFast.cpp:8-48)
+ *   vvgpu_vortex_shed                      <- MFlowmove::vortex_shed()
+ *                                             (libvvhd/headers/MFlowmove.hpp:12,
+ *                                              libvvhd/src/MFlowmove.cpp:217-235)
+ *   vvgpu_gsum                             <- Space::gsum() (libvvhd/headers/TSpace.hpp:93-99)
+ *
+ * The Space state crosses the boundary as structure-of-arrays of doubles
+ * (TObj r.x, r.y, g, _1_eps, v.x, v.y; libvvhd/headers/TObj.hpp:10-35) and body corners
+ * (TAtt::corner; libvvhd/headers/TBody.hpp:17-55).  The tree permutes the vortex list in
+ * place exactly as the reference does; vvgpu_get_vortices returns the permuted list and,
+ * per slot, the index the vortex had when it was set.
+ *
+ * Errors: every call returns VVGPU_OK (0) or a negative VVGPU_ERR_* code and never exits;
+ * vvgpu_last_error gives a message.  The reference reports the same conditions with
+ * exit() / std::invalid_argument / stderr (libvvhd/src/TMatrix.cpp:60-61, 201-213,
+ * libvvhd/src/MConvectiveFast.cpp:237-239, libvvhd/src/TSortedTree.cpp:234, 279-281).
+ *
+ * Threading: a context is used from one host thread at a time; all work is queued on the
+ * context's stream and the calls that return results to host memory synchronise it.
+ */
+#ifndef VVGPU_H
+#define VVGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    VVGPU_OK = 0,
+    VVGPU_ERR_ARG = -1,          /* invalid argument                                     */
+    VVGPU_ERR_STATE = -2,        /* wrong call order (e.g. tree already built)            */
+    VVGPU_ERR_NOT_BUILT = -3,    /* tree not built                                       */
+    VVGPU_ERR_UNSUPPORTED = -4,  /* body kinematics outside this implementation's scope  */
+    VVGPU_ERR_SINGULAR = -5,     /* singular SLAE (zero pivot)                           */
+    VVGPU_ERR_CUDA = -6,         /* CUDA runtime error                                   */
+    VVGPU_ERR_NOMEM = -7,        /* device allocation failed                             */
+    VVGPU_ERR_TIMEOUT = -8,      /* an iterative pass did not converge in its bound      */
+    VVGPU_ERR_LIMIT = -9         /* size beyond a documented limit                       */
+};
+
+/* Arithmetic used for the pairwise sums (convective near/far field, diffusive).
+ * Tree decisions, epsilon/merge, the SLAE and circulation totals are FP64 in both. */
+enum { VVGPU_FP64 = 0, VVGPU_FP32 = 1 };
+
+typedef struct vvgpu_ctx vvgpu_ctx;
+
+typedef struct vvgpu_cfg {
+    int device;                 /* CUDA device ordinal                                  */
+    int precision;              /* VVGPU_FP64 or VVGPU_FP32                              */
+    int64_t reserve_vortices;   /* optional capacity hint                               */
+    int64_t reserve_segments;   /* optional capacity hint                               */
+} vvgpu_cfg;
+
+/* Rigid-body parameters (TBody fields, libvvhd/headers/TBody.hpp:57-158); time functions
+ * (speed_x/y/o) are passed evaluated at the current time.  Same layout as the oracle's. */
+typedef struct vvgpu_body_params {
+    double holder_x, holder_y, holder_o;
+    double dpos_x, dpos_y, dpos_o;
+    double speed_x, speed_y, speed_o;
+    double speed_slae_x, speed_slae_y, speed_slae_o;
+    double speed_slae_prev_x, speed_slae_prev_y, speed_slae_prev_o;
+    double friction_prev_x, friction_prev_y, friction_prev_o;
+    double fdt_dead_x, fdt_dead_y, fdt_dead_o;
+    double g_dead;
+    double density;
+    double kspring_x, kspring_y, kspring_o;
+    int32_t special_segment_no;
+    int32_t bc_kutta;
+} vvgpu_body_params;
+
+/* SLAE outputs per body (TBody::speed_slae, force_hydro, force_holder). */
+typedef struct vvgpu_body_out {
+    double speed_slae_x, speed_slae_y, speed_slae_o;
+    double force_hydro_x, force_hydro_y, force_hydro_o;
+    double force_holder_x, force_holder_y, force_holder_o;
+} vvgpu_body_out;
+
+/* Per-call counters of the last step's work (algorithmic, counted from the built tree). */
+typedef struct vvgpu_stats {
+    int64_t n_vortices, n_segments, n_nodes, n_leaves, tree_depth;
+    int64_t near_pairs;         /* sum over leaves |L| * sum over near leaves |N|        */
+    int64_t far_pairs;          /* sum over leaves |Far(L)| (two monopoles each)         */
+    int64_t near_runs;          /* near lists stored as runs of consecutive leaves       */
+    int64_t merge_rounds;       /* fixed-point rounds of the last epsilon pass           */
+    int64_t merged;             /* merges in the last epsilon pass                       */
+    int64_t diff_candidates;    /* vortex pairs inside the 8-eps cut-off boxes           */
+    int64_t reserved[8];        /* reserved[0]: kernels launched by the context so far   */
+} vvgpu_stats;
+
+/* ---- context --------------------------------------------------------------------- */
+int vvgpu_ctx_create(const vvgpu_cfg* cfg, vvgpu_ctx** out);
+int vvgpu_ctx_destroy(vvgpu_ctx* ctx);
+const char* vvgpu_last_error(const vvgpu_ctx* ctx);
+int vvgpu_set_precision(vvgpu_ctx* ctx, int precision);
+/* Use the caller's CUDA stream (cudaStream_t passed as void*); NULL = context's own. */
+int vvgpu_set_stream(vvgpu_ctx* ctx, void* stream);
+int vvgpu_synchronize(vvgpu_ctx* ctx);
+int vvgpu_get_stats(const vvgpu_ctx* ctx, vvgpu_stats* out);
+
+/* ---- Space state (host pointers) -------------------------------------------------- */
+/* Space::re, dt, inf_speed(), inf_g, time, gravity (libvvhd/headers/TSpace.hpp:19-36). */
+int vvgpu_set_params(vvgpu_ctx* ctx, double re, double dt, double inf_vx, double inf_vy,
+                     double inf_g, double time, double gravity_x, double gravity_y);
+/* Appends a body (TBody with alist corners in contour order; r, dl and _1_eps are derived
+ * as in TBody::doUpdateSegments, libvvhd/src/TBody.cpp:200-215). */
+int vvgpu_add_body(vvgpu_ctx* ctx, int64_t nseg, const double* corner_x, const double* corner_y,
+                   const uint32_t* slip, const vvgpu_body_params* params);
+int vvgpu_set_segment_g(vvgpu_ctx* ctx, const double* g);
+int vvgpu_set_sinks(vvgpu_ctx* ctx, int64_t n, const double* x, const double* y, const double* g);
+/* Replaces the vortex list (v = 0).  inv_eps may be NULL (= 0, a freshly loaded list). */
+int vvgpu_set_vortices(vvgpu_ctx* ctx, int64_t n, const double* x, const double* y,
+                       const double* g, const double* inv_eps);
+/* Same with device pointers (data already resident in HBM on the context's device). */
+int vvgpu_set_vortices_device(vvgpu_ctx* ctx, int64_t n, const double* x, const double* y,
+                              const double* g, const double* inv_eps);
+int64_t vvgpu_num_vortices(const vvgpu_ctx* ctx);
+int64_t vvgpu_num_segments(const vvgpu_ctx* ctx);
+/* Copies the vortex list back to host memory; any pointer may be NULL. */
+int vvgpu_get_vortices(vvgpu_ctx* ctx, double* x, double* y, double* g, double* inv_eps,
+                       double* vx, double* vy, int64_t* orig);
+/* Device pointers to the resident SoA arrays (valid until the next call that resizes). */
+int vvgpu_device_arrays(vvgpu_ctx* ctx, double** x, double** y, double** g, double** inv_eps,
+                        double** vx, double** vy);
+int vvgpu_get_segments(vvgpu_ctx* ctx, double* rx, double* ry, double* dlx, double* dly,
+                       double* inv_eps, double* g, double* fric, double* gsum);
+int vvgpu_get_body_geom(vvgpu_ctx* ctx, int body, double* area, double* cofm_x, double* cofm_y,
+                        double* moi_axis, double* slen);
+
+/* ---- hot path --------------------------------------------------------------------- */
+/* stree(S, farCriteria, minNodeSize, maxNodeSize).build(); far_criteria is a double here
+ * (the reference takes an int; theta = sqrt(2 / far_criteria)). */
+int vvgpu_tree_build(vvgpu_ctx* ctx, double far_criteria, double min_node, double max_node);
+int vvgpu_tree_destroy(vvgpu_ctx* ctx);
+int vvgpu_eps(vvgpu_ctx* ctx, int merge, int64_t* merged);
+int vvgpu_convective(vvgpu_ctx* ctx);
+int vvgpu_diffusive(vvgpu_ctx* ctx);
+int vvgpu_velocity_points(vvgpu_ctx* ctx, int64_t n, const double* px, const double* py,
+                          double* vx, double* vy);
+/* calc_circulation with no collision; rigid bodies at rest or in prescribed translation
+ * are in scope (VVGPU_ERR_UNSUPPORTED otherwise). */
+int vvgpu_slae(vvgpu_ctx* ctx, vvgpu_body_out* out);
+int vvgpu_vortex_shed(vvgpu_ctx* ctx);
+int vvgpu_gsum(vvgpu_ctx* ctx, double* out);
+
+/* ---- inspection (parity tests; same meaning as the oracle's exports) -------------- */
+int vvgpu_tree_sizes(vvgpu_ctx* ctx, int64_t* nnodes, int64_t* nleaves, int64_t* nnear,
+                     int64_t* nfar);
+int vvgpu_tree_leaves(vvgpu_ctx* ctx, double* x, double* y, double* h, double* w,
+                      int64_t* vfirst, int64_t* vlast, int32_t* depth, int64_t* path,
+                      int64_t* sfirst, int64_t* slast);
+int vvgpu_tree_nodes(vvgpu_ctx* ctx, double* x, double* y, double* h, double* w,
+                     int64_t* vfirst, int64_t* vlast, int32_t* depth, int64_t* path,
+                     double* cmp_x, double* cmp_y, double* cmp_g,
+                     double* cmm_x, double* cmm_y, double* cmm_g);
+int vvgpu_tree_seg_order(vvgpu_ctx* ctx, int64_t* seg_order);
+int vvgpu_tree_lists(vvgpu_ctx* ctx, int64_t* near_off, int32_t* near_depth, int64_t* near_path,
+                     int64_t* far_off, int32_t* far_depth, int64_t* far_path);
+int64_t vvgpu_slae_size(const vvgpu_ctx* ctx);
+int vvgpu_slae_export(vvgpu_ctx* ctx, double* matrix, double* rhs, double* solution);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VVGPU_H */

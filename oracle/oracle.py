@@ -109,6 +109,9 @@ def _load(kind: str):
     }
     if kind == "port":
         sig["direct_velocity"] = (C.c_int, [H, C.c_int64, _D, _D, _D, _D])
+        sig["set_sample"] = (C.c_int, [H, C.c_int64])
+        sig["slae_rhs_step"] = (C.c_int, [H, _D])
+        sig["last_timings"] = (C.c_int, [H, _D])
     fns = {}
     for name, (res, args) in sig.items():
         f = getattr(lib, pre + name)
@@ -306,3 +309,14 @@ class OracleSpace:
 
     def gsum(self):
         return float(self.f["gsum"](self.h))
+
+    def set_sample(self, stride: int):
+        self._ok(self.f["set_sample"](self.h, int(stride)), "set_sample")
+
+    def last_timings(self):
+        out = np.zeros(3)
+        self._ok(self.f["last_timings"](self.h, _p(out)), "last_timings")
+        return dict(zip(("partition", "cmass", "lists"), out.tolist()))
+
+    def slae_rhs_step(self):
+        self._ok(self.f["slae_rhs_step"](self.h, None), "slae_rhs_step")

@@ -12,6 +12,13 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
 
 #define C_PI    3.14159265358979323846
 #define C_2PI   (2. * C_PI)
@@ -73,6 +80,9 @@ struct vvo_space {
     int64_t* seg_order;
     int64_t* near_off; int32_t* near_list; int64_t nnear, nearcap;
     int64_t* far_off;  int32_t* far_list;  int64_t nfar, farcap;
+    /* timing sample: phases over leaves process only leaves L with L % stride == 0 */
+    int64_t stride;
+    double t_partition, t_cmass, t_lists;
     /* SLAE */
     int64_t neq;
     double *mat, *rhs, *sol;
@@ -89,6 +99,7 @@ vvo_space* vvo_create(void) {
     /* Space::Space, libvvhd/src/TSpace.cpp:14-36 */
     S->re = INFINITY;
     S->dt = 1.0;
+    S->stride = 1;
     return S;
 }
 
@@ -331,6 +342,8 @@ static void swap_slots(vvo_space* S, int64_t a, int64_t b) {
     int64_t o = S->orig[a]; S->orig[a] = S->orig[b]; S->orig[b] = o;
 }
 
+static int32_t find_node(const vvo_space* S, double px, double py);
+
 /* snode::DivideNode (TSortedTree.cpp:36-79) with DistributeContent (:81-99, :139-148). */
 static void divide(vvo_space* S, int32_t ni) {
     onode nd = S->nodes[ni];
@@ -461,16 +474,34 @@ int vvo_tree_build(vvo_space* S, double far_criteria, double min_node, double ma
     int32_t root = new_node(S);
     onode* r = &S->nodes[root];
     r->vf = 0; r->vl = S->n; r->sf = 0; r->sl = S->m; r->depth = 0; r->path = 0;
+    double t0 = now_s();
     stretch(S, r);
     divide(S, root);
+    double t1 = now_s();
     cmass(S, root);
+    double t2 = now_s();
     S->near_off = (int64_t*)xrealloc(NULL, sizeof(int64_t) * (size_t)(S->nleaves + 1));
     S->far_off = (int64_t*)xrealloc(NULL, sizeof(int64_t) * (size_t)(S->nleaves + 1));
+    /* with a timing sample, lists are built for the sampled leaves and for the leaves that
+     * hold segment centres (the SLAE right-hand side reads those) */
+    char* need = NULL;
+    if (S->stride > 1) {
+        need = (char*)calloc((size_t)S->nleaves + 1, 1);
+        int32_t* pos = (int32_t*)malloc(sizeof(int32_t) * (size_t)S->nnodes);
+        for (int64_t L = 0; L < S->nleaves; L++) pos[S->leaves[L]] = (int32_t)L;
+        for (int64_t sg = 0; sg < S->m; sg++) need[pos[find_node(S, S->rx[sg], S->ry[sg])]] = 1;
+        free(pos);
+    }
     for (int64_t L = 0; L < S->nleaves; L++) {
         S->near_off[L] = S->nnear; S->far_off[L] = S->nfar;
+        if (need && (L % S->stride) && !need[L]) continue;
         onode me = S->nodes[S->leaves[L]];
         find_near(S, &me, root);
     }
+    free(need);
+    S->t_partition = t1 - t0;
+    S->t_cmass = t2 - t1;
+    S->t_lists = now_s() - t2;
     S->near_off[S->nleaves] = S->nnear; S->far_off[S->nleaves] = S->nfar;
     S->built = 1;
     return 0;
@@ -643,6 +674,7 @@ int vvo_eps(vvo_space* S, int merge, int64_t* merged) {
     if (!S->built) return -3;
     g_merged = 0;
     for (int64_t L = 0; L < S->nleaves; L++) {
+        if (L % S->stride) continue;
         const onode* nd = &S->nodes[S->leaves[L]];
         double cx = nd->x, cy = nd->y;
         int64_t att = nearest_body_segment_L(S, L, cx, cy);
@@ -737,6 +769,7 @@ int vvo_convective(vvo_space* S) {
     if (!S->built) return -3;
     if (!bodies_at_rest(S)) return -4;
     for (int64_t L = 0; L < S->nleaves; L++) {
+        if (L % S->stride) continue;
         const onode* nd = &S->nodes[S->leaves[L]];
         double t1 = 0, t2 = 0, t3 = 0, t4 = 0;
         for (int64_t k = S->far_off[L]; k < S->far_off[L + 1]; k++) {
@@ -753,6 +786,8 @@ int vvo_convective(vvo_space* S) {
             t4 += (fp2 * (sqr(dpy) - sqr(dpx)) + fm2 * (sqr(dmy) - sqr(dmx)));
         }
         t1 *= C_1_2PI; t2 *= C_1_2PI; t3 *= C_1_PI; t4 *= C_1_2PI;
+        /* the reference opens one parallel region per leaf (MConvectiveFast.cpp:73-75) */
+#pragma omp parallel for schedule(dynamic, 256)
         for (int64_t i = nd->vf; i < nd->vl; i++) {
             if (!S->g[i]) continue;
             double px = S->x[i], py = S->y[i];
@@ -834,6 +869,7 @@ int vvo_diffusive(vvo_space* S) {
     if (!S->built) return -3;
     const double re = S->re;
     for (int64_t L = 0; L < S->nleaves; L++) {
+        if (L % S->stride) continue;
         const onode* nd = &S->nodes[S->leaves[L]];
         for (int64_t i = nd->vf; i < nd->vl; i++) {
             if (!S->g[i]) continue;
@@ -1167,6 +1203,55 @@ int vvo_slae(vvo_space* S, vvo_body_out* out) {
 #undef SEGCOL
 #undef BCOL
     free(col0);
+    return 0;
+}
+
+int vvo_set_sample(vvo_space* S, int64_t stride) {
+    if (stride < 1) return -1;
+    S->stride = stride;
+    return 0;
+}
+
+/* The reference's steady-state SLAE work per step (time > 0, rigid bodies at rest): the
+ * right-hand side of every slip row (fillSlipEquationForSegment with rightColOnly,
+ * MConvectiveFast.cpp:459-467; rows sampled with the timing stride) followed by one dense
+ * matrix-vector product with the cached inverse (cblas_dgemv, TMatrix.cpp:176-189). */
+int vvo_slae_rhs_step(vvo_space* S, double* rhs_out) {
+    if (!S->built) return -3;
+    int64_t n = vvo_slae_size(S);
+    double* inv = (double*)calloc((size_t)(n * n), sizeof(double));
+    double* b = (double*)calloc((size_t)n, sizeof(double));
+    double* y = (double*)calloc((size_t)n, sizeof(double));
+    if (!inv || !b || !y) { free(inv); free(b); free(y); return -7; }
+    for (int64_t i = 0; i < n; i++) inv[i * n + i] = 1.0;
+    int64_t row = 0;
+    for (int bi = 0; bi < S->nb; bi++) {
+        const obody* bd = &S->bodies[bi];
+        for (int64_t k = 0; k < bd->count; k++, row++) {
+            if (k == bd->p.special_segment_no || (k % S->stride)) continue;
+            int64_t s = bd->first + k;
+            double r = (-S->inf_vy) * S->dlx[s] + S->inf_vx * S->dly[s];
+            int32_t nk = find_node(S, S->rx[s], S->ry[s]);
+            int64_t L = -1;
+            for (int64_t t = 0; t < S->nleaves; t++) if (S->leaves[t] == nk) { L = t; break; }
+            r -= node_influence(S, L, s);
+            b[row] = r;
+        }
+        row += 9;
+    }
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; i++) {
+        double acc = 0;
+        for (int64_t j = 0; j < n; j++) acc += inv[i * n + j] * b[j];
+        y[i] = acc;
+    }
+    if (rhs_out) memcpy(rhs_out, y, sizeof(double) * (size_t)n);
+    free(inv); free(b); free(y);
+    return 0;
+}
+
+int vvo_last_timings(const vvo_space* S, double* out3) {
+    out3[0] = S->t_partition; out3[1] = S->t_cmass; out3[2] = S->t_lists;
     return 0;
 }
 

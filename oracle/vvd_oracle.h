@@ -122,6 +122,13 @@ int vvo_velocity_points(vvo_space* S, int64_t n, const double* px, const double*
 int vvo_slae(vvo_space* S, vvo_body_out* out);
 int64_t vvo_slae_size(const vvo_space* S);
 int vvo_slae_export(const vvo_space* S, double* matrix, double* rhs, double* solution);
+/* Timing sample for the CPU baseline: eps/convective/diffusive and the SLAE right-hand
+ * side process only leaves (rows) whose index is a multiple of stride (default 1 = all). */
+int vvo_set_sample(vvo_space* S, int64_t stride);
+/* Seconds spent in the last tree build: partition, centroids, near/far lists. */
+int vvo_last_timings(const vvo_space* S, double* out3);
+/* Steady-state per-step SLAE work of the reference (right-hand side + dense GEMV). */
+int vvo_slae_rhs_step(vvo_space* S, double* rhs_out);
 /* MFlowmove::vortex_shed (MFlowmove.cpp:217-235). */
 int vvo_vortex_shed(vvo_space* S);
 /* Space::gsum (TSpace.hpp:93-99). */

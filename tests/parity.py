@@ -61,8 +61,12 @@ def check_exact(ref, got, keys=None, prefix=""):
             bad.append(f"{gk} missing")
             continue
         a, b = np.asarray(ref[rk]), np.asarray(got[gk])
-        if a.shape != b.shape or not np.array_equal(a, b):
-            bad.append(f"{gk}: mismatch")
+        if a.shape != b.shape:
+            bad.append(f"{gk}: shape {b.shape} != {a.shape}")
+        elif not np.array_equal(a, b):
+            nbad = int(np.sum(a != b)) if a.dtype.kind != "U" else 1
+            d = float(np.max(np.abs(a.astype(np.float64) - b.astype(np.float64)))) if a.dtype.kind in "fiu" else -1
+            bad.append(f"{gk}: {nbad}/{a.size} differ (max |d| {d:.3g})")
     return bad
 
 

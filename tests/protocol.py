@@ -48,8 +48,12 @@ def tree_record(S, prefix: str, out: dict, full_lists: bool):
         out[prefix + "node_" + k] = nd[k][order]
 
 
-def run_step(S, wl, *, merge=None, full_lists=True, far_criteria=None, record_tree=True):
-    """Runs one step on backend ``S`` (already loaded with ``wl``); returns a dict."""
+def run_step(S, wl, *, merge=None, full_lists=True, far_criteria=None, record_tree=True, seg_g=None):
+    """Runs one step on backend ``S`` (already loaded with ``wl``); returns a dict.
+
+    ``seg_g``: segment circulations to shed instead of this backend's own SLAE solution.
+    Parity runs pass the reference's solution so that every call after the SLAE sees
+    identical inputs (the solve itself is compared with a tolerance)."""
     out = {}
     mn, mx = wl.node_sizes()
     fc = wl.far_criteria if far_criteria is None else far_criteria
@@ -63,6 +67,8 @@ def run_step(S, wl, *, merge=None, full_lists=True, far_criteria=None, record_tr
         out["slae_A"], out["slae_b"], out["slae_x"] = A, b, x
         out["slae_body"] = np.array([[d[k] for k in sorted(d)] for d in bo])
         S.tree_destroy()
+        if seg_g is not None:
+            S.set_segment_g(seg_g)
     S.vortex_shed()
     seg = S.segments()
     out["seg_g"] = seg["g"]

@@ -1,0 +1,78 @@
+"""Parity of the CUDA path (through the C ABI) with the reference.
+
+* Golden fixtures (outputs of the reference's own compiled sources): tree geometry,
+  permutation, near/far lists, centroids, merges, positions and epsilon bit-exact in both
+  precisions; sums within the tolerances below.
+* Larger seeded workloads against the C restatement of the reference (bit-exact with the
+  reference, see test_oracle_pin.py).
+
+Tolerances (per-vortex relative error with a floor of 1e-3 rms, parity.rel_err_vec):
+  FP64 path: convective 1e-12, diffusive 1e-11, friction 1e-10, SLAE cells/rhs 1e-12.
+  FP32 path: convective 1e-5, diffusive 1e-5, friction 1e-5 (wall terms are FP64).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from parity import check_step, golden_cases, load_workload
+from protocol import advance, run_step
+from vvflow_gb300 import workloads as W
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+TOL64 = dict(vel_tol=1e-12, diff_tol=1e-11, fric_tol=1e-10, slae_tol=1e-12)
+TOL32 = dict(vel_tol=1e-5, diff_tol=1e-5, fric_tol=1e-5, slae_tol=1e-12)
+
+
+def gpu_space(precision):
+    from vvflow_gb300 import build as B
+    from vvflow_gb300.vvgpu import GpuSpace
+    B.build()
+    return GpuSpace(precision)
+
+
+def run_gpu(wl, precision, d=None, full_lists=True):
+    """One step (two for fixtures that hold a second step).  Inputs of every call equal the
+    reference's: the shed uses the reference's SLAE solution, and the second step starts
+    from the reference's moved state."""
+    S = gpu_space(precision)
+    S.load(wl)
+    out = run_step(S, wl, full_lists=full_lists, seg_g=None if d is None else d["seg_g"])
+    if d is not None and "s2_in_x" in d:
+        S.set_params(wl.re, wl.dt, wl.inf_vx, wl.inf_vy, 0.0, wl.dt)
+        S.set_vortices(d["s2_in_x"], d["s2_in_y"], d["s2_in_g"], d["s2_in_inv_eps"])
+        out2 = run_step(S, wl, full_lists=full_lists, seg_g=d["s2_seg_g"])
+        out.update({"s2_" + k: v for k, v in out2.items()})
+    st = S.stats()
+    S.close()
+    return out, st
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("case", golden_cases(GOLDEN))
+def test_gpu_matches_golden(case, precision):
+    wl, d = load_workload(os.path.join(GOLDEN, case + ".npz"))
+    got, _ = run_gpu(wl, precision, d, full_lists="t1_near_path" in d or "t2_near_path" in d)
+    tol = TOL64 if precision == 0 else TOL32
+    bad = check_step(d, got, **tol)
+    if "s2_in_x" in d:
+        bad += check_step(d, got, prefix="s2_", **tol)
+    assert not bad, bad
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_gpu_matches_oracle_wake_200k(precision):
+    wl = W.cylinder_wake(200_000, 2000, seed=4)
+    S = oracle.OracleSpace("port")
+    S.load(wl)
+    ref = run_step(S, wl, full_lists=False)
+    S.close()
+    got, st = run_gpu(wl, precision, d={"seg_g": ref["seg_g"]}, full_lists=False)
+    tol = TOL64 if precision == 0 else TOL32
+    bad = check_step(ref, got, **tol)
+    assert not bad, bad
+    assert st["merge_rounds"] >= 1

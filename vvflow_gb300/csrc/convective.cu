@@ -1,0 +1,448 @@
+// Convective velocity (MConvectiveFast::process_all_lists, libvvhd/src/MConvectiveFast.cpp:36-114)
+// and point queries (MConvectiveFast::velocity, :20-34).
+//
+// One warp per target leaf.  The leaf's targets are held in registers in chunks of TC; the
+// 32 lanes stride over the leaf's near sources (each near run is one contiguous vortex
+// range), so every source is loaded once per chunk and applied to all TC targets.  Lane
+// partials are reduced with shuffles.  The far field (two monopoles per far node, expanded
+// to first order about the leaf centre, :48-69 and :84-85) is computed by the same warp.
+//
+// FP64 path: Biot-Savart kernel rotl(dr) g / (|dr|^2 + eps^2) / 2pi in double precision,
+// the reciprocal by Newton-Raphson iteration from the hardware approximation.
+// FP32 path: sources in local frames (frame.cuh), FP32 pair arithmetic, lane partials
+// accumulated per near run and folded into a two-sum (Knuth's TwoSum) compensated pair,
+// final reduction in FP64.
+#include <cfloat>
+
+#include "frame.cuh"
+#include "vvgpu_internal.cuh"
+
+namespace vvgpu {
+
+namespace {
+
+constexpr int CW = 4;  // warps per block
+
+// Reciprocal by Newton-Raphson refinement r <- r (2 - x r) of the PTX approximation.
+__device__ __forceinline__ double rcp64(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+
+__device__ __forceinline__ float rcp32(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bp = s - a;
+    float ap = s - bp;
+    e = (a - ap) + (b - bp);
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+struct ConvArgs {
+    int64_t nl;
+    const int32_t* lvf; const int32_t* lvl;
+    const double4* lgeom;
+    const int32_t* near_off; const int2* near_run;
+    const double4* taylor;
+    const double* cm;
+    const double* x; const double* y; const double* g; const double* ie;
+    double* vx; double* vy;
+    // sinks and slip segments
+    int64_t ns; const double* kx; const double* ky; const double* kg; double sink_e2;
+    int64_t m; const double* srx; const double* sry; const double* sg; const double* sie; const uint32_t* slip;
+    int any_slip;
+    double inf_vx, inf_vy;
+    double fc; int64_t nnodes;
+    // FP32 records
+    const float4* src32; const int2* src_k; const int2* anchor; double G; float Gf;
+};
+
+// sink_list_influence + slip-segment part of body_list_influence, FP64 (per target).
+__device__ __forceinline__ void extra_terms(const ConvArgs& a, double px, double py, double& ox, double& oy) {
+    double rx = 0, ry = 0;
+    for (int64_t k = 0; k < a.ns; k++) {
+        double dx = px - a.kx[k], dy = py - a.ky[k];
+        double s = a.kg[k] / (dx * dx + dy * dy + a.sink_e2 * fabs(a.kg[k]));
+        rx += dx * s; ry += dy * s;
+    }
+    double bx = 0, by = 0;
+    if (a.any_slip) {
+        for (int64_t k = 0; k < a.m; k++) {
+            if (!a.slip[k]) continue;
+            double dx = px - a.srx[k], dy = py - a.sry[k];
+            double e = 1. / a.sie[k];
+            double s = a.sg[k] / (dx * dx + dy * dy + e * e);
+            bx -= dy * s; by += dx * s;
+        }
+    }
+    ox = (rx + bx) * C_1_2PI;
+    oy = (ry + by) * C_1_2PI;
+}
+
+template <int TC>
+__global__ void __launch_bounds__(CW * 32) k_conv64(ConvArgs a) {
+    const int64_t L = (int64_t)blockIdx.x * CW + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (L >= a.nl) return;
+    const double4 me = a.lgeom[L];
+    const double4 tc = a.taylor[L];
+    const double t1 = tc.x, t2 = tc.y, t3 = tc.z, t4 = tc.w;
+    const int32_t v0 = a.lvf[L], v1 = a.lvl[L];
+    const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
+    for (int32_t c0 = v0; c0 < v1; c0 += TC) {
+        double tx[TC], ty[TC], ax[TC], ay[TC];
+#pragma unroll
+        for (int t = 0; t < TC; t++) {
+            int32_t i = c0 + t;
+            tx[t] = (i < v1) ? a.x[i] : 0.;
+            ty[t] = (i < v1) ? a.y[i] : 0.;
+            ax[t] = 0; ay[t] = 0;
+        }
+        for (int32_t r = r0; r < r1; r++) {
+            int2 run = a.near_run[r];
+            int32_t j0 = a.lvf[run.x], j1 = a.lvl[run.y - 1];
+            for (int32_t j = j0 + lane; j < j1; j += 32) {
+                double gj = a.g[j], iej = a.ie[j];
+                if (gj == 0. || iej == 0.) continue;
+                double e = rcp64(iej);
+                double e2 = e * e;
+                double xj = a.x[j], yj = a.y[j];
+#pragma unroll
+                for (int t = 0; t < TC; t++) {
+                    double dx = tx[t] - xj, dy = ty[t] - yj;
+                    double s = gj * rcp64(fma(dx, dx, fma(dy, dy, e2)));
+                    ax[t] = fma(-dy, s, ax[t]);
+                    ay[t] = fma(dx, s, ay[t]);
+                }
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < TC; t++) {
+            ax[t] = warp_sum(ax[t]);
+            ay[t] = warp_sum(ay[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < TC; t++) {
+            int32_t i = c0 + t;
+            if (lane == t && i < v1 && a.g[i] != 0.) {
+                double ex, ey;
+                extra_terms(a, tx[t], ty[t], ex, ey);
+                double lx = tx[t] - me.x, ly = ty[t] - me.y;
+                double vx = a.vx[i], vy = a.vy[i];
+                vx += a.inf_vx; vy += a.inf_vy;
+                vx += ax[t] * C_1_2PI; vy += ay[t] * C_1_2PI;
+                vx += ex; vy += ey;
+                vx += t1; vy += t2;
+                vx += t3 * lx + t4 * ly;
+                vy += t4 * lx + (-t3) * ly;
+                a.vx[i] = vx; a.vy[i] = vy;
+            }
+        }
+    }
+}
+
+template <int TC>
+__global__ void __launch_bounds__(CW * 32) k_conv32(ConvArgs a) {
+    const int64_t L = (int64_t)blockIdx.x * CW + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (L >= a.nl) return;
+    const double4 me = a.lgeom[L];
+    const double4 tc = a.taylor[L];
+    const double t1 = tc.x, t2 = tc.y, t3 = tc.z, t4 = tc.w;
+    const int2 kL = a.anchor[L];
+    const double axL = (double)kL.x * a.G, ayL = (double)kL.y * a.G;
+    const int32_t v0 = a.lvf[L], v1 = a.lvl[L];
+    const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
+    for (int32_t c0 = v0; c0 < v1; c0 += TC) {
+        float tx[TC], ty[TC], hx[TC], hy[TC], lx[TC], ly[TC];
+#pragma unroll
+        for (int t = 0; t < TC; t++) {
+            int32_t i = c0 + t;
+            tx[t] = (i < v1) ? (float)(a.x[i] - axL) : 0.f;
+            ty[t] = (i < v1) ? (float)(a.y[i] - ayL) : 0.f;
+            hx[t] = hy[t] = lx[t] = ly[t] = 0.f;
+        }
+        for (int32_t r = r0; r < r1; r++) {
+            int2 run = a.near_run[r];
+            int32_t j0 = a.lvf[run.x], j1 = a.lvl[run.y - 1];
+            float px[TC], py[TC];
+#pragma unroll
+            for (int t = 0; t < TC; t++) { px[t] = 0.f; py[t] = 0.f; }
+            for (int32_t j = j0 + lane; j < j1; j += 32) {
+                float4 s = a.src32[j];
+                int2 k = a.src_k[j];
+                float sx = s.x + (float)(k.x - kL.x) * a.Gf;
+                float sy = s.y + (float)(k.y - kL.y) * a.Gf;
+#pragma unroll
+                for (int t = 0; t < TC; t++) {
+                    float dx = tx[t] - sx, dy = ty[t] - sy;
+                    float q = s.z * rcp32(fmaf(dx, dx, fmaf(dy, dy, s.w)));
+                    px[t] = fmaf(-dy, q, px[t]);
+                    py[t] = fmaf(dx, q, py[t]);
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < TC; t++) {
+                float s, e;
+                two_sum(hx[t], px[t], s, e); hx[t] = s; lx[t] += e;
+                two_sum(hy[t], py[t], s, e); hy[t] = s; ly[t] += e;
+            }
+        }
+        double ax[TC], ay[TC];
+#pragma unroll
+        for (int t = 0; t < TC; t++) {
+            ax[t] = warp_sum((double)hx[t] + (double)lx[t]);
+            ay[t] = warp_sum((double)hy[t] + (double)ly[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < TC; t++) {
+            int32_t i = c0 + t;
+            if (lane == t && i < v1 && a.g[i] != 0.) {
+                double pxd = a.x[i], pyd = a.y[i];
+                double ex, ey;
+                extra_terms(a, pxd, pyd, ex, ey);
+                double dlx = pxd - me.x, dly = pyd - me.y;
+                double vx = a.vx[i], vy = a.vy[i];
+                vx += a.inf_vx; vy += a.inf_vy;
+                vx += ax[t] * C_1_2PI; vy += ay[t] * C_1_2PI;
+                vx += ex; vy += ey;
+                vx += t1; vy += t2;
+                vx += t3 * dlx + t4 * dly;
+                vy += t4 * dlx + (-t3) * dly;
+                a.vx[i] = vx; a.vy[i] = vy;
+            }
+        }
+    }
+}
+
+// FP32 source records: position in own leaf frame, g, eps^2 (eps = 1/_1_eps; a zero
+// _1_eps or zero g gives a record that contributes exactly zero).
+__global__ void k_src32(int64_t n, const int32_t* __restrict__ leaf_of, const int2* __restrict__ anchor, double G,
+                        const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ g,
+                        const double* __restrict__ ie, float4* src, int2* src_k) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int2 k = anchor[leaf_of[i]];
+    double e = 1. / ie[i];
+    float gf = (float)g[i];
+    float e2 = (float)(e * e);
+    if (ie[i] == 0.) { gf = 0.f; e2 = 1.f; }
+    src[i] = make_float4((float)(x[i] - (double)k.x * G), (float)(y[i] - (double)k.y * G), gf, e2);
+    src_k[i] = k;
+}
+
+__global__ void k_anchor2(int64_t nl, const double4* __restrict__ lgeom, double G, int2* anchor) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    double4 me = lgeom[L];
+    double cx = isfinite(me.x) ? me.x : 0., cy = isfinite(me.y) ? me.y : 0.;
+    anchor[L] = anchor_of(cx, cy, G);
+}
+
+// stree::findNode (TSortedTree.cpp:284-303) + near/far (exact monopoles) + extra terms.
+__global__ void k_points(int64_t np, const double* __restrict__ qx, const double* __restrict__ qy,
+                         const double4* __restrict__ geom, const int32_t* __restrict__ ch1,
+                         const int32_t* __restrict__ dfs, ConvArgs a, double* ovx, double* ovy) {
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    double px = qx[q], py = qy[q];
+    int32_t k = 0;
+    for (int it = 0; it <= MAX_DEPTH && ch1[k] >= 0; it++) {
+        double4 gm = geom[k];
+        if (gm.z < gm.w) k = (px < gm.x) ? ch1[k] : ch1[k] + 1;
+        else k = (py < gm.y) ? ch1[k] : ch1[k] + 1;
+    }
+    int32_t L = dfs[k];
+    double rx = 0, ry = 0;
+    for (int32_t r = a.near_off[L]; r < a.near_off[L + 1]; r++) {
+        int2 run = a.near_run[r];
+        for (int32_t j = a.lvf[run.x]; j < a.lvl[run.y - 1]; j++) {
+            if (a.g[j] == 0.) continue;
+            double dx = px - a.x[j], dy = py - a.y[j];
+            double e = 1. / a.ie[j];
+            double s = a.g[j] / (dx * dx + dy * dy + e * e);
+            rx -= dy * s; ry += dx * s;
+        }
+    }
+    // far nodes of leaf k by the reference's walk (exact FP64 decisions)
+    double fx = 0, fy = 0;
+    {
+        const double4 me = geom[k];
+        int32_t stack[MAX_DEPTH + 2];
+        int sp = 0;
+        stack[sp++] = 0;
+        int64_t guard = 0;
+        while (sp && ++guard <= a.nnodes) {
+            const int32_t t = stack[--sp];
+            const double4 tg = geom[t];
+            double ddx = dsub(tg.x, me.x), ddy = dsub(tg.y, me.y);
+            double hp = dadd(dadd(dadd(tg.z, tg.w), me.z), me.w);
+            if (dabs2(ddx, ddy) > dmul(dmul(a.fc, hp), hp)) {
+                const double* c = a.cm + 6 * (size_t)t;
+                double dx = px - c[0], dy = py - c[1];
+                double s = c[2] / (dx * dx + dy * dy);
+                fx -= dy * s; fy += dx * s;
+                dx = px - c[3]; dy = py - c[4];
+                s = c[5] / (dx * dx + dy * dy);
+                fx -= dy * s; fy += dx * s;
+                continue;
+            }
+            const int32_t c1 = ch1[t];
+            if (c1 >= 0 && sp + 2 <= MAX_DEPTH + 2) {
+                stack[sp++] = c1 + 1;
+                stack[sp++] = c1;
+            }
+        }
+    }
+    double ex, ey;
+    extra_terms(a, px, py, ex, ey);
+    ovx[q] = rx * C_1_2PI + fx * C_1_2PI + ex + a.inf_vx;
+    ovy[q] = ry * C_1_2PI + fy * C_1_2PI + ey + a.inf_vy;
+}
+
+// Algorithmic near-pair count: sum over leaves of (non-zero targets) x (non-zero sources
+// in the near runs).
+__global__ void k_leaf_nz(int64_t nl, const int32_t* __restrict__ lvf, const int32_t* __restrict__ lvl,
+                          const double* __restrict__ g, int32_t* nz) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    int32_t k = 0;
+    for (int32_t i = lvf[L]; i < lvl[L]; i++) k += (g[i] != 0.);
+    nz[L] = k;
+}
+
+__global__ void k_near_pairs(int64_t nl, const int32_t* __restrict__ nz, const int32_t* __restrict__ pre,
+                             const int32_t* __restrict__ near_off, const int2* __restrict__ near_run,
+                             unsigned long long* out) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long v = 0;
+    if (L < nl && nz[L]) {
+        int64_t src = 0;
+        for (int32_t r = near_off[L]; r < near_off[L + 1]; r++) src += pre[near_run[r].y] - pre[near_run[r].x];
+        v = (unsigned long long)nz[L] * (unsigned long long)src;
+    }
+    v = warp_sum_u64(v);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(out, v);
+}
+
+ConvArgs make_args(Ctx& c) {
+    ConvArgs a{};
+    a.nl = c.nleaves;
+    a.lvf = c.lf_vf.p; a.lvl = c.lf_vl.p; a.lgeom = c.lf_geom.p;
+    a.near_off = c.near_off.p; a.near_run = c.near_run.p;
+    a.taylor = c.lf_taylor.p; a.cm = c.nd_cm.p;
+    a.x = c.x.p; a.y = c.y.p; a.g = c.g.p; a.ie = c.ie.p; a.vx = c.vx.p; a.vy = c.vy.p;
+    a.ns = c.ns; a.kx = c.k_x.p; a.ky = c.k_y.p; a.kg = c.k_g.p; a.sink_e2 = c.dt * C_1_PI;
+    a.m = c.m; a.srx = c.s_rx.p; a.sry = c.s_ry.p; a.sg = c.s_g.p; a.sie = c.s_ie.p; a.slip = c.s_slip.p;
+    a.any_slip = 0;
+    for (auto s : c.h_slip) a.any_slip |= (s != 0);
+    a.inf_vx = c.inf_vx; a.inf_vy = c.inf_vy;
+    a.fc = c.far_criteria; a.nnodes = c.nnodes;
+    return a;
+}
+
+void check_bodies_at_rest(Ctx& c) {
+    for (auto& b : c.bodies) {
+        const vvgpu_body_params& p = b.p;
+        if (!(std::fabs(p.speed_slae_x) + std::fabs(p.speed_slae_y) + std::fabs(p.speed_slae_o) < 1E-10))
+            throw ApiError{VVGPU_ERR_UNSUPPORTED, "moving bodies (attached sheets) are not supported"};
+    }
+}
+
+}  // namespace
+
+void build_frames(Ctx& c) {
+    cudaStream_t s = c.st();
+    const int64_t n = c.n, nl = c.nleaves;
+    double4 root;
+    VV_CUDA(cudaMemcpyAsync(&root, c.nd_geom.p, sizeof root, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    Frame fr = make_frame(std::fmax(std::fabs(root.x), std::fabs(root.y)) + std::fmax(root.z, root.w));
+    c.frame_G = fr.G;
+    c.lf_anchor.reserve(nl + 1);
+    c.src32.reserve(n + 1);
+    c.src_k.reserve(n + 1);
+    if (nl) {
+        k_anchor2<<<grid_for(nl, 128), 128, 0, s>>>(nl, c.lf_geom.p, fr.G, c.lf_anchor.p);
+        VV_LAUNCH_CHECK();
+    }
+    if (n) {
+        k_src32<<<grid_for(n, 256), 256, 0, s>>>(n, c.leaf_of.p, c.lf_anchor.p, fr.G, c.x.p, c.y.p, c.g.p, c.ie.p,
+                                                 c.src32.p, c.src_k.p);
+        VV_LAUNCH_CHECK();
+    }
+}
+
+void count_near_pairs(Ctx& c) {
+    cudaStream_t s = c.st();
+    const int64_t nl = c.nleaves;
+    DArr<int32_t> nz, pre;
+    nz.reserve(nl + 1);
+    pre.reserve(nl + 2);
+    k_leaf_nz<<<grid_for(nl, 256), 256, 0, s>>>(nl, c.lf_vf.p, c.lf_vl.p, c.g.p, nz.p);
+    VV_LAUNCH_CHECK();
+    exclusive_scan(c, nz.p, pre.p, nl);
+    unsigned long long* out = c.counters.p + 11;
+    VV_CUDA(cudaMemsetAsync(out, 0, 8, s));
+    k_near_pairs<<<grid_for(nl, 256), 256, 0, s>>>(nl, nz.p, pre.p, c.near_off.p, c.near_run.p, out);
+    VV_LAUNCH_CHECK();
+    unsigned long long v = 0;
+    VV_CUDA(cudaMemcpyAsync(&v, out, 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    c.stats.near_pairs = (int64_t)v;
+}
+
+void convective(Ctx& c) {
+    check_bodies_at_rest(c);
+    if (c.n == 0 || c.nleaves == 0) return;
+    cudaStream_t s = c.st();
+    if (c.count_pairs) count_near_pairs(c);
+    ConvArgs a = make_args(c);
+    unsigned grid = grid_for(c.nleaves, CW);
+    if (c.precision == VVGPU_FP32) {
+        build_frames(c);
+        a.src32 = c.src32.p; a.src_k = c.src_k.p; a.anchor = c.lf_anchor.p; a.G = c.frame_G; a.Gf = (float)c.frame_G;
+        k_conv32<16><<<grid, CW * 32, 0, s>>>(a);
+    } else {
+        k_conv64<8><<<grid, CW * 32, 0, s>>>(a);
+    }
+    VV_LAUNCH_CHECK();
+    VV_CUDA(cudaStreamSynchronize(s));
+}
+
+void velocity_points(Ctx& c, int64_t np, const double* px, const double* py, double* vx, double* vy) {
+    check_bodies_at_rest(c);
+    if (np == 0) return;
+    cudaStream_t s = c.st();
+    DArr<double> q;
+    q.reserve(4 * np);
+    VV_CUDA(cudaMemcpyAsync(q.p, px, np * 8, cudaMemcpyHostToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(q.p + np, py, np * 8, cudaMemcpyHostToDevice, s));
+    ConvArgs a = make_args(c);
+    k_points<<<grid_for(np, 128), 128, 0, s>>>(np, q.p, q.p + np, c.nd_geom.p, c.nd_ch1.p, c.nd_dfs.p, a,
+                                              q.p + 2 * np, q.p + 3 * np);
+    VV_LAUNCH_CHECK();
+    VV_CUDA(cudaMemcpyAsync(vx, q.p + 2 * np, np * 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaMemcpyAsync(vy, q.p + 3 * np, np * 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace vvgpu

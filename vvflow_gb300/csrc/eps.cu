@@ -1,0 +1,560 @@
+// Epsilon / merge pass of libvvhd (MEpsilonFast, libvvhd/src/MEpsilonFast.cpp:11-253).
+//
+// The reference walks the vortices in list order; each one finds its two nearest non-zero
+// neighbours among its leaf's near leaves, may absorb the nearest (MergeVortexes: move
+// and add circulation, zero the neighbour) and then sets _1_eps.  Later vortices see those
+// changes, so the pass is order dependent.
+//
+// Here every vortex i computes its outcome from the state "as of its turn": a vortex j is
+// zero if some k < i absorbed it, and sits at its merged position with its merged
+// circulation if j < i merged at its own turn.  Given guesses of all outcomes, every
+// vortex evaluates in parallel; the outcome of i only depends on outcomes of k < i, so
+// repeating until nothing changes converges to the unique fixed point, which is the
+// sequential result, bit for bit.  Typical runs need 5-7 rounds; after the first round
+// only leaves near a changed outcome are evaluated again.
+//
+// Candidate leaves: for each target leaf L, R_L bounds every target's second-nearest
+// distance from above (the farthest corner distance to a leaf that holds two live
+// vortices, or three for L itself); only near leaves whose box comes within 2 R_L of L's
+// box can hold a top-two candidate (2 R_L also covers the re-search from a merged
+// position, which lies within R_L of the original one).
+//
+// The two-nearest search filters candidates in FP32 in local frames (frame.cuh) with a
+// rigorous margin and evaluates only the candidates inside the margin in FP64, with the
+// reference's operation order and its tie rule (first in list order wins), so every
+// decision equals the reference's.
+#include <cfloat>
+#include <climits>
+
+#include "frame.cuh"
+#include "vvgpu_internal.cuh"
+
+namespace vvgpu {
+
+namespace {
+
+constexpr int EB = 128;
+constexpr int32_t SKIPPED = -2;  // partner code: vortex not evaluated (g = 0 at its turn)
+constexpr int CAND_CAP = 96;     // candidate leaves kept per target leaf
+
+// MEpsilonFast::nearestBodySegment (MEpsilonFast.cpp:214-253) and the per-leaf merge
+// criterion / epsilon floor (MEpsilonFast.cpp:25-47).
+__global__ void k_leaf_params(int64_t nl, const double4* __restrict__ lgeom, const int32_t* __restrict__ near_off,
+                              const int2* __restrict__ near_run, const int32_t* __restrict__ lsf,
+                              const int32_t* __restrict__ lsl, const int32_t* __restrict__ seg_order,
+                              const double* __restrict__ rx, const double* __restrict__ ry,
+                              const double* __restrict__ dlx, const double* __restrict__ dly,
+                              const int64_t* __restrict__ body_first, const int64_t* __restrict__ body_count,
+                              int nbodies, int merge, double* mcs_out, double* epr_out) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    double4 me = lgeom[L];
+    const double px = me.x, py = me.y;
+    int64_t att = -1;
+    double res = DBL_MAX;
+    for (int32_t r = near_off[L]; r < near_off[L + 1]; r++) {
+        int2 run = near_run[r];
+        int32_t q0 = lsf[run.x], q1 = lsl[run.y - 1];
+        for (int32_t q = q0; q < q1; q++) {
+            int32_t s = seg_order[q];
+            double d = dabs2(dsub(px, rx[s]), dsub(py, ry[s]));
+            if (d < res) { res = d; att = s; }
+        }
+    }
+    if (att < 0) {
+        for (int b = 0; b < nbodies; b++) {
+            int64_t f = body_first[b], cnt = body_count[b];
+            for (int64_t k = 0; k < cnt; k++) {
+                int64_t s = f + k;
+                double d = dabs2(dsub(px, rx[s]), dsub(py, ry[s]));
+                if (d < res) { res = d; att = s; }
+                else k += 9;  // MEpsilonFast.cpp:248
+            }
+        }
+    }
+    double mcs, epr;
+    if (merge) {
+        mcs = (att >= 0) ? dmul(dmul(0.16, dabs2(dlx[att], dly[att])),
+                                dadd(1., __dsqrt_rn(dabs2(dsub(px, rx[att]), dsub(py, ry[att])))))
+                         : 0.;
+    } else {
+        mcs = __longlong_as_double(0x7ff8000000000000ll);  // quiet NaN: never merge
+    }
+    epr = (att >= 0) ? dmul(__dsqrt_rn(dabs2(dlx[att], dly[att])), (1.0 / 3.0)) : 0.;
+    mcs_out[L] = mcs;
+    epr_out[L] = epr;
+}
+
+__global__ void k_anchor(int64_t nl, const double4* __restrict__ lgeom, double G, int2* anchor) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    double4 me = lgeom[L];
+    double cx = isfinite(me.x) ? me.x : 0., cy = isfinite(me.y) ? me.y : 0.;
+    anchor[L] = anchor_of(cx, cy, G);
+}
+
+__device__ __forceinline__ float rel(double v, int k, double G) { return (float)(v - (double)k * G); }
+
+// Initial records: position in own leaf frame and the sign of g.
+__global__ void k_rec0(int64_t n, const int32_t* __restrict__ leaf_of, const int2* __restrict__ anchor, double G,
+                       const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ g,
+                       float4* rec0, double* x0, double* y0, double* g0, int32_t* partner, int32_t* zb,
+                       int32_t* zb_prev) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int2 a = anchor[leaf_of[i]];
+    double xi = x[i], yi = y[i], gi = g[i];
+    rec0[i] = make_float4(rel(xi, a.x, G), rel(yi, a.y, G), (float)dsgn(gi), 0.f);
+    x0[i] = xi; y0[i] = yi; g0[i] = gi;
+    partner[i] = -1;
+    zb[i] = INT_MAX;
+    zb_prev[i] = INT_MAX;
+}
+
+// Per-leaf FP32 box (own frame) over every position a non-zero member may have this round,
+// and the number of members that are live for every target (never absorbed, non-zero).
+__global__ void k_eps_box(int64_t nl, const int32_t* __restrict__ lvf, const int32_t* __restrict__ lvl,
+                          const float4* __restrict__ rec0, const float4* __restrict__ recO,
+                          const int32_t* __restrict__ partner, const int32_t* __restrict__ zb, float4* box,
+                          int32_t* live) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+    int32_t nlive = 0;
+    for (int32_t i = lvf[L]; i < lvl[L]; i++) {
+        float4 r = rec0[i];
+        if (r.z != 0.f) {
+            mnx = fminf(mnx, r.x); mny = fminf(mny, r.y); mxx = fmaxf(mxx, r.x); mxy = fmaxf(mxy, r.y);
+        }
+        bool moved = partner[i] >= 0;
+        if (moved) {
+            float4 o = recO[i];
+            mnx = fminf(mnx, o.x); mny = fminf(mny, o.y); mxx = fmaxf(mxx, o.x); mxy = fmaxf(mxy, o.y);
+        }
+        if (r.z != 0.f && zb[i] == INT_MAX && (!moved || recO[i].z != 0.f)) nlive++;
+    }
+    box[L] = make_float4(mnx, mny, mxx, mxy);
+    live[L] = nlive;
+}
+
+// Candidate leaves of every target leaf (one warp per target leaf).  Also the extent of
+// the candidate region in L's frame (bounds every FP32 coordinate the search forms).
+__global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, const int2* __restrict__ near_run,
+                           const int2* __restrict__ anchor, const float4* __restrict__ box,
+                           const int32_t* __restrict__ live, float Gf, int32_t* cand, int32_t* ncand, float* rn,
+                           const int32_t* __restrict__ leaf_changed, int32_t* dirty, int first_round) {
+    const int64_t L = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (L >= nl) return;
+    const float4 bL = box[L];
+    const int2 aL = anchor[L];
+    const int32_t r0 = near_off[L], r1 = near_off[L + 1];
+    // pass A: upper bound on every target's second-nearest distance
+    float R2 = INFINITY;
+    if (bL.x <= bL.z) {
+        for (int32_t r = r0; r < r1; r++) {
+            int2 run = near_run[r];
+            for (int32_t q = run.x + lane; q < run.y; q += 32) {
+                int need = (q == L) ? 3 : 2;
+                if (live[q] < need) continue;
+                float4 b = box[q];
+                float2 sh = frame_shift(anchor[q], aL, Gf);
+                float ux = fmaxf(fabsf(b.z + sh.x - bL.x), fabsf(bL.z - (b.x + sh.x)));
+                float uy = fmaxf(fabsf(b.w + sh.y - bL.y), fabsf(bL.w - (b.y + sh.y)));
+                R2 = fminf(R2, ux * ux + uy * uy);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) R2 = fminf(R2, __shfl_xor_sync(0xffffffffu, R2, o));
+    // pass B: near leaves within 2 R_L (FP32 with a relative and an absolute margin)
+    float ext = 0.f;
+    int32_t cnt = 0;
+    bool overflow = false;
+    bool is_dirty = first_round != 0;
+    const float lim = isfinite(R2) ? 2.f * sqrtf(R2) * (1.f + 1e-4f) : INFINITY;
+    for (int32_t r = r0; r < r1; r++) {
+        int2 run = near_run[r];
+        for (int32_t qb = run.x; qb < run.y; qb += 32) {
+            int32_t q = qb + lane;
+            bool hit = false;
+            float e = 0.f;
+            if (q < run.y) {
+                float4 b = box[q];
+                if (b.x <= b.z) {
+                    float2 sh = frame_shift(anchor[q], aL, Gf);
+                    float bx0 = b.x + sh.x, bx1 = b.z + sh.x, by0 = b.y + sh.y, by1 = b.w + sh.y;
+                    float dx = fmaxf(fmaxf(bx0 - bL.z, bL.x - bx1), 0.f);
+                    float dy = fmaxf(fmaxf(by0 - bL.w, bL.y - by1), 0.f);
+                    float pad = lim + ldexpf(fabsf(bx0) + fabsf(bx1) + fabsf(by0) + fabsf(by1) + Gf, -14);
+                    hit = (dx <= pad && dy <= pad && dx * dx + dy * dy <= pad * pad) || !isfinite(lim);
+                    if (hit) e = fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)), fmaxf(fabsf(by0), fabsf(by1)));
+                }
+            }
+            unsigned mask = __ballot_sync(0xffffffffu, hit);
+            if (hit) {
+                int pos = cnt + __popc(mask & ((1u << lane) - 1));
+                if (pos < CAND_CAP) cand[(size_t)L * CAND_CAP + pos] = q;
+                if (!first_round && leaf_changed[q]) is_dirty = true;
+            }
+            cnt += __popc(mask);
+            ext = fmaxf(ext, e);
+        }
+    }
+    if (cnt > CAND_CAP) overflow = true;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
+        is_dirty = __shfl_xor_sync(0xffffffffu, (int)is_dirty, o) || is_dirty;
+    }
+    if (lane == 0) {
+        ncand[L] = overflow ? -1 : cnt;  // -1: use the whole near list
+        rn[L] = ext + fmaxf(fmaxf(fabsf(bL.x), fabsf(bL.z)), fmaxf(fabsf(bL.y), fabsf(bL.w)));
+        dirty[L] = is_dirty ? 1 : 0;
+    }
+}
+
+struct Top2 {
+    double r1, r2;
+    int32_t l1, l2;
+};
+
+__device__ __forceinline__ void top2_push(Top2& t, double d, int32_t j) {
+    if (!(d < DBL_MAX)) return;  // the reference never registers DBL_MAX or NaN
+    // lexicographic (distance, list position); list position = slot index
+    if (d < t.r1 || (d == t.r1 && j < t.l1)) { t.r2 = t.r1; t.l2 = t.l1; t.r1 = d; t.l1 = j; }
+    else if (d < t.r2 || (d == t.r2 && j < t.l2)) { t.r2 = d; t.l2 = j; }
+}
+
+struct EpsView {
+    const int32_t* lvf; const int32_t* lvl;
+    const int2* anchor; const float4* box; const float* rn;
+    const int32_t* near_off; const int2* near_run;
+    const int32_t* cand; const int32_t* ncand;
+    const float4* rec0; const float4* recO;
+    const double* x0; const double* y0; const double* g0;
+    const int32_t* partner; const int32_t* zb;
+    const double* ox; const double* oy; const double* og;
+    double G; float Gf;
+};
+
+// Candidate state as of the turn of target i.
+struct Cand {
+    bool live;
+    float4 rec;
+};
+__device__ __forceinline__ Cand cand_state(const EpsView& v, int32_t j, int32_t i, int32_t excl) {
+    Cand c;
+    c.live = false;
+    if (j == i || j == excl) return c;
+    if (v.zb[j] < i) return c;
+    bool moved = (j < i) && (v.partner[j] >= 0);
+    c.rec = moved ? v.recO[j] : v.rec0[j];
+    c.live = c.rec.z != 0.f;
+    return c;
+}
+__device__ __forceinline__ void cand_exact(const EpsView& v, int32_t j, int32_t i, double& xj, double& yj, double& gj) {
+    bool moved = (j < i) && (v.partner[j] >= 0);
+    xj = moved ? v.ox[j] : v.x0[j];
+    yj = moved ? v.oy[j] : v.y0[j];
+    gj = moved ? v.og[j] : v.g0[j];
+}
+
+__device__ __forceinline__ float thr_of(float t2, float D) {
+    if (!(t2 < INFINITY)) return INFINITY;
+    float r = sqrtf(t2) * (1.f + 1e-5f) + 2.f * D;
+    return r * r * (1.f + 1e-6f);
+}
+
+__device__ __forceinline__ float box_lb(float4 b, float2 sh, float tx, float ty) {
+    float bx0 = b.x + sh.x, bx1 = b.z + sh.x, by0 = b.y + sh.y, by1 = b.w + sh.y;
+    float dx = fmaxf(fmaxf(bx0 - tx, tx - bx1), 0.f);
+    float dy = fmaxf(fmaxf(by0 - ty, ty - by1), 0.f);
+    return dx * dx + dy * dy;
+}
+
+// Visits leaf q's live candidates for target i (shared by both passes).
+template <int PASS>
+__device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, int2 aL, int32_t i, int32_t excl, float tx,
+                                          float ty, double px, double py, float D, float& t1, float& t2,
+                                          float& thr, Top2& best) {
+    float2 sh = frame_shift(v.anchor[q], aL, v.Gf);
+    if (box_lb(v.box[q], sh, tx, ty) > thr) return;
+    for (int32_t j = v.lvf[q]; j < v.lvl[q]; j++) {
+        Cand c = cand_state(v, j, i, excl);
+        if (!c.live) continue;
+        float dx = tx - (c.rec.x + sh.x), dy = ty - (c.rec.y + sh.y);
+        float d = dx * dx + dy * dy;
+        if (PASS == 0) {
+            if (d < t1) { t2 = t1; t1 = d; thr = thr_of(t2, D); }
+            else if (d < t2) { t2 = d; thr = thr_of(t2, D); }
+        } else if (d <= thr) {
+            double xj, yj, gj;
+            cand_exact(v, j, i, xj, yj, gj);
+            top2_push(best, dabs2(dsub(px, xj), dsub(py, yj)), j);
+        }
+    }
+}
+
+// Two nearest live candidates of target i (at exact position px,py) among leaf L's
+// candidate leaves, excluding slot excl.  Returns the exact FP64 top-2 of the reference.
+__device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl, double px, double py) {
+    const int2 aL = v.anchor[L];
+    const float tx = (float)(px - (double)aL.x * v.G), ty = (float)(py - (double)aL.y * v.G);
+    const float D = ldexpf(v.rn[L] + fabsf(tx) + fabsf(ty) + v.Gf, -17);
+    float t1 = INFINITY, t2 = INFINITY, thr = INFINITY;
+    Top2 best{DBL_MAX, DBL_MAX, INT_MAX, INT_MAX};
+    const int32_t nc = v.ncand[L];
+    // pass 0: FP32 second-smallest distance; pass 1: exact top-2 within the margin
+#pragma unroll 1
+    for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1) thr = thr_of(t2, D);
+        if (pass == 0) scan_leaf<0>(v, L, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
+        else scan_leaf<1>(v, L, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
+        if (nc >= 0) {
+            const int32_t* cl = v.cand + (size_t)L * CAND_CAP;
+            for (int32_t k = 0; k < nc; k++) {
+                int32_t q = cl[k];
+                if (q == L) continue;
+                if (pass == 0) scan_leaf<0>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
+                else scan_leaf<1>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
+            }
+        } else {
+            for (int32_t r = v.near_off[L]; r < v.near_off[L + 1]; r++) {
+                int2 run = v.near_run[r];
+                for (int32_t q = run.x; q < run.y; q++) {
+                    if (q == L) continue;
+                    if (pass == 0) scan_leaf<0>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
+                    else scan_leaf<1>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
+                }
+            }
+        }
+    }
+    return best;
+}
+
+__global__ void k_eps_round(int64_t n, EpsView v, const int32_t* __restrict__ leaf_of,
+                            const double* __restrict__ mcs_l, const double* __restrict__ epr_l,
+                            const double* __restrict__ ie_in, const int32_t* __restrict__ dirty,
+                            const double* __restrict__ oie_old, int32_t* partner_new, double* ox_new,
+                            double* oy_new, double* og_new, double* oie_new, int32_t* changed) {
+    int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ii >= n) return;
+    const int32_t i = (int32_t)ii;
+    const int32_t L = leaf_of[i];
+    if (!dirty[L]) {  // no input of this leaf's targets changed: keep the outcome
+        partner_new[i] = v.partner[i];
+        ox_new[i] = v.ox[i]; oy_new[i] = v.oy[i]; og_new[i] = v.og[i]; oie_new[i] = oie_old[i];
+        return;
+    }
+    const double gi0 = v.g0[i];
+    int32_t partner = SKIPPED;
+    double px = v.x0[i], py = v.y0[i], gi = gi0, ie = ie_in[i];
+    if (gi0 != 0 && !(v.zb[i] < i)) {
+        const double mcs = mcs_l[L];
+        Top2 t = two_nearest(v, L, i, -1, px, py);
+        double e;
+        partner = -1;
+        if (t.l1 == INT_MAX) e = DBL_MIN;
+        else if (t.l2 == INT_MAX) e = __dsqrt_rn(t.r1);
+        else if (isnan(mcs)) e = __dsqrt_rn(t.r2);
+        else {
+            double x1, y1, g1, x2, y2, g2;
+            cand_exact(v, t.l1, i, x1, y1, g1);
+            cand_exact(v, t.l2, i, x2, y2, g2);
+            if ((t.r1 < mcs) || ((dsgn(g1) == dsgn(g2)) && (dsgn(g1) != dsgn(gi)))) {
+                // MergeVortexes (MEpsilonFast.cpp:111-126)
+                if (dsgn(gi) == dsgn(g1)) {
+                    double sx = dadd(dmul(px, gi), dmul(x1, g1));
+                    double sy = dadd(dmul(py, gi), dmul(y1, g1));
+                    double inv = ddiv(1., dadd(gi, g1));
+                    px = dmul(sx, inv);
+                    py = dmul(sy, inv);
+                } else if (fabs(gi) < fabs(g1)) {
+                    px = x1;
+                    py = y1;
+                }
+                gi = dadd(gi, g1);
+                partner = t.l1;
+                Top2 u = two_nearest(v, L, i, t.l1, px, py);
+                if (u.l1 == INT_MAX) e = DBL_MIN;
+                else if (u.l2 == INT_MAX) e = __dsqrt_rn(u.r1);
+                else e = __dsqrt_rn(u.r2);
+            } else {
+                e = __dsqrt_rn(t.r2);
+            }
+        }
+        ie = ddiv(1.0, smax(e, epr_l[L]));
+    }
+    bool ch = (partner != v.partner[i] && !(partner == SKIPPED && v.partner[i] == SKIPPED)) ||
+              (__double_as_longlong(px) != __double_as_longlong(v.ox[i])) ||
+              (__double_as_longlong(py) != __double_as_longlong(v.oy[i])) ||
+              (__double_as_longlong(gi) != __double_as_longlong(v.og[i])) ||
+              (__double_as_longlong(ie) != __double_as_longlong(oie_old[i]));
+    partner_new[i] = partner;
+    ox_new[i] = px; oy_new[i] = py; og_new[i] = gi; oie_new[i] = ie;
+    if (ch) *changed = 1;
+}
+
+__global__ void k_zb_reset(int64_t n, const int32_t* __restrict__ zb, int32_t* zb_prev, int32_t* zb_new) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) { zb_prev[i] = zb[i]; zb_new[i] = INT_MAX; }
+}
+
+__global__ void k_zb_scatter(int64_t n, const int32_t* __restrict__ partner, const int32_t* __restrict__ leaf_of,
+                             const int2* __restrict__ anchor, double G, const double* __restrict__ ox,
+                             const double* __restrict__ oy, const double* __restrict__ og, int32_t* zb, float4* recO) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t p = partner[i];
+    if (p >= 0) {
+        atomicMin(&zb[p], (int32_t)i);
+        int2 a = anchor[leaf_of[i]];
+        recO[i] = make_float4(rel(ox[i], a.x, G), rel(oy[i], a.y, G), (float)dsgn(og[i]), 0.f);
+    }
+}
+
+// Leaves whose members' state (as other vortices see it) changed in the last round.
+__global__ void k_leaf_changed(int64_t n, const int32_t* __restrict__ leaf_of, const int32_t* __restrict__ p_old,
+                               const int32_t* __restrict__ p_new, const double* __restrict__ x_old,
+                               const double* __restrict__ x_new, const double* __restrict__ y_old,
+                               const double* __restrict__ y_new, const double* __restrict__ g_old,
+                               const double* __restrict__ g_new, const int32_t* __restrict__ zb_old,
+                               const int32_t* __restrict__ zb_new, int32_t* leaf_changed) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t po = p_old[i] < 0 ? -1 : p_old[i], pn = p_new[i] < 0 ? -1 : p_new[i];
+    bool ch = (po != pn) || (zb_old[i] != zb_new[i]);
+    if (pn >= 0) {
+        ch = ch || __double_as_longlong(x_old[i]) != __double_as_longlong(x_new[i]) ||
+             __double_as_longlong(y_old[i]) != __double_as_longlong(y_new[i]) ||
+             __double_as_longlong(g_old[i]) != __double_as_longlong(g_new[i]);
+    }
+    if (ch) leaf_changed[leaf_of[i]] = 1;
+}
+
+__global__ void k_eps_final(int64_t n, const int32_t* __restrict__ partner, const int32_t* __restrict__ zb,
+                            const double* __restrict__ ox, const double* __restrict__ oy,
+                            const double* __restrict__ og, const double* __restrict__ oie, double* x, double* y,
+                            double* g, double* ie, unsigned long long* merged) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t p = partner[i];
+    if (p != SKIPPED) ie[i] = oie[i];
+    if (p >= 0) {
+        x[i] = ox[i]; y[i] = oy[i]; g[i] = og[i];
+        atomicAdd(merged, 1ull);
+    }
+    if (zb[i] != INT_MAX) g[i] = 0.;
+}
+
+}  // namespace
+
+void eps_pass(Ctx& c, int merge, int64_t* merged) {
+    cudaStream_t s = c.st();
+    const int64_t n = c.n, nl = c.nleaves;
+    // per-leaf merge criterion and epsilon floor
+    c.lf_mcs.reserve(nl + 1);
+    c.lf_epr.reserve(nl + 1);
+    std::vector<int64_t> bf(c.bodies.size() + 1), bc(c.bodies.size() + 1);
+    for (size_t b = 0; b < c.bodies.size(); b++) { bf[b] = c.bodies[b].first; bc[b] = c.bodies[b].count; }
+    DArr<int64_t> dbf, dbc;
+    dbf.reserve(bf.size());
+    dbc.reserve(bc.size());
+    VV_CUDA(cudaMemcpyAsync(dbf.p, bf.data(), bf.size() * 8, cudaMemcpyHostToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(dbc.p, bc.data(), bc.size() * 8, cudaMemcpyHostToDevice, s));
+    if (nl > 0) {
+        k_leaf_params<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.lf_geom.p, c.near_off.p, c.near_run.p, c.lf_sf.p,
+                                                      c.lf_sl.p, c.seg_order.p, c.s_rx.p, c.s_ry.p, c.s_dlx.p,
+                                                      c.s_dly.p, dbf.p, dbc.p, (int)c.bodies.size(), merge,
+                                                      c.lf_mcs.p, c.lf_epr.p);
+        VV_LAUNCH_CHECK();
+    }
+    if (n == 0) {
+        if (merged) *merged = 0;
+        VV_CUDA(cudaStreamSynchronize(s));
+        c.stats.merged = 0;
+        c.stats.merge_rounds = 0;
+        return;
+    }
+    // frames
+    const Frame fr{c.frame_G, (float)c.frame_G};
+    c.lf_anchor.reserve(nl + 1);
+    c.lf_box32.reserve(nl + 1);
+    c.lf_rn.reserve(nl + 1);
+    c.e_live.reserve(nl + 1);
+    c.e_cand.reserve((size_t)nl * CAND_CAP + 1);
+    c.e_ncand.reserve(nl + 1);
+    c.e_dirty.reserve(nl + 1);
+    c.e_lchanged.reserve(nl + 1);
+    k_anchor<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.lf_geom.p, fr.G, c.lf_anchor.p);
+    VV_LAUNCH_CHECK();
+    c.e_rec0.reserve(n); c.e_recO.reserve(n);
+    c.e_x0.reserve(n); c.e_y0.reserve(n); c.e_g0.reserve(n); c.e_zb.reserve(n); c.e_zb_prev.reserve(n);
+    for (int k = 0; k < 2; k++) {
+        c.e_partner[k].reserve(n); c.e_ox[k].reserve(n); c.e_oy[k].reserve(n); c.e_og[k].reserve(n);
+        c.e_oie[k].reserve(n);
+    }
+    c.e_changed.reserve(4);
+    k_rec0<<<grid_for(n, EB), EB, 0, s>>>(n, c.leaf_of.p, c.lf_anchor.p, fr.G, c.x.p, c.y.p, c.g.p, c.e_rec0.p,
+                                          c.e_x0.p, c.e_y0.p, c.e_g0.p, c.e_partner[0].p, c.e_zb.p, c.e_zb_prev.p);
+    VV_LAUNCH_CHECK();
+    // round-0 guess: nobody merges; outcomes equal to the input state
+    VV_CUDA(cudaMemcpyAsync(c.e_ox[0].p, c.x.p, n * 8, cudaMemcpyDeviceToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(c.e_oy[0].p, c.y.p, n * 8, cudaMemcpyDeviceToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(c.e_og[0].p, c.g.p, n * 8, cudaMemcpyDeviceToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(c.e_oie[0].p, c.ie.p, n * 8, cudaMemcpyDeviceToDevice, s));
+    int cur = 0;
+    int64_t rounds = 0;
+    const int64_t max_rounds = 4096;
+    for (;;) {
+        rounds++;
+        // boxes and candidate leaves from the current guesses
+        k_eps_box<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.lf_vf.p, c.lf_vl.p, c.e_rec0.p, c.e_recO.p,
+                                                  c.e_partner[cur].p, c.e_zb.p, c.lf_box32.p, c.e_live.p);
+        VV_LAUNCH_CHECK();
+        k_eps_cand<<<grid_for(nl, EB / 32), EB, 0, s>>>(nl, c.near_off.p, c.near_run.p, c.lf_anchor.p,
+                                                       c.lf_box32.p, c.e_live.p, fr.Gf, c.e_cand.p, c.e_ncand.p,
+                                                       c.lf_rn.p, c.e_lchanged.p, c.e_dirty.p, rounds == 1);
+        VV_LAUNCH_CHECK();
+        VV_CUDA(cudaMemsetAsync(c.e_changed.p, 0, 4, s));
+        EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.near_off.p, c.near_run.p,
+                  c.e_cand.p, c.e_ncand.p, c.e_rec0.p, c.e_recO.p, c.e_x0.p, c.e_y0.p, c.e_g0.p,
+                  c.e_partner[cur].p, c.e_zb.p, c.e_ox[cur].p, c.e_oy[cur].p, c.e_og[cur].p, fr.G, fr.Gf};
+        const int nx = cur ^ 1;
+        k_eps_round<<<grid_for(n, EB), EB, 0, s>>>(n, v, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_dirty.p,
+                                                   c.e_oie[cur].p, c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p,
+                                                   c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p);
+        VV_LAUNCH_CHECK();
+        // new absorber table and merged records; leaves whose members changed
+        k_zb_reset<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_zb.p, c.e_zb_prev.p, c.e_zb.p);
+        VV_LAUNCH_CHECK();
+        k_zb_scatter<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_partner[nx].p, c.leaf_of.p, c.lf_anchor.p, fr.G,
+                                                    c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_zb.p,
+                                                    c.e_recO.p);
+        VV_LAUNCH_CHECK();
+        VV_CUDA(cudaMemsetAsync(c.e_lchanged.p, 0, (nl + 1) * 4, s));
+        k_leaf_changed<<<grid_for(n, EB), EB, 0, s>>>(n, c.leaf_of.p, c.e_partner[cur].p, c.e_partner[nx].p,
+                                                      c.e_ox[cur].p, c.e_ox[nx].p, c.e_oy[cur].p, c.e_oy[nx].p,
+                                                      c.e_og[cur].p, c.e_og[nx].p, c.e_zb_prev.p, c.e_zb.p,
+                                                      c.e_lchanged.p);
+        VV_LAUNCH_CHECK();
+        cur = nx;
+        int32_t changed = read_i32(c, c.e_changed.p);
+        if (!changed) break;
+        if (rounds >= max_rounds) throw ApiError{VVGPU_ERR_TIMEOUT, "epsilon/merge rounds did not converge"};
+    }
+    VV_CUDA(cudaMemsetAsync(c.counters.p, 0, 8, s));
+    k_eps_final<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_partner[cur].p, c.e_zb.p, c.e_ox[cur].p, c.e_oy[cur].p,
+                                               c.e_og[cur].p, c.e_oie[cur].p, c.x.p, c.y.p, c.g.p, c.ie.p,
+                                               c.counters.p);
+    VV_LAUNCH_CHECK();
+    unsigned long long mcount = 0;
+    VV_CUDA(cudaMemcpyAsync(&mcount, c.counters.p, 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    if (merged) *merged = (int64_t)mcount;
+    c.stats.merged = (int64_t)mcount;
+    c.stats.merge_rounds = rounds;
+}
+
+}  // namespace vvgpu

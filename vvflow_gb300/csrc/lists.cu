@@ -1,0 +1,323 @@
+// Near/far classification per leaf (snode::FindNearNodes, libvvhd/src/TSortedTree.cpp:199-217)
+// fused with the far-field expansion of the convective velocity
+// (MConvectiveFast::process_all_lists, libvvhd/src/MConvectiveFast.cpp:48-69).
+//
+// A leaf's depth-first walk decides "far" when |dc|^2 > farCriteria (h+w+h'+w')^2.  The
+// test runs in FP32 on anchor-relative node centres (frame.cuh); only when the two sides are
+// within a relative 2^-16 of each other is it repeated in FP64 with the reference's
+// operation order, so every decision equals the reference's.
+//
+// Near leaves come out in depth-first order (increasing leaf index) and are stored as runs
+// of consecutive leaves, i.e. contiguous vortex ranges.  Far nodes are not stored: the walk
+// folds each far node's two monopoles straight into the leaf's expansion coefficients
+// T1..T4 (the reference computes the same coefficients from the same centroids, which are
+// fixed when the tree is built).  Far lists are kept only for leaves that hold a segment
+// centre (the SLAE right-hand side reads them), and an exact walk rebuilds full lists on
+// request for inspection.
+#include <cfloat>
+
+#include "frame.cuh"
+#include "vvgpu_internal.cuh"
+
+namespace vvgpu {
+
+namespace {
+
+constexpr int LB = 128;
+
+struct ListView {
+    const double4* geom;     // exact node geometry
+    const int32_t* ch1;
+    const int32_t* dfs;
+    const float4* nf_geo;    // x, y (anchor frame), h + w, 0
+    const int2* nf_k;        // node anchors
+    const float4* nf_cm;     // CMp x, y, CMm x, y (anchor frame)
+    const float2* nf_g;      // CMp g, CMm g
+    const double* cm;        // exact centroids (6 per node)
+    double fc;
+    float fcf;
+    float Gf;
+};
+
+// Exact FP64 far test with the reference's operation order.
+__device__ __forceinline__ bool far_exact(const double4& tg, const double4& me, double fc) {
+    double dx = dsub(tg.x, me.x), dy = dsub(tg.y, me.y);
+    double hp = dadd(dadd(dadd(tg.z, tg.w), me.z), me.w);
+    return dabs2(dx, dy) > dmul(dmul(fc, hp), hp);
+}
+
+// FP32 filter, FP64 on the boundary.
+__device__ __forceinline__ bool far_test(const ListView& v, int32_t t, int32_t meN, float4 mg, int2 mk) {
+    float4 tg = v.nf_geo[t];
+    int2 tk = v.nf_k[t];
+    float dx = (float)(tk.x - mk.x) * v.Gf + (tg.x - mg.x);
+    float dy = (float)(tk.y - mk.y) * v.Gf + (tg.y - mg.y);
+    float lhs = dx * dx + dy * dy;
+    float hp = tg.z + mg.z;
+    float rhs = v.fcf * hp * hp;
+    if (isfinite(lhs) && isfinite(rhs)) {
+        const float m = 1.52587890625e-05f;  // 2^-16
+        if (lhs > rhs * (1.f + m) + 1e-37f) return true;
+        if (lhs < rhs * (1.f - m) - 1e-37f) return false;
+    }
+    return far_exact(v.geom[t], v.geom[meN], v.fc);
+}
+
+__global__ void k_node_frames(int64_t nn, const double4* __restrict__ geom, const double* __restrict__ cm, double G,
+                              float4* nf_geo, int2* nf_k, float4* nf_cm, float2* nf_g) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nn) return;
+    double4 gm = geom[k];
+    double cx = isfinite(gm.x) ? gm.x : 0., cy = isfinite(gm.y) ? gm.y : 0.;
+    int2 a = anchor_of(cx, cy, G);
+    double ax = (double)a.x * G, ay = (double)a.y * G;
+    nf_geo[k] = make_float4((float)(gm.x - ax), (float)(gm.y - ay), (float)(gm.z + gm.w), 0.f);
+    nf_k[k] = a;
+    const double* c = cm + 6 * k;
+    nf_cm[k] = make_float4((float)(c[0] - ax), (float)(c[1] - ay), (float)(c[3] - ax), (float)(c[4] - ay));
+    nf_g[k] = make_float2((float)c[2], (float)c[5]);
+}
+
+// Marks the leaves that hold a segment centre (stree::findNode, TSortedTree.cpp:284-303).
+__global__ void k_flag_seg_leaves(int64_t m, const double* __restrict__ rx, const double* __restrict__ ry,
+                                  const double4* __restrict__ geom, const int32_t* __restrict__ ch1,
+                                  const int32_t* __restrict__ dfs, int32_t* flag) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    double px = rx[s], py = ry[s];
+    int32_t k = 0;
+    for (int it = 0; it <= MAX_DEPTH && ch1[k] >= 0; it++) {
+        double4 gm = geom[k];
+        if (gm.z < gm.w) k = (px < gm.x) ? ch1[k] : ch1[k] + 1;
+        else k = (py < gm.y) ? ch1[k] : ch1[k] + 1;
+    }
+    flag[dfs[k]] = 1;
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
+    float s = hi + v;
+    float bp = s - hi;
+    lo += (hi - (s - bp)) + (v - bp);
+    hi = s;
+}
+
+// PASS 0: count near runs (+ far nodes of flagged leaves).
+// PASS 1: write near runs, far nodes of flagged leaves and the expansion coefficients.
+template <int PASS, bool FP32>
+__global__ void __launch_bounds__(LB) k_walk(int64_t nl, ListView v, const int32_t* __restrict__ leaf_node,
+                                             const int32_t* __restrict__ flag, int32_t* near_cnt,
+                                             int32_t* far_cnt, const int32_t* __restrict__ near_off,
+                                             const int32_t* __restrict__ far_off, int2* near_run,
+                                             int32_t* far_node, double4* taylor, int64_t nodes_bound,
+                                             int32_t* err, unsigned long long* far_total) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    const int32_t meN = leaf_node[L];
+    const float4 mg = v.nf_geo[meN];
+    const int2 mk = v.nf_k[meN];
+    const double4 me = v.geom[meN];
+    const bool keep_far = flag[L] != 0;
+    int32_t stack[MAX_DEPTH + 2];
+    int sp = 0;
+    stack[sp++] = 0;
+    int32_t nr = 0, nf = 0, last = -2, rfirst = -1, nfar_all = 0;
+    const int32_t nbase = PASS ? near_off[L] : 0, fbase = PASS ? far_off[L] : 0;
+    double d1 = 0, d2 = 0, d3 = 0, d4 = 0;             // FP64 path
+    float h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0, h4 = 0, l4 = 0;  // FP32 path
+    int64_t guard = 0;
+    while (sp) {
+        if (++guard > nodes_bound) { atomicExch(err, 2); break; }
+        const int32_t t = stack[--sp];
+        if (far_test(v, t, meN, mg, mk)) {
+            nfar_all++;
+            if (keep_far) {
+                if (PASS) far_node[fbase + nf] = t;
+                nf++;
+            }
+            if (PASS) {
+                if (FP32) {
+                    const int2 tk = v.nf_k[t];
+                    const float sx = (float)(mk.x - tk.x) * v.Gf, sy = (float)(mk.y - tk.y) * v.Gf;
+                    const float4 c4 = v.nf_cm[t];
+                    const float2 gg = v.nf_g[t];
+                    float dpx = sx + (mg.x - c4.x), dpy = sy + (mg.y - c4.y);
+                    float dmx = sx + (mg.x - c4.z), dmy = sy + (mg.y - c4.w);
+                    float ap = dpx * dpx + dpy * dpy, am = dmx * dmx + dmy * dmy;
+                    float ip = rcp_approx(ap), im = rcp_approx(am);
+                    float fp1 = gg.x * ip, fm1 = gg.y * im;
+                    float fp2 = fp1 * ip, fm2 = fm1 * im;
+                    two_sum_acc(h1, l1, -(fp1 * dpy + fm1 * dmy));
+                    two_sum_acc(h2, l2, fp1 * dpx + fm1 * dmx);
+                    two_sum_acc(h3, l3, fp2 * dpy * dpx + fm2 * dmy * dmx);
+                    two_sum_acc(h4, l4, fp2 * (dpy * dpy - dpx * dpx) + fm2 * (dmy * dmy - dmx * dmx));
+                } else {
+                    const double* c = v.cm + 6 * (size_t)t;
+                    double dpx = me.x - c[0], dpy = me.y - c[1], dmx = me.x - c[3], dmy = me.y - c[4];
+                    double ap = dpx * dpx + dpy * dpy, am = dmx * dmx + dmy * dmy;
+                    double fp1 = c[2] / ap, fm1 = c[5] / am;
+                    double fp2 = c[2] / (ap * ap), fm2 = c[5] / (am * am);
+                    d1 -= (fp1 * dpy + fm1 * dmy);
+                    d2 += (fp1 * dpx + fm1 * dmx);
+                    d3 += (fp2 * dpy * dpx + fm2 * dmy * dmx);
+                    d4 += (fp2 * (dpy * dpy - dpx * dpx) + fm2 * (dmy * dmy - dmx * dmx));
+                }
+            }
+            continue;
+        }
+        const int32_t c1 = v.ch1[t];
+        if (c1 >= 0) {
+            if (sp + 2 > MAX_DEPTH + 2) { atomicExch(err, 2); break; }
+            stack[sp++] = c1 + 1;
+            stack[sp++] = c1;
+            continue;
+        }
+        const int32_t q = v.dfs[t];
+        if (q == last + 1) {
+            last = q;
+        } else {
+            if (PASS && rfirst >= 0) near_run[nbase + nr - 1] = make_int2(rfirst, last + 1);
+            rfirst = q;
+            last = q;
+            nr++;
+        }
+    }
+    if (PASS) {
+        if (rfirst >= 0) near_run[nbase + nr - 1] = make_int2(rfirst, last + 1);
+        if (FP32) {
+            d1 = (double)h1 + (double)l1; d2 = (double)h2 + (double)l2;
+            d3 = (double)h3 + (double)l3; d4 = (double)h4 + (double)l4;
+        }
+        taylor[L] = make_double4(d1 * C_1_2PI, d2 * C_1_2PI, d3 * C_1_PI, d4 * C_1_2PI);
+        atomicAdd(far_total, (unsigned long long)nfar_all);
+    } else {
+        near_cnt[L] = nr;
+        far_cnt[L] = nf;
+    }
+}
+
+// Exact walk writing every leaf's far list (inspection only).
+template <bool FILL>
+__global__ void k_walk_exact(int64_t nl, const int32_t* __restrict__ leaf_node, const double4* __restrict__ geom,
+                             const int32_t* __restrict__ ch1, double fc, int32_t* far_cnt,
+                             const int32_t* __restrict__ far_off, int32_t* far_node, int64_t nodes_bound,
+                             int32_t* err) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    const double4 me = geom[leaf_node[L]];
+    int32_t stack[MAX_DEPTH + 2];
+    int sp = 0;
+    stack[sp++] = 0;
+    int32_t nf = 0;
+    const int32_t fbase = FILL ? far_off[L] : 0;
+    int64_t guard = 0;
+    while (sp) {
+        if (++guard > nodes_bound) { atomicExch(err, 2); break; }
+        const int32_t t = stack[--sp];
+        if (far_exact(geom[t], me, fc)) {
+            if (FILL) far_node[fbase + nf] = t;
+            nf++;
+            continue;
+        }
+        const int32_t c1 = ch1[t];
+        if (c1 >= 0) {
+            if (sp + 2 > MAX_DEPTH + 2) { atomicExch(err, 2); break; }
+            stack[sp++] = c1 + 1;
+            stack[sp++] = c1;
+        }
+    }
+    if (!FILL) far_cnt[L] = nf;
+}
+
+}  // namespace
+
+void tree_lists(Ctx& c) {
+    cudaStream_t s = c.st();
+    const int64_t nl = c.nleaves, nn = c.nnodes;
+    int32_t* err = (int32_t*)c.counters.p + 1;
+    VV_CUDA(cudaMemsetAsync(err, 0, 4, s));
+    // frames of every node
+    double4 root;
+    VV_CUDA(cudaMemcpyAsync(&root, c.nd_geom.p, sizeof root, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    Frame fr = make_frame(std::fmax(std::fabs(root.x), std::fabs(root.y)) + std::fmax(root.z, root.w));
+    c.frame_G = fr.G;
+    c.nf_geo.reserve(nn); c.nf_k.reserve(nn); c.nf_cm.reserve(nn); c.nf_g.reserve(nn);
+    k_node_frames<<<grid_for(nn, 256), 256, 0, s>>>(nn, c.nd_geom.p, c.nd_cm.p, fr.G, c.nf_geo.p, c.nf_k.p,
+                                                    c.nf_cm.p, c.nf_g.p);
+    VV_LAUNCH_CHECK();
+    c.lf_flag.reserve(nl + 1);
+    VV_CUDA(cudaMemsetAsync(c.lf_flag.p, 0, (nl + 1) * 4, s));
+    if (c.m > 0) {
+        k_flag_seg_leaves<<<grid_for(c.m, 256), 256, 0, s>>>(c.m, c.s_rx.p, c.s_ry.p, c.nd_geom.p, c.nd_ch1.p,
+                                                             c.nd_dfs.p, c.lf_flag.p);
+        VV_LAUNCH_CHECK();
+    }
+    ListView v{c.nd_geom.p, c.nd_ch1.p, c.nd_dfs.p, c.nf_geo.p, c.nf_k.p, c.nf_cm.p, c.nf_g.p, c.nd_cm.p,
+               c.far_criteria, (float)c.far_criteria, (float)fr.G};
+    c.near_cnt.reserve(nl + 1); c.far_cnt.reserve(nl + 1);
+    c.near_off.reserve(nl + 2); c.far_off.reserve(nl + 2);
+    c.lf_taylor.reserve(nl + 1);
+    const bool fp32 = c.precision == VVGPU_FP32;
+    if (fp32) k_walk<0, true><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, c.near_cnt.p,
+                                                              c.far_cnt.p, nullptr, nullptr, nullptr, nullptr,
+                                                              nullptr, nn, err, nullptr);
+    else k_walk<0, false><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, c.near_cnt.p,
+                                                           c.far_cnt.p, nullptr, nullptr, nullptr, nullptr,
+                                                           nullptr, nn, err, nullptr);
+    VV_LAUNCH_CHECK();
+    exclusive_scan(c, c.near_cnt.p, c.near_off.p, nl);
+    exclusive_scan(c, c.far_cnt.p, c.far_off.p, nl);
+    if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
+    c.n_near_runs = read_i32(c, c.near_off.p + nl);
+    c.n_far = read_i32(c, c.far_off.p + nl);
+    c.near_run.reserve(c.n_near_runs + 1);
+    c.far_node.reserve(c.n_far + 1);
+    unsigned long long* far_total = c.counters.p + 10;
+    VV_CUDA(cudaMemsetAsync(far_total, 0, 8, s));
+    if (fp32) k_walk<1, true><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, nullptr, nullptr,
+                                                              c.near_off.p, c.far_off.p, c.near_run.p,
+                                                              c.far_node.p, c.lf_taylor.p, nn, err, far_total);
+    else k_walk<1, false><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, nullptr, nullptr,
+                                                           c.near_off.p, c.far_off.p, c.near_run.p, c.far_node.p,
+                                                           c.lf_taylor.p, nn, err, far_total);
+    VV_LAUNCH_CHECK();
+    c.stats.near_runs = c.n_near_runs;
+    c.taylor_precision = c.precision;
+    unsigned long long ft = 0;
+    VV_CUDA(cudaMemcpyAsync(&ft, far_total, 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    c.stats.far_pairs = 2 * (int64_t)ft;  // two monopoles per far node
+}
+
+void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t>& far_node) {
+    cudaStream_t s = c.st();
+    const int64_t nl = c.nleaves, nn = c.nnodes;
+    int32_t* err = (int32_t*)c.counters.p + 1;
+    VV_CUDA(cudaMemsetAsync(err, 0, 4, s));
+    DArr<int32_t> cnt, off, fnode;
+    cnt.reserve(nl + 1);
+    off.reserve(nl + 2);
+    k_walk_exact<false><<<grid_for(nl, LB), LB, 0, s>>>(nl, c.leaf_node.p, c.nd_geom.p, c.nd_ch1.p, c.far_criteria,
+                                                        cnt.p, nullptr, nullptr, nn, err);
+    VV_LAUNCH_CHECK();
+    exclusive_scan(c, cnt.p, off.p, nl);
+    int32_t tot = read_i32(c, off.p + nl);
+    fnode.reserve(tot + 1);
+    k_walk_exact<true><<<grid_for(nl, LB), LB, 0, s>>>(nl, c.leaf_node.p, c.nd_geom.p, c.nd_ch1.p, c.far_criteria,
+                                                       nullptr, off.p, fnode.p, nn, err);
+    VV_LAUNCH_CHECK();
+    far_off.resize(nl + 1);
+    far_node.resize(tot);
+    VV_CUDA(cudaMemcpyAsync(far_off.data(), off.p, (nl + 1) * 4, cudaMemcpyDeviceToHost, s));
+    if (tot) VV_CUDA(cudaMemcpyAsync(far_node.data(), fnode.p, (size_t)tot * 4, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
+}
+
+}  // namespace vvgpu

@@ -1,0 +1,595 @@
+// Body SLAE of libvvhd (MConvectiveFast::calc_circulation / fill_matrix,
+// libvvhd/src/MConvectiveFast.cpp:235-273, 882-1017) for rigid bodies.
+//
+// Rows and columns follow the reference's equation numbering and solution-pointer map
+// (MConvectiveFast.cpp:250-267, 896-975): per body [segments..., speed_slae x,y,o,
+// force_hydro x,y,o, force_holder x,y,o].
+//   * slip rows (fillSlipEquationForSegment, :459-482): one thread block per row; the
+//     M cells are 2 pi Xi_gamma (:286-310) of every segment's corner, the right-hand side
+//     is the free stream, sinks and NodeInfluence (:398-418) through the tree.
+//   * special rows (InfSteady / Steady / Zero, :484-522) and the nine body rows (Speed,
+//     Hydro, Newton, :533-862): one thread each.
+// Solve: the inverse is computed on the GPU by in-place Gauss-Jordan elimination with
+// partial pivoting and cached while the matrix bytes are unchanged (the reference caches
+// its LAPACK inverse by a hash of the matrix, TMatrix.cpp:225-259).  FP64 mode inverts in
+// FP64; FP32 mode inverts in FP32.  Either way x = inv b is refined with FP64 residuals
+// r = b - A x until |r| / |b| < 1e-13 (at most 12 sweeps).
+#include <cfloat>
+
+#include "vvgpu_internal.cuh"
+
+namespace vvgpu {
+
+namespace {
+
+struct SegDev {
+    const double* cx; const double* cy; const double* rx; const double* ry; const double* dlx; const double* dly;
+};
+
+__device__ __forceinline__ double xi_g_near(double px, double py, double pcx, double pcy, double dlx, double dly,
+                                            double rd) {
+    return ((pcx - px) * dlx + (pcy - py) * dly) / (rd * rd);
+}
+__device__ __forceinline__ double xi_g_dist(double px, double py, double p1x, double p1y, double p2x, double p2y) {
+    double a = (px - p2x) * (px - p2x) + (py - p2y) * (py - p2y);
+    double b = (px - p1x) * (px - p1x) + (py - p1y) * (py - p1y);
+    return 0.5 * log(a / b);
+}
+// _2PI_Xi_g (MConvectiveFast.cpp:286-310)
+__device__ double xi_g(const SegDev& S, double px, double py, int32_t s, double rd) {
+    double cx = S.cx[s], cy = S.cy[s], dlx = S.dlx[s], dly = S.dly[s];
+    double rd_sqr = rd * rd;
+    double dr1 = (px - cx) * (px - cx) + (py - cy) * (py - cy);
+    double ex = (px - cx) - dlx, ey = (py - cy) - dly;
+    double dr2 = ex * ex + ey * ey;
+    if (dr1 >= rd_sqr && dr2 >= rd_sqr) return 0.5 * log(dr2 / dr1);
+    double rx = S.rx[s], ry = S.ry[s];
+    if (dr1 <= rd_sqr && dr2 <= rd_sqr) return xi_g_near(px, py, rx, ry, dlx, dly, rd);
+    double a0 = dlx * dlx + dly * dly;
+    double b0 = (px - rx) * dlx + (py - ry) * dly;
+    double d = sqrt(b0 * b0 - a0 * (((px - rx) * (px - rx) + (py - ry) * (py - ry)) - rd * rd));
+    double k = (b0 + d) / a0;
+    if ((k <= -0.5) || (k >= 0.5)) k = (b0 - d) / a0;
+    double p3x = rx + dlx * k, p3y = ry + dly * k;
+    if (dr1 < rd_sqr)
+        return xi_g_near(px, py, (p3x + cx) * 0.5, (p3y + cy) * 0.5, p3x - cx, p3y - cy, rd) +
+               xi_g_dist(px, py, p3x, p3y, cx + dlx, cy + dly);
+    return xi_g_dist(px, py, cx, cy, p3x, p3y) +
+           xi_g_near(px, py, ((cx + dlx) + p3x) * 0.5, ((cy + dly) + p3y) * 0.5, (cx + dlx) - p3x,
+                     (cy + dly) - p3y, rd);
+}
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < nw; w++) t += sh[w];
+    __syncthreads();
+    return t;  // valid in thread 0
+}
+
+struct RowInfo {
+    int32_t seg;     // global segment index of the row (slip rows)
+    int32_t body;
+};
+
+struct FillArgs {
+    int64_t n;       // system size
+    double* A; double* B;
+    SegDev S;
+    const int32_t* slip_rows; int64_t nslip;  // row index of each slip row
+    const int32_t* row_seg; const int32_t* row_body;
+    const int32_t* col_seg0; const int32_t* body_first; const int32_t* body_count; int nbodies;
+    // tree
+    const double4* geom; const int32_t* ch1; const int32_t* dfs;
+    const int32_t* lvf; const int32_t* lvl; const int32_t* near_off; const int2* near_run;
+    const int32_t* far_off; const int32_t* far_node; const double* cm;
+    const double* x; const double* y; const double* g; const double* ie;
+    int64_t ns; const double* kx; const double* ky; const double* kg; double sink_e2;
+    double inf_vx, inf_vy;
+    bool rhs_only;
+};
+
+// One block per slip row: RHS through the tree, then (unless rhs_only) the M + 3 nb cells.
+__global__ void k_slip_rows(FillArgs a) {
+    __shared__ double sh[32];
+    const int64_t ri = blockIdx.x;
+    if (ri >= a.nslip) return;
+    const int32_t row = a.slip_rows[ri];
+    const int32_t s = a.row_seg[row];
+    const int32_t bi = a.row_body[row];
+    const double srx = a.S.rx[s], sry = a.S.ry[s], dlx = a.S.dlx[s], dly = a.S.dly[s];
+    // findNode(seg.r)
+    int32_t k = 0;
+    for (int it = 0; it <= MAX_DEPTH && a.ch1[k] >= 0; it++) {
+        double4 gm = a.geom[k];
+        if (gm.z < gm.w) k = (srx < gm.x) ? a.ch1[k] : a.ch1[k] + 1;
+        else k = (sry < gm.y) ? a.ch1[k] : a.ch1[k] + 1;
+    }
+    const int32_t L = a.dfs[k];
+    double part = 0;
+    for (int32_t r = a.near_off[L]; r < a.near_off[L + 1]; r++) {
+        int2 run = a.near_run[r];
+        for (int32_t j = a.lvf[run.x] + threadIdx.x; j < a.lvl[run.y - 1]; j += blockDim.x) {
+            double gj = a.g[j];
+            if (gj == 0.) continue;
+            part += xi_g(a.S, a.x[j], a.y[j], s, 1. / a.ie[j]) * gj;
+        }
+    }
+    const double c1x = a.S.cx[s], c1y = a.S.cy[s], c2x = c1x + dlx, c2y = c1y + dly;
+    for (int32_t t = a.far_off[L] + threadIdx.x; t < a.far_off[L + 1]; t += blockDim.x) {
+        const double* c = a.cm + 6 * (size_t)a.far_node[t];
+        part += xi_g_dist(c[0], c[1], c1x, c1y, c2x, c2y) * c[2];
+        part += xi_g_dist(c[3], c[4], c1x, c1y, c2x, c2y) * c[5];
+    }
+    double node_inf = block_sum(part, sh);
+    if (threadIdx.x == 0) {
+        double rhs = (-a.inf_vy) * dlx + a.inf_vx * dly;
+        double kxs = 0, kys = 0;
+        for (int64_t q = 0; q < a.ns; q++) {
+            double dx = srx - a.kx[q], dy = sry - a.ky[q];
+            double f = a.kg[q] / (dx * dx + dy * dy + a.sink_e2 * fabs(a.kg[q]));
+            kxs += dx * f; kys += dy * f;
+        }
+        kxs *= C_1_2PI; kys *= C_1_2PI;
+        rhs += (-kys) * dlx + kxs * dly;
+        rhs -= node_inf * C_1_2PI;
+        a.B[row] = rhs;
+    }
+    if (a.rhs_only) return;
+    double* Arow = a.A + (size_t)row * a.n;
+    for (int bj = 0; bj < a.nbodies; bj++) {
+        const int32_t f = a.body_first[bj], cnt = a.body_count[bj], c0 = a.col_seg0[bj];
+        for (int32_t q = threadIdx.x; q < cnt; q += blockDim.x) {
+            int32_t sj = f + q;
+            double rd = sqrt(a.S.dlx[sj] * a.S.dlx[sj] + a.S.dly[sj] * a.S.dly[sj]) * 0.25;
+            Arow[c0 + q] = xi_g(a.S, a.S.cx[sj], a.S.cy[sj], s, rd) * C_1_2PI;
+        }
+        if (threadIdx.x == 0) {
+            double a1 = (bi == bj) ? C_2PI * dly : 0;
+            double a2 = (bi == bj) ? -C_2PI * dlx : 0;
+            Arow[c0 + cnt + 0] = a1 * C_1_2PI;
+            Arow[c0 + cnt + 1] = a2 * C_1_2PI;
+            Arow[c0 + cnt + 2] = 0.;
+        }
+    }
+}
+
+struct BodyDev {
+    double area, cofx, cofy, axx, axy, moi, dens;
+    double pvx, pvy, pvo, fpx, fpy, fpo, fdx, fdy, fdo, gdead;
+    double spx, spy, spo;
+    int32_t special, kutta;
+};
+
+// Special and body rows; one thread per body (cheap scalar work).
+__global__ void k_body_rows(int64_t n, double* A, double* B, const BodyDev* bd, int nb,
+                            const int32_t* col_seg0, const int32_t* body_count, const double* cy_,
+                            const double* cx_, const int32_t* body_first, double dt, double gsum, double inf_g,
+                            double gx, double gy, bool rhs_only) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const double _1_dt = 1 / dt, _1_2dt = 0.5 / dt;
+    int once = 0;
+    for (int bi = 0; bi < nb; bi++) {
+        const BodyDev& b = bd[bi];
+        const int32_t c0 = col_seg0[bi], cnt = body_count[bi], f = body_first[bi];
+        // special segment row
+        {
+            int32_t eq = c0 + b.special;
+            double* Ar = A + (size_t)eq * n;
+            if (b.kutta) {
+                B[eq] = 0;
+                if (!rhs_only) Ar[c0 + b.special] = 1;
+            } else if (!once++) {
+                B[eq] = -gsum - inf_g;
+                if (!rhs_only)
+                    for (int bj = 0; bj < nb; bj++) {
+                        for (int32_t q = 0; q < body_count[bj]; q++) Ar[col_seg0[bj] + q] = 1;
+                        Ar[col_seg0[bj] + body_count[bj] + 2] = 2 * bd[bj].area;
+                    }
+            } else {
+                B[eq] = b.gdead + 2 * b.area * b.pvo;
+                if (!rhs_only) {
+                    for (int32_t q = 0; q < cnt; q++) Ar[c0 + q] = 1;
+                    Ar[c0 + cnt + 2] = 2 * b.area;
+                }
+            }
+        }
+        const int32_t e0 = c0 + cnt;
+        auto cell = [&](int32_t eq, int q, double v) { if (!rhs_only) A[(size_t)eq * n + e0 + q] = v; };
+        B[e0 + 0] = b.spx; cell(e0 + 0, 0, 1);
+        B[e0 + 1] = b.spy; cell(e0 + 1, 1, 1);
+        B[e0 + 2] = b.spo; cell(e0 + 2, 2, 1);
+        const double area = b.area, rcx = b.cofx - b.axx, rcy = b.cofy - b.axy, moi = b.moi, dens = b.dens;
+        // Hydro X/Y/O (:533-623)
+        {
+            int32_t eq = e0 + 3;
+            double ty = b.cofy * 2 + rcy;
+            B[eq] = area * _1_dt * b.pvx + area * _1_dt * (-ty) * b.pvo + (b.pvo * b.pvo) * area * rcx - b.fpx +
+                    b.fdx * _1_dt;
+            if (!rhs_only) for (int32_t q = 0; q < cnt; q++) A[(size_t)eq * n + c0 + q] = _1_dt * (-cy_[f + q]);
+            cell(eq, 0, area * _1_dt); cell(eq, 1, 0); cell(eq, 2, area * _1_dt * (-2 * b.cofy - rcy)); cell(eq, 3, -1);
+        }
+        {
+            int32_t eq = e0 + 4;
+            double tx = b.cofx * 2 + rcx;
+            B[eq] = area * _1_dt * b.pvy + area * _1_dt * tx * b.pvo + (b.pvo * b.pvo) * area * rcy - b.fpy +
+                    b.fdy * _1_dt;
+            if (!rhs_only) for (int32_t q = 0; q < cnt; q++) A[(size_t)eq * n + c0 + q] = _1_dt * (cx_[f + q]);
+            cell(eq, 0, 0); cell(eq, 1, area * _1_dt); cell(eq, 2, area * _1_dt * (2 * b.cofx + rcx)); cell(eq, 4, -1);
+        }
+        {
+            int32_t eq = e0 + 5;
+            double c = area * _1_dt;
+            double lx = (-rcy) * c, ly = rcx * c;
+            B[eq] = (lx * b.pvx + ly * b.pvy) + 2 * moi * _1_dt * b.pvo - b.fpo + b.fdo * _1_2dt;
+            if (!rhs_only)
+                for (int32_t q = 0; q < cnt; q++) {
+                    double dx = cx_[f + q] - b.axx, dy = cy_[f + q] - b.axy;
+                    A[(size_t)eq * n + c0 + q] = _1_2dt * (dx * dx + dy * dy);
+                }
+            cell(eq, 0, area * _1_dt * (-rcy)); cell(eq, 1, area * _1_dt * rcx); cell(eq, 2, 2 * moi * _1_dt);
+            cell(eq, 5, -1);
+        }
+        // Newton X/Y/O (:634-739)
+        {
+            int32_t eq = e0 + 6;
+            B[eq] = -area * _1_dt * dens * b.pvx + area * _1_dt * dens * rcy * b.pvo -
+                    area * dens * rcx * (b.pvo * b.pvo) - (dens - 1.0) * gx * area;
+            cell(eq, 0, -area * _1_dt * dens); cell(eq, 1, 0); cell(eq, 2, area * _1_dt * dens * rcy);
+            cell(eq, 3, 1); cell(eq, 6, -1);
+        }
+        {
+            int32_t eq = e0 + 7;
+            B[eq] = -area * _1_dt * dens * b.pvy - area * _1_dt * dens * rcx * b.pvo -
+                    area * dens * rcy * (b.pvo * b.pvo) - (dens - 1.0) * gy * area;
+            cell(eq, 0, 0); cell(eq, 1, -area * _1_dt * dens); cell(eq, 2, -area * _1_dt * dens * rcx);
+            cell(eq, 4, 1); cell(eq, 7, -1);
+        }
+        {
+            int32_t eq = e0 + 8;
+            double rlx = -rcy, rly = rcx;
+            B[eq] = -area * _1_dt * dens * (rlx * b.pvx + rly * b.pvy) - moi * _1_dt * dens * b.pvo -
+                    (dens - 1.0) * (rlx * gx + rly * gy) * area;
+            cell(eq, 0, +area * _1_dt * dens * rcy); cell(eq, 1, -area * _1_dt * dens * rcx);
+            cell(eq, 2, -moi * _1_dt * dens); cell(eq, 5, 1); cell(eq, 8, -1);
+        }
+    }
+}
+
+// ---- Gauss-Jordan inversion in place (row pivoting; columns unscrambled at the end) ----
+
+template <class T>
+__global__ void k_gj_pivot(int64_t n, int64_t k, T* M, int32_t* perm, T* col, int32_t* singular) {
+    __shared__ double bv[1024];
+    __shared__ int32_t bi[1024];
+    double best = -1;
+    int32_t arg = -1;
+    for (int64_t i = k + threadIdx.x; i < n; i += blockDim.x) {
+        double v = fabs((double)M[i * n + k]);
+        if (v > best) { best = v; arg = (int32_t)i; }
+    }
+    bv[threadIdx.x] = best;
+    bi[threadIdx.x] = arg;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            double v2 = bv[threadIdx.x + o];
+            int32_t i2 = bi[threadIdx.x + o];
+            if (v2 > bv[threadIdx.x] || (v2 == bv[threadIdx.x] && i2 >= 0 && i2 < bi[threadIdx.x])) {
+                bv[threadIdx.x] = v2;
+                bi[threadIdx.x] = i2;
+            }
+        }
+        __syncthreads();
+    }
+    const int32_t p = bi[0];
+    if (bv[0] <= 0 || p < 0) {
+        if (threadIdx.x == 0) { *singular = 1; perm[k] = (int32_t)k; }
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) col[i] = 0;
+        return;
+    }
+    if (threadIdx.x == 0) perm[k] = p;
+    if (p != k)
+        for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+            T t = M[k * n + j];
+            M[k * n + j] = M[(int64_t)p * n + j];
+            M[(int64_t)p * n + j] = t;
+        }
+    __syncthreads();
+    const T d = M[k * n + k];
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) col[i] = M[i * n + k];
+    __syncthreads();
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+        if (j == k) M[k * n + k] = (T)1 / d;
+        else M[k * n + j] = M[k * n + j] / d;
+    }
+}
+
+template <class T>
+__global__ void k_gj_elim(int64_t n, int64_t k, T* M, const T* __restrict__ col) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i = blockIdx.y;
+    if (j >= n || i == k) return;
+    const T f = col[i];
+    if (j == k) M[i * n + k] = -f * M[k * n + k];
+    else M[i * n + j] -= f * M[k * n + j];
+}
+
+template <class T>
+__global__ void k_gj_colswap(int64_t n, T* M, const int32_t* perm, int64_t k) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t p = perm[k];
+    if (p == k) return;
+    T t = M[i * n + k];
+    M[i * n + k] = M[i * n + p];
+    M[i * n + p] = t;
+}
+
+template <class T>
+void invert(Ctx& c, T* M, int64_t n, int32_t* singular) {
+    cudaStream_t s = c.st();
+    DArr<T> col;
+    col.reserve(n);
+    c.piv.reserve(n);
+    for (int64_t k = 0; k < n; k++) {
+        k_gj_pivot<T><<<1, 1024, 0, s>>>(n, k, M, c.piv.p, col.p, singular);
+        VV_LAUNCH_CHECK();
+        dim3 grid(grid_for(n, 256), (unsigned)n);
+        k_gj_elim<T><<<grid, 256, 0, s>>>(n, k, M, col.p);
+        VV_LAUNCH_CHECK();
+    }
+    for (int64_t k = n - 1; k >= 0; k--) {
+        k_gj_colswap<T><<<grid_for(n, 256), 256, 0, s>>>(n, M, c.piv.p, k);
+        VV_LAUNCH_CHECK();
+    }
+    VV_CUDA(cudaStreamSynchronize(s));
+}
+
+__global__ void k_differs(int64_t n, const unsigned long long* __restrict__ a,
+                          const unsigned long long* __restrict__ b, int32_t* diff) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && a[i] != b[i]) *diff = 1;
+}
+
+__global__ void k_to_f32(int64_t n, const double* a, float* b) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+// y = M v (+ y0): one warp per row, FP64 accumulation.
+template <class T>
+__global__ void k_gemv(int64_t n, const T* __restrict__ M, const double* __restrict__ v, double* y, bool add) {
+    int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double acc = 0;
+    const T* r = M + row * n;
+    for (int64_t j = lane; j < n; j += 32) acc += (double)r[j] * v[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[row] = add ? y[row] + acc : acc;
+}
+
+// r = b - A x, and |r|^2, |b|^2 accumulated in acc[0], acc[1]
+__global__ void k_residual(int64_t n, const double* __restrict__ A, const double* __restrict__ x,
+                           const double* __restrict__ b, double* r, double* acc) {
+    int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double s = 0;
+    const double* Ar = A + row * n;
+    for (int64_t j = lane; j < n; j += 32) s += Ar[j] * x[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        double rr = b[row] - s;
+        r[row] = rr;
+        atomicAdd(&acc[0], rr * rr);
+        atomicAdd(&acc[1], b[row] * b[row]);
+    }
+}
+
+__global__ void k_scatter_solution(int64_t nb, const int32_t* col_seg0, const int32_t* body_first,
+                                   const int32_t* body_count, const double* X, double* sg) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int b = 0; b < nb; b++) {
+        if (t < body_count[b]) sg[body_first[b] + t] = X[col_seg0[b] + t];
+    }
+}
+
+__global__ void k_gsum(int64_t n, const double* __restrict__ g, double* out) {
+    __shared__ double sh[32];
+    double v = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v += g[i];
+    double t = block_sum(v, sh);
+    if (threadIdx.x == 0) atomicAdd(out, t);
+}
+
+}  // namespace
+
+double gsum(Ctx& c) {
+    cudaStream_t s = c.st();
+    c.counters.reserve(16);
+    double* out = (double*)(c.counters.p + 4);
+    VV_CUDA(cudaMemsetAsync(out, 0, 8, s));
+    if (c.n) {
+        k_gsum<<<304, 256, 0, s>>>(c.n, c.g.p, out);
+        VV_LAUNCH_CHECK();
+    }
+    double v = 0;
+    VV_CUDA(cudaMemcpyAsync(&v, out, 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    return v;
+}
+
+void slae(Ctx& c, vvgpu_body_out* out) {
+    const int nb = (int)c.bodies.size();
+    for (auto& b : c.bodies) {
+        auto rigid = [](double k) { return !(k >= 0 && std::isfinite(k)); };
+        if (!rigid(b.p.kspring_x) || !rigid(b.p.kspring_y) || !rigid(b.p.kspring_o))
+            throw ApiError{VVGPU_ERR_UNSUPPORTED, "spring-mounted bodies are not supported"};
+        if (b.p.speed_o != 0) throw ApiError{VVGPU_ERR_UNSUPPORTED, "rotating bodies are not supported"};
+        if (b.p.special_segment_no < 0 || b.p.special_segment_no >= b.count)
+            throw ApiError{VVGPU_ERR_ARG, "special_segment_no out of range"};
+    }
+    if (nb == 0) return;
+    cudaStream_t s = c.st();
+    const int64_t n = c.m + 9 * (int64_t)nb;
+    c.neq = n;
+    const double gs = gsum(c);
+    // host-side row/column maps
+    std::vector<int32_t> col0(nb), bfirst(nb), bcount(nb), row_seg(n, -1), row_body(n, -1), slip_rows;
+    std::vector<BodyDev> bd(nb);
+    {
+        int32_t cc = 0;
+        for (int bi = 0; bi < nb; bi++) {
+            const BodyHost& b = c.bodies[bi];
+            col0[bi] = cc;
+            bfirst[bi] = (int32_t)b.first;
+            bcount[bi] = (int32_t)b.count;
+            for (int32_t k = 0; k < b.count; k++) {
+                row_seg[cc + k] = (int32_t)(b.first + k);
+                row_body[cc + k] = bi;
+                if (k != b.p.special_segment_no) slip_rows.push_back(cc + k);
+            }
+            cc += (int32_t)b.count + 9;
+            BodyDev& d = bd[bi];
+            d.area = b.area; d.cofx = b.cofm_x; d.cofy = b.cofm_y;
+            d.axx = b.p.holder_x + b.p.dpos_x; d.axy = b.p.holder_y + b.p.dpos_y;
+            double dx = d.axx - b.cofm_x, dy = d.axy - b.cofm_y;
+            d.moi = b.moi_cofm + (dx * dx + dy * dy) * b.area;
+            d.dens = b.p.density;
+            d.pvx = b.p.speed_slae_prev_x; d.pvy = b.p.speed_slae_prev_y; d.pvo = b.p.speed_slae_prev_o;
+            d.fpx = b.p.friction_prev_x; d.fpy = b.p.friction_prev_y; d.fpo = b.p.friction_prev_o;
+            d.fdx = b.p.fdt_dead_x; d.fdy = b.p.fdt_dead_y; d.fdo = b.p.fdt_dead_o; d.gdead = b.p.g_dead;
+            d.spx = b.p.speed_x; d.spy = b.p.speed_y; d.spo = b.p.speed_o;
+            d.special = b.p.special_segment_no; d.kutta = b.p.bc_kutta;
+        }
+    }
+    DArr<int32_t> dmaps;
+    const size_t nsl = slip_rows.size();
+    dmaps.reserve(3 * nb + 2 * n + nsl + 1);
+    int32_t* d_col0 = dmaps.p;
+    int32_t* d_bfirst = d_col0 + nb;
+    int32_t* d_bcount = d_bfirst + nb;
+    int32_t* d_rowseg = d_bcount + nb;
+    int32_t* d_rowbody = d_rowseg + n;
+    int32_t* d_slip = d_rowbody + n;
+    VV_CUDA(cudaMemcpyAsync(d_col0, col0.data(), nb * 4, cudaMemcpyHostToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(d_bfirst, bfirst.data(), nb * 4, cudaMemcpyHostToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(d_bcount, bcount.data(), nb * 4, cudaMemcpyHostToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(d_rowseg, row_seg.data(), n * 4, cudaMemcpyHostToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(d_rowbody, row_body.data(), n * 4, cudaMemcpyHostToDevice, s));
+    if (nsl) VV_CUDA(cudaMemcpyAsync(d_slip, slip_rows.data(), nsl * 4, cudaMemcpyHostToDevice, s));
+    DArr<BodyDev> dbd;
+    dbd.reserve(nb);
+    VV_CUDA(cudaMemcpyAsync(dbd.p, bd.data(), nb * sizeof(BodyDev), cudaMemcpyHostToDevice, s));
+
+    c.A.reserve(n * n);
+    c.B.reserve(n);
+    c.X.reserve(n);
+    VV_CUDA(cudaMemsetAsync(c.A.p, 0, n * n * sizeof(double), s));
+    VV_CUDA(cudaMemsetAsync(c.B.p, 0, n * sizeof(double), s));
+    FillArgs fa{};
+    fa.n = n; fa.A = c.A.p; fa.B = c.B.p;
+    fa.S = SegDev{c.s_cx.p, c.s_cy.p, c.s_rx.p, c.s_ry.p, c.s_dlx.p, c.s_dly.p};
+    fa.slip_rows = d_slip; fa.nslip = (int64_t)nsl; fa.row_seg = d_rowseg; fa.row_body = d_rowbody;
+    fa.col_seg0 = d_col0; fa.body_first = d_bfirst; fa.body_count = d_bcount; fa.nbodies = nb;
+    fa.geom = c.nd_geom.p; fa.ch1 = c.nd_ch1.p; fa.dfs = c.nd_dfs.p;
+    fa.lvf = c.lf_vf.p; fa.lvl = c.lf_vl.p; fa.near_off = c.near_off.p; fa.near_run = c.near_run.p;
+    fa.far_off = c.far_off.p; fa.far_node = c.far_node.p; fa.cm = c.nd_cm.p;
+    fa.x = c.x.p; fa.y = c.y.p; fa.g = c.g.p; fa.ie = c.ie.p;
+    fa.ns = c.ns; fa.kx = c.k_x.p; fa.ky = c.k_y.p; fa.kg = c.k_g.p; fa.sink_e2 = c.dt * C_1_PI;
+    fa.inf_vx = c.inf_vx; fa.inf_vy = c.inf_vy;
+    fa.rhs_only = false;
+    if (nsl) {
+        k_slip_rows<<<(unsigned)nsl, 256, 0, s>>>(fa);
+        VV_LAUNCH_CHECK();
+    }
+    k_body_rows<<<1, 1, 0, s>>>(n, c.A.p, c.B.p, dbd.p, nb, d_col0, d_bcount, c.s_cy.p, c.s_cx.p, d_bfirst, c.dt,
+                                gs, c.inf_g, c.grav_x, c.grav_y, false);
+    VV_LAUNCH_CHECK();
+
+    // reuse the cached inverse while the matrix bytes are unchanged
+    bool same = false;
+    int32_t* singular = (int32_t*)(c.counters.p + 6);
+    if (c.lu_valid && c.lu_precision == c.precision && c.neq_cached == n) {
+        int32_t* diff = (int32_t*)(c.counters.p + 7);
+        VV_CUDA(cudaMemsetAsync(diff, 0, 4, s));
+        k_differs<<<grid_for(n * n, 256), 256, 0, s>>>(n * n, (const unsigned long long*)c.A.p,
+                                                      (const unsigned long long*)c.Acache.p, diff);
+        VV_LAUNCH_CHECK();
+        same = read_i32(c, diff) == 0;
+    }
+    if (!same) {
+        c.Acache.reserve(n * n);
+        VV_CUDA(cudaMemcpyAsync(c.Acache.p, c.A.p, n * n * 8, cudaMemcpyDeviceToDevice, s));
+        VV_CUDA(cudaMemsetAsync(singular, 0, 4, s));
+        if (c.precision == VVGPU_FP32) {
+            c.inv32.reserve(n * n);
+            k_to_f32<<<grid_for(n * n, 256), 256, 0, s>>>(n * n, c.A.p, c.inv32.p);
+            VV_LAUNCH_CHECK();
+            invert<float>(c, c.inv32.p, n, singular);
+        } else {
+            c.inv.reserve(n * n);
+            VV_CUDA(cudaMemcpyAsync(c.inv.p, c.A.p, n * n * 8, cudaMemcpyDeviceToDevice, s));
+            invert<double>(c, c.inv.p, n, singular);
+        }
+        if (read_i32(c, singular)) {
+            c.lu_valid = false;
+            throw ApiError{VVGPU_ERR_SINGULAR, "singular SLAE"};
+        }
+        c.lu_valid = true;
+        c.lu_precision = c.precision;
+        c.neq_cached = n;
+    }
+    // x = inv b, then FP64 iterative refinement
+    DArr<double> r;
+    r.reserve(n);
+    double* acc = (double*)(c.counters.p + 8);
+    const unsigned gg = grid_for(n, 8);
+    auto apply_inv = [&](const double* v, double* y, bool add) {
+        if (c.lu_precision == VVGPU_FP32) k_gemv<float><<<gg, 256, 0, s>>>(n, c.inv32.p, v, y, add);
+        else k_gemv<double><<<gg, 256, 0, s>>>(n, c.inv.p, v, y, add);
+        VV_LAUNCH_CHECK();
+    };
+    apply_inv(c.B.p, c.X.p, false);
+    for (int it = 0; it < 12; it++) {
+        VV_CUDA(cudaMemsetAsync(acc, 0, 16, s));
+        k_residual<<<gg, 256, 0, s>>>(n, c.A.p, c.X.p, c.B.p, r.p, acc);
+        VV_LAUNCH_CHECK();
+        double h[2];
+        VV_CUDA(cudaMemcpyAsync(h, acc, 16, cudaMemcpyDeviceToHost, s));
+        VV_CUDA(cudaStreamSynchronize(s));
+        if (!(h[0] > 1e-26 * h[1])) break;
+        apply_inv(r.p, c.X.p, true);
+    }
+    int64_t maxcnt = 0;
+    for (auto& b : c.bodies) maxcnt = std::max<int64_t>(maxcnt, b.count);
+    k_scatter_solution<<<grid_for(maxcnt, 256), 256, 0, s>>>(nb, d_col0, d_bfirst, d_bcount, c.X.p, c.s_g.p);
+    VV_LAUNCH_CHECK();
+    std::vector<double> hx(n);
+    VV_CUDA(cudaMemcpyAsync(hx.data(), c.X.p, n * 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    for (int bi = 0; bi < nb; bi++) {
+        const double* u = hx.data() + col0[bi] + c.bodies[bi].count;
+        vvgpu_body_params& p = c.bodies[bi].p;
+        p.speed_slae_x = u[0]; p.speed_slae_y = u[1]; p.speed_slae_o = u[2];
+        if (out) {
+            vvgpu_body_out& o = out[bi];
+            o.speed_slae_x = u[0]; o.speed_slae_y = u[1]; o.speed_slae_o = u[2];
+            o.force_hydro_x = u[3]; o.force_hydro_y = u[4]; o.force_hydro_o = u[5];
+            o.force_holder_x = u[6]; o.force_holder_y = u[7]; o.force_holder_o = u[8];
+        }
+    }
+}
+
+}  // namespace vvgpu

@@ -1,0 +1,257 @@
+// Internal definitions shared by the CUDA translation units of libvvgpu.
+//
+// Device layout (structure of arrays, one context per Space):
+//   vortices  x, y, g, ie (= TObj::_1_eps), vx, vy : double[n]; orig : int64[n]
+//   segments  corner, r, dl, ie, g, fric, gsum     : double[m] (all bodies concatenated)
+//   nodes     geom (x, y, h, w) : double4[nn]; vortex range vf/vl, segment range sf/sl,
+//             first child ch1 (ch2 = ch1 + 1, -1 for a leaf), depth, path bits,
+//             +/- centroids cm (px, py, pg, mx, my, mg)
+//   leaves    in bottomNodes (depth-first) order, which is also increasing vortex index
+//   near      per leaf, runs of consecutive leaves (each run is one contiguous vortex range)
+//   far       per leaf, node ids in depth-first order
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/vvgpu.h"
+
+namespace vvgpu {
+
+constexpr double C_PI = 3.14159265358979323846;
+constexpr double C_2PI = 2. * C_PI;
+constexpr double C_1_2PI = 1. / (2. * C_PI);
+constexpr double C_1_PI = 1. / C_PI;
+constexpr int TREE_MAX_LIST_SIZE = 16;   // TSortedTree.cpp:10
+constexpr double EXP_ARG_RESTRICTION = -8.;  // MDiffusiveFast.cpp:6
+constexpr double REMOVE_EPS = 1e-10;         // MFlowmove.hpp:8
+constexpr int MAX_DEPTH = 62;            // path bits are kept in an int64
+
+struct CudaError {
+    cudaError_t err;
+    const char* what;
+};
+
+#define VV_CUDA(call)                                                          \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess) throw ::vvgpu::CudaError{e_, #call};            \
+    } while (0)
+
+// Checks the last launch and counts it in the context (c must be in scope).
+#define VV_LAUNCH_CHECK()                   \
+    do {                                    \
+        VV_CUDA(cudaGetLastError());        \
+        ++c.launches;                       \
+    } while (0)
+
+struct ApiError {
+    int code;
+    std::string msg;
+};
+
+// Growable device array (capacity only grows; contents not preserved on growth unless asked).
+template <class T>
+struct DArr {
+    T* p = nullptr;
+    size_t cap = 0;
+    DArr() = default;
+    DArr(const DArr&) = delete;
+    DArr& operator=(const DArr&) = delete;
+    DArr(DArr&& o) noexcept : p(o.p), cap(o.cap) { o.p = nullptr; o.cap = 0; }
+    DArr& operator=(DArr&& o) noexcept {
+        if (this != &o) { release(); p = o.p; cap = o.cap; o.p = nullptr; o.cap = 0; }
+        return *this;
+    }
+    ~DArr() { release(); }
+    void reserve(size_t n, bool keep = false, size_t keep_n = 0, cudaStream_t s = 0) {
+        if (n <= cap) return;
+        size_t nc = cap ? cap : 256;
+        while (nc < n) nc *= 2;
+        T* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, nc * sizeof(T));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            throw ApiError{VVGPU_ERR_NOMEM, "cudaMalloc failed"};
+        }
+        if (keep && p && keep_n) VV_CUDA(cudaMemcpyAsync(q, p, keep_n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+        if (p) {
+            if (keep) VV_CUDA(cudaStreamSynchronize(s));
+            cudaFree(p);
+        }
+        p = q;
+        cap = nc;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct BodyHost {
+    int64_t first, count;
+    vvgpu_body_params p;
+    double slen, area, cofm_x, cofm_y, moi_cofm;
+};
+
+struct Ctx {
+    int device = 0;
+    int precision = VVGPU_FP64;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+
+    double re = 1.0 / 0.0, dt = 1.0, inf_vx = 0, inf_vy = 0, inf_g = 0, time = 0, grav_x = 0, grav_y = 0;
+
+    // vortices
+    int64_t n = 0;
+    DArr<double> x, y, g, ie, vx, vy;
+    DArr<int64_t> orig;
+    int64_t next_orig = 0;
+
+    // segments (host copies of geometry are kept for body bookkeeping)
+    int64_t m = 0;
+    std::vector<double> h_cx, h_cy, h_rx, h_ry, h_dlx, h_dly, h_sie;
+    std::vector<uint32_t> h_slip;
+    std::vector<BodyHost> bodies;
+    DArr<double> s_cx, s_cy, s_rx, s_ry, s_dlx, s_dly, s_ie, s_g, s_fric, s_gsum;
+    DArr<uint32_t> s_slip;
+    bool segs_dirty = true;
+    // sinks
+    int64_t ns = 0;
+    DArr<double> k_x, k_y, k_g;
+
+    // tree
+    bool built = false;
+    double far_criteria = 8, min_node = 0, max_node = 0;
+    int64_t nnodes = 0, nleaves = 0, depth = 0;
+    std::vector<int64_t> level_begin;
+    DArr<double4> nd_geom;          // x, y, h, w
+    DArr<int32_t> nd_vf, nd_vl, nd_sf, nd_sl, nd_ch1, nd_depth;
+    DArr<int64_t> nd_path;
+    DArr<double> nd_cm;             // 6 per node: px, py, pg, mx, my, mg
+    DArr<unsigned long long> nd_bbox;  // 4 per node: encoded min x, min y, max x, max y
+    DArr<double> nd_pivot;
+    DArr<int32_t> nd_axis, nd_split, nd_nlow, nd_nlow_s, nd_lc, nd_dfs;
+    DArr<int32_t> node_of, seg_node_of, seg_node_of2, flags, scan;
+    DArr<int32_t> tab_lh, tab_rl;
+    DArr<int32_t> seg_order, seg_order2;
+    DArr<int32_t> leaf_node;        // DFS order -> node id
+    DArr<int32_t> lf_vf, lf_vl, lf_sf, lf_sl;
+    DArr<double4> lf_geom;
+    DArr<int32_t> near_off, far_off, near_cnt, far_cnt;
+    DArr<int2> near_run;
+    DArr<int32_t> far_node;         // far lists of flagged leaves only (see lists.cu)
+    DArr<int32_t> lf_flag;          // leaf holds a segment centre
+    DArr<double4> lf_taylor;        // far-field expansion coefficients T1..T4 per leaf
+    int taylor_precision = 0;
+    DArr<float4> nf_geo, nf_cm;     // per node, anchor frame: centre + (h+w); centroids
+    DArr<int2> nf_k;                // per node anchor
+    DArr<float2> nf_g;              // per node centroid circulations
+    int64_t n_near_runs = 0, n_far = 0;
+    DArr<int32_t> leaf_of;          // vortex -> leaf (DFS index)
+
+    // scratch for reductions / counters
+    DArr<unsigned long long> counters;
+    DArr<int32_t> scan_tmp;
+
+    // epsilon / merge (fixed-point rounds; [2] = double buffer)
+    DArr<int32_t> e_partner[2], e_zb, e_changed;
+    DArr<double> e_x0, e_y0, e_g0, e_ox[2], e_oy[2], e_og[2], e_oie[2];
+    DArr<float4> e_rec0, e_recO;
+    DArr<double> lf_mcs, lf_epr;
+    DArr<int32_t> e_zb_prev, e_live, e_cand, e_ncand, e_dirty, e_lchanged;
+
+    // local FP32 frames (frame.cuh)
+    double frame_G = 1.0;
+    DArr<int2> lf_anchor;
+    DArr<float4> lf_box32;          // per leaf: min x, min y, max x, max y in its own frame
+    DArr<float> lf_rn;              // per leaf: extent of its near region in its frame
+    DArr<float4> src32;             // per vortex: x, y in own leaf frame, g, eps^2
+    DArr<int2> src_k;               // per vortex: anchor of its leaf
+    DArr<float4> lf_dbox;           // per leaf (diffusive): box of non-zero vortices and segment centres
+
+    // SLAE
+    int64_t neq = 0;
+    DArr<double> A, B, X, Acache, LU, inv;
+    DArr<float> inv32;
+    DArr<int32_t> piv;
+    bool lu_valid = false;
+    int lu_precision = 0;
+    int64_t neq_cached = 0;
+    vvgpu_stats stats{};
+    int64_t launches = 0;           // kernels launched by this context
+    bool count_pairs = true;        // count algorithmic near pairs before each convective pass
+
+    cudaStream_t st() const { return stream; }
+};
+
+// ---- exact FP64 arithmetic (no FMA contraction: the reference is built without FMA) ----
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double dabs2(double x, double y) { return dadd(dmul(x, x), dmul(y, y)); }
+// std::max / std::min as libstdc++ defines them
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double dsgn(double v) { return (v > 0) ? 1. : ((v < 0) ? -1. : 0.); }
+
+// Order-preserving map double -> uint64 for atomicMin/atomicMax on doubles.
+__device__ __forceinline__ unsigned long long dkey(double v) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dunkey(unsigned long long k) {
+    unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double((long long)u);
+}
+inline unsigned long long dkey_host(double v) {
+    unsigned long long u;
+    memcpy(&u, &v, 8);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+inline unsigned grid_for(int64_t n, int block) {
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 0x7fffffff) g = 0x7fffffff;
+    return (unsigned)g;
+}
+
+// ---- scan.cu ----
+// Exclusive prefix sum of n int32 values into out[0..n] (out[n] = total).
+void exclusive_scan(Ctx& c, const int32_t* in, int32_t* out, int64_t n);
+// Reads one int32 from device memory (synchronises the stream).
+int32_t read_i32(Ctx& c, const int32_t* p);
+
+// ---- per-module entry points (throw ApiError / CudaError) ----
+void ensure_vortex_capacity(Ctx& c, int64_t n, bool keep);
+// Leaf anchors (frame.cuh) and per-leaf FP32 boxes of the current vortex positions.
+void build_frames(Ctx& c);
+void tree_build(Ctx& c, double far_criteria, double min_node, double max_node);
+void tree_lists(Ctx& c);
+// Full far lists by an exact FP64 walk (inspection).
+void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t>& far_node);
+void eps_pass(Ctx& c, int merge, int64_t* merged);
+void convective(Ctx& c);
+void velocity_points(Ctx& c, int64_t n, const double* px, const double* py, double* vx, double* vy);
+void diffusive(Ctx& c);
+void slae(Ctx& c, vvgpu_body_out* out);
+void upload_segments(Ctx& c);
+void vortex_shed(Ctx& c);
+double gsum(Ctx& c);
+
+}  // namespace vvgpu

@@ -1,0 +1,350 @@
+"""ctypes binding of libvvgpu.so (include/vvgpu.h).
+
+``GpuSpace`` mirrors the reference's hot-path call surface (stree::build/destroy,
+MEpsilonFast::CalcEpsilonFast, MConvectiveFast::process_all_lists / velocity /
+calc_circulation, MDiffusiveFast::process_vort_list, MFlowmove::vortex_shed) on one
+Space held in GPU memory.  There is no CPU fallback: constructing a GpuSpace without the
+compiled library or without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libvvgpu.so")
+
+VVGPU_FP64 = 0
+VVGPU_FP32 = 1
+
+ERRORS = {
+    -1: "VVGPU_ERR_ARG", -2: "VVGPU_ERR_STATE", -3: "VVGPU_ERR_NOT_BUILT", -4: "VVGPU_ERR_UNSUPPORTED",
+    -5: "VVGPU_ERR_SINGULAR", -6: "VVGPU_ERR_CUDA", -7: "VVGPU_ERR_NOMEM", -8: "VVGPU_ERR_TIMEOUT",
+    -9: "VVGPU_ERR_LIMIT",
+}
+
+
+class Cfg(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("reserve_vortices", C.c_int64),
+                ("reserve_segments", C.c_int64)]
+
+
+class BodyParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "holder_x", "holder_y", "holder_o", "dpos_x", "dpos_y", "dpos_o",
+        "speed_x", "speed_y", "speed_o",
+        "speed_slae_x", "speed_slae_y", "speed_slae_o",
+        "speed_slae_prev_x", "speed_slae_prev_y", "speed_slae_prev_o",
+        "friction_prev_x", "friction_prev_y", "friction_prev_o",
+        "fdt_dead_x", "fdt_dead_y", "fdt_dead_o", "g_dead", "density",
+        "kspring_x", "kspring_y", "kspring_o")] + [
+        ("special_segment_no", C.c_int32), ("bc_kutta", C.c_int32)]
+
+
+class BodyOut(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "speed_slae_x", "speed_slae_y", "speed_slae_o",
+        "force_hydro_x", "force_hydro_y", "force_hydro_o",
+        "force_holder_x", "force_holder_y", "force_holder_o")]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "n_vortices", "n_segments", "n_nodes", "n_leaves", "tree_depth", "near_pairs", "far_pairs",
+        "near_runs", "merge_rounds", "merged", "diff_candidates")] + [("reserved", C.c_int64 * 8)]
+
+
+class VVGpuError(RuntimeError):
+    def __init__(self, code, where, msg=""):
+        super().__init__(f"{where}: {ERRORS.get(code, code)} {msg}".strip())
+        self.code = code
+
+
+_D = C.POINTER(C.c_double)
+_I64 = C.POINTER(C.c_int64)
+_I32 = C.POINTER(C.c_int32)
+_U32 = C.POINTER(C.c_uint32)
+_H = C.c_void_p
+
+# name -> (restype, argtypes); the same list is the ABI surface checked by the tests
+SIGNATURES = {
+    "vvgpu_ctx_create": (C.c_int, [C.POINTER(Cfg), C.POINTER(_H)]),
+    "vvgpu_ctx_destroy": (C.c_int, [_H]),
+    "vvgpu_last_error": (C.c_char_p, [_H]),
+    "vvgpu_set_precision": (C.c_int, [_H, C.c_int]),
+    "vvgpu_set_stream": (C.c_int, [_H, C.c_void_p]),
+    "vvgpu_synchronize": (C.c_int, [_H]),
+    "vvgpu_get_stats": (C.c_int, [_H, C.POINTER(Stats)]),
+    "vvgpu_set_params": (C.c_int, [_H] + [C.c_double] * 8),
+    "vvgpu_add_body": (C.c_int, [_H, C.c_int64, _D, _D, _U32, C.POINTER(BodyParams)]),
+    "vvgpu_set_segment_g": (C.c_int, [_H, _D]),
+    "vvgpu_set_sinks": (C.c_int, [_H, C.c_int64, _D, _D, _D]),
+    "vvgpu_set_vortices": (C.c_int, [_H, C.c_int64, _D, _D, _D, _D]),
+    "vvgpu_set_vortices_device": (C.c_int, [_H, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vvgpu_num_vortices": (C.c_int64, [_H]),
+    "vvgpu_num_segments": (C.c_int64, [_H]),
+    "vvgpu_get_vortices": (C.c_int, [_H, _D, _D, _D, _D, _D, _D, _I64]),
+    "vvgpu_device_arrays": (C.c_int, [_H] + [C.POINTER(C.c_void_p)] * 6),
+    "vvgpu_get_segments": (C.c_int, [_H] + [_D] * 8),
+    "vvgpu_get_body_geom": (C.c_int, [_H, C.c_int] + [_D] * 5),
+    "vvgpu_tree_build": (C.c_int, [_H, C.c_double, C.c_double, C.c_double]),
+    "vvgpu_tree_destroy": (C.c_int, [_H]),
+    "vvgpu_eps": (C.c_int, [_H, C.c_int, _I64]),
+    "vvgpu_convective": (C.c_int, [_H]),
+    "vvgpu_diffusive": (C.c_int, [_H]),
+    "vvgpu_velocity_points": (C.c_int, [_H, C.c_int64, _D, _D, _D, _D]),
+    "vvgpu_slae": (C.c_int, [_H, C.POINTER(BodyOut)]),
+    "vvgpu_vortex_shed": (C.c_int, [_H]),
+    "vvgpu_gsum": (C.c_int, [_H, _D]),
+    "vvgpu_tree_sizes": (C.c_int, [_H, _I64, _I64, _I64, _I64]),
+    "vvgpu_tree_leaves": (C.c_int, [_H, _D, _D, _D, _D, _I64, _I64, _I32, _I64, _I64, _I64]),
+    "vvgpu_tree_nodes": (C.c_int, [_H, _D, _D, _D, _D, _I64, _I64, _I32, _I64] + [_D] * 6),
+    "vvgpu_tree_seg_order": (C.c_int, [_H, _I64]),
+    "vvgpu_tree_lists": (C.c_int, [_H, _I64, _I32, _I64, _I64, _I32, _I64]),
+    "vvgpu_slae_size": (C.c_int64, [_H]),
+    "vvgpu_slae_export": (C.c_int, [_H, _D, _D, _D]),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads libvvgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m vvflow_gb300.build`")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _p(a, ct=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ct)) if a is not None else None
+
+
+def default_body_params() -> BodyParams:
+    bp = BodyParams()
+    bp.density = 1.0
+    bp.kspring_x = bp.kspring_y = bp.kspring_o = float("inf")
+    return bp
+
+
+class GpuSpace:
+    """One Space on the GPU; method names follow the oracle's driver."""
+
+    kind = "gpu"
+
+    def __init__(self, precision: int = VVGPU_FP64, device: int = 0, reserve: int = 0):
+        self.lib = load_library()
+        cfg = Cfg(device, precision, reserve, 0)
+        h = _H()
+        rc = self.lib.vvgpu_ctx_create(C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise VVGpuError(rc, "vvgpu_ctx_create", "(needs a CUDA device)")
+        self.h = h
+        self.nbodies = 0
+        self.precision = precision
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vvgpu_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc, what):
+        if rc != 0:
+            msg = self.lib.vvgpu_last_error(self.h)
+            raise VVGpuError(rc, what, msg.decode() if msg else "")
+
+    def stats(self):
+        s = Stats()
+        self._ok(self.lib.vvgpu_get_stats(self.h, C.byref(s)), "get_stats")
+        d = {k: getattr(s, k) for k, _ in Stats._fields_ if k != "reserved"}
+        d["launches"] = int(s.reserved[0])
+        return d
+
+    # -- state -----------------------------------------------------------------------
+    def set_params(self, re, dt, inf_vx=1.0, inf_vy=0.0, inf_g=0.0, time=0.0, gx=0.0, gy=0.0):
+        self._ok(self.lib.vvgpu_set_params(self.h, re, dt, inf_vx, inf_vy, inf_g, time, gx, gy), "set_params")
+
+    def add_body(self, cx, cy, slip=None, params: BodyParams | None = None):
+        cx = np.ascontiguousarray(cx, np.float64)
+        cy = np.ascontiguousarray(cy, np.float64)
+        sl = None if slip is None else np.ascontiguousarray(slip, np.uint32)
+        bp = params if params is not None else default_body_params()
+        self._ok(self.lib.vvgpu_add_body(self.h, len(cx), _p(cx), _p(cy), _p(sl, C.c_uint32), C.byref(bp)), "add_body")
+        self.nbodies += 1
+
+    def set_segment_g(self, g):
+        g = np.ascontiguousarray(g, np.float64)
+        self._ok(self.lib.vvgpu_set_segment_g(self.h, _p(g)), "set_segment_g")
+
+    def set_vortices(self, x, y, g, inv_eps=None):
+        x, y, g = (np.ascontiguousarray(a, np.float64) for a in (x, y, g))
+        ie = None if inv_eps is None else np.ascontiguousarray(inv_eps, np.float64)
+        self._ok(self.lib.vvgpu_set_vortices(self.h, len(x), _p(x), _p(y), _p(g), _p(ie)), "set_vortices")
+
+    def set_vortices_device(self, n, x_ptr, y_ptr, g_ptr, ie_ptr=None):
+        self._ok(self.lib.vvgpu_set_vortices_device(self.h, n, x_ptr, y_ptr, g_ptr, ie_ptr), "set_vortices_device")
+
+    def load(self, wl, inv_eps=None, time=0.0):
+        self.set_params(wl.re, wl.dt, wl.inf_vx, wl.inf_vy, 0.0, time)
+        for cx, cy in wl.bodies:
+            self.add_body(cx, cy)
+        self.set_vortices(wl.x, wl.y, wl.g, inv_eps)
+
+    @property
+    def n(self):
+        return int(self.lib.vvgpu_num_vortices(self.h))
+
+    @property
+    def m(self):
+        return int(self.lib.vvgpu_num_segments(self.h))
+
+    def vortices(self):
+        n = self.n
+        out = {k: np.empty(n) for k in ("x", "y", "g", "inv_eps", "vx", "vy")}
+        out["orig"] = np.empty(n, np.int64)
+        self._ok(self.lib.vvgpu_get_vortices(self.h, *(_p(out[k]) for k in ("x", "y", "g", "inv_eps", "vx", "vy")),
+                                             _p(out["orig"], C.c_int64)), "get_vortices")
+        return out
+
+    def segments(self):
+        m = self.m
+        keys = ("rx", "ry", "dlx", "dly", "inv_eps", "g", "fric", "gsum")
+        out = {k: np.empty(m) for k in keys}
+        self._ok(self.lib.vvgpu_get_segments(self.h, *(_p(out[k]) for k in keys)), "get_segments")
+        return out
+
+    def body_geom(self, b=0):
+        vals = [C.c_double() for _ in range(5)]
+        self._ok(self.lib.vvgpu_get_body_geom(self.h, b, *(C.byref(v) for v in vals)), "get_body_geom")
+        return dict(zip(("area", "cofm_x", "cofm_y", "moi_axis", "slen"), (v.value for v in vals)))
+
+    # -- hot path ----------------------------------------------------------------------
+    def tree_build(self, far_criteria, min_node, max_node):
+        self._ok(self.lib.vvgpu_tree_build(self.h, far_criteria, min_node, max_node), "tree_build")
+
+    def tree_destroy(self):
+        self._ok(self.lib.vvgpu_tree_destroy(self.h), "tree_destroy")
+
+    def eps(self, merge=True):
+        m = C.c_int64()
+        self._ok(self.lib.vvgpu_eps(self.h, int(bool(merge)), C.byref(m)), "eps")
+        return m.value
+
+    def convective(self):
+        self._ok(self.lib.vvgpu_convective(self.h), "convective")
+
+    def diffusive(self):
+        self._ok(self.lib.vvgpu_diffusive(self.h), "diffusive")
+
+    def velocity_points(self, px, py):
+        px = np.ascontiguousarray(px, np.float64)
+        py = np.ascontiguousarray(py, np.float64)
+        vx = np.empty_like(px)
+        vy = np.empty_like(px)
+        self._ok(self.lib.vvgpu_velocity_points(self.h, len(px), _p(px), _p(py), _p(vx), _p(vy)), "velocity_points")
+        return vx, vy
+
+    def slae(self):
+        out = (BodyOut * max(self.nbodies, 1))()
+        self._ok(self.lib.vvgpu_slae(self.h, out), "slae")
+        return [{k: getattr(out[i], k) for k, _ in BodyOut._fields_} for i in range(self.nbodies)]
+
+    def slae_export(self):
+        n = int(self.lib.vvgpu_slae_size(self.h))
+        A = np.empty((n, n))
+        b = np.empty(n)
+        x = np.empty(n)
+        self._ok(self.lib.vvgpu_slae_export(self.h, _p(A), _p(b), _p(x)), "slae_export")
+        return A, b, x
+
+    def vortex_shed(self):
+        self._ok(self.lib.vvgpu_vortex_shed(self.h), "vortex_shed")
+
+    def gsum(self):
+        v = C.c_double()
+        self._ok(self.lib.vvgpu_gsum(self.h, C.byref(v)), "gsum")
+        return v.value
+
+    def set_stream(self, stream_ptr: int | None):
+        """Queues all work on the caller's CUDA stream (cudaStream_t as an integer)."""
+        self._ok(self.lib.vvgpu_set_stream(self.h, C.c_void_p(stream_ptr) if stream_ptr else None), "set_stream")
+
+    def get_vortices_into(self, x=0, y=0, g=0, ie=0, vx=0, vy=0, orig=0):
+        """Copies the vortex list into caller-owned host buffers given as addresses (0 = skip)."""
+        D = C.POINTER(C.c_double)
+        f = lambda a, t=D: C.cast(C.c_void_p(a), t) if a else None
+        self._ok(self.lib.vvgpu_get_vortices(self.h, f(x), f(y), f(g), f(ie), f(vx), f(vy),
+                                             f(orig, C.POINTER(C.c_int64))), "get_vortices")
+
+    def set_vortices_from(self, n, x, y, g, ie=0):
+        """Replaces the vortex list from host buffers given as addresses (e.g. pinned memory)."""
+        D = C.POINTER(C.c_double)
+        f = lambda a: C.cast(C.c_void_p(a), D) if a else None
+        self._ok(self.lib.vvgpu_set_vortices(self.h, n, f(x), f(y), f(g), f(ie)), "set_vortices")
+
+    def synchronize(self):
+        self._ok(self.lib.vvgpu_synchronize(self.h), "synchronize")
+
+    # -- inspection -------------------------------------------------------------------
+    def tree_sizes(self):
+        v = [C.c_int64() for _ in range(4)]
+        self._ok(self.lib.vvgpu_tree_sizes(self.h, *(C.byref(a) for a in v)), "tree_sizes")
+        return tuple(a.value for a in v)
+
+    def tree_leaves(self):
+        _, nl, _, _ = self.tree_sizes()
+        d = {k: np.empty(nl) for k in ("x", "y", "h", "w")}
+        for k in ("vfirst", "vlast", "path", "sfirst", "slast"):
+            d[k] = np.empty(nl, np.int64)
+        d["depth"] = np.empty(nl, np.int32)
+        self._ok(self.lib.vvgpu_tree_leaves(self.h, _p(d["x"]), _p(d["y"]), _p(d["h"]), _p(d["w"]),
+                                            _p(d["vfirst"], C.c_int64), _p(d["vlast"], C.c_int64),
+                                            _p(d["depth"], C.c_int32), _p(d["path"], C.c_int64),
+                                            _p(d["sfirst"], C.c_int64), _p(d["slast"], C.c_int64)), "tree_leaves")
+        return d
+
+    def tree_nodes(self):
+        nn, _, _, _ = self.tree_sizes()
+        keys_d = ("x", "y", "h", "w")
+        keys_c = ("cmp_x", "cmp_y", "cmp_g", "cmm_x", "cmm_y", "cmm_g")
+        d = {k: np.empty(nn) for k in keys_d + keys_c}
+        d["vfirst"] = np.empty(nn, np.int64)
+        d["vlast"] = np.empty(nn, np.int64)
+        d["depth"] = np.empty(nn, np.int32)
+        d["path"] = np.empty(nn, np.int64)
+        self._ok(self.lib.vvgpu_tree_nodes(self.h, *(_p(d[k]) for k in keys_d),
+                                           _p(d["vfirst"], C.c_int64), _p(d["vlast"], C.c_int64),
+                                           _p(d["depth"], C.c_int32), _p(d["path"], C.c_int64),
+                                           *(_p(d[k]) for k in keys_c)), "tree_nodes")
+        return d
+
+    def tree_seg_order(self):
+        so = np.empty(self.m, np.int64)
+        self._ok(self.lib.vvgpu_tree_seg_order(self.h, _p(so, C.c_int64)), "tree_seg_order")
+        return so
+
+    def tree_lists(self):
+        _, nl, nnear, nfar = self.tree_sizes()
+        d = {"near_off": np.empty(nl + 1, np.int64), "far_off": np.empty(nl + 1, np.int64),
+             "near_depth": np.empty(nnear, np.int32), "near_path": np.empty(nnear, np.int64),
+             "far_depth": np.empty(nfar, np.int32), "far_path": np.empty(nfar, np.int64)}
+        self._ok(self.lib.vvgpu_tree_lists(self.h, _p(d["near_off"], C.c_int64), _p(d["near_depth"], C.c_int32),
+                                           _p(d["near_path"], C.c_int64), _p(d["far_off"], C.c_int64),
+                                           _p(d["far_depth"], C.c_int32), _p(d["far_path"], C.c_int64)), "tree_lists")
+        return d
