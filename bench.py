@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-stride", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="run the warm-up, then exactly one step between cudaProfilerStart/Stop and exit "
+                         "(for `ncu --profile-from-start off`)")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="path used by --profile")
     return ap.parse_args()
 
 
@@ -156,6 +160,24 @@ def gpu_arm(args):
 
     def restore(S):
         S.set_vortices_device(N, dx.data_ptr(), dy.data_ptr(), dg.data_ptr(), None)
+
+    if args.profile:
+        S = make(VVGPU_FP32 if args.precision == "fp32" else VVGPU_FP64)
+        for _ in range(max(args.warmup, 1)):
+            restore(S)
+            hot_path(S, wl, mn, mx)
+        restore(S)
+        torch.cuda.synchronize()
+        st0 = S.stats()
+        torch.cuda.profiler.start()
+        hot_path(S, wl, mn, mx)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        st1 = S.stats()
+        print(json.dumps({"profiled_step": args.precision, "vortices": N,
+                          "kernels": int(st1["launches"] - st0["launches"])}), flush=True)
+        S.close()
+        return
 
     def barrier():
         if dist is not None:

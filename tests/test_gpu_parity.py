@@ -7,7 +7,8 @@
   reference, see test_oracle_pin.py).
 
 Tolerances (per-vortex relative error with a floor of 1e-3 rms, parity.rel_err_vec):
-  FP64 path: convective 1e-12, diffusive 1e-11, friction 1e-10, SLAE cells/rhs 1e-12.
+  FP64 path: convective 1e-12, diffusive 1e-11, friction 1e-10, SLAE cells 1e-12, right-hand
+  side 1e-11 (a sum of ~1e3 logarithms in a different order), solution 1e-10.
   FP32 path: convective 1e-5, diffusive 1e-5, friction 1e-5 (wall terms are FP64).
 """
 import os

@@ -159,74 +159,98 @@ __global__ void __launch_bounds__(CW * 32) k_conv64(ConvArgs a) {
     }
 }
 
-template <int TC>
-__global__ void __launch_bounds__(CW * 32) k_conv32(ConvArgs a) {
+// FP32 near field.  Eight targets per lane.  A leaf with at most 8 targets uses all 32
+// lanes over its sources; with 9..16 targets each half-warp takes 8 targets and strides
+// over the sources by 16 (larger leaves loop in groups of 16).  Each lane keeps plain FP32
+// partial sums for up to 16 sources and then folds them into a TwoSum-compensated pair.
+constexpr int TC32 = 8;
+
+__global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
     const int64_t L = (int64_t)blockIdx.x * CW + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (L >= a.nl) return;
     const double4 me = a.lgeom[L];
     const double4 tc = a.taylor[L];
-    const double t1 = tc.x, t2 = tc.y, t3 = tc.z, t4 = tc.w;
     const int2 kL = a.anchor[L];
     const double axL = (double)kL.x * a.G, ayL = (double)kL.y * a.G;
     const int32_t v0 = a.lvf[L], v1 = a.lvl[L];
     const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
-    for (int32_t c0 = v0; c0 < v1; c0 += TC) {
-        float tx[TC], ty[TC], hx[TC], hy[TC], lx[TC], ly[TC];
+    for (int32_t c0 = v0; c0 < v1; c0 += 2 * TC32) {
+        const int32_t nt = min(v1 - c0, 2 * TC32);
+        const bool split = nt > TC32;                 // two groups of 8 targets
+        const int half = split ? (lane >> 4) : 0;
+        const int sub = split ? (lane & 15) : lane;   // lane index within the source stride
+        const int stride = split ? 16 : 32;
+        const int32_t t0 = c0 + half * TC32;
+        float tx[TC32], ty[TC32], hx[TC32], hy[TC32], lx[TC32], ly[TC32], px[TC32], py[TC32];
 #pragma unroll
-        for (int t = 0; t < TC; t++) {
-            int32_t i = c0 + t;
-            tx[t] = (i < v1) ? (float)(a.x[i] - axL) : 0.f;
-            ty[t] = (i < v1) ? (float)(a.y[i] - ayL) : 0.f;
-            hx[t] = hy[t] = lx[t] = ly[t] = 0.f;
+        for (int t = 0; t < TC32; t++) {
+            const int32_t i = t0 + t;
+            const bool ok = i < c0 + nt;
+            tx[t] = ok ? (float)(a.x[i] - axL) : 0.f;
+            ty[t] = ok ? (float)(a.y[i] - ayL) : 0.f;
+            hx[t] = hy[t] = lx[t] = ly[t] = px[t] = py[t] = 0.f;
         }
+        int since = 0;
         for (int32_t r = r0; r < r1; r++) {
-            int2 run = a.near_run[r];
-            int32_t j0 = a.lvf[run.x], j1 = a.lvl[run.y - 1];
-            float px[TC], py[TC];
+            const int2 run = a.near_run[r];
+            const int32_t j0 = a.lvf[run.x], j1 = a.lvl[run.y - 1];
+            for (int32_t j = j0 + sub; j < j1; j += stride) {
+                const float4 s4 = a.src32[j];
+                const int2 k = a.src_k[j];
+                const float sx = s4.x + (float)(k.x - kL.x) * a.Gf;
+                const float sy = s4.y + (float)(k.y - kL.y) * a.Gf;
 #pragma unroll
-            for (int t = 0; t < TC; t++) { px[t] = 0.f; py[t] = 0.f; }
-            for (int32_t j = j0 + lane; j < j1; j += 32) {
-                float4 s = a.src32[j];
-                int2 k = a.src_k[j];
-                float sx = s.x + (float)(k.x - kL.x) * a.Gf;
-                float sy = s.y + (float)(k.y - kL.y) * a.Gf;
-#pragma unroll
-                for (int t = 0; t < TC; t++) {
-                    float dx = tx[t] - sx, dy = ty[t] - sy;
-                    float q = s.z * rcp32(fmaf(dx, dx, fmaf(dy, dy, s.w)));
+                for (int t = 0; t < TC32; t++) {
+                    const float dx = tx[t] - sx, dy = ty[t] - sy;
+                    const float q = s4.z * rcp32(fmaf(dx, dx, fmaf(dy, dy, s4.w)));
                     px[t] = fmaf(-dy, q, px[t]);
                     py[t] = fmaf(dx, q, py[t]);
                 }
-            }
+                if (++since == 16) {
+                    since = 0;
 #pragma unroll
-            for (int t = 0; t < TC; t++) {
-                float s, e;
-                two_sum(hx[t], px[t], s, e); hx[t] = s; lx[t] += e;
-                two_sum(hy[t], py[t], s, e); hy[t] = s; ly[t] += e;
+                    for (int t = 0; t < TC32; t++) {
+                        float sv, e;
+                        two_sum(hx[t], px[t], sv, e); hx[t] = sv; lx[t] += e; px[t] = 0.f;
+                        two_sum(hy[t], py[t], sv, e); hy[t] = sv; ly[t] += e; py[t] = 0.f;
+                    }
+                }
             }
         }
-        double ax[TC], ay[TC];
+        double ax[TC32], ay[TC32];
 #pragma unroll
-        for (int t = 0; t < TC; t++) {
-            ax[t] = warp_sum((double)hx[t] + (double)lx[t]);
-            ay[t] = warp_sum((double)hy[t] + (double)ly[t]);
+        for (int t = 0; t < TC32; t++) {
+            float sv, e;
+            two_sum(hx[t], px[t], sv, e); lx[t] += e; hx[t] = sv;
+            two_sum(hy[t], py[t], sv, e); ly[t] += e; hy[t] = sv;
+            ax[t] = (double)hx[t] + (double)lx[t];
+            ay[t] = (double)hy[t] + (double)ly[t];
+#pragma unroll
+            for (int o = 8; o > 0; o >>= 1) {
+                ax[t] += __shfl_xor_sync(0xffffffffu, ax[t], o);
+                ay[t] += __shfl_xor_sync(0xffffffffu, ay[t], o);
+            }
+            if (!split) {
+                ax[t] += __shfl_xor_sync(0xffffffffu, ax[t], 16);
+                ay[t] += __shfl_xor_sync(0xffffffffu, ay[t], 16);
+            }
         }
 #pragma unroll
-        for (int t = 0; t < TC; t++) {
-            int32_t i = c0 + t;
-            if (lane == t && i < v1 && a.g[i] != 0.) {
-                double pxd = a.x[i], pyd = a.y[i];
+        for (int t = 0; t < TC32; t++) {
+            const int32_t i = t0 + t;
+            if (sub == t && i < c0 + nt && a.g[i] != 0.) {
+                const double pxd = a.x[i], pyd = a.y[i];
                 double ex, ey;
                 extra_terms(a, pxd, pyd, ex, ey);
-                double dlx = pxd - me.x, dly = pyd - me.y;
+                const double dlx = pxd - me.x, dly = pyd - me.y;
                 double vx = a.vx[i], vy = a.vy[i];
                 vx += a.inf_vx; vy += a.inf_vy;
                 vx += ax[t] * C_1_2PI; vy += ay[t] * C_1_2PI;
                 vx += ex; vy += ey;
-                vx += t1; vy += t2;
-                vx += t3 * dlx + t4 * dly;
-                vy += t4 * dlx + (-t3) * dly;
+                vx += tc.x; vy += tc.y;
+                vx += tc.z * dlx + tc.w * dly;
+                vy += tc.w * dlx + (-tc.z) * dly;
                 a.vx[i] = vx; a.vy[i] = vy;
             }
         }
@@ -420,7 +444,7 @@ void convective(Ctx& c) {
     if (c.precision == VVGPU_FP32) {
         build_frames(c);
         a.src32 = c.src32.p; a.src_k = c.src_k.p; a.anchor = c.lf_anchor.p; a.G = c.frame_G; a.Gf = (float)c.frame_G;
-        k_conv32<16><<<grid, CW * 32, 0, s>>>(a);
+        k_conv32<<<grid, CW * 32, 0, s>>>(a);
     } else {
         k_conv64<8><<<grid, CW * 32, 0, s>>>(a);
     }

@@ -24,8 +24,8 @@ __global__ void k_shed_append(int64_t m, int64_t n0, const int32_t* __restrict__
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= m || !flags[s]) return;
     int64_t i = n0 + pos[s];
-    x[i] = cx[s] + (-dly[s]) * 1e-4;
-    y[i] = cy[s] + dlx[s] * 1e-4;
+    x[i] = dadd(cx[s], dmul(-dly[s], 1e-4));  // corner + rotl(dl) * 1e-4, two roundings
+    y[i] = dadd(cy[s], dmul(dlx[s], 1e-4));
     g[i] = sg[s];
     ie[i] = 0.;
     vx[i] = 0.;
