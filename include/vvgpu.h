@@ -133,6 +133,12 @@ int vvgpu_set_params(vvgpu_ctx* ctx, double re, double dt, double inf_vx, double
 int vvgpu_add_body(vvgpu_ctx* ctx, int64_t nseg, const double* corner_x, const double* corner_y,
                    const uint32_t* slip, const vvgpu_body_params* params);
 int vvgpu_set_segment_g(vvgpu_ctx* ctx, const double* g);
+/* Per-segment state TAtt::g, fric, gsum (any pointer may be NULL = keep). */
+int vvgpu_set_segment_state(vvgpu_ctx* ctx, const double* g, const double* fric, const double* gsum);
+/* Removes all bodies (before re-adding bodies whose geometry changed). */
+int vvgpu_clear_bodies(vvgpu_ctx* ctx);
+/* Updates the parameters of body b (time functions evaluated at the current time). */
+int vvgpu_set_body_params(vvgpu_ctx* ctx, int body, const vvgpu_body_params* params);
 int vvgpu_set_sinks(vvgpu_ctx* ctx, int64_t n, const double* x, const double* y, const double* g);
 /* Replaces the vortex list (v = 0).  inv_eps may be NULL (= 0, a freshly loaded list). */
 int vvgpu_set_vortices(vvgpu_ctx* ctx, int64_t n, const double* x, const double* y,
@@ -140,6 +146,8 @@ int vvgpu_set_vortices(vvgpu_ctx* ctx, int64_t n, const double* x, const double*
 /* Same with device pointers (data already resident in HBM on the context's device). */
 int vvgpu_set_vortices_device(vvgpu_ctx* ctx, int64_t n, const double* x, const double* y,
                               const double* g, const double* inv_eps);
+/* Sets TObj::v of the current list (the reference accumulates into v). */
+int vvgpu_set_velocities(vvgpu_ctx* ctx, const double* vx, const double* vy);
 int64_t vvgpu_num_vortices(const vvgpu_ctx* ctx);
 int64_t vvgpu_num_segments(const vvgpu_ctx* ctx);
 /* Copies the vortex list back to host memory; any pointer may be NULL. */

@@ -166,7 +166,9 @@ __global__ void __launch_bounds__(CW * 32) k_conv64(ConvArgs a) {
 constexpr int TC32 = 8;
 
 __global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
-    const int64_t L = (int64_t)blockIdx.x * CW + (threadIdx.x >> 5);
+    __shared__ int2 s_runs[CW][32];
+    const int wq = threadIdx.x >> 5;
+    const int64_t L = (int64_t)blockIdx.x * CW + wq;
     const int lane = threadIdx.x & 31;
     if (L >= a.nl) return;
     const double4 me = a.lgeom[L];
@@ -192,14 +194,39 @@ __global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
             hx[t] = hy[t] = lx[t] = ly[t] = px[t] = py[t] = 0.f;
         }
         int since = 0;
-        for (int32_t r = r0; r < r1; r++) {
-            const int2 run = a.near_run[r];
-            const int32_t j0 = a.lvf[run.x], j1 = a.lvl[run.y - 1];
-            for (int32_t j = j0 + sub; j < j1; j += stride) {
+        // near runs in groups of 32: one lane resolves each run's vortex range, then the
+        // group's sources are walked as one flattened sequence (no per-run bubbles)
+        for (int32_t rb = r0; rb < r1; rb += 32) {
+            const int32_t rr = rb + lane;
+            int32_t j0 = 0, len = 0;
+            if (rr < r1) {
+                const int2 run = a.near_run[rr];
+                j0 = a.lvf[run.x];
+                len = a.lvl[run.y - 1] - j0;
+            }
+            int32_t incl = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            const int32_t nrun = min(32, r1 - rb);
+            s_runs[wq][lane] = make_int2(incl - len, j0);
+            __syncwarp();
+            int cur = 0;
+            int32_t nextb = (nrun > 1) ? s_runs[wq][1].x : total;
+            for (int32_t k = sub; k < total; k += stride) {
+                while (k >= nextb) {
+                    cur++;
+                    nextb = (cur + 1 < nrun) ? s_runs[wq][cur + 1].x : total;
+                }
+                const int2 rc = s_runs[wq][cur];
+                const int32_t j = rc.y + (k - rc.x);
                 const float4 s4 = a.src32[j];
-                const int2 k = a.src_k[j];
-                const float sx = s4.x + (float)(k.x - kL.x) * a.Gf;
-                const float sy = s4.y + (float)(k.y - kL.y) * a.Gf;
+                const int2 kk = a.src_k[j];
+                const float sx = s4.x + (float)(kk.x - kL.x) * a.Gf;
+                const float sy = s4.y + (float)(kk.y - kL.y) * a.Gf;
 #pragma unroll
                 for (int t = 0; t < TC32; t++) {
                     const float dx = tx[t] - sx, dy = ty[t] - sy;
@@ -217,6 +244,7 @@ __global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
                     }
                 }
             }
+            __syncwarp();
         }
         double ax[TC32], ay[TC32];
 #pragma unroll

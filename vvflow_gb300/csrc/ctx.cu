@@ -276,6 +276,48 @@ int vvgpu_set_segment_g(vvgpu_ctx* h, const double* g) {
     API_END
 }
 
+int vvgpu_set_segment_state(vvgpu_ctx* h, const double* g, const double* fric, const double* gsum) {
+    API_BEGIN(h)
+    cudaStream_t s = c.st();
+    if (c.m) {
+        if (g) VV_CUDA(cudaMemcpyAsync(c.s_g.p, g, c.m * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (fric) VV_CUDA(cudaMemcpyAsync(c.s_fric.p, fric, c.m * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (gsum) VV_CUDA(cudaMemcpyAsync(c.s_gsum.p, gsum, c.m * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    VV_CUDA(cudaStreamSynchronize(s));
+    API_END
+}
+
+int vvgpu_clear_bodies(vvgpu_ctx* h) {
+    API_BEGIN(h)
+    if (c.built) throw ApiError{VVGPU_ERR_STATE, "cannot clear bodies while the tree is built"};
+    c.bodies.clear();
+    c.m = 0;
+    for (auto* v : {&c.h_cx, &c.h_cy, &c.h_rx, &c.h_ry, &c.h_dlx, &c.h_dly, &c.h_sie}) v->clear();
+    c.h_slip.clear();
+    c.segs_dirty = true;
+    c.lu_valid = false;
+    API_END
+}
+
+int vvgpu_set_body_params(vvgpu_ctx* h, int body, const vvgpu_body_params* params) {
+    API_BEGIN(h)
+    if (body < 0 || body >= (int)c.bodies.size() || !params) throw ApiError{VVGPU_ERR_ARG, "no such body"};
+    c.bodies[body].p = *params;
+    API_END
+}
+
+int vvgpu_set_velocities(vvgpu_ctx* h, const double* vx, const double* vy) {
+    API_BEGIN(h)
+    if (c.n && (!vx || !vy)) throw ApiError{VVGPU_ERR_ARG, "null pointer"};
+    if (c.n) {
+        VV_CUDA(cudaMemcpyAsync(c.vx.p, vx, c.n * sizeof(double), cudaMemcpyHostToDevice, c.st()));
+        VV_CUDA(cudaMemcpyAsync(c.vy.p, vy, c.n * sizeof(double), cudaMemcpyHostToDevice, c.st()));
+    }
+    VV_CUDA(cudaStreamSynchronize(c.st()));
+    API_END
+}
+
 int vvgpu_set_sinks(vvgpu_ctx* h, int64_t n, const double* x, const double* y, const double* g) {
     API_BEGIN(h)
     if (n < 0 || (n && (!x || !y || !g))) throw ApiError{VVGPU_ERR_ARG, "bad sink arrays"};

@@ -8,7 +8,8 @@
 // reference, so whole near leaves farther than 8 eps from all targets of a leaf are
 // skipped: the warp tests boxes once per (target leaf, near leaf) in FP32 with a margin.
 //
-// One warp per target leaf, a lane per target.  FP64 path: every pair in double precision
+// One warp per target leaf: eight target slots times four source lanes.  FP64 path: every
+// pair in double precision
 // with the reference's formulas.  FP32 path: vortex pairs in local frames (frame.cuh) with
 // FP32 exp/sqrt; pairs whose cut-off or coincidence test falls within a margin of its
 // threshold are re-evaluated in FP64 so the set of contributing pairs is the reference's.
@@ -75,30 +76,34 @@ __device__ __forceinline__ void vortex_term64(double xi, double yi, double gi, d
     s1 += t;
 }
 
+// Warp per target leaf.  Lane = target slot (lane & 7) x source lane (lane >> 3): eight
+// targets per pass, the four source lanes split each candidate leaf's vortices.  Candidate
+// leaves come from a lane-parallel box test against the targets' box grown by 8 eps.
 template <bool FP32>
 __global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
     const int64_t L = (int64_t)blockIdx.x * DW + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
+    const int ts = lane & 7, sl = lane >> 3;
     if (L >= a.nl) return;
     const int2 kL = a.anchor[L];
     const double axL = (double)kL.x * a.G, ayL = (double)kL.y * a.G;
     const int32_t v0 = a.lvf[L], v1 = a.lvl[L];
     const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
     unsigned long long ncand = 0;
-    for (int32_t c0 = v0; c0 < v1; c0 += 32) {
-        const int32_t i = c0 + lane;
+    for (int32_t c0 = v0; c0 < v1; c0 += 8) {
+        const int32_t i = c0 + ts;
         const bool act = (i < v1) && (a.g[i] != 0.);
         double xi = 0, yi = 0, gi = 0, ie = 0;
-        float txf = 0, tyf = 0, ief = 0, sgi = 0;
-        float reach = 0.f;  // 8 eps in FP32 with margin
+        float txf = 0, tyf = 0, ief = 0;
+        bool pos = false;
+        float reach = 0.f;
         if (act) {
             xi = a.x[i]; yi = a.y[i]; gi = a.g[i]; ie = a.ie[i];
             txf = (float)(xi - axL); tyf = (float)(yi - ayL);
             ief = (float)ie;
-            sgi = (float)dsgn(gi);
+            pos = gi > 0;
             reach = (float)(8.0 / ie) * (1.f + 1e-4f);
         }
-        // warp box of active targets and the largest reach
         float bx0 = act ? txf : INFINITY, by0 = act ? tyf : INFINITY;
         float bx1 = act ? txf : -INFINITY, by1 = act ? tyf : -INFINITY;
         float rmax = reach;
@@ -110,22 +115,21 @@ __global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
             by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
             rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
         }
-        if (!(bx0 <= bx1)) continue;  // no active target in this chunk
+        if (!(bx0 <= bx1)) continue;  // no active target in this group (warp-uniform)
         const float pad = rmax + ldexpf(fabsf(bx0) + fabsf(bx1) + fabsf(by0) + fabsf(by1) + a.Gf, -16);
         double s2x = 0, s2y = 0, s3x = 0, s3y = 0, s1 = 0, s0 = 0;
         float f2x = 0, f2y = 0, f1 = 0, c2x = 0, c2y = 0, c1 = 0;
         for (int32_t r = r0; r < r1; r++) {
             const int2 run = a.near_run[r];
             for (int32_t qb = run.x; qb < run.y; qb += 32) {
-                // lane-parallel box test of up to 32 near leaves
-                int32_t q = qb + lane;
+                const int32_t q = qb + lane;
                 bool hit = false;
                 if (q < run.y) {
-                    float4 b = a.box[q];
+                    const float4 b = a.box[q];
                     if (b.x <= b.z) {
-                        float2 sh = frame_shift(a.anchor[q], kL, a.Gf);
-                        float dx = fmaxf(fmaxf(b.x + sh.x - bx1, bx0 - (b.z + sh.x)), 0.f);
-                        float dy = fmaxf(fmaxf(b.y + sh.y - by1, by0 - (b.w + sh.y)), 0.f);
+                        const float2 sh = frame_shift(a.anchor[q], kL, a.Gf);
+                        const float dx = fmaxf(fmaxf(b.x + sh.x - bx1, bx0 - (b.z + sh.x)), 0.f);
+                        const float dy = fmaxf(fmaxf(b.y + sh.y - by1, by0 - (b.w + sh.y)), 0.f);
                         hit = dx <= pad && dy <= pad && (dx * dx + dy * dy) <= pad * pad;
                     }
                 }
@@ -134,68 +138,75 @@ __global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
                     const int32_t qq = qb + __ffs(mask) - 1;
                     mask &= mask - 1;
                     const int32_t j0 = a.lvf[qq], j1 = a.lvl[qq];
-                    if (act) {
-                        ncand += (unsigned long long)(j1 - j0);
-                        if (FP32) {
-                            const float2 sh = frame_shift(a.anchor[qq], kL, a.Gf);
-                            float p2x = 0, p2y = 0, p1 = 0;
-                            for (int32_t j = j0; j < j1; j++) {
-                                const float4 s = a.src32[j];
-                                if (s.z == 0.f) continue;
-                                if ((s.z > 0.f) != (sgi > 0.f)) continue;
-                                const float dx = txf - (s.x + sh.x), dy = tyf - (s.y + sh.y);
-                                const float r2 = dx * dx + dy * dy;
-                                const float u = r2 * ief * ief;  // (|dr|/eps)^2
-                                const bool band = fabsf(u - 64.f) < 64.f * 1e-4f || (fabsf(dx) + fabsf(dy)) < 1e-8f;
-                                if (band) {
-                                    double ts2x = 0, ts2y = 0, ts1 = 0;
-                                    vortex_term64(xi, yi, gi, ie, a.x[j], a.y[j], a.g[j], ts2x, ts2y, ts1);
-                                    s2x += ts2x; s2y += ts2y; s1 += ts1;
-                                    continue;
-                                }
-                                if (u > 64.f) continue;
-                                const float dr = sqrtf(r2);
-                                const float t = s.z * __expf(-dr * ief);
-                                const float qv = t / dr;
-                                p2x = fmaf(dx, qv, p2x);
-                                p2y = fmaf(dy, qv, p2y);
-                                p1 += t;
+                    if (!act) continue;
+                    if (sl == 0) ncand += (unsigned long long)(j1 - j0);
+                    if (FP32) {
+                        const float2 sh = frame_shift(a.anchor[qq], kL, a.Gf);
+                        float p2x = 0, p2y = 0, p1 = 0;
+                        for (int32_t j = j0 + sl; j < j1; j += 4) {
+                            const float4 s4 = a.src32[j];
+                            if (s4.z == 0.f || ((s4.z > 0.f) != pos)) continue;
+                            const float dx = txf - (s4.x + sh.x), dy = tyf - (s4.y + sh.y);
+                            const float r2 = dx * dx + dy * dy;
+                            const float u = r2 * ief * ief;  // (|dr| / eps)^2
+                            if (fabsf(u - 64.f) < 64.f * 1e-4f || (fabsf(dx) + fabsf(dy)) < 1e-6f) {
+                                double ts2x = 0, ts2y = 0, ts1 = 0;
+                                vortex_term64(xi, yi, gi, ie, a.x[j], a.y[j], a.g[j], ts2x, ts2y, ts1);
+                                s2x += ts2x; s2y += ts2y; s1 += ts1;
+                                continue;
                             }
-                            float sv, e;
-                            sv = f2x + p2x; e = (f2x - sv) + p2x; f2x = sv; c2x += e;
-                            sv = f2y + p2y; e = (f2y - sv) + p2y; f2y = sv; c2y += e;
-                            sv = f1 + p1; e = (f1 - sv) + p1; f1 = sv; c1 += e;
-                        } else {
-                            for (int32_t j = j0; j < j1; j++) {
-                                const double gj = a.g[j];
-                                if (gj == 0.) continue;
-                                vortex_term64(xi, yi, gi, ie, a.x[j], a.y[j], gj, s2x, s2y, s1);
-                            }
+                            if (u > 64.f) continue;
+                            const float rs = rsqrtf(r2);
+                            const float t = s4.z * __expf(-(r2 * rs) * ief);
+                            const float qv = t * rs;
+                            p2x = fmaf(dx, qv, p2x);
+                            p2y = fmaf(dy, qv, p2y);
+                            p1 += t;
                         }
-                        // wall segments of this near leaf (segment_influence), FP64
-                        for (int32_t qs = a.lsf[qq]; qs < a.lsl[qq]; qs++) {
-                            const int32_t sgm = a.seg_order[qs];
-                            const double dx = xi - a.rx[sgm], dy = yi - a.ry[sgm];
-                            const double dr2 = dx * dx + dy * dy;
-                            const double dr = sqrt(dr2);
-                            const double ea = -dr * ie;
-                            if (ea < EXP_ARG_RESTRICTION) continue;
-                            const double ex = exp(ea);
-                            const double dsx = -a.dly[sgm], dsy = a.dlx[sgm];
-                            s3x += dsx * ex; s3y += dsy * ex;
-                            s0 += (dr * ie + 1) / dr2 * (dx * dsx + dy * dsy) * ex;
-                            atomicAdd(&a.fric[sgm], ie * ie * gi * ex * sqrt(dsx * dsx + dsy * dsy));
+                        float sv, e;
+                        sv = f2x + p2x; e = (f2x - sv) + p2x; f2x = sv; c2x += e;
+                        sv = f2y + p2y; e = (f2y - sv) + p2y; f2y = sv; c2y += e;
+                        sv = f1 + p1; e = (f1 - sv) + p1; f1 = sv; c1 += e;
+                    } else {
+                        for (int32_t j = j0 + sl; j < j1; j += 4) {
+                            const double gj = a.g[j];
+                            if (gj == 0.) continue;
+                            vortex_term64(xi, yi, gi, ie, a.x[j], a.y[j], gj, s2x, s2y, s1);
                         }
+                    }
+                    // wall segments of this near leaf (segment_influence), FP64, split over source lanes
+                    for (int32_t qs = a.lsf[qq] + sl; qs < a.lsl[qq]; qs += 4) {
+                        const int32_t sgm = a.seg_order[qs];
+                        const double dx = xi - a.rx[sgm], dy = yi - a.ry[sgm];
+                        const double dr2 = dx * dx + dy * dy;
+                        const double dr = sqrt(dr2);
+                        const double ea = -dr * ie;
+                        if (ea < EXP_ARG_RESTRICTION) continue;
+                        const double ex = exp(ea);
+                        const double dsx = -a.dly[sgm], dsy = a.dlx[sgm];
+                        s3x += dsx * ex; s3y += dsy * ex;
+                        s0 += (dr * ie + 1) / dr2 * (dx * dsx + dy * dsy) * ex;
+                        atomicAdd(&a.fric[sgm], ie * ie * gi * ex * sqrt(dsx * dsx + dsy * dsy));
                     }
                 }
             }
         }
-        if (act) {
-            if (FP32) {
-                s2x += (double)f2x + (double)c2x;
-                s2y += (double)f2y + (double)c2y;
-                s1 += (double)f1 + (double)c1;
-            }
+        if (FP32) {
+            s2x += (double)f2x + (double)c2x;
+            s2y += (double)f2y + (double)c2y;
+            s1 += (double)f1 + (double)c1;
+        }
+        // combine the four source lanes of each target slot
+#pragma unroll
+        for (int o = 8; o < 32; o <<= 1) {
+            s2x += __shfl_xor_sync(0xffffffffu, s2x, o);
+            s2y += __shfl_xor_sync(0xffffffffu, s2y, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+            s3x += __shfl_xor_sync(0xffffffffu, s3x, o);
+            s3y += __shfl_xor_sync(0xffffffffu, s3y, o);
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        }
+        if (act && sl == 0) {
             if ((dsgn(s1) != dsgn(gi)) || (fabs(s1) < fabs(0.1 * gi))) s1 = 0.1 * gi;
             double f = ie / (a.re * s1);
             double vx = a.vx[i] + s2x * f, vy = a.vy[i] + s2y * f;

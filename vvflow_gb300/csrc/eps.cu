@@ -15,9 +15,9 @@
 //
 // Candidate leaves: for each target leaf L, R_L bounds every target's second-nearest
 // distance from above (the farthest corner distance to a leaf that holds two live
-// vortices, or three for L itself); only near leaves whose box comes within 2 R_L of L's
-// box can hold a top-two candidate (2 R_L also covers the re-search from a merged
-// position, which lies within R_L of the original one).
+// vortices, or three for L itself); only near leaves whose box comes within 3 R_L of L's
+// box can hold a top-two candidate of the search or of the re-search from a merged
+// position (see k_eps_cand).
 //
 // The two-nearest search filters candidates in FP32 in local frames (frame.cuh) with a
 // rigorous margin and evaluates only the candidates inside the margin in FP64, with the
@@ -137,63 +137,91 @@ __global__ void k_eps_box(int64_t nl, const int32_t* __restrict__ lvf, const int
     live[L] = nlive;
 }
 
-// Candidate leaves of every target leaf (one warp per target leaf).  Also the extent of
-// the candidate region in L's frame (bounds every FP32 coordinate the search forms).
+// Candidate leaves of every target leaf (one warp per target leaf).
+//
+// R_L bounds every target's second-nearest distance from above: the farthest-corner
+// distance between L's box and a leaf holding two live vortices (three for L itself, which
+// contains the target; then R_L is L's own diagonal).  The first search of a target needs
+// only candidates within R_L of it.  The list keeps near leaves within 2 R_L of L's box and
+// remembers that radius; in later rounds it stays valid while R_L (now) plus the largest
+// merge displacement fits inside it (boxes only grow by merged positions), otherwise it is
+// rebuilt.  The re-search after a merge (from a point up to R_L away) walks the whole near
+// list instead.  The warp also marks L dirty when a candidate leaf changed in the last
+// round, and records the extents of the list and of the near region in L's frame.
 __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, const int2* __restrict__ near_run,
                            const int2* __restrict__ anchor, const float4* __restrict__ box,
                            const int32_t* __restrict__ live, float Gf, int32_t* cand, int32_t* ncand, float* rn,
-                           const int32_t* __restrict__ leaf_changed, int32_t* dirty, int first_round) {
+                           float* rlist, float* rnear, const int32_t* __restrict__ leaf_changed, int32_t* dirty,
+                           int first_round, const float* __restrict__ dmax_p) {
     const int64_t L = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (L >= nl) return;
     const float4 bL = box[L];
     const int2 aL = anchor[L];
     const int32_t r0 = near_off[L], r1 = near_off[L + 1];
-    // pass A: upper bound on every target's second-nearest distance
+    const float dmax = first_round ? 0.f : *dmax_p;
+    // upper bound on every target's second-nearest distance (squared)
     float R2 = INFINITY;
     if (bL.x <= bL.z) {
-        for (int32_t r = r0; r < r1; r++) {
-            int2 run = near_run[r];
-            for (int32_t q = run.x + lane; q < run.y; q += 32) {
-                int need = (q == L) ? 3 : 2;
-                if (live[q] < need) continue;
-                float4 b = box[q];
-                float2 sh = frame_shift(anchor[q], aL, Gf);
-                float ux = fmaxf(fabsf(b.z + sh.x - bL.x), fabsf(bL.z - (b.x + sh.x)));
-                float uy = fmaxf(fabsf(b.w + sh.y - bL.y), fabsf(bL.w - (b.y + sh.y)));
-                R2 = fminf(R2, ux * ux + uy * uy);
+        if (live[L] >= 3) {
+            const float ux = bL.z - bL.x, uy = bL.w - bL.y;
+            R2 = ux * ux + uy * uy;
+        } else {
+            for (int32_t r = r0; r < r1; r++) {
+                const int2 run = near_run[r];
+                for (int32_t q = run.x + lane; q < run.y; q += 32) {
+                    const int need = (q == L) ? 3 : 2;
+                    if (live[q] < need) continue;
+                    const float4 b = box[q];
+                    const float2 sh = frame_shift(anchor[q], aL, Gf);
+                    const float ux = fmaxf(fabsf(b.z + sh.x - bL.x), fabsf(bL.z - (b.x + sh.x)));
+                    const float uy = fmaxf(fabsf(b.w + sh.y - bL.y), fabsf(bL.w - (b.y + sh.y)));
+                    R2 = fminf(R2, ux * ux + uy * uy);
+                }
             }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) R2 = fminf(R2, __shfl_xor_sync(0xffffffffu, R2, o));
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) R2 = fminf(R2, __shfl_xor_sync(0xffffffffu, R2, o));
-    // pass B: near leaves within 2 R_L (FP32 with a relative and an absolute margin)
-    float ext = 0.f;
-    int32_t cnt = 0;
-    bool overflow = false;
+    const float absm = ldexpf(fabsf(bL.x) + fabsf(bL.z) + fabsf(bL.y) + fabsf(bL.w) + Gf, -12);
+    const float need_r = isfinite(R2) ? sqrtf(R2) * (1.f + 1e-4f) + dmax + absm : INFINITY;
+    const int32_t nc_old = first_round ? -2 : ncand[L];
+    const bool reuse = !first_round && nc_old >= 0 && need_r <= rlist[L];
     bool is_dirty = first_round != 0;
-    const float lim = isfinite(R2) ? 2.f * sqrtf(R2) * (1.f + 1e-4f) : INFINITY;
+    if (reuse) {
+        const int32_t* cl = cand + (size_t)L * CAND_CAP;
+        bool d = false;
+        for (int32_t k = lane; k < nc_old; k += 32) d = d || leaf_changed[cl[k]];
+        is_dirty = __any_sync(0xffffffffu, d);
+        if (lane == 0) dirty[L] = is_dirty ? 1 : 0;
+        return;
+    }
+    // (re)build: near leaves within 2 R_L of L's box (FP32 with margins)
+    const float lim = isfinite(R2) ? 2.f * sqrtf(R2) * (1.f + 1e-4f) + absm : INFINITY;
+    float ext = 0.f, next = 0.f;
+    int32_t cnt = 0;
     for (int32_t r = r0; r < r1; r++) {
-        int2 run = near_run[r];
+        const int2 run = near_run[r];
         for (int32_t qb = run.x; qb < run.y; qb += 32) {
-            int32_t q = qb + lane;
+            const int32_t q = qb + lane;
             bool hit = false;
             float e = 0.f;
             if (q < run.y) {
-                float4 b = box[q];
+                const float4 b = box[q];
                 if (b.x <= b.z) {
-                    float2 sh = frame_shift(anchor[q], aL, Gf);
-                    float bx0 = b.x + sh.x, bx1 = b.z + sh.x, by0 = b.y + sh.y, by1 = b.w + sh.y;
-                    float dx = fmaxf(fmaxf(bx0 - bL.z, bL.x - bx1), 0.f);
-                    float dy = fmaxf(fmaxf(by0 - bL.w, bL.y - by1), 0.f);
-                    float pad = lim + ldexpf(fabsf(bx0) + fabsf(bx1) + fabsf(by0) + fabsf(by1) + Gf, -14);
-                    hit = (dx <= pad && dy <= pad && dx * dx + dy * dy <= pad * pad) || !isfinite(lim);
-                    if (hit) e = fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)), fmaxf(fabsf(by0), fabsf(by1)));
+                    const float2 sh = frame_shift(anchor[q], aL, Gf);
+                    const float bx0 = b.x + sh.x, bx1 = b.z + sh.x, by0 = b.y + sh.y, by1 = b.w + sh.y;
+                    const float dx = fmaxf(fmaxf(bx0 - bL.z, bL.x - bx1), 0.f);
+                    const float dy = fmaxf(fmaxf(by0 - bL.w, bL.y - by1), 0.f);
+                    hit = !isfinite(lim) || (dx <= lim && dy <= lim && dx * dx + dy * dy <= lim * lim);
+                    e = fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)), fmaxf(fabsf(by0), fabsf(by1)));
+                    next = fmaxf(next, e);
+                    if (!hit) e = 0.f;
                 }
             }
-            unsigned mask = __ballot_sync(0xffffffffu, hit);
+            const unsigned mask = __ballot_sync(0xffffffffu, hit);
             if (hit) {
-                int pos = cnt + __popc(mask & ((1u << lane) - 1));
+                const int pos = cnt + __popc(mask & ((1u << lane) - 1));
                 if (pos < CAND_CAP) cand[(size_t)L * CAND_CAP + pos] = q;
                 if (!first_round && leaf_changed[q]) is_dirty = true;
             }
@@ -201,15 +229,19 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
             ext = fmaxf(ext, e);
         }
     }
-    if (cnt > CAND_CAP) overflow = true;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
+        next = fmaxf(next, __shfl_xor_sync(0xffffffffu, next, o));
         is_dirty = __shfl_xor_sync(0xffffffffu, (int)is_dirty, o) || is_dirty;
     }
     if (lane == 0) {
-        ncand[L] = overflow ? -1 : cnt;  // -1: use the whole near list
-        rn[L] = ext + fmaxf(fmaxf(fabsf(bL.x), fabsf(bL.z)), fmaxf(fabsf(bL.y), fabsf(bL.w)));
+        ncand[L] = (cnt > CAND_CAP) ? -1 : cnt;  // -1: use the whole near list
+        rlist[L] = (cnt > CAND_CAP) ? -1.f : lim;
+        // extents of the coordinates the searches form in L's frame
+        const float own = fmaxf(fmaxf(fabsf(bL.x), fabsf(bL.z)), fmaxf(fabsf(bL.y), fabsf(bL.w)));
+        rn[L] = fmaxf(ext, own + (isfinite(lim) ? lim : 0.f));
+        if (first_round) rnear[L] = fmaxf(next, own);
         dirty[L] = is_dirty ? 1 : 0;
     }
 }
@@ -228,7 +260,7 @@ __device__ __forceinline__ void top2_push(Top2& t, double d, int32_t j) {
 
 struct EpsView {
     const int32_t* lvf; const int32_t* lvl;
-    const int2* anchor; const float4* box; const float* rn;
+    const int2* anchor; const float4* box; const float* rn; const float* rnear; const float* dmax;
     const int32_t* near_off; const int2* near_run;
     const int32_t* cand; const int32_t* ncand;
     const float4* rec0; const float4* recO;
@@ -298,13 +330,15 @@ __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, int2 aL, 
 
 // Two nearest live candidates of target i (at exact position px,py) among leaf L's
 // candidate leaves, excluding slot excl.  Returns the exact FP64 top-2 of the reference.
-__device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl, double px, double py) {
+__device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl, double px, double py,
+                            bool use_list) {
     const int2 aL = v.anchor[L];
     const float tx = (float)(px - (double)aL.x * v.G), ty = (float)(py - (double)aL.y * v.G);
-    const float D = ldexpf(v.rn[L] + fabsf(tx) + fabsf(ty) + v.Gf, -17);
+    const float ext = (use_list ? v.rn[L] : v.rnear[L]) + *v.dmax;
+    const float D = ldexpf(ext + fabsf(tx) + fabsf(ty) + v.Gf, -17);
     float t1 = INFINITY, t2 = INFINITY, thr = INFINITY;
     Top2 best{DBL_MAX, DBL_MAX, INT_MAX, INT_MAX};
-    const int32_t nc = v.ncand[L];
+    const int32_t nc = use_list ? v.ncand[L] : -1;
     // pass 0: FP32 second-smallest distance; pass 1: exact top-2 within the margin
 #pragma unroll 1
     for (int pass = 0; pass < 2; pass++) {
@@ -352,7 +386,7 @@ __global__ void k_eps_round(int64_t n, EpsView v, const int32_t* __restrict__ le
     double px = v.x0[i], py = v.y0[i], gi = gi0, ie = ie_in[i];
     if (gi0 != 0 && !(v.zb[i] < i)) {
         const double mcs = mcs_l[L];
-        Top2 t = two_nearest(v, L, i, -1, px, py);
+        Top2 t = two_nearest(v, L, i, -1, px, py, true);
         double e;
         partner = -1;
         if (t.l1 == INT_MAX) e = DBL_MIN;
@@ -376,7 +410,7 @@ __global__ void k_eps_round(int64_t n, EpsView v, const int32_t* __restrict__ le
                 }
                 gi = dadd(gi, g1);
                 partner = t.l1;
-                Top2 u = two_nearest(v, L, i, t.l1, px, py);
+                Top2 u = two_nearest(v, L, i, t.l1, px, py, false);
                 if (u.l1 == INT_MAX) e = DBL_MIN;
                 else if (u.l2 == INT_MAX) e = __dsqrt_rn(u.r1);
                 else e = __dsqrt_rn(u.r2);
@@ -403,7 +437,9 @@ __global__ void k_zb_reset(int64_t n, const int32_t* __restrict__ zb, int32_t* z
 
 __global__ void k_zb_scatter(int64_t n, const int32_t* __restrict__ partner, const int32_t* __restrict__ leaf_of,
                              const int2* __restrict__ anchor, double G, const double* __restrict__ ox,
-                             const double* __restrict__ oy, const double* __restrict__ og, int32_t* zb, float4* recO) {
+                             const double* __restrict__ oy, const double* __restrict__ og,
+                             const double* __restrict__ x0, const double* __restrict__ y0, int32_t* zb, float4* recO,
+                             int32_t* dmax_bits) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int32_t p = partner[i];
@@ -411,6 +447,9 @@ __global__ void k_zb_scatter(int64_t n, const int32_t* __restrict__ partner, con
         atomicMin(&zb[p], (int32_t)i);
         int2 a = anchor[leaf_of[i]];
         recO[i] = make_float4(rel(ox[i], a.x, G), rel(oy[i], a.y, G), (float)dsgn(og[i]), 0.f);
+        // displacement of the merged position (rounded up), for the candidate-list check
+        float d = (float)(fabs(ox[i] - x0[i]) + fabs(oy[i] - y0[i])) * (1.f + 1e-5f);
+        atomicMax(dmax_bits, __float_as_int(d));
     }
 }
 
@@ -507,6 +546,10 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
     int cur = 0;
     int64_t rounds = 0;
     const int64_t max_rounds = 4096;
+    c.e_rlist.reserve(nl + 1);
+    c.e_rnear.reserve(nl + 1);
+    int32_t* dmax_bits = (int32_t*)(c.counters.p + 13);
+    VV_CUDA(cudaMemsetAsync(dmax_bits, 0, 4, s));
     for (;;) {
         rounds++;
         // boxes and candidate leaves from the current guesses
@@ -515,10 +558,12 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
         VV_LAUNCH_CHECK();
         k_eps_cand<<<grid_for(nl, EB / 32), EB, 0, s>>>(nl, c.near_off.p, c.near_run.p, c.lf_anchor.p,
                                                        c.lf_box32.p, c.e_live.p, fr.Gf, c.e_cand.p, c.e_ncand.p,
-                                                       c.lf_rn.p, c.e_lchanged.p, c.e_dirty.p, rounds == 1);
+                                                       c.lf_rn.p, c.e_rlist.p, c.e_rnear.p, c.e_lchanged.p,
+                                                       c.e_dirty.p, rounds == 1, (const float*)dmax_bits);
         VV_LAUNCH_CHECK();
         VV_CUDA(cudaMemsetAsync(c.e_changed.p, 0, 4, s));
-        EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.near_off.p, c.near_run.p,
+        EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.e_rnear.p,
+                  (const float*)dmax_bits, c.near_off.p, c.near_run.p,
                   c.e_cand.p, c.e_ncand.p, c.e_rec0.p, c.e_recO.p, c.e_x0.p, c.e_y0.p, c.e_g0.p,
                   c.e_partner[cur].p, c.e_zb.p, c.e_ox[cur].p, c.e_oy[cur].p, c.e_og[cur].p, fr.G, fr.Gf};
         const int nx = cur ^ 1;
@@ -529,9 +574,10 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
         // new absorber table and merged records; leaves whose members changed
         k_zb_reset<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_zb.p, c.e_zb_prev.p, c.e_zb.p);
         VV_LAUNCH_CHECK();
+        VV_CUDA(cudaMemsetAsync(dmax_bits, 0, 4, s));
         k_zb_scatter<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_partner[nx].p, c.leaf_of.p, c.lf_anchor.p, fr.G,
-                                                    c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_zb.p,
-                                                    c.e_recO.p);
+                                                    c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_x0.p, c.e_y0.p,
+                                                    c.e_zb.p, c.e_recO.p, dmax_bits);
         VV_LAUNCH_CHECK();
         VV_CUDA(cudaMemsetAsync(c.e_lchanged.p, 0, (nl + 1) * 4, s));
         k_leaf_changed<<<grid_for(n, EB), EB, 0, s>>>(n, c.leaf_of.p, c.e_partner[cur].p, c.e_partner[nx].p,

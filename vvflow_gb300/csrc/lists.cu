@@ -107,67 +107,38 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
     hi = s;
 }
 
-// PASS 0: count near runs (+ far nodes of flagged leaves).
-// PASS 1: write near runs, far nodes of flagged leaves and the expansion coefficients.
-template <int PASS, bool FP32>
+// Per-leaf walk (one thread per leaf) for selected leaves only (sel[L] != 0).
+// MODE 1: write the near runs at near_off[L] (leaves whose runs overflowed the warp walk's
+//         buffer).  MODE 2: count (PASS 0) or write (PASS 1) the far list of the leaf.
+template <int PASS, bool FP32_UNUSED>
 __global__ void __launch_bounds__(LB) k_walk(int64_t nl, ListView v, const int32_t* __restrict__ leaf_node,
-                                             const int32_t* __restrict__ flag, int32_t* near_cnt,
+                                             const int32_t* __restrict__ sel, int32_t* near_cnt_unused,
                                              int32_t* far_cnt, const int32_t* __restrict__ near_off,
                                              const int32_t* __restrict__ far_off, int2* near_run,
-                                             int32_t* far_node, double4* taylor, int64_t nodes_bound,
-                                             int32_t* err, unsigned long long* far_total) {
+                                             int32_t* far_node, double4* taylor_unused, int64_t nodes_bound,
+                                             int32_t* err, unsigned long long* far_total_unused, int mode) {
     int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= nl) return;
+    if (!sel[L]) {
+        if (mode == 2 && PASS == 0) far_cnt[L] = 0;
+        return;
+    }
     const int32_t meN = leaf_node[L];
     const float4 mg = v.nf_geo[meN];
     const int2 mk = v.nf_k[meN];
-    const double4 me = v.geom[meN];
-    const bool keep_far = flag[L] != 0;
     int32_t stack[MAX_DEPTH + 2];
     int sp = 0;
     stack[sp++] = 0;
-    int32_t nr = 0, nf = 0, last = -2, rfirst = -1, nfar_all = 0;
-    const int32_t nbase = PASS ? near_off[L] : 0, fbase = PASS ? far_off[L] : 0;
-    double d1 = 0, d2 = 0, d3 = 0, d4 = 0;             // FP64 path
-    float h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0, h4 = 0, l4 = 0;  // FP32 path
+    int32_t nr = 0, nf = 0, last = -2, rfirst = -1;
+    const int32_t nbase = (mode == 1) ? near_off[L] : 0;
+    const int32_t fbase = (mode == 2 && PASS) ? far_off[L] : 0;
     int64_t guard = 0;
     while (sp) {
         if (++guard > nodes_bound) { atomicExch(err, 2); break; }
         const int32_t t = stack[--sp];
         if (far_test(v, t, meN, mg, mk)) {
-            nfar_all++;
-            if (keep_far) {
-                if (PASS) far_node[fbase + nf] = t;
-                nf++;
-            }
-            if (PASS) {
-                if (FP32) {
-                    const int2 tk = v.nf_k[t];
-                    const float sx = (float)(mk.x - tk.x) * v.Gf, sy = (float)(mk.y - tk.y) * v.Gf;
-                    const float4 c4 = v.nf_cm[t];
-                    const float2 gg = v.nf_g[t];
-                    float dpx = sx + (mg.x - c4.x), dpy = sy + (mg.y - c4.y);
-                    float dmx = sx + (mg.x - c4.z), dmy = sy + (mg.y - c4.w);
-                    float ap = dpx * dpx + dpy * dpy, am = dmx * dmx + dmy * dmy;
-                    float ip = rcp_approx(ap), im = rcp_approx(am);
-                    float fp1 = gg.x * ip, fm1 = gg.y * im;
-                    float fp2 = fp1 * ip, fm2 = fm1 * im;
-                    two_sum_acc(h1, l1, -(fp1 * dpy + fm1 * dmy));
-                    two_sum_acc(h2, l2, fp1 * dpx + fm1 * dmx);
-                    two_sum_acc(h3, l3, fp2 * dpy * dpx + fm2 * dmy * dmx);
-                    two_sum_acc(h4, l4, fp2 * (dpy * dpy - dpx * dpx) + fm2 * (dmy * dmy - dmx * dmx));
-                } else {
-                    const double* c = v.cm + 6 * (size_t)t;
-                    double dpx = me.x - c[0], dpy = me.y - c[1], dmx = me.x - c[3], dmy = me.y - c[4];
-                    double ap = dpx * dpx + dpy * dpy, am = dmx * dmx + dmy * dmy;
-                    double fp1 = c[2] / ap, fm1 = c[5] / am;
-                    double fp2 = c[2] / (ap * ap), fm2 = c[5] / (am * am);
-                    d1 -= (fp1 * dpy + fm1 * dmy);
-                    d2 += (fp1 * dpx + fm1 * dmx);
-                    d3 += (fp2 * dpy * dpx + fm2 * dmy * dmx);
-                    d4 += (fp2 * (dpy * dpy - dpx * dpx) + fm2 * (dmy * dmy - dmx * dmx));
-                }
-            }
+            if (mode == 2 && PASS) far_node[fbase + nf] = t;
+            nf++;
             continue;
         }
         const int32_t c1 = v.ch1[t];
@@ -181,24 +152,149 @@ __global__ void __launch_bounds__(LB) k_walk(int64_t nl, ListView v, const int32
         if (q == last + 1) {
             last = q;
         } else {
-            if (PASS && rfirst >= 0) near_run[nbase + nr - 1] = make_int2(rfirst, last + 1);
+            if (mode == 1 && rfirst >= 0) near_run[nbase + nr - 1] = make_int2(rfirst, last + 1);
             rfirst = q;
             last = q;
             nr++;
         }
     }
-    if (PASS) {
-        if (rfirst >= 0) near_run[nbase + nr - 1] = make_int2(rfirst, last + 1);
+    if (mode == 1 && rfirst >= 0) near_run[nbase + nr - 1] = make_int2(rfirst, last + 1);
+    if (mode == 2 && PASS == 0) far_cnt[L] = nf;
+}
+
+// Far-field contribution of far node t to leaf (mg, mk | me), FP32 or FP64.
+template <bool FP32>
+struct Taylor {
+    double d1 = 0, d2 = 0, d3 = 0, d4 = 0;
+    float h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0, h4 = 0, l4 = 0;
+    __device__ __forceinline__ void add(const ListView& v, int32_t t, float4 mg, int2 mk, const double4& me) {
         if (FP32) {
-            d1 = (double)h1 + (double)l1; d2 = (double)h2 + (double)l2;
-            d3 = (double)h3 + (double)l3; d4 = (double)h4 + (double)l4;
+            const int2 tk = v.nf_k[t];
+            const float sx = (float)(mk.x - tk.x) * v.Gf, sy = (float)(mk.y - tk.y) * v.Gf;
+            const float4 c4 = v.nf_cm[t];
+            const float2 gg = v.nf_g[t];
+            float dpx = sx + (mg.x - c4.x), dpy = sy + (mg.y - c4.y);
+            float dmx = sx + (mg.x - c4.z), dmy = sy + (mg.y - c4.w);
+            float ap = dpx * dpx + dpy * dpy, am = dmx * dmx + dmy * dmy;
+            float ip = rcp_approx(ap), im = rcp_approx(am);
+            float fp1 = gg.x * ip, fm1 = gg.y * im;
+            float fp2 = fp1 * ip, fm2 = fm1 * im;
+            two_sum_acc(h1, l1, -(fp1 * dpy + fm1 * dmy));
+            two_sum_acc(h2, l2, fp1 * dpx + fm1 * dmx);
+            two_sum_acc(h3, l3, fp2 * dpy * dpx + fm2 * dmy * dmx);
+            two_sum_acc(h4, l4, fp2 * (dpy * dpy - dpx * dpx) + fm2 * (dmy * dmy - dmx * dmx));
+        } else {
+            const double* c = v.cm + 6 * (size_t)t;
+            double dpx = me.x - c[0], dpy = me.y - c[1], dmx = me.x - c[3], dmy = me.y - c[4];
+            double ap = dpx * dpx + dpy * dpy, am = dmx * dmx + dmy * dmy;
+            double fp1 = c[2] / ap, fm1 = c[5] / am;
+            double fp2 = c[2] / (ap * ap), fm2 = c[5] / (am * am);
+            d1 -= (fp1 * dpy + fm1 * dmy);
+            d2 += (fp1 * dpx + fm1 * dmx);
+            d3 += (fp2 * dpy * dpx + fm2 * dmy * dmx);
+            d4 += (fp2 * (dpy * dpy - dpx * dpx) + fm2 * (dmy * dmy - dmx * dmx));
         }
-        taylor[L] = make_double4(d1 * C_1_2PI, d2 * C_1_2PI, d3 * C_1_PI, d4 * C_1_2PI);
-        atomicAdd(far_total, (unsigned long long)nfar_all);
-    } else {
-        near_cnt[L] = nr;
-        far_cnt[L] = nf;
     }
+    __device__ __forceinline__ double4 result() const {
+        double a = d1, b = d2, cc = d3, d = d4;
+        if (FP32) {
+            a = (double)h1 + (double)l1; b = (double)h2 + (double)l2;
+            cc = (double)h3 + (double)l3; d = (double)h4 + (double)l4;
+        }
+        return make_double4(a * C_1_2PI, b * C_1_2PI, cc * C_1_PI, d * C_1_2PI);
+    }
+};
+
+constexpr int RUN_CAP = 64;   // near runs kept per leaf by the warp walk
+constexpr int WW = 4;         // warps per block in the warp walk
+
+// One warp walks the tree for 32 consecutive leaves at once (they are neighbours in space,
+// so their walks share most nodes).  The stack holds (node, mask of lanes still walking
+// below it); node data are broadcast loads.  Each lane keeps its own near runs (in depth-
+// first order) and far-field coefficients.  Runs beyond RUN_CAP are counted, not stored.
+template <bool FP32>
+__global__ void __launch_bounds__(WW * 32) k_walk_warp(int64_t nl, ListView v, const int32_t* __restrict__ leaf_node,
+                                                       int32_t* near_cnt, int2* run_buf, double4* taylor,
+                                                       unsigned long long* far_total, int64_t nodes_bound,
+                                                       int32_t* err) {
+    __shared__ int32_t s_node[WW][MAX_DEPTH + 2];
+    __shared__ uint32_t s_mask[WW][MAX_DEPTH + 2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t L = ((int64_t)blockIdx.x * WW + w) * 32 + lane;
+    const bool valid = L < nl;
+    const uint32_t all = __ballot_sync(0xffffffffu, valid);
+    if (!all) return;
+    const int32_t meN = valid ? leaf_node[L] : 0;
+    const float4 mg = v.nf_geo[meN];
+    const int2 mk = v.nf_k[meN];
+    const double4 me = v.geom[meN];
+    Taylor<FP32> tay;
+    int32_t nr = 0, last = -2, rfirst = -1, nfar = 0;
+    int2* myruns = run_buf + (size_t)(valid ? L : 0) * RUN_CAP;
+    if (lane == 0) { s_node[w][0] = 0; s_mask[w][0] = all; }
+    int sp = 1;
+    __syncwarp();
+    int64_t guard = 0;
+    while (sp > 0) {
+        if (++guard > nodes_bound) { if (lane == 0) atomicExch(err, 2); break; }
+        sp--;
+        const int32_t t = s_node[w][sp];
+        const uint32_t mask = s_mask[w][sp];
+        __syncwarp();
+        const bool act = (mask >> lane) & 1u;
+        const bool far = act && far_test(v, t, meN, mg, mk);
+        if (far) {
+            tay.add(v, t, mg, mk, me);
+            nfar++;
+        }
+        const uint32_t rest = mask & ~__ballot_sync(0xffffffffu, far);
+        if (rest) {
+            const int32_t c1 = v.ch1[t];
+            if (c1 >= 0) {
+                if (sp + 2 > MAX_DEPTH + 2) { if (lane == 0) atomicExch(err, 2); break; }
+                if (lane == 0) {
+                    s_node[w][sp] = c1 + 1; s_mask[w][sp] = rest;
+                    s_node[w][sp + 1] = c1; s_mask[w][sp + 1] = rest;
+                }
+                sp += 2;
+            } else if ((rest >> lane) & 1u) {
+                const int32_t q = v.dfs[t];
+                if (q == last + 1) {
+                    last = q;
+                } else {
+                    if (rfirst >= 0 && nr <= RUN_CAP) myruns[nr - 1] = make_int2(rfirst, last + 1);
+                    rfirst = q;
+                    last = q;
+                    nr++;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (valid) {
+        if (rfirst >= 0 && nr <= RUN_CAP) myruns[nr - 1] = make_int2(rfirst, last + 1);
+        near_cnt[L] = nr;
+        taylor[L] = tay.result();
+    }
+    unsigned long long f = warp_sum_u64(valid ? (unsigned long long)nfar : 0ull);
+    if (lane == 0) atomicAdd(far_total, f);
+}
+
+__global__ void k_runs_compact(int64_t nl, const int32_t* __restrict__ near_cnt, const int32_t* __restrict__ near_off,
+                               const int2* __restrict__ run_buf, int2* near_run, int32_t* overflow,
+                               int32_t* n_overflow) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    int32_t n = near_cnt[L];
+    if (n > RUN_CAP) {
+        overflow[L] = 1;
+        atomicAdd(n_overflow, 1);
+        return;
+    }
+    overflow[L] = 0;
+    const int2* src = run_buf + (size_t)L * RUN_CAP;
+    int2* dst = near_run + near_off[L];
+    for (int32_t k = 0; k < n; k++) dst[k] = src[k];
 }
 
 // Exact walk writing every leaf's far list (inspection only).
@@ -263,30 +359,45 @@ void tree_lists(Ctx& c) {
     c.near_cnt.reserve(nl + 1); c.far_cnt.reserve(nl + 1);
     c.near_off.reserve(nl + 2); c.far_off.reserve(nl + 2);
     c.lf_taylor.reserve(nl + 1);
-    const bool fp32 = c.precision == VVGPU_FP32;
-    if (fp32) k_walk<0, true><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, c.near_cnt.p,
-                                                              c.far_cnt.p, nullptr, nullptr, nullptr, nullptr,
-                                                              nullptr, nn, err, nullptr);
-    else k_walk<0, false><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, c.near_cnt.p,
-                                                           c.far_cnt.p, nullptr, nullptr, nullptr, nullptr,
-                                                           nullptr, nn, err, nullptr);
-    VV_LAUNCH_CHECK();
-    exclusive_scan(c, c.near_cnt.p, c.near_off.p, nl);
-    exclusive_scan(c, c.far_cnt.p, c.far_off.p, nl);
-    if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
-    c.n_near_runs = read_i32(c, c.near_off.p + nl);
-    c.n_far = read_i32(c, c.far_off.p + nl);
-    c.near_run.reserve(c.n_near_runs + 1);
-    c.far_node.reserve(c.n_far + 1);
+    c.run_buf.reserve((size_t)nl * RUN_CAP + 1);
+    c.lf_overflow.reserve(nl + 1);
     unsigned long long* far_total = c.counters.p + 10;
     VV_CUDA(cudaMemsetAsync(far_total, 0, 8, s));
-    if (fp32) k_walk<1, true><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, nullptr, nullptr,
-                                                              c.near_off.p, c.far_off.p, c.near_run.p,
-                                                              c.far_node.p, c.lf_taylor.p, nn, err, far_total);
-    else k_walk<1, false><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, nullptr, nullptr,
-                                                           c.near_off.p, c.far_off.p, c.near_run.p, c.far_node.p,
-                                                           c.lf_taylor.p, nn, err, far_total);
+    const bool fp32 = c.precision == VVGPU_FP32;
+    const unsigned gw = grid_for((nl + 31) / 32, WW);
+    if (fp32) k_walk_warp<true><<<gw, WW * 32, 0, s>>>(nl, v, c.leaf_node.p, c.near_cnt.p, c.run_buf.p,
+                                                        c.lf_taylor.p, far_total, nn, err);
+    else k_walk_warp<false><<<gw, WW * 32, 0, s>>>(nl, v, c.leaf_node.p, c.near_cnt.p, c.run_buf.p,
+                                                     c.lf_taylor.p, far_total, nn, err);
     VV_LAUNCH_CHECK();
+    exclusive_scan(c, c.near_cnt.p, c.near_off.p, nl);
+    c.n_near_runs = read_i32(c, c.near_off.p + nl);
+    c.near_run.reserve(c.n_near_runs + 1);
+    int32_t* n_over = (int32_t*)(c.counters.p + 12);
+    VV_CUDA(cudaMemsetAsync(n_over, 0, 4, s));
+    k_runs_compact<<<grid_for(nl, 256), 256, 0, s>>>(nl, c.near_cnt.p, c.near_off.p, c.run_buf.p, c.near_run.p,
+                                                     c.lf_overflow.p, n_over);
+    VV_LAUNCH_CHECK();
+    if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
+    const int32_t nover = read_i32(c, n_over);
+    if (nover > 0) {
+        // leaves with more than RUN_CAP runs: write their runs with the per-leaf walk
+        k_walk<1, true><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_overflow.p, nullptr, nullptr,
+                                                         c.near_off.p, nullptr, c.near_run.p, nullptr, nullptr, nn,
+                                                         err, nullptr, 1);
+        VV_LAUNCH_CHECK();
+    }
+    // far lists of the leaves that hold a segment centre (read by the SLAE right-hand side)
+    k_walk<0, true><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, nullptr, c.far_cnt.p,
+                                                     nullptr, nullptr, nullptr, nullptr, nullptr, nn, err, nullptr, 2);
+    VV_LAUNCH_CHECK();
+    exclusive_scan(c, c.far_cnt.p, c.far_off.p, nl);
+    c.n_far = read_i32(c, c.far_off.p + nl);
+    c.far_node.reserve(c.n_far + 1);
+    k_walk<1, true><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, nullptr, nullptr, nullptr,
+                                                     c.far_off.p, nullptr, c.far_node.p, nullptr, nn, err, nullptr, 2);
+    VV_LAUNCH_CHECK();
+    if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
     c.stats.near_runs = c.n_near_runs;
     c.taylor_precision = c.precision;
     unsigned long long ft = 0;

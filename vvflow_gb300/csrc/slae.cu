@@ -166,98 +166,100 @@ struct BodyDev {
     int32_t special, kutta;
 };
 
-// Special and body rows; one thread per body (cheap scalar work).
+// Special and body rows: one block per body; the threads fill the per-segment cells, thread
+// 0 the scalar cells and right-hand sides.  inf_body is the body whose special segment
+// carries the InfSteady row (the first non-Kutta body, MConvectiveFast.cpp:905-913).
 __global__ void k_body_rows(int64_t n, double* A, double* B, const BodyDev* bd, int nb,
                             const int32_t* col_seg0, const int32_t* body_count, const double* cy_,
                             const double* cx_, const int32_t* body_first, double dt, double gsum, double inf_g,
-                            double gx, double gy, bool rhs_only) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+                            double gx, double gy, int inf_body, bool rhs_only) {
+    const int bi = blockIdx.x;
+    if (bi >= nb) return;
     const double _1_dt = 1 / dt, _1_2dt = 0.5 / dt;
-    int once = 0;
-    for (int bi = 0; bi < nb; bi++) {
-        const BodyDev& b = bd[bi];
-        const int32_t c0 = col_seg0[bi], cnt = body_count[bi], f = body_first[bi];
-        // special segment row
-        {
-            int32_t eq = c0 + b.special;
-            double* Ar = A + (size_t)eq * n;
-            if (b.kutta) {
-                B[eq] = 0;
-                if (!rhs_only) Ar[c0 + b.special] = 1;
-            } else if (!once++) {
-                B[eq] = -gsum - inf_g;
-                if (!rhs_only)
-                    for (int bj = 0; bj < nb; bj++) {
-                        for (int32_t q = 0; q < body_count[bj]; q++) Ar[col_seg0[bj] + q] = 1;
-                        Ar[col_seg0[bj] + body_count[bj] + 2] = 2 * bd[bj].area;
-                    }
-            } else {
-                B[eq] = b.gdead + 2 * b.area * b.pvo;
-                if (!rhs_only) {
-                    for (int32_t q = 0; q < cnt; q++) Ar[c0 + q] = 1;
-                    Ar[c0 + cnt + 2] = 2 * b.area;
-                }
-            }
-        }
-        const int32_t e0 = c0 + cnt;
-        auto cell = [&](int32_t eq, int q, double v) { if (!rhs_only) A[(size_t)eq * n + e0 + q] = v; };
-        B[e0 + 0] = b.spx; cell(e0 + 0, 0, 1);
-        B[e0 + 1] = b.spy; cell(e0 + 1, 1, 1);
-        B[e0 + 2] = b.spo; cell(e0 + 2, 2, 1);
-        const double area = b.area, rcx = b.cofx - b.axx, rcy = b.cofy - b.axy, moi = b.moi, dens = b.dens;
-        // Hydro X/Y/O (:533-623)
-        {
-            int32_t eq = e0 + 3;
-            double ty = b.cofy * 2 + rcy;
-            B[eq] = area * _1_dt * b.pvx + area * _1_dt * (-ty) * b.pvo + (b.pvo * b.pvo) * area * rcx - b.fpx +
-                    b.fdx * _1_dt;
-            if (!rhs_only) for (int32_t q = 0; q < cnt; q++) A[(size_t)eq * n + c0 + q] = _1_dt * (-cy_[f + q]);
-            cell(eq, 0, area * _1_dt); cell(eq, 1, 0); cell(eq, 2, area * _1_dt * (-2 * b.cofy - rcy)); cell(eq, 3, -1);
-        }
-        {
-            int32_t eq = e0 + 4;
-            double tx = b.cofx * 2 + rcx;
-            B[eq] = area * _1_dt * b.pvy + area * _1_dt * tx * b.pvo + (b.pvo * b.pvo) * area * rcy - b.fpy +
-                    b.fdy * _1_dt;
-            if (!rhs_only) for (int32_t q = 0; q < cnt; q++) A[(size_t)eq * n + c0 + q] = _1_dt * (cx_[f + q]);
-            cell(eq, 0, 0); cell(eq, 1, area * _1_dt); cell(eq, 2, area * _1_dt * (2 * b.cofx + rcx)); cell(eq, 4, -1);
-        }
-        {
-            int32_t eq = e0 + 5;
-            double c = area * _1_dt;
-            double lx = (-rcy) * c, ly = rcx * c;
-            B[eq] = (lx * b.pvx + ly * b.pvy) + 2 * moi * _1_dt * b.pvo - b.fpo + b.fdo * _1_2dt;
+    const BodyDev& b = bd[bi];
+    const int32_t c0 = col_seg0[bi], cnt = body_count[bi], f = body_first[bi];
+    const int32_t e0 = c0 + cnt;
+    const double area = b.area, rcx = b.cofx - b.axx, rcy = b.cofy - b.axy, moi = b.moi, dens = b.dens;
+    // special segment row
+    {
+        const int32_t eq = c0 + b.special;
+        double* Ar = A + (size_t)eq * n;
+        if (b.kutta) {
+            if (threadIdx.x == 0) { B[eq] = 0; if (!rhs_only) Ar[c0 + b.special] = 1; }
+        } else if (bi == inf_body) {
+            if (threadIdx.x == 0) B[eq] = -gsum - inf_g;
             if (!rhs_only)
-                for (int32_t q = 0; q < cnt; q++) {
-                    double dx = cx_[f + q] - b.axx, dy = cy_[f + q] - b.axy;
-                    A[(size_t)eq * n + c0 + q] = _1_2dt * (dx * dx + dy * dy);
+                for (int bj = 0; bj < nb; bj++) {
+                    for (int32_t q = threadIdx.x; q < body_count[bj]; q += blockDim.x) Ar[col_seg0[bj] + q] = 1;
+                    if (threadIdx.x == 0) Ar[col_seg0[bj] + body_count[bj] + 2] = 2 * bd[bj].area;
                 }
-            cell(eq, 0, area * _1_dt * (-rcy)); cell(eq, 1, area * _1_dt * rcx); cell(eq, 2, 2 * moi * _1_dt);
-            cell(eq, 5, -1);
+        } else {
+            if (threadIdx.x == 0) {
+                B[eq] = b.gdead + 2 * b.area * b.pvo;
+                if (!rhs_only) Ar[c0 + cnt + 2] = 2 * b.area;
+            }
+            if (!rhs_only) for (int32_t q = threadIdx.x; q < cnt; q += blockDim.x) Ar[c0 + q] = 1;
         }
-        // Newton X/Y/O (:634-739)
-        {
-            int32_t eq = e0 + 6;
-            B[eq] = -area * _1_dt * dens * b.pvx + area * _1_dt * dens * rcy * b.pvo -
-                    area * dens * rcx * (b.pvo * b.pvo) - (dens - 1.0) * gx * area;
-            cell(eq, 0, -area * _1_dt * dens); cell(eq, 1, 0); cell(eq, 2, area * _1_dt * dens * rcy);
-            cell(eq, 3, 1); cell(eq, 6, -1);
+    }
+    // per-segment cells of the Hydro rows (:551-552, :582-583, :612-613)
+    if (!rhs_only)
+        for (int32_t q = threadIdx.x; q < cnt; q += blockDim.x) {
+            A[(size_t)(e0 + 3) * n + c0 + q] = _1_dt * (-cy_[f + q]);
+            A[(size_t)(e0 + 4) * n + c0 + q] = _1_dt * (cx_[f + q]);
+            const double dx = cx_[f + q] - b.axx, dy = cy_[f + q] - b.axy;
+            A[(size_t)(e0 + 5) * n + c0 + q] = _1_2dt * (dx * dx + dy * dy);
         }
-        {
-            int32_t eq = e0 + 7;
-            B[eq] = -area * _1_dt * dens * b.pvy - area * _1_dt * dens * rcx * b.pvo -
-                    area * dens * rcy * (b.pvo * b.pvo) - (dens - 1.0) * gy * area;
-            cell(eq, 0, 0); cell(eq, 1, -area * _1_dt * dens); cell(eq, 2, -area * _1_dt * dens * rcx);
-            cell(eq, 4, 1); cell(eq, 7, -1);
-        }
-        {
-            int32_t eq = e0 + 8;
-            double rlx = -rcy, rly = rcx;
-            B[eq] = -area * _1_dt * dens * (rlx * b.pvx + rly * b.pvy) - moi * _1_dt * dens * b.pvo -
-                    (dens - 1.0) * (rlx * gx + rly * gy) * area;
-            cell(eq, 0, +area * _1_dt * dens * rcy); cell(eq, 1, -area * _1_dt * dens * rcx);
-            cell(eq, 2, -moi * _1_dt * dens); cell(eq, 5, 1); cell(eq, 8, -1);
-        }
+    if (threadIdx.x != 0) return;
+    auto cell = [&](int32_t eq, int q, double v) { if (!rhs_only) A[(size_t)eq * n + e0 + q] = v; };
+    // Speed rows (rigid bodies, :803-862)
+    B[e0 + 0] = b.spx; cell(e0 + 0, 0, 1);
+    B[e0 + 1] = b.spy; cell(e0 + 1, 1, 1);
+    B[e0 + 2] = b.spo; cell(e0 + 2, 2, 1);
+    // Hydro X/Y/O (:533-623)
+    {
+        const int32_t eq = e0 + 3;
+        const double ty = b.cofy * 2 + rcy;
+        B[eq] = area * _1_dt * b.pvx + area * _1_dt * (-ty) * b.pvo + (b.pvo * b.pvo) * area * rcx - b.fpx +
+                b.fdx * _1_dt;
+        cell(eq, 0, area * _1_dt); cell(eq, 1, 0); cell(eq, 2, area * _1_dt * (-2 * b.cofy - rcy)); cell(eq, 3, -1);
+    }
+    {
+        const int32_t eq = e0 + 4;
+        const double tx = b.cofx * 2 + rcx;
+        B[eq] = area * _1_dt * b.pvy + area * _1_dt * tx * b.pvo + (b.pvo * b.pvo) * area * rcy - b.fpy +
+                b.fdy * _1_dt;
+        cell(eq, 0, 0); cell(eq, 1, area * _1_dt); cell(eq, 2, area * _1_dt * (2 * b.cofx + rcx)); cell(eq, 4, -1);
+    }
+    {
+        const int32_t eq = e0 + 5;
+        const double c = area * _1_dt;
+        const double lx = (-rcy) * c, ly = rcx * c;
+        B[eq] = (lx * b.pvx + ly * b.pvy) + 2 * moi * _1_dt * b.pvo - b.fpo + b.fdo * _1_2dt;
+        cell(eq, 0, area * _1_dt * (-rcy)); cell(eq, 1, area * _1_dt * rcx); cell(eq, 2, 2 * moi * _1_dt);
+        cell(eq, 5, -1);
+    }
+    // Newton X/Y/O (:634-739)
+    {
+        const int32_t eq = e0 + 6;
+        B[eq] = -area * _1_dt * dens * b.pvx + area * _1_dt * dens * rcy * b.pvo -
+                area * dens * rcx * (b.pvo * b.pvo) - (dens - 1.0) * gx * area;
+        cell(eq, 0, -area * _1_dt * dens); cell(eq, 1, 0); cell(eq, 2, area * _1_dt * dens * rcy);
+        cell(eq, 3, 1); cell(eq, 6, -1);
+    }
+    {
+        const int32_t eq = e0 + 7;
+        B[eq] = -area * _1_dt * dens * b.pvy - area * _1_dt * dens * rcx * b.pvo -
+                area * dens * rcy * (b.pvo * b.pvo) - (dens - 1.0) * gy * area;
+        cell(eq, 0, 0); cell(eq, 1, -area * _1_dt * dens); cell(eq, 2, -area * _1_dt * dens * rcx);
+        cell(eq, 4, 1); cell(eq, 7, -1);
+    }
+    {
+        const int32_t eq = e0 + 8;
+        const double rlx = -rcy, rly = rcx;
+        B[eq] = -area * _1_dt * dens * (rlx * b.pvx + rly * b.pvy) - moi * _1_dt * dens * b.pvo -
+                (dens - 1.0) * (rlx * gx + rly * gy) * area;
+        cell(eq, 0, +area * _1_dt * dens * rcy); cell(eq, 1, -area * _1_dt * dens * rcx);
+        cell(eq, 2, -moi * _1_dt * dens); cell(eq, 5, 1); cell(eq, 8, -1);
     }
 }
 
@@ -514,8 +516,11 @@ void slae(Ctx& c, vvgpu_body_out* out) {
         k_slip_rows<<<(unsigned)nsl, 256, 0, s>>>(fa);
         VV_LAUNCH_CHECK();
     }
-    k_body_rows<<<1, 1, 0, s>>>(n, c.A.p, c.B.p, dbd.p, nb, d_col0, d_bcount, c.s_cy.p, c.s_cx.p, d_bfirst, c.dt,
-                                gs, c.inf_g, c.grav_x, c.grav_y, false);
+    int inf_body = -1;
+    for (int bi = 0; bi < nb; bi++)
+        if (!c.bodies[bi].p.bc_kutta) { inf_body = bi; break; }
+    k_body_rows<<<nb, 256, 0, s>>>(n, c.A.p, c.B.p, dbd.p, nb, d_col0, d_bcount, c.s_cy.p, c.s_cx.p, d_bfirst, c.dt,
+                                   gs, c.inf_g, c.grav_x, c.grav_y, inf_body, false);
     VV_LAUNCH_CHECK();
 
     // reuse the cached inverse while the matrix bytes are unchanged

@@ -149,6 +149,8 @@ struct Ctx {
     DArr<int2> near_run;
     DArr<int32_t> far_node;         // far lists of flagged leaves only (see lists.cu)
     DArr<int32_t> lf_flag;          // leaf holds a segment centre
+    DArr<int2> run_buf;             // warp walk: fixed-capacity near runs per leaf
+    DArr<int32_t> lf_overflow;      // leaf had more runs than the buffer holds
     DArr<double4> lf_taylor;        // far-field expansion coefficients T1..T4 per leaf
     int taylor_precision = 0;
     DArr<float4> nf_geo, nf_cm;     // per node, anchor frame: centre + (h+w); centroids
@@ -167,6 +169,7 @@ struct Ctx {
     DArr<float4> e_rec0, e_recO;
     DArr<double> lf_mcs, lf_epr;
     DArr<int32_t> e_zb_prev, e_live, e_cand, e_ncand, e_dirty, e_lchanged;
+    DArr<float> e_rlist, e_rnear;
 
     // local FP32 frames (frame.cuh)
     double frame_G = 1.0;

@@ -80,6 +80,10 @@ SIGNATURES = {
     "vvgpu_set_params": (C.c_int, [_H] + [C.c_double] * 8),
     "vvgpu_add_body": (C.c_int, [_H, C.c_int64, _D, _D, _U32, C.POINTER(BodyParams)]),
     "vvgpu_set_segment_g": (C.c_int, [_H, _D]),
+    "vvgpu_set_segment_state": (C.c_int, [_H, _D, _D, _D]),
+    "vvgpu_clear_bodies": (C.c_int, [_H]),
+    "vvgpu_set_body_params": (C.c_int, [_H, C.c_int, C.POINTER(BodyParams)]),
+    "vvgpu_set_velocities": (C.c_int, [_H, _D, _D]),
     "vvgpu_set_sinks": (C.c_int, [_H, C.c_int64, _D, _D, _D]),
     "vvgpu_set_vortices": (C.c_int, [_H, C.c_int64, _D, _D, _D, _D]),
     "vvgpu_set_vortices_device": (C.c_int, [_H, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
