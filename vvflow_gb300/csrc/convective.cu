@@ -72,7 +72,7 @@ struct ConvArgs {
     double inf_vx, inf_vy;
     double fc; int64_t nnodes;
     // FP32 records
-    const float4* src32; const int2* src_k; const int2* anchor; double G; float Gf;
+    const float4* src32; const float2* src_k; const float2* anchor; double G; float Gf;
 };
 
 // sink_list_influence + slip-segment part of body_list_influence, FP64 (per target).
@@ -173,8 +173,8 @@ __global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
     if (L >= a.nl) return;
     const double4 me = a.lgeom[L];
     const double4 tc = a.taylor[L];
-    const int2 kL = a.anchor[L];
-    const double axL = (double)kL.x * a.G, ayL = (double)kL.y * a.G;
+    const float2 kL = a.anchor[L];
+    const double axL = (double)kL.x, ayL = (double)kL.y;
     const int32_t v0 = a.lvf[L], v1 = a.lvl[L];
     const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
     for (int32_t c0 = v0; c0 < v1; c0 += 2 * TC32) {
@@ -224,9 +224,9 @@ __global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
                 const int2 rc = s_runs[wq][cur];
                 const int32_t j = rc.y + (k - rc.x);
                 const float4 s4 = a.src32[j];
-                const int2 kk = a.src_k[j];
-                const float sx = s4.x + (float)(kk.x - kL.x) * a.Gf;
-                const float sy = s4.y + (float)(kk.y - kL.y) * a.Gf;
+                const float2 kk = a.src_k[j];
+                const float sx = s4.x + (kk.x - kL.x);
+                const float sy = s4.y + (kk.y - kL.y);
 #pragma unroll
                 for (int t = 0; t < TC32; t++) {
                     const float dx = tx[t] - sx, dy = ty[t] - sy;
@@ -287,21 +287,21 @@ __global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
 
 // FP32 source records: position in own leaf frame, g, eps^2 (eps = 1/_1_eps; a zero
 // _1_eps or zero g gives a record that contributes exactly zero).
-__global__ void k_src32(int64_t n, const int32_t* __restrict__ leaf_of, const int2* __restrict__ anchor, double G,
+__global__ void k_src32(int64_t n, const int32_t* __restrict__ leaf_of, const float2* __restrict__ anchor, double G,
                         const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ g,
-                        const double* __restrict__ ie, float4* src, int2* src_k) {
+                        const double* __restrict__ ie, float4* src, float2* src_k) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int2 k = anchor[leaf_of[i]];
+    float2 k = anchor[leaf_of[i]];
     double e = 1. / ie[i];
     float gf = (float)g[i];
     float e2 = (float)(e * e);
     if (ie[i] == 0.) { gf = 0.f; e2 = 1.f; }
-    src[i] = make_float4((float)(x[i] - (double)k.x * G), (float)(y[i] - (double)k.y * G), gf, e2);
+    src[i] = make_float4((float)(x[i] - (double)k.x), (float)(y[i] - (double)k.y), gf, e2);
     src_k[i] = k;
 }
 
-__global__ void k_anchor2(int64_t nl, const double4* __restrict__ lgeom, double G, int2* anchor) {
+__global__ void k_anchor2(int64_t nl, const double4* __restrict__ lgeom, double G, float2* anchor) {
     int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= nl) return;
     double4 me = lgeom[L];

@@ -30,11 +30,11 @@ __global__ void k_dbox(int64_t nl, const int32_t* __restrict__ lvf, const int32_
                        const int32_t* __restrict__ lsf, const int32_t* __restrict__ lsl,
                        const int32_t* __restrict__ seg_order, const double* __restrict__ x,
                        const double* __restrict__ y, const double* __restrict__ g, const double* __restrict__ rx,
-                       const double* __restrict__ ry, const int2* __restrict__ anchor, double G, float4* box) {
+                       const double* __restrict__ ry, const float2* __restrict__ anchor, double G, float4* box) {
     int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= nl) return;
-    int2 k = anchor[L];
-    double ax = (double)k.x * G, ay = (double)k.y * G;
+    float2 k = anchor[L];
+    double ax = (double)k.x, ay = (double)k.y;
     float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
     for (int32_t i = lvf[L]; i < lvl[L]; i++) {
         if (g[i] == 0.) continue;
@@ -56,7 +56,7 @@ struct DiffArgs {
     const double* x; const double* y; const double* g; const double* ie;
     double* vx; double* vy;
     const double* rx; const double* ry; const double* dlx; const double* dly; double* fric;
-    const int2* anchor; const float4* box; const float4* src32; const int2* src_k;
+    const float2* anchor; const float4* box; const float4* src32; const float2* src_k;
     double G; float Gf; double re;
     unsigned long long* cand;
 };
@@ -85,8 +85,8 @@ __global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
     const int lane = threadIdx.x & 31;
     const int ts = lane & 7, sl = lane >> 3;
     if (L >= a.nl) return;
-    const int2 kL = a.anchor[L];
-    const double axL = (double)kL.x * a.G, ayL = (double)kL.y * a.G;
+    const float2 kL = a.anchor[L];
+    const double axL = (double)kL.x, ayL = (double)kL.y;
     const int32_t v0 = a.lvf[L], v1 = a.lvl[L];
     const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
     unsigned long long ncand = 0;

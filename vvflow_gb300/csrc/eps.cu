@@ -85,7 +85,7 @@ __global__ void k_leaf_params(int64_t nl, const double4* __restrict__ lgeom, con
     epr_out[L] = epr;
 }
 
-__global__ void k_anchor(int64_t nl, const double4* __restrict__ lgeom, double G, int2* anchor) {
+__global__ void k_anchor(int64_t nl, const double4* __restrict__ lgeom, double G, float2* anchor) {
     int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= nl) return;
     double4 me = lgeom[L];
@@ -93,18 +93,18 @@ __global__ void k_anchor(int64_t nl, const double4* __restrict__ lgeom, double G
     anchor[L] = anchor_of(cx, cy, G);
 }
 
-__device__ __forceinline__ float rel(double v, int k, double G) { return (float)(v - (double)k * G); }
+__device__ __forceinline__ float rel(double v, float a) { return (float)(v - (double)a); }
 
 // Initial records: position in own leaf frame and the sign of g.
-__global__ void k_rec0(int64_t n, const int32_t* __restrict__ leaf_of, const int2* __restrict__ anchor, double G,
+__global__ void k_rec0(int64_t n, const int32_t* __restrict__ leaf_of, const float2* __restrict__ anchor, double G,
                        const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ g,
                        float4* rec0, double* x0, double* y0, double* g0, int32_t* partner, int32_t* zb,
                        int32_t* zb_prev) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int2 a = anchor[leaf_of[i]];
+    float2 a = anchor[leaf_of[i]];
     double xi = x[i], yi = y[i], gi = g[i];
-    rec0[i] = make_float4(rel(xi, a.x, G), rel(yi, a.y, G), (float)dsgn(gi), 0.f);
+    rec0[i] = make_float4(rel(xi, a.x), rel(yi, a.y), (float)dsgn(gi), 0.f);
     x0[i] = xi; y0[i] = yi; g0[i] = gi;
     partner[i] = -1;
     zb[i] = INT_MAX;
@@ -149,7 +149,7 @@ __global__ void k_eps_box(int64_t nl, const int32_t* __restrict__ lvf, const int
 // list instead.  The warp also marks L dirty when a candidate leaf changed in the last
 // round, and records the extents of the list and of the near region in L's frame.
 __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, const int2* __restrict__ near_run,
-                           const int2* __restrict__ anchor, const float4* __restrict__ box,
+                           const float2* __restrict__ anchor, const float4* __restrict__ box,
                            const int32_t* __restrict__ live, float Gf, int32_t* cand, int32_t* ncand, float* rn,
                            float* rlist, float* rnear, const int32_t* __restrict__ leaf_changed, int32_t* dirty,
                            int first_round, const float* __restrict__ dmax_p) {
@@ -157,7 +157,7 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
     const int lane = threadIdx.x & 31;
     if (L >= nl) return;
     const float4 bL = box[L];
-    const int2 aL = anchor[L];
+    const float2 aL = anchor[L];
     const int32_t r0 = near_off[L], r1 = near_off[L + 1];
     const float dmax = first_round ? 0.f : *dmax_p;
     // upper bound on every target's second-nearest distance (squared)
@@ -260,7 +260,7 @@ __device__ __forceinline__ void top2_push(Top2& t, double d, int32_t j) {
 
 struct EpsView {
     const int32_t* lvf; const int32_t* lvl;
-    const int2* anchor; const float4* box; const float* rn; const float* rnear; const float* dmax;
+    const float2* anchor; const float4* box; const float* rn; const float* rnear; const float* dmax;
     const int32_t* near_off; const int2* near_run;
     const int32_t* cand; const int32_t* ncand;
     const float4* rec0; const float4* recO;
@@ -307,7 +307,7 @@ __device__ __forceinline__ float box_lb(float4 b, float2 sh, float tx, float ty)
 
 // Visits leaf q's live candidates for target i (shared by both passes).
 template <int PASS>
-__device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, int2 aL, int32_t i, int32_t excl, float tx,
+__device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, float2 aL, int32_t i, int32_t excl, float tx,
                                           float ty, double px, double py, float D, float& t1, float& t2,
                                           float& thr, Top2& best) {
     float2 sh = frame_shift(v.anchor[q], aL, v.Gf);
@@ -332,8 +332,8 @@ __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, int2 aL, 
 // candidate leaves, excluding slot excl.  Returns the exact FP64 top-2 of the reference.
 __device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl, double px, double py,
                             bool use_list) {
-    const int2 aL = v.anchor[L];
-    const float tx = (float)(px - (double)aL.x * v.G), ty = (float)(py - (double)aL.y * v.G);
+    const float2 aL = v.anchor[L];
+    const float tx = (float)(px - (double)aL.x), ty = (float)(py - (double)aL.y);
     const float ext = (use_list ? v.rn[L] : v.rnear[L]) + *v.dmax;
     const float D = ldexpf(ext + fabsf(tx) + fabsf(ty) + v.Gf, -17);
     float t1 = INFINITY, t2 = INFINITY, thr = INFINITY;
@@ -436,7 +436,7 @@ __global__ void k_zb_reset(int64_t n, const int32_t* __restrict__ zb, int32_t* z
 }
 
 __global__ void k_zb_scatter(int64_t n, const int32_t* __restrict__ partner, const int32_t* __restrict__ leaf_of,
-                             const int2* __restrict__ anchor, double G, const double* __restrict__ ox,
+                             const float2* __restrict__ anchor, double G, const double* __restrict__ ox,
                              const double* __restrict__ oy, const double* __restrict__ og,
                              const double* __restrict__ x0, const double* __restrict__ y0, int32_t* zb, float4* recO,
                              int32_t* dmax_bits) {
@@ -445,8 +445,8 @@ __global__ void k_zb_scatter(int64_t n, const int32_t* __restrict__ partner, con
     int32_t p = partner[i];
     if (p >= 0) {
         atomicMin(&zb[p], (int32_t)i);
-        int2 a = anchor[leaf_of[i]];
-        recO[i] = make_float4(rel(ox[i], a.x, G), rel(oy[i], a.y, G), (float)dsgn(og[i]), 0.f);
+        float2 a = anchor[leaf_of[i]];
+        recO[i] = make_float4(rel(ox[i], a.x), rel(oy[i], a.y), (float)dsgn(og[i]), 0.f);
         // displacement of the merged position (rounded up), for the candidate-list check
         float d = (float)(fabs(ox[i] - x0[i]) + fabs(oy[i] - y0[i])) * (1.f + 1e-5f);
         atomicMax(dmax_bits, __float_as_int(d));

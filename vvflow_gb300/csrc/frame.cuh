@@ -1,10 +1,11 @@
 // Local FP32 frames for pairwise kernels.
 //
-// Every leaf gets an anchor point a = G * (kx, ky) on a power-of-two grid G.  A vortex is
-// stored in FP32 relative to the anchor of its own leaf.  For a target leaf L and a source
-// leaf q the shift between frames, G * (kq - kL), is exact in FP32 (an integer below 2^24
-// times a power of two), so a source coordinate in the target's frame costs one rounded
-// addition.  Positions of order 100 with spacings of order 1e-3 keep ~1e-7 relative
+// Every leaf gets an anchor point a = G * (kx, ky) on a power-of-two grid G, stored as FP32
+// (exact: |k| < 2^21).  A vortex is stored in FP32 relative to the anchor of its own leaf.
+// For a target leaf L and a source leaf q the shift between frames, aq - aL = G (kq - kL),
+// is an exact FP32 subtraction, so a source coordinate in the target's frame costs one
+// rounded addition and no integer-to-float conversion (those run on the narrow FP64 /
+// conversion pipe of sm_103).  Positions of order 100 with spacings of order 1e-3 keep ~1e-7 relative
 // precision in every pair displacement, where a global FP32 frame would keep ~1e-3.
 #pragma once
 
@@ -29,13 +30,13 @@ inline Frame make_frame(double extent) {
     return f;
 }
 
-__device__ __forceinline__ int2 anchor_of(double cx, double cy, double G) {
-    return make_int2((int)rint(cx / G), (int)rint(cy / G));
+__device__ __forceinline__ float2 anchor_of(double cx, double cy, double G) {
+    return make_float2((float)(rint(cx / G) * G), (float)(rint(cy / G) * G));
 }
 
 // Exact FP32 shift between two anchors.
-__device__ __forceinline__ float2 frame_shift(int2 from, int2 to, float Gf) {
-    return make_float2((float)(from.x - to.x) * Gf, (float)(from.y - to.y) * Gf);
+__device__ __forceinline__ float2 frame_shift(float2 from, float2 to, float) {
+    return make_float2(from.x - to.x, from.y - to.y);
 }
 
 }  // namespace vvgpu

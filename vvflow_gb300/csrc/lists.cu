@@ -30,7 +30,7 @@ struct ListView {
     const int32_t* ch1;
     const int32_t* dfs;
     const float4* nf_geo;    // x, y (anchor frame), h + w, 0
-    const int2* nf_k;        // node anchors
+    const float2* nf_k;      // node anchors (FP32, exact)
     const float4* nf_cm;     // CMp x, y, CMm x, y (anchor frame)
     const float2* nf_g;      // CMp g, CMm g
     const double* cm;        // exact centroids (6 per node)
@@ -47,11 +47,11 @@ __device__ __forceinline__ bool far_exact(const double4& tg, const double4& me, 
 }
 
 // FP32 filter, FP64 on the boundary.
-__device__ __forceinline__ bool far_test(const ListView& v, int32_t t, int32_t meN, float4 mg, int2 mk) {
+__device__ __forceinline__ bool far_test(const ListView& v, int32_t t, int32_t meN, float4 mg, float2 mk) {
     float4 tg = v.nf_geo[t];
-    int2 tk = v.nf_k[t];
-    float dx = (float)(tk.x - mk.x) * v.Gf + (tg.x - mg.x);
-    float dy = (float)(tk.y - mk.y) * v.Gf + (tg.y - mg.y);
+    float2 tk = v.nf_k[t];
+    float dx = (tk.x - mk.x) + (tg.x - mg.x);
+    float dy = (tk.y - mk.y) + (tg.y - mg.y);
     float lhs = dx * dx + dy * dy;
     float hp = tg.z + mg.z;
     float rhs = v.fcf * hp * hp;
@@ -64,13 +64,13 @@ __device__ __forceinline__ bool far_test(const ListView& v, int32_t t, int32_t m
 }
 
 __global__ void k_node_frames(int64_t nn, const double4* __restrict__ geom, const double* __restrict__ cm, double G,
-                              float4* nf_geo, int2* nf_k, float4* nf_cm, float2* nf_g) {
+                              float4* nf_geo, float2* nf_k, float4* nf_cm, float2* nf_g) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nn) return;
     double4 gm = geom[k];
     double cx = isfinite(gm.x) ? gm.x : 0., cy = isfinite(gm.y) ? gm.y : 0.;
-    int2 a = anchor_of(cx, cy, G);
-    double ax = (double)a.x * G, ay = (double)a.y * G;
+    float2 a = anchor_of(cx, cy, G);
+    double ax = (double)a.x, ay = (double)a.y;
     nf_geo[k] = make_float4((float)(gm.x - ax), (float)(gm.y - ay), (float)(gm.z + gm.w), 0.f);
     nf_k[k] = a;
     const double* c = cm + 6 * k;
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(LB) k_walk(int64_t nl, ListView v, const int32
     }
     const int32_t meN = leaf_node[L];
     const float4 mg = v.nf_geo[meN];
-    const int2 mk = v.nf_k[meN];
+    const float2 mk = v.nf_k[meN];
     int32_t stack[MAX_DEPTH + 2];
     int sp = 0;
     stack[sp++] = 0;
@@ -167,10 +167,10 @@ template <bool FP32>
 struct Taylor {
     double d1 = 0, d2 = 0, d3 = 0, d4 = 0;
     float h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0, h4 = 0, l4 = 0;
-    __device__ __forceinline__ void add(const ListView& v, int32_t t, float4 mg, int2 mk, const double4& me) {
+    __device__ __forceinline__ void add(const ListView& v, int32_t t, float4 mg, float2 mk, const double4& me) {
         if (FP32) {
-            const int2 tk = v.nf_k[t];
-            const float sx = (float)(mk.x - tk.x) * v.Gf, sy = (float)(mk.y - tk.y) * v.Gf;
+            const float2 tk = v.nf_k[t];
+            const float sx = mk.x - tk.x, sy = mk.y - tk.y;
             const float4 c4 = v.nf_cm[t];
             const float2 gg = v.nf_g[t];
             float dpx = sx + (mg.x - c4.x), dpy = sy + (mg.y - c4.y);
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(WW * 32) k_walk_warp(int64_t nl, ListView v, c
     if (!all) return;
     const int32_t meN = valid ? leaf_node[L] : 0;
     const float4 mg = v.nf_geo[meN];
-    const int2 mk = v.nf_k[meN];
+    const float2 mk = v.nf_k[meN];
     const double4 me = v.geom[meN];
     Taylor<FP32> tay;
     int32_t nr = 0, last = -2, rfirst = -1, nfar = 0;

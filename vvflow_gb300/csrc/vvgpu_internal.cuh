@@ -154,7 +154,7 @@ struct Ctx {
     DArr<double4> lf_taylor;        // far-field expansion coefficients T1..T4 per leaf
     int taylor_precision = 0;
     DArr<float4> nf_geo, nf_cm;     // per node, anchor frame: centre + (h+w); centroids
-    DArr<int2> nf_k;                // per node anchor
+    DArr<float2> nf_k;              // per node anchor (FP32, exact)
     DArr<float2> nf_g;              // per node centroid circulations
     int64_t n_near_runs = 0, n_far = 0;
     DArr<int32_t> leaf_of;          // vortex -> leaf (DFS index)
@@ -173,11 +173,11 @@ struct Ctx {
 
     // local FP32 frames (frame.cuh)
     double frame_G = 1.0;
-    DArr<int2> lf_anchor;
+    DArr<float2> lf_anchor;
     DArr<float4> lf_box32;          // per leaf: min x, min y, max x, max y in its own frame
     DArr<float> lf_rn;              // per leaf: extent of its near region in its frame
     DArr<float4> src32;             // per vortex: x, y in own leaf frame, g, eps^2
-    DArr<int2> src_k;               // per vortex: anchor of its leaf
+    DArr<float2> src_k;             // per vortex: anchor of its leaf
     DArr<float4> lf_dbox;           // per leaf (diffusive): box of non-zero vortices and segment centres
 
     // SLAE
