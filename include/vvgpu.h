@@ -171,6 +171,16 @@ int vvgpu_convective(vvgpu_ctx* ctx);
 int vvgpu_diffusive(vvgpu_ctx* ctx);
 int vvgpu_velocity_points(vvgpu_ctx* ctx, int64_t n, const double* px, const double* py,
                           double* vx, double* vy);
+/* Same as vvgpu_velocity_points, for callers that must not allocate device memory (a fixed
+ * device-memory budget, or probes that must not trigger the synchronisation cudaMalloc and
+ * cudaFree imply).  It has no counterpart in the reference.  Points and results are staged
+ * in one fixed device array of VVGPU_NOALLOC_MAX_POINTS points that every call shares: at
+ * most that many points per call (VVGPU_ERR_LIMIT otherwise), and calls whose GPU work
+ * overlaps race on the array.  The first call on each device looks the array's device
+ * address up (cudaGetSymbolAddress); make it before any stream capture. */
+#define VVGPU_NOALLOC_MAX_POINTS 16384
+int vvgpu_velocity_points_noalloc(vvgpu_ctx* ctx, int64_t n, const double* px, const double* py,
+                                  double* vx, double* vy);
 /* calc_circulation with no collision; rigid bodies at rest or in prescribed translation
  * are in scope (VVGPU_ERR_UNSUPPORTED otherwise). */
 int vvgpu_slae(vvgpu_ctx* ctx, vvgpu_body_out* out);

@@ -497,4 +497,15 @@ void velocity_points(Ctx& c, int64_t np, const double* px, const double* py, dou
     VV_CUDA(cudaStreamSynchronize(s));
 }
 
+// Point velocities for points already in device memory: the same kernel as
+// velocity_points, launched on caller-provided device buffers, allocating nothing.
+void velocity_points_on_device(Ctx& c, int64_t np, const double* dpx, const double* dpy, double* dvx,
+                               double* dvy) {
+    check_bodies_at_rest(c);
+    if (np == 0) return;
+    ConvArgs a = make_args(c);
+    k_points<<<grid_for(np, 128), 128, 0, c.st()>>>(np, dpx, dpy, c.nd_geom.p, c.nd_ch1.p, c.nd_dfs.p, a, dvx, dvy);
+    VV_LAUNCH_CHECK();
+}
+
 }  // namespace vvgpu

@@ -251,6 +251,7 @@ void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t
 void eps_pass(Ctx& c, int merge, int64_t* merged);
 void convective(Ctx& c);
 void velocity_points(Ctx& c, int64_t n, const double* px, const double* py, double* vx, double* vy);
+void velocity_points_on_device(Ctx& c, int64_t n, const double* dpx, const double* dpy, double* dvx, double* dvy);
 void diffusive(Ctx& c);
 void slae(Ctx& c, vvgpu_body_out* out);
 void upload_segments(Ctx& c);

@@ -99,6 +99,7 @@ SIGNATURES = {
     "vvgpu_convective": (C.c_int, [_H]),
     "vvgpu_diffusive": (C.c_int, [_H]),
     "vvgpu_velocity_points": (C.c_int, [_H, C.c_int64, _D, _D, _D, _D]),
+    "vvgpu_velocity_points_noalloc": (C.c_int, [_H, C.c_int64, _D, _D, _D, _D]),
     "vvgpu_slae": (C.c_int, [_H, C.POINTER(BodyOut)]),
     "vvgpu_vortex_shed": (C.c_int, [_H]),
     "vvgpu_gsum": (C.c_int, [_H, _D]),
