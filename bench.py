@@ -370,7 +370,8 @@ def gpu_arm(args):
                        "parallelism": f"replicas x{world}"},
             "fp64": fp64, "accuracy": acc, "phases_ms": phases,
             "tree": {k: stp[k] for k in ("n_leaves", "n_nodes", "tree_depth", "near_runs", "merge_rounds",
-                                         "merged", "near_pairs", "far_pairs", "diff_candidates")},
+                                         "merged", "eps_evaluations", "near_pairs", "far_pairs",
+                                         "diff_candidates")},
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": world * N / (e2e_ms / 1e3), "unit": "vortex-steps/s", "ms_per_step": e2e_ms,

@@ -111,7 +111,8 @@ typedef struct vvgpu_stats {
     int64_t merge_rounds;       /* fixed-point rounds of the last epsilon pass           */
     int64_t merged;             /* merges in the last epsilon pass                       */
     int64_t diff_candidates;    /* vortex pairs inside the 8-eps cut-off boxes           */
-    int64_t reserved[8];        /* reserved[0]: kernels launched by the context so far   */
+    int64_t reserved[8];        /* reserved[0]: kernels launched by the context so far;
+                                   reserved[1]: target evaluations over all epsilon rounds */
 } vvgpu_stats;
 
 /* ---- context --------------------------------------------------------------------- */
@@ -163,7 +164,9 @@ int vvgpu_get_body_geom(vvgpu_ctx* ctx, int body, double* area, double* cofm_x, 
 
 /* ---- hot path --------------------------------------------------------------------- */
 /* stree(S, farCriteria, minNodeSize, maxNodeSize).build(); far_criteria is a double here
- * (the reference takes an int; theta = sqrt(2 / far_criteria)). */
+ * (the reference takes an int; theta = sqrt(2 / far_criteria)).  The build makes the near
+ * and far lists of the leaves holding a segment centre (all vvgpu_slae reads); the near
+ * lists of the other leaves follow on the first call that needs them. */
 int vvgpu_tree_build(vvgpu_ctx* ctx, double far_criteria, double min_node, double max_node);
 int vvgpu_tree_destroy(vvgpu_ctx* ctx);
 int vvgpu_eps(vvgpu_ctx* ctx, int merge, int64_t* merged);
@@ -177,7 +180,9 @@ int vvgpu_velocity_points(vvgpu_ctx* ctx, int64_t n, const double* px, const dou
  * in one fixed device array of VVGPU_NOALLOC_MAX_POINTS points that every call shares: at
  * most that many points per call (VVGPU_ERR_LIMIT otherwise), and calls whose GPU work
  * overlaps race on the array.  The first call on each device looks the array's device
- * address up (cudaGetSymbolAddress); make it before any stream capture. */
+ * address up (cudaGetSymbolAddress); make it before any stream capture.  It reads the near
+ * lists of every leaf, which the tree builds on its first vvgpu_eps, vvgpu_convective,
+ * vvgpu_diffusive or vvgpu_velocity_points call; before that it returns VVGPU_ERR_STATE. */
 #define VVGPU_NOALLOC_MAX_POINTS 16384
 int vvgpu_velocity_points_noalloc(vvgpu_ctx* ctx, int64_t n, const double* px, const double* py,
                                   double* vx, double* vy);

@@ -11,7 +11,8 @@
 // the reciprocal by Newton-Raphson iteration from the hardware approximation.
 // FP32 path: sources in local frames (frame.cuh), FP32 pair arithmetic, lane partials
 // accumulated per near run and folded into a two-sum (Knuth's TwoSum) compensated pair,
-// final reduction in FP64.
+// lane partials reduced as double-float pairs; FP64 (a narrow pipe on sm_103) only in the
+// final per-target update.
 #include <cfloat>
 
 #include "frame.cuh"
@@ -47,6 +48,16 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     float bp = s - a;
     float ap = s - bp;
     e = (a - ap) + (b - bp);
+}
+
+// Double-float addition (a_h, a_l) += (b_h, b_l): TwoSum of the heads, the tails added to
+// the error term, renormalised by Dekker's Fast2Sum.
+__device__ __forceinline__ void ff_add(float& ah, float& al, float bh, float bl) {
+    float s, e;
+    two_sum(ah, bh, s, e);
+    e += al + bl;
+    ah = s + e;
+    al = e - (ah - s);
 }
 
 template <class T>
@@ -165,7 +176,7 @@ __global__ void __launch_bounds__(CW * 32) k_conv64(ConvArgs a) {
 // partial sums for up to 16 sources and then folds them into a TwoSum-compensated pair.
 constexpr int TC32 = 8;
 
-__global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
+__global__ void __launch_bounds__(CW * 32, 4) k_conv32(ConvArgs a) {
     __shared__ int2 s_runs[CW][32];
     const int wq = threadIdx.x >> 5;
     const int64_t L = (int64_t)blockIdx.x * CW + wq;
@@ -174,7 +185,6 @@ __global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
     const double4 me = a.lgeom[L];
     const double4 tc = a.taylor[L];
     const float2 kL = a.anchor[L];
-    const double axL = (double)kL.x, ayL = (double)kL.y;
     const int32_t v0 = a.lvf[L], v1 = a.lvl[L];
     const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
     for (int32_t c0 = v0; c0 < v1; c0 += 2 * TC32) {
@@ -188,9 +198,10 @@ __global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
 #pragma unroll
         for (int t = 0; t < TC32; t++) {
             const int32_t i = t0 + t;
-            const bool ok = i < c0 + nt;
-            tx[t] = ok ? (float)(a.x[i] - axL) : 0.f;
-            ty[t] = ok ? (float)(a.y[i] - ayL) : 0.f;
+            // a target's own source record is already in this leaf's frame
+            const float4 r4 = (i < c0 + nt) ? a.src32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            tx[t] = r4.x;
+            ty[t] = r4.y;
             hx[t] = hy[t] = lx[t] = ly[t] = px[t] = py[t] = 0.f;
         }
         int since = 0;
@@ -246,40 +257,54 @@ __global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
             }
             __syncwarp();
         }
-        double ax[TC32], ay[TC32];
+        // Reduce-scatter of the 16 float-float partials (x and y of 8 targets) over the 16
+        // lanes of each source stride: after the xor-8/4/2/1 steps lane k (= lane & 15)
+        // holds value k, i.e. coordinate k >> 3 of target k & 7, summed over its 16 lanes.
+        float vh[2 * TC32], vl[2 * TC32];
 #pragma unroll
         for (int t = 0; t < TC32; t++) {
             float sv, e;
-            two_sum(hx[t], px[t], sv, e); lx[t] += e; hx[t] = sv;
-            two_sum(hy[t], py[t], sv, e); ly[t] += e; hy[t] = sv;
-            ax[t] = (double)hx[t] + (double)lx[t];
-            ay[t] = (double)hy[t] + (double)ly[t];
-#pragma unroll
-            for (int o = 8; o > 0; o >>= 1) {
-                ax[t] += __shfl_xor_sync(0xffffffffu, ax[t], o);
-                ay[t] += __shfl_xor_sync(0xffffffffu, ay[t], o);
-            }
-            if (!split) {
-                ax[t] += __shfl_xor_sync(0xffffffffu, ax[t], 16);
-                ay[t] += __shfl_xor_sync(0xffffffffu, ay[t], 16);
-            }
+            two_sum(hx[t], px[t], sv, e); vh[t] = sv; vl[t] = lx[t] + e;
+            two_sum(hy[t], py[t], sv, e); vh[t + TC32] = sv; vl[t + TC32] = ly[t] + e;
         }
 #pragma unroll
-        for (int t = 0; t < TC32; t++) {
-            const int32_t i = t0 + t;
-            if (sub == t && i < c0 + nt && a.g[i] != 0.) {
-                const double pxd = a.x[i], pyd = a.y[i];
-                double ex, ey;
-                extra_terms(a, pxd, pyd, ex, ey);
-                const double dlx = pxd - me.x, dly = pyd - me.y;
-                double vx = a.vx[i], vy = a.vy[i];
-                vx += a.inf_vx; vy += a.inf_vy;
-                vx += ax[t] * C_1_2PI; vy += ay[t] * C_1_2PI;
-                vx += ex; vy += ey;
-                vx += tc.x; vy += tc.y;
+        for (int m = TC32; m >= 1; m >>= 1) {
+            const bool up = (lane & m) != 0;
+#pragma unroll
+            for (int k = 0; k < m; k++) {
+                float kh = up ? vh[k + m] : vh[k], kl = up ? vl[k + m] : vl[k];
+                const float sh = up ? vh[k] : vh[k + m], sl = up ? vl[k] : vl[k + m];
+                ff_add(kh, kl, __shfl_xor_sync(0xffffffffu, sh, m), __shfl_xor_sync(0xffffffffu, sl, m));
+                vh[k] = kh; vl[k] = kl;
+            }
+        }
+        float rh = vh[0], rl = vl[0];
+        if (!split) ff_add(rh, rl, __shfl_xor_sync(0xffffffffu, rh, 16), __shfl_xor_sync(0xffffffffu, rl, 16));
+        // FP64 only from here on, once per (target, coordinate) and with all lanes converged.
+        const int k = lane & 15;
+        const int32_t i = t0 + (k & (TC32 - 1));
+        if ((split || lane < 16) && i < c0 + nt && a.g[i] != 0.) {
+            const double pxd = a.x[i], pyd = a.y[i];
+            const double acc = ((double)rh + (double)rl) * C_1_2PI;
+            double ex, ey;
+            extra_terms(a, pxd, pyd, ex, ey);
+            const double dlx = pxd - me.x, dly = pyd - me.y;
+            if (k < TC32) {
+                double vx = a.vx[i];
+                vx += a.inf_vx;
+                vx += acc;
+                vx += ex;
+                vx += tc.x;
                 vx += tc.z * dlx + tc.w * dly;
+                a.vx[i] = vx;
+            } else {
+                double vy = a.vy[i];
+                vy += a.inf_vy;
+                vy += acc;
+                vy += ey;
+                vy += tc.y;
                 vy += tc.w * dlx + (-tc.z) * dly;
-                a.vx[i] = vx; a.vy[i] = vy;
+                a.vy[i] = vy;
             }
         }
     }
@@ -289,7 +314,7 @@ __global__ void __launch_bounds__(CW * 32, 5) k_conv32(ConvArgs a) {
 // _1_eps or zero g gives a record that contributes exactly zero).
 __global__ void k_src32(int64_t n, const int32_t* __restrict__ leaf_of, const float2* __restrict__ anchor, double G,
                         const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ g,
-                        const double* __restrict__ ie, float4* src, float2* src_k) {
+                        const double* __restrict__ ie, float4* src, float2* src_k, float* src_ie) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float2 k = anchor[leaf_of[i]];
@@ -299,6 +324,7 @@ __global__ void k_src32(int64_t n, const int32_t* __restrict__ leaf_of, const fl
     if (ie[i] == 0.) { gf = 0.f; e2 = 1.f; }
     src[i] = make_float4((float)(x[i] - (double)k.x), (float)(y[i] - (double)k.y), gf, e2);
     src_k[i] = k;
+    src_ie[i] = (float)ie[i];
 }
 
 __global__ void k_anchor2(int64_t nl, const double4* __restrict__ lgeom, double G, float2* anchor) {
@@ -432,13 +458,14 @@ void build_frames(Ctx& c) {
     c.lf_anchor.reserve(nl + 1);
     c.src32.reserve(n + 1);
     c.src_k.reserve(n + 1);
+    c.src_ie.reserve(n + 1);
     if (nl) {
         k_anchor2<<<grid_for(nl, 128), 128, 0, s>>>(nl, c.lf_geom.p, fr.G, c.lf_anchor.p);
         VV_LAUNCH_CHECK();
     }
     if (n) {
         k_src32<<<grid_for(n, 256), 256, 0, s>>>(n, c.leaf_of.p, c.lf_anchor.p, fr.G, c.x.p, c.y.p, c.g.p, c.ie.p,
-                                                 c.src32.p, c.src_k.p);
+                                                 c.src32.p, c.src_k.p, c.src_ie.p);
         VV_LAUNCH_CHECK();
     }
 }

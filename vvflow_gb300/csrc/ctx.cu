@@ -216,6 +216,7 @@ int vvgpu_get_stats(const vvgpu_ctx* h, vvgpu_stats* out) {
     if (!h || !out) return VVGPU_ERR_ARG;
     *out = h->c.stats;
     out->reserved[0] = h->c.launches;
+    out->reserved[1] = h->c.eps_evaluations;
     return VVGPU_OK;
 }
 
@@ -435,12 +436,14 @@ int vvgpu_tree_build(vvgpu_ctx* h, double far_criteria, double min_node, double 
 int vvgpu_tree_destroy(vvgpu_ctx* h) {
     API_BEGIN(h)
     c.built = false;
+    c.lists_full = false;
     API_END
 }
 
 int vvgpu_eps(vvgpu_ctx* h, int merge, int64_t* merged) {
     API_BEGIN(h)
     if (!c.built) throw ApiError{VVGPU_ERR_NOT_BUILT, "tree is not built"};
+    ensure_full_lists(c);
     eps_pass(c, merge, merged);
     API_END
 }
@@ -448,6 +451,7 @@ int vvgpu_eps(vvgpu_ctx* h, int merge, int64_t* merged) {
 int vvgpu_convective(vvgpu_ctx* h) {
     API_BEGIN(h)
     if (!c.built) throw ApiError{VVGPU_ERR_NOT_BUILT, "tree is not built"};
+    ensure_full_lists(c);
     convective(c);
     API_END
 }
@@ -455,6 +459,7 @@ int vvgpu_convective(vvgpu_ctx* h) {
 int vvgpu_diffusive(vvgpu_ctx* h) {
     API_BEGIN(h)
     if (!c.built) throw ApiError{VVGPU_ERR_NOT_BUILT, "tree is not built"};
+    ensure_full_lists(c);
     diffusive(c);
     API_END
 }
@@ -463,6 +468,7 @@ int vvgpu_velocity_points(vvgpu_ctx* h, int64_t n, const double* px, const doubl
     API_BEGIN(h)
     if (!c.built) throw ApiError{VVGPU_ERR_NOT_BUILT, "tree is not built"};
     if (n < 0 || (n && (!px || !py || !vx || !vy))) throw ApiError{VVGPU_ERR_ARG, "bad point arrays"};
+    ensure_full_lists(c);
     velocity_points(c, n, px, py, vx, vy);
     API_END
 }
@@ -491,6 +497,7 @@ int vvgpu_gsum(vvgpu_ctx* h, double* out) {
 int vvgpu_tree_sizes(vvgpu_ctx* h, int64_t* nnodes, int64_t* nleaves, int64_t* nnear, int64_t* nfar) {
     API_BEGIN(h)
     if (!c.built) throw ApiError{VVGPU_ERR_NOT_BUILT, "tree is not built"};
+    ensure_full_lists(c);
     std::vector<int2> runs(c.n_near_runs);
     d2h(runs.data(), c.near_run.p, c.n_near_runs, c.st());
     VV_CUDA(cudaStreamSynchronize(c.st()));
@@ -589,6 +596,7 @@ int vvgpu_tree_lists(vvgpu_ctx* h, int64_t* near_off, int32_t* near_depth, int64
                      int32_t* far_depth, int64_t* far_path) {
     API_BEGIN(h)
     if (!c.built) throw ApiError{VVGPU_ERR_NOT_BUILT, "tree is not built"};
+    ensure_full_lists(c);
     int64_t nl = c.nleaves, nn = c.nnodes;
     cudaStream_t s = c.st();
     std::vector<int32_t> noff(nl + 1), foff, fnode, ln(nl), dep(nn);

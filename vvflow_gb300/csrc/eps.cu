@@ -10,8 +10,9 @@
 // circulation if j < i merged at its own turn.  Given guesses of all outcomes, every
 // vortex evaluates in parallel; the outcome of i only depends on outcomes of k < i, so
 // repeating until nothing changes converges to the unique fixed point, which is the
-// sequential result, bit for bit.  Typical runs need 5-7 rounds; after the first round
-// only leaves near a changed outcome are evaluated again.
+// sequential result, bit for bit.  Typical runs need 5-7 rounds.  After the first round a
+// target is evaluated again only when its absorber changed or a vortex whose outcome
+// changed lies (before or after the change) inside a region its last searches examined.
 //
 // Candidate leaves: for each target leaf L, R_L bounds every target's second-nearest
 // distance from above (the farthest corner distance to a leaf that holds two live
@@ -23,6 +24,7 @@
 // rigorous margin and evaluates only the candidates inside the margin in FP64, with the
 // reference's operation order and its tie rule (first in list order wins), so every
 // decision equals the reference's.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 
@@ -36,6 +38,7 @@ namespace {
 constexpr int EB = 128;
 constexpr int32_t SKIPPED = -2;  // partner code: vortex not evaluated (g = 0 at its turn)
 constexpr int CAND_CAP = 96;     // candidate leaves kept per target leaf
+constexpr int CHG_CAP = 48;      // changed near leaves kept per target leaf
 
 // MEpsilonFast::nearestBodySegment (MEpsilonFast.cpp:214-253) and the per-leaf merge
 // criterion / epsilon floor (MEpsilonFast.cpp:25-47).
@@ -113,14 +116,20 @@ __global__ void k_rec0(int64_t n, const int32_t* __restrict__ leaf_of, const flo
 
 // Per-leaf FP32 box (own frame) over every position a non-zero member may have this round,
 // and the number of members that are live for every target (never absorbed, non-zero).
+// Also keeps the previous round's box, and the largest squared search radius any member's
+// last evaluation used (rreg; -1 when no member searched).
 __global__ void k_eps_box(int64_t nl, const int32_t* __restrict__ lvf, const int32_t* __restrict__ lvl,
                           const float4* __restrict__ rec0, const float4* __restrict__ recO,
                           const int32_t* __restrict__ partner, const int32_t* __restrict__ zb, float4* box,
-                          int32_t* live) {
+                          float4* box_prev, int32_t* live, const float* __restrict__ sr1,
+                          const float* __restrict__ sr2, float* rreg, int first_round) {
     int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= nl) return;
     float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
     int32_t nlive = 0;
+    float rr = -1.f;
+    if (!first_round)
+        for (int32_t i = lvf[L]; i < lvl[L]; i++) rr = fmaxf(rr, fmaxf(sr1[i], sr2[i]));
     for (int32_t i = lvf[L]; i < lvl[L]; i++) {
         float4 r = rec0[i];
         if (r.z != 0.f) {
@@ -133,8 +142,11 @@ __global__ void k_eps_box(int64_t nl, const int32_t* __restrict__ lvf, const int
         }
         if (r.z != 0.f && zb[i] == INT_MAX && (!moved || recO[i].z != 0.f)) nlive++;
     }
-    box[L] = make_float4(mnx, mny, mxx, mxy);
+    const float4 nb = make_float4(mnx, mny, mxx, mxy);
+    box_prev[L] = first_round ? nb : box[L];
+    box[L] = nb;
     live[L] = nlive;
+    rreg[L] = first_round ? INFINITY : rr;
 }
 
 // Candidate leaves of every target leaf (one warp per target leaf).
@@ -146,14 +158,18 @@ __global__ void k_eps_box(int64_t nl, const int32_t* __restrict__ lvf, const int
 // remembers that radius; in later rounds it stays valid while R_L (now) plus the largest
 // merge displacement fits inside it (boxes only grow by merged positions), otherwise it is
 // rebuilt.  The re-search after a merge (from a point up to R_L away) walks the whole near
-// list instead.  The warp also marks L dirty when a candidate leaf changed in the last
-// round, and records the extents of the list and of the near region in L's frame.
+// list instead.  The warp also collects the near leaves whose members' outcomes changed in
+// the last round (L is dirty when there is one) and records the extents of the list and of
+// the near region in L's frame.
 __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, const int2* __restrict__ near_run,
                            const float2* __restrict__ anchor, const float4* __restrict__ box,
                            const int32_t* __restrict__ live, float Gf, int32_t* cand, int32_t* ncand, float* rn,
                            float* rlist, float* rnear, const int32_t* __restrict__ leaf_changed, int32_t* dirty,
-                           int first_round, const float* __restrict__ dmax_p) {
-    const int64_t L = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+                           int32_t* chg, int32_t* nchg, const float4* __restrict__ box_prev,
+                           const float* __restrict__ rreg, int first_round, const float* __restrict__ dmax_p) {
+    __shared__ int2 s_runs[EB / 32][32];
+    const int wq = threadIdx.x >> 5;
+    const int64_t L = (int64_t)blockIdx.x * (blockDim.x / 32) + wq;
     const int lane = threadIdx.x & 31;
     if (L >= nl) return;
     const float4 bL = box[L];
@@ -167,18 +183,16 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
             const float ux = bL.z - bL.x, uy = bL.w - bL.y;
             R2 = ux * ux + uy * uy;
         } else {
-            for (int32_t r = r0; r < r1; r++) {
-                const int2 run = near_run[r];
-                for (int32_t q = run.x + lane; q < run.y; q += 32) {
-                    const int need = (q == L) ? 3 : 2;
-                    if (live[q] < need) continue;
-                    const float4 b = box[q];
-                    const float2 sh = frame_shift(anchor[q], aL, Gf);
-                    const float ux = fmaxf(fabsf(b.z + sh.x - bL.x), fabsf(bL.z - (b.x + sh.x)));
-                    const float uy = fmaxf(fabsf(b.w + sh.y - bL.y), fabsf(bL.w - (b.y + sh.y)));
-                    R2 = fminf(R2, ux * ux + uy * uy);
-                }
-            }
+            for_near_leaves(near_run, r0, r1, s_runs[wq], [&](int32_t q, bool ok) {
+                if (!ok) return;
+                const int need = (q == L) ? 3 : 2;
+                if (live[q] < need) return;
+                const float4 b = box[q];
+                const float2 sh = frame_shift(anchor[q], aL, Gf);
+                const float ux = fmaxf(fabsf(b.z + sh.x - bL.x), fabsf(bL.z - (b.x + sh.x)));
+                const float uy = fmaxf(fabsf(b.w + sh.y - bL.y), fabsf(bL.w - (b.y + sh.y)));
+                R2 = fminf(R2, ux * ux + uy * uy);
+            });
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) R2 = fminf(R2, __shfl_xor_sync(0xffffffffu, R2, o));
         }
@@ -187,53 +201,79 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
     const float need_r = isfinite(R2) ? sqrtf(R2) * (1.f + 1e-4f) + dmax + absm : INFINITY;
     const int32_t nc_old = first_round ? -2 : ncand[L];
     const bool reuse = !first_round && nc_old >= 0 && need_r <= rlist[L];
-    bool is_dirty = first_round != 0;
+    // Near leaves whose members' outcomes changed in the last round and whose box (this or
+    // the last round's, which hold every position those members had) comes within the
+    // largest search radius of L's targets; each target then checks them against its own
+    // search regions.  L itself always counts (a member's absorber may have changed).
+    int32_t nch = 0;
+    const float rr2 = first_round ? -1.f : rreg[L];
+    const float rreach = isfinite(rr2) ? sqrtf(fmaxf(rr2, 0.f)) * (1.f + 1e-4f) : INFINITY;
+    auto box_gap = [&](float4 b, float2 sh) {
+        if (!(b.x <= b.z)) return INFINITY;
+        const float dx = fmaxf(fmaxf(b.x + sh.x - bL.z, bL.x - (b.z + sh.x)), 0.f);
+        const float dy = fmaxf(fmaxf(b.y + sh.y - bL.w, bL.y - (b.w + sh.y)), 0.f);
+        const float slack = ldexpf(fabsf(b.x + sh.x) + fabsf(b.z + sh.x) + fabsf(b.y + sh.y) + fabsf(b.w + sh.y), -12);
+        return sqrtf(dx * dx + dy * dy) - slack;
+    };
+    auto collect = [&](int32_t q, bool ok) {
+        bool ch = ok && !first_round && leaf_changed[q];
+        if (ch && q != L) {
+            if (!(rr2 >= 0.f)) {
+                ch = false;  // no member of L searched: only its own absorbers matter
+            } else if (isfinite(rreach)) {
+                const float2 sh = frame_shift(anchor[q], aL, Gf);
+                const float gap = fminf(box_gap(box[q], sh), box_gap(box_prev[q], sh));
+                ch = gap <= rreach + absm;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, ch);
+        if (ch) {
+            const int pos = nch + __popc(m & ((1u << lane) - 1));
+            if (pos < CHG_CAP) chg[(size_t)L * CHG_CAP + pos] = q;
+        }
+        nch += __popc(m);
+    };
     if (reuse) {
-        const int32_t* cl = cand + (size_t)L * CAND_CAP;
-        bool d = false;
-        for (int32_t k = lane; k < nc_old; k += 32) d = d || leaf_changed[cl[k]];
-        is_dirty = __any_sync(0xffffffffu, d);
-        if (lane == 0) dirty[L] = is_dirty ? 1 : 0;
+        for_near_leaves(near_run, r0, r1, s_runs[wq], collect);
+        if (lane == 0) {
+            nchg[L] = (nch > CHG_CAP) ? -1 : nch;
+            dirty[L] = nch > 0 ? 1 : 0;
+        }
         return;
     }
     // (re)build: near leaves within 2 R_L of L's box (FP32 with margins)
     const float lim = isfinite(R2) ? 2.f * sqrtf(R2) * (1.f + 1e-4f) + absm : INFINITY;
     float ext = 0.f, next = 0.f;
     int32_t cnt = 0;
-    for (int32_t r = r0; r < r1; r++) {
-        const int2 run = near_run[r];
-        for (int32_t qb = run.x; qb < run.y; qb += 32) {
-            const int32_t q = qb + lane;
-            bool hit = false;
-            float e = 0.f;
-            if (q < run.y) {
-                const float4 b = box[q];
-                if (b.x <= b.z) {
-                    const float2 sh = frame_shift(anchor[q], aL, Gf);
-                    const float bx0 = b.x + sh.x, bx1 = b.z + sh.x, by0 = b.y + sh.y, by1 = b.w + sh.y;
-                    const float dx = fmaxf(fmaxf(bx0 - bL.z, bL.x - bx1), 0.f);
-                    const float dy = fmaxf(fmaxf(by0 - bL.w, bL.y - by1), 0.f);
-                    hit = !isfinite(lim) || (dx <= lim && dy <= lim && dx * dx + dy * dy <= lim * lim);
-                    e = fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)), fmaxf(fabsf(by0), fabsf(by1)));
-                    next = fmaxf(next, e);
-                    if (!hit) e = 0.f;
-                }
+    for_near_leaves(near_run, r0, r1, s_runs[wq], [&](int32_t q, bool ok) {
+        bool hit = false;
+        float e = 0.f;
+        if (ok) {
+            const float4 b = box[q];
+            if (b.x <= b.z) {
+                const float2 sh = frame_shift(anchor[q], aL, Gf);
+                const float bx0 = b.x + sh.x, bx1 = b.z + sh.x, by0 = b.y + sh.y, by1 = b.w + sh.y;
+                const float dx = fmaxf(fmaxf(bx0 - bL.z, bL.x - bx1), 0.f);
+                const float dy = fmaxf(fmaxf(by0 - bL.w, bL.y - by1), 0.f);
+                hit = !isfinite(lim) || (dx <= lim && dy <= lim && dx * dx + dy * dy <= lim * lim);
+                e = fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)), fmaxf(fabsf(by0), fabsf(by1)));
+                next = fmaxf(next, e);
+                if (!hit) e = 0.f;
             }
-            const unsigned mask = __ballot_sync(0xffffffffu, hit);
-            if (hit) {
-                const int pos = cnt + __popc(mask & ((1u << lane) - 1));
-                if (pos < CAND_CAP) cand[(size_t)L * CAND_CAP + pos] = q;
-                if (!first_round && leaf_changed[q]) is_dirty = true;
-            }
-            cnt += __popc(mask);
-            ext = fmaxf(ext, e);
         }
-    }
+        const unsigned mask = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const int pos = cnt + __popc(mask & ((1u << lane) - 1));
+            if (pos < CAND_CAP) cand[(size_t)L * CAND_CAP + pos] = q;
+        }
+        cnt += __popc(mask);
+        ext = fmaxf(ext, e);
+        collect(q, ok);
+    });
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
         next = fmaxf(next, __shfl_xor_sync(0xffffffffu, next, o));
-        is_dirty = __shfl_xor_sync(0xffffffffu, (int)is_dirty, o) || is_dirty;
     }
     if (lane == 0) {
         ncand[L] = (cnt > CAND_CAP) ? -1 : cnt;  // -1: use the whole near list
@@ -242,13 +282,15 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
         const float own = fmaxf(fmaxf(fabsf(bL.x), fabsf(bL.z)), fmaxf(fabsf(bL.y), fabsf(bL.w)));
         rn[L] = fmaxf(ext, own + (isfinite(lim) ? lim : 0.f));
         if (first_round) rnear[L] = fmaxf(next, own);
-        dirty[L] = is_dirty ? 1 : 0;
+        nchg[L] = (nch > CHG_CAP) ? -1 : nch;
+        dirty[L] = (first_round || nch > 0) ? 1 : 0;
     }
 }
 
 struct Top2 {
     double r1, r2;
     int32_t l1, l2;
+    float thr;  // FP32 squared radius in the leaf frame holding every candidate that can decide
 };
 
 __device__ __forceinline__ void top2_push(Top2& t, double d, int32_t j) {
@@ -305,11 +347,32 @@ __device__ __forceinline__ float box_lb(float4 b, float2 sh, float tx, float ty)
     return dx * dx + dy * dy;
 }
 
+// Candidates met by the FP32 pass whose distance was within the threshold at the time
+// (the threshold only shrinks, so they include every candidate within the final one).
+// When it overflows, the exact pass scans the candidate leaves again.
+constexpr int NBUF = 12;
+struct NearBuf {
+    float d[NBUF];
+    int32_t j[NBUF];
+    int n = 0;
+    bool ovf = false;
+    __device__ __forceinline__ void push(float dd, int32_t jj, float thr) {
+        if (n == NBUF) {  // drop what the threshold has excluded since
+            int m = 0;
+            for (int k = 0; k < NBUF; k++)
+                if (d[k] <= thr) { d[m] = d[k]; j[m] = j[k]; m++; }
+            n = m;
+        }
+        if (n < NBUF) { d[n] = dd; j[n] = jj; n++; }
+        else ovf = true;
+    }
+};
+
 // Visits leaf q's live candidates for target i (shared by both passes).
 template <int PASS>
 __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, float2 aL, int32_t i, int32_t excl, float tx,
                                           float ty, double px, double py, float D, float& t1, float& t2,
-                                          float& thr, Top2& best) {
+                                          float& thr, Top2& best, NearBuf& buf) {
     float2 sh = frame_shift(v.anchor[q], aL, v.Gf);
     if (box_lb(v.box[q], sh, tx, ty) > thr) return;
     for (int32_t j = v.lvf[q]; j < v.lvl[q]; j++) {
@@ -320,6 +383,7 @@ __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, float2 aL
         if (PASS == 0) {
             if (d < t1) { t2 = t1; t1 = d; thr = thr_of(t2, D); }
             else if (d < t2) { t2 = d; thr = thr_of(t2, D); }
+            if (d <= thr) buf.push(d, j, thr);
         } else if (d <= thr) {
             double xj, yj, gj;
             cand_exact(v, j, i, xj, yj, gj);
@@ -337,97 +401,189 @@ __device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl
     const float ext = (use_list ? v.rn[L] : v.rnear[L]) + *v.dmax;
     const float D = ldexpf(ext + fabsf(tx) + fabsf(ty) + v.Gf, -17);
     float t1 = INFINITY, t2 = INFINITY, thr = INFINITY;
-    Top2 best{DBL_MAX, DBL_MAX, INT_MAX, INT_MAX};
+    Top2 best{DBL_MAX, DBL_MAX, INT_MAX, INT_MAX, INFINITY};
     const int32_t nc = use_list ? v.ncand[L] : -1;
-    // pass 0: FP32 second-smallest distance; pass 1: exact top-2 within the margin
+    NearBuf buf;
+    // pass 0: FP32 second-smallest distance, buffering the candidates within the running
+    // threshold; then the exact top-2 over the buffered candidates within the final margin
+    // (pass 1 rescans the leaves only when the buffer overflowed)
 #pragma unroll 1
     for (int pass = 0; pass < 2; pass++) {
-        if (pass == 1) thr = thr_of(t2, D);
-        if (pass == 0) scan_leaf<0>(v, L, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
-        else scan_leaf<1>(v, L, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
+        if (pass == 1) {
+            thr = thr_of(t2, D);
+            if (!buf.ovf) {
+                for (int k = 0; k < buf.n; k++) {
+                    if (!(buf.d[k] <= thr)) continue;
+                    double xj, yj, gj;
+                    cand_exact(v, buf.j[k], i, xj, yj, gj);
+                    top2_push(best, dabs2(dsub(px, xj), dsub(py, yj)), buf.j[k]);
+                }
+                break;
+            }
+        }
+        if (pass == 0) scan_leaf<0>(v, L, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
+        else scan_leaf<1>(v, L, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
         if (nc >= 0) {
             const int32_t* cl = v.cand + (size_t)L * CAND_CAP;
             for (int32_t k = 0; k < nc; k++) {
                 int32_t q = cl[k];
                 if (q == L) continue;
-                if (pass == 0) scan_leaf<0>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
-                else scan_leaf<1>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
+                if (pass == 0) scan_leaf<0>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
+                else scan_leaf<1>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
             }
         } else {
             for (int32_t r = v.near_off[L]; r < v.near_off[L + 1]; r++) {
                 int2 run = v.near_run[r];
                 for (int32_t q = run.x; q < run.y; q++) {
                     if (q == L) continue;
-                    if (pass == 0) scan_leaf<0>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
-                    else scan_leaf<1>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best);
+                    if (pass == 0) scan_leaf<0>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
+                    else scan_leaf<1>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
                 }
             }
         }
     }
+    best.thr = thr;
     return best;
 }
 
-__global__ void k_eps_round(int64_t n, EpsView v, const int32_t* __restrict__ leaf_of,
-                            const double* __restrict__ mcs_l, const double* __restrict__ epr_l,
-                            const double* __restrict__ ie_in, const int32_t* __restrict__ dirty,
-                            const double* __restrict__ oie_old, int32_t* partner_new, double* ox_new,
-                            double* oy_new, double* og_new, double* oie_new, int32_t* changed) {
+// Inputs of the last round's evaluation of a target, to tell whether it must run again.
+struct DirtyView {
+    const int32_t* zb_prev;   // absorber table the last evaluation saw
+    const int32_t* vch;       // vortex outcome changed in the last round
+    const int32_t* chg; const int32_t* nchg;
+    const float4* recO_old;   // merged records of the outcomes before the last round
+    float* sr1; float* sr2;   // search radii^2 of the last evaluation (< 0: no search)
+};
+
+// True when target i's evaluation can differ from its last one: its absorber changed, or a
+// vortex whose outcome changed had (or now has) a position inside one of the regions its
+// last searches examined (the first search around its own position, the re-search around
+// its merged position).  Positions and distances are formed exactly as the searches form
+// them, so every candidate that could enter a top-2 is seen.
+__device__ __forceinline__ bool touched(const EpsView& v, const DirtyView& d, int32_t L, int32_t i) {
+    if (d.zb_prev[i] != v.zb[i]) return true;
+    const float r1 = d.sr1[i], r2 = d.sr2[i];
+    if (!(r1 >= 0.f) && !(r2 >= 0.f)) return false;  // skipped last time, for the same reason now
+    const int32_t nch = d.nchg[L];
+    if (nch < 0) return true;
+    const float2 aL = v.anchor[L];
+    const float4 me = v.rec0[i];
+    const float4 mo = v.recO[i];
+    const float r1m = r1 * (1.f + 1e-5f), r2m = r2 * (1.f + 1e-5f);
+    for (int32_t k = 0; k < nch; k++) {
+        const int32_t q = d.chg[(size_t)L * CHG_CAP + k];
+        const float2 sh = frame_shift(v.anchor[q], aL, v.Gf);
+        for (int32_t j = v.lvf[q]; j < v.lvl[q]; j++) {
+            if (!d.vch[j] || j == i) continue;
+#pragma unroll
+            for (int w = 0; w < 3; w++) {
+                const float4 p = (w == 0) ? v.rec0[j] : (w == 1 ? v.recO[j] : d.recO_old[j]);
+                const float px = p.x + sh.x, py = p.y + sh.y;
+                if (r1 >= 0.f) {
+                    const float dx = me.x - px, dy = me.y - py;
+                    if (!(dx * dx + dy * dy > r1m)) return true;
+                }
+                if (r2 >= 0.f) {
+                    const float dx = mo.x - px, dy = mo.y - py;
+                    if (!(dx * dx + dy * dy > r2m)) return true;
+                }
+            }
+        }
+    }
+    return false;
+}
+
+// Rounds after the first: targets whose inputs did not change keep their outcome; the
+// others are flagged for evaluation (compacted in index order, so that neighbouring targets
+// stay together in a warp).
+__global__ void k_eps_mark(int64_t n, EpsView v, DirtyView dv, const int32_t* __restrict__ leaf_of,
+                           const int32_t* __restrict__ dirty, const double* __restrict__ oie_old,
+                           int32_t* partner_new, double* ox_new, double* oy_new, double* og_new, double* oie_new,
+                           int32_t* flag) {
     int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (ii >= n) return;
     const int32_t i = (int32_t)ii;
     const int32_t L = leaf_of[i];
-    if (!dirty[L]) {  // no input of this leaf's targets changed: keep the outcome
+    const bool keep = !dirty[L] || !touched(v, dv, L, i);
+    flag[i] = keep ? 0 : 1;
+    if (keep) {  // no input of this target changed
         partner_new[i] = v.partner[i];
         ox_new[i] = v.ox[i]; oy_new[i] = v.oy[i]; og_new[i] = v.og[i]; oie_new[i] = oie_old[i];
-        return;
     }
-    const double gi0 = v.g0[i];
-    int32_t partner = SKIPPED;
-    double px = v.x0[i], py = v.y0[i], gi = gi0, ie = ie_in[i];
-    if (gi0 != 0 && !(v.zb[i] < i)) {
-        const double mcs = mcs_l[L];
-        Top2 t = two_nearest(v, L, i, -1, px, py, true);
-        double e;
-        partner = -1;
-        if (t.l1 == INT_MAX) e = DBL_MIN;
-        else if (t.l2 == INT_MAX) e = __dsqrt_rn(t.r1);
-        else if (isnan(mcs)) e = __dsqrt_rn(t.r2);
-        else {
-            double x1, y1, g1, x2, y2, g2;
-            cand_exact(v, t.l1, i, x1, y1, g1);
-            cand_exact(v, t.l2, i, x2, y2, g2);
-            if ((t.r1 < mcs) || ((dsgn(g1) == dsgn(g2)) && (dsgn(g1) != dsgn(gi)))) {
-                // MergeVortexes (MEpsilonFast.cpp:111-126)
-                if (dsgn(gi) == dsgn(g1)) {
-                    double sx = dadd(dmul(px, gi), dmul(x1, g1));
-                    double sy = dadd(dmul(py, gi), dmul(y1, g1));
-                    double inv = ddiv(1., dadd(gi, g1));
-                    px = dmul(sx, inv);
-                    py = dmul(sy, inv);
-                } else if (fabs(gi) < fabs(g1)) {
-                    px = x1;
-                    py = y1;
+}
+
+__global__ void k_eps_compact(int64_t n, const int32_t* __restrict__ flag, const int32_t* __restrict__ pos,
+                              int32_t* list) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flag[i]) list[pos[i]] = (int32_t)i;
+}
+
+// Evaluates the targets list[0 .. *count) (every target when list is null; count = n).
+__global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* __restrict__ list,
+                            const int32_t* __restrict__ count, const int32_t* __restrict__ leaf_of,
+                            const double* __restrict__ mcs_l, const double* __restrict__ epr_l,
+                            const double* __restrict__ ie_in, const double* __restrict__ oie_old,
+                            int32_t* partner_new, double* ox_new, double* oy_new, double* og_new, double* oie_new,
+                            int32_t* changed, unsigned long long* evals) {
+    const int64_t cnt = list ? (int64_t)*count : n;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(evals, (unsigned long long)cnt);
+    for (int64_t kk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; kk < cnt;
+         kk += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t i = list ? list[kk] : (int32_t)kk;
+        const int32_t L = leaf_of[i];
+        const double gi0 = v.g0[i];
+        int32_t partner = SKIPPED;
+        double px = v.x0[i], py = v.y0[i], gi = gi0, ie = ie_in[i];
+        float sr1 = -1.f, sr2 = -1.f;
+        if (gi0 != 0 && !(v.zb[i] < i)) {
+            const double mcs = mcs_l[L];
+            Top2 t = two_nearest(v, L, i, -1, px, py, true);
+            sr1 = t.thr;
+            double e;
+            partner = -1;
+            if (t.l1 == INT_MAX) e = DBL_MIN;
+            else if (t.l2 == INT_MAX) e = __dsqrt_rn(t.r1);
+            else if (isnan(mcs)) e = __dsqrt_rn(t.r2);
+            else {
+                double x1, y1, g1, x2, y2, g2;
+                cand_exact(v, t.l1, i, x1, y1, g1);
+                cand_exact(v, t.l2, i, x2, y2, g2);
+                if ((t.r1 < mcs) || ((dsgn(g1) == dsgn(g2)) && (dsgn(g1) != dsgn(gi)))) {
+                    // MergeVortexes (MEpsilonFast.cpp:111-126)
+                    if (dsgn(gi) == dsgn(g1)) {
+                        double sx = dadd(dmul(px, gi), dmul(x1, g1));
+                        double sy = dadd(dmul(py, gi), dmul(y1, g1));
+                        double inv = ddiv(1., dadd(gi, g1));
+                        px = dmul(sx, inv);
+                        py = dmul(sy, inv);
+                    } else if (fabs(gi) < fabs(g1)) {
+                        px = x1;
+                        py = y1;
+                    }
+                    gi = dadd(gi, g1);
+                    partner = t.l1;
+                    Top2 u = two_nearest(v, L, i, t.l1, px, py, false);
+                    sr2 = u.thr;
+                    if (u.l1 == INT_MAX) e = DBL_MIN;
+                    else if (u.l2 == INT_MAX) e = __dsqrt_rn(u.r1);
+                    else e = __dsqrt_rn(u.r2);
+                } else {
+                    e = __dsqrt_rn(t.r2);
                 }
-                gi = dadd(gi, g1);
-                partner = t.l1;
-                Top2 u = two_nearest(v, L, i, t.l1, px, py, false);
-                if (u.l1 == INT_MAX) e = DBL_MIN;
-                else if (u.l2 == INT_MAX) e = __dsqrt_rn(u.r1);
-                else e = __dsqrt_rn(u.r2);
-            } else {
-                e = __dsqrt_rn(t.r2);
             }
+            ie = ddiv(1.0, smax(e, epr_l[L]));
         }
-        ie = ddiv(1.0, smax(e, epr_l[L]));
+        bool ch = (partner != v.partner[i] && !(partner == SKIPPED && v.partner[i] == SKIPPED)) ||
+                  (__double_as_longlong(px) != __double_as_longlong(v.ox[i])) ||
+                  (__double_as_longlong(py) != __double_as_longlong(v.oy[i])) ||
+                  (__double_as_longlong(gi) != __double_as_longlong(v.og[i])) ||
+                  (__double_as_longlong(ie) != __double_as_longlong(oie_old[i]));
+        partner_new[i] = partner;
+        ox_new[i] = px; oy_new[i] = py; og_new[i] = gi; oie_new[i] = ie;
+        dv.sr1[i] = sr1;
+        dv.sr2[i] = sr2;
+        if (ch) *changed = 1;
     }
-    bool ch = (partner != v.partner[i] && !(partner == SKIPPED && v.partner[i] == SKIPPED)) ||
-              (__double_as_longlong(px) != __double_as_longlong(v.ox[i])) ||
-              (__double_as_longlong(py) != __double_as_longlong(v.oy[i])) ||
-              (__double_as_longlong(gi) != __double_as_longlong(v.og[i])) ||
-              (__double_as_longlong(ie) != __double_as_longlong(oie_old[i]));
-    partner_new[i] = partner;
-    ox_new[i] = px; oy_new[i] = py; og_new[i] = gi; oie_new[i] = ie;
-    if (ch) *changed = 1;
 }
 
 __global__ void k_zb_reset(int64_t n, const int32_t* __restrict__ zb, int32_t* zb_prev, int32_t* zb_new) {
@@ -459,7 +615,7 @@ __global__ void k_leaf_changed(int64_t n, const int32_t* __restrict__ leaf_of, c
                                const double* __restrict__ x_new, const double* __restrict__ y_old,
                                const double* __restrict__ y_new, const double* __restrict__ g_old,
                                const double* __restrict__ g_new, const int32_t* __restrict__ zb_old,
-                               const int32_t* __restrict__ zb_new, int32_t* leaf_changed) {
+                               const int32_t* __restrict__ zb_new, int32_t* leaf_changed, int32_t* vch) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int32_t po = p_old[i] < 0 ? -1 : p_old[i], pn = p_new[i] < 0 ? -1 : p_new[i];
@@ -469,6 +625,7 @@ __global__ void k_leaf_changed(int64_t n, const int32_t* __restrict__ leaf_of, c
              __double_as_longlong(y_old[i]) != __double_as_longlong(y_new[i]) ||
              __double_as_longlong(g_old[i]) != __double_as_longlong(g_new[i]);
     }
+    vch[i] = ch ? 1 : 0;
     if (ch) leaf_changed[leaf_of[i]] = 1;
 }
 
@@ -528,7 +685,17 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
     c.e_lchanged.reserve(nl + 1);
     k_anchor<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.lf_geom.p, fr.G, c.lf_anchor.p);
     VV_LAUNCH_CHECK();
-    c.e_rec0.reserve(n); c.e_recO.reserve(n);
+    c.e_rec0.reserve(n); c.e_recO[0].reserve(n); c.e_recO[1].reserve(n);
+    c.e_vch.reserve(n); c.e_sr1.reserve(n); c.e_sr2.reserve(n);
+    c.e_chg.reserve((size_t)nl * CHG_CAP + 1);
+    c.e_nchg.reserve(nl + 1);
+    c.e_box_prev.reserve(nl + 1);
+    c.e_flag.reserve(n + 1);
+    c.e_pos.reserve(n + 2);
+    c.e_list.reserve(n + 1);
+    c.e_rreg.reserve(nl + 1);
+    VV_CUDA(cudaMemsetAsync(c.e_recO[0].p, 0, n * sizeof(float4), s));
+    VV_CUDA(cudaMemsetAsync(c.e_recO[1].p, 0, n * sizeof(float4), s));
     c.e_x0.reserve(n); c.e_y0.reserve(n); c.e_g0.reserve(n); c.e_zb.reserve(n); c.e_zb_prev.reserve(n);
     for (int k = 0; k < 2; k++) {
         c.e_partner[k].reserve(n); c.e_ox[k].reserve(n); c.e_oy[k].reserve(n); c.e_og[k].reserve(n);
@@ -550,26 +717,42 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
     c.e_rnear.reserve(nl + 1);
     int32_t* dmax_bits = (int32_t*)(c.counters.p + 13);
     VV_CUDA(cudaMemsetAsync(dmax_bits, 0, 4, s));
+    VV_CUDA(cudaMemsetAsync(c.counters.p + 14, 0, 8, s));
     for (;;) {
         rounds++;
         // boxes and candidate leaves from the current guesses
-        k_eps_box<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.lf_vf.p, c.lf_vl.p, c.e_rec0.p, c.e_recO.p,
-                                                  c.e_partner[cur].p, c.e_zb.p, c.lf_box32.p, c.e_live.p);
+        k_eps_box<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.lf_vf.p, c.lf_vl.p, c.e_rec0.p, c.e_recO[cur].p,
+                                                  c.e_partner[cur].p, c.e_zb.p, c.lf_box32.p, c.e_box_prev.p,
+                                                  c.e_live.p, c.e_sr1.p, c.e_sr2.p, c.e_rreg.p, rounds == 1);
         VV_LAUNCH_CHECK();
         k_eps_cand<<<grid_for(nl, EB / 32), EB, 0, s>>>(nl, c.near_off.p, c.near_run.p, c.lf_anchor.p,
                                                        c.lf_box32.p, c.e_live.p, fr.Gf, c.e_cand.p, c.e_ncand.p,
                                                        c.lf_rn.p, c.e_rlist.p, c.e_rnear.p, c.e_lchanged.p,
-                                                       c.e_dirty.p, rounds == 1, (const float*)dmax_bits);
+                                                       c.e_dirty.p, c.e_chg.p, c.e_nchg.p, c.e_box_prev.p,
+                                                       c.e_rreg.p, rounds == 1, (const float*)dmax_bits);
         VV_LAUNCH_CHECK();
         VV_CUDA(cudaMemsetAsync(c.e_changed.p, 0, 4, s));
         EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.e_rnear.p,
                   (const float*)dmax_bits, c.near_off.p, c.near_run.p,
-                  c.e_cand.p, c.e_ncand.p, c.e_rec0.p, c.e_recO.p, c.e_x0.p, c.e_y0.p, c.e_g0.p,
+                  c.e_cand.p, c.e_ncand.p, c.e_rec0.p, c.e_recO[cur].p, c.e_x0.p, c.e_y0.p, c.e_g0.p,
                   c.e_partner[cur].p, c.e_zb.p, c.e_ox[cur].p, c.e_oy[cur].p, c.e_og[cur].p, fr.G, fr.Gf};
         const int nx = cur ^ 1;
-        k_eps_round<<<grid_for(n, EB), EB, 0, s>>>(n, v, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_dirty.p,
-                                                   c.e_oie[cur].p, c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p,
-                                                   c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p);
+        DirtyView dv{c.e_zb_prev.p, c.e_vch.p, c.e_chg.p, c.e_nchg.p, c.e_recO[nx].p, c.e_sr1.p, c.e_sr2.p};
+        const int32_t* list = nullptr;
+        if (rounds > 1) {
+            k_eps_mark<<<grid_for(n, EB), EB, 0, s>>>(n, v, dv, c.leaf_of.p, c.e_dirty.p, c.e_oie[cur].p,
+                                                      c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p,
+                                                      c.e_oie[nx].p, c.e_flag.p);
+            VV_LAUNCH_CHECK();
+            exclusive_scan(c, c.e_flag.p, c.e_pos.p, n);
+            k_eps_compact<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_flag.p, c.e_pos.p, c.e_list.p);
+            VV_LAUNCH_CHECK();
+            list = c.e_list.p;
+        }
+        const unsigned eg = rounds > 1 ? std::min<unsigned>(grid_for(n, EB), 152u * 32u) : grid_for(n, EB);
+        k_eps_round<<<eg, EB, 0, s>>>(n, v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p,
+                                      c.e_oie[cur].p, c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p,
+                                      c.e_oie[nx].p, c.e_changed.p, c.counters.p + 14);
         VV_LAUNCH_CHECK();
         // new absorber table and merged records; leaves whose members changed
         k_zb_reset<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_zb.p, c.e_zb_prev.p, c.e_zb.p);
@@ -577,13 +760,13 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
         VV_CUDA(cudaMemsetAsync(dmax_bits, 0, 4, s));
         k_zb_scatter<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_partner[nx].p, c.leaf_of.p, c.lf_anchor.p, fr.G,
                                                     c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_x0.p, c.e_y0.p,
-                                                    c.e_zb.p, c.e_recO.p, dmax_bits);
+                                                    c.e_zb.p, c.e_recO[nx].p, dmax_bits);
         VV_LAUNCH_CHECK();
         VV_CUDA(cudaMemsetAsync(c.e_lchanged.p, 0, (nl + 1) * 4, s));
         k_leaf_changed<<<grid_for(n, EB), EB, 0, s>>>(n, c.leaf_of.p, c.e_partner[cur].p, c.e_partner[nx].p,
                                                       c.e_ox[cur].p, c.e_ox[nx].p, c.e_oy[cur].p, c.e_oy[nx].p,
                                                       c.e_og[cur].p, c.e_og[nx].p, c.e_zb_prev.p, c.e_zb.p,
-                                                      c.e_lchanged.p);
+                                                      c.e_lchanged.p, c.e_vch.p);
         VV_LAUNCH_CHECK();
         cur = nx;
         int32_t changed = read_i32(c, c.e_changed.p);
@@ -595,9 +778,11 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                c.e_og[cur].p, c.e_oie[cur].p, c.x.p, c.y.p, c.g.p, c.ie.p,
                                                c.counters.p);
     VV_LAUNCH_CHECK();
-    unsigned long long mcount = 0;
+    unsigned long long mcount = 0, nev = 0;
     VV_CUDA(cudaMemcpyAsync(&mcount, c.counters.p, 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaMemcpyAsync(&nev, c.counters.p + 14, 8, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));
+    c.eps_evaluations = (int64_t)nev;
     if (merged) *merged = (int64_t)mcount;
     c.stats.merged = (int64_t)mcount;
     c.stats.merge_rounds = rounds;

@@ -108,19 +108,21 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
 }
 
 // Per-leaf walk (one thread per leaf) for selected leaves only (sel[L] != 0).
-// MODE 1: write the near runs at near_off[L] (leaves whose runs overflowed the warp walk's
-//         buffer).  MODE 2: count (PASS 0) or write (PASS 1) the far list of the leaf.
-template <int PASS, bool FP32_UNUSED>
+// PASS 0 counts, PASS 1 writes at the offsets.  Bit 1 of `what`: near runs (near_cnt /
+// near_off / near_run); bit 2: far nodes (far_cnt / far_off / far_node).  Unselected leaves
+// count zero.
+template <int PASS>
 __global__ void __launch_bounds__(LB) k_walk(int64_t nl, ListView v, const int32_t* __restrict__ leaf_node,
-                                             const int32_t* __restrict__ sel, int32_t* near_cnt_unused,
-                                             int32_t* far_cnt, const int32_t* __restrict__ near_off,
-                                             const int32_t* __restrict__ far_off, int2* near_run,
-                                             int32_t* far_node, double4* taylor_unused, int64_t nodes_bound,
-                                             int32_t* err, unsigned long long* far_total_unused, int mode) {
+                                             const int32_t* __restrict__ sel, int32_t* near_cnt, int32_t* far_cnt,
+                                             const int32_t* __restrict__ near_off, const int32_t* __restrict__ far_off,
+                                             int2* near_run, int32_t* far_node, int64_t nodes_bound, int32_t* err,
+                                             int what) {
     int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= nl) return;
+    const bool want_near = what & 1, want_far = what & 2;
     if (!sel[L]) {
-        if (mode == 2 && PASS == 0) far_cnt[L] = 0;
+        if (PASS == 0 && want_near) near_cnt[L] = 0;
+        if (PASS == 0 && want_far) far_cnt[L] = 0;
         return;
     }
     const int32_t meN = leaf_node[L];
@@ -130,14 +132,14 @@ __global__ void __launch_bounds__(LB) k_walk(int64_t nl, ListView v, const int32
     int sp = 0;
     stack[sp++] = 0;
     int32_t nr = 0, nf = 0, last = -2, rfirst = -1;
-    const int32_t nbase = (mode == 1) ? near_off[L] : 0;
-    const int32_t fbase = (mode == 2 && PASS) ? far_off[L] : 0;
+    const int32_t nbase = (PASS && want_near) ? near_off[L] : 0;
+    const int32_t fbase = (PASS && want_far) ? far_off[L] : 0;
     int64_t guard = 0;
     while (sp) {
         if (++guard > nodes_bound) { atomicExch(err, 2); break; }
         const int32_t t = stack[--sp];
         if (far_test(v, t, meN, mg, mk)) {
-            if (mode == 2 && PASS) far_node[fbase + nf] = t;
+            if (PASS && want_far) far_node[fbase + nf] = t;
             nf++;
             continue;
         }
@@ -152,14 +154,15 @@ __global__ void __launch_bounds__(LB) k_walk(int64_t nl, ListView v, const int32
         if (q == last + 1) {
             last = q;
         } else {
-            if (mode == 1 && rfirst >= 0) near_run[nbase + nr - 1] = make_int2(rfirst, last + 1);
+            if (PASS && want_near && rfirst >= 0) near_run[nbase + nr - 1] = make_int2(rfirst, last + 1);
             rfirst = q;
             last = q;
             nr++;
         }
     }
-    if (mode == 1 && rfirst >= 0) near_run[nbase + nr - 1] = make_int2(rfirst, last + 1);
-    if (mode == 2 && PASS == 0) far_cnt[L] = nf;
+    if (PASS && want_near && rfirst >= 0) near_run[nbase + nr - 1] = make_int2(rfirst, last + 1);
+    if (PASS == 0 && want_near) near_cnt[L] = nr;
+    if (PASS == 0 && want_far) far_cnt[L] = nf;
 }
 
 // Far-field contribution of far node t to leaf (mg, mk | me), FP32 or FP64.
@@ -332,6 +335,13 @@ __global__ void k_walk_exact(int64_t nl, const int32_t* __restrict__ leaf_node, 
 
 }  // namespace
 
+namespace {
+ListView list_view(Ctx& c) {
+    return ListView{c.nd_geom.p, c.nd_ch1.p, c.nd_dfs.p, c.nf_geo.p, c.nf_k.p, c.nf_cm.p, c.nf_g.p, c.nd_cm.p,
+                    c.far_criteria, (float)c.far_criteria, (float)c.frame_G};
+}
+}  // namespace
+
 void tree_lists(Ctx& c) {
     cudaStream_t s = c.st();
     const int64_t nl = c.nleaves, nn = c.nnodes;
@@ -354,10 +364,35 @@ void tree_lists(Ctx& c) {
                                                              c.nd_dfs.p, c.lf_flag.p);
         VV_LAUNCH_CHECK();
     }
-    ListView v{c.nd_geom.p, c.nd_ch1.p, c.nd_dfs.p, c.nf_geo.p, c.nf_k.p, c.nf_cm.p, c.nf_g.p, c.nd_cm.p,
-               c.far_criteria, (float)c.far_criteria, (float)fr.G};
+    const ListView v = list_view(c);
     c.near_cnt.reserve(nl + 1); c.far_cnt.reserve(nl + 1);
     c.near_off.reserve(nl + 2); c.far_off.reserve(nl + 2);
+    // near runs and far lists of the leaves that hold a segment centre
+    k_walk<0><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, c.near_cnt.p, c.far_cnt.p, nullptr,
+                                              nullptr, nullptr, nullptr, nn, err, 3);
+    VV_LAUNCH_CHECK();
+    exclusive_scan(c, c.near_cnt.p, c.near_off.p, nl);
+    exclusive_scan(c, c.far_cnt.p, c.far_off.p, nl);
+    c.n_near_runs = read_i32(c, c.near_off.p + nl);
+    c.n_far = read_i32(c, c.far_off.p + nl);
+    c.near_run.reserve(c.n_near_runs + 1);
+    c.far_node.reserve(c.n_far + 1);
+    k_walk<1><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, nullptr, nullptr, c.near_off.p,
+                                              c.far_off.p, c.near_run.p, c.far_node.p, nn, err, 3);
+    VV_LAUNCH_CHECK();
+    if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
+    c.lists_full = false;
+    c.stats.near_runs = c.n_near_runs;
+    c.stats.far_pairs = 0;
+}
+
+void ensure_full_lists(Ctx& c) {
+    if (c.lists_full) return;
+    cudaStream_t s = c.st();
+    const int64_t nl = c.nleaves, nn = c.nnodes;
+    int32_t* err = (int32_t*)c.counters.p + 1;
+    VV_CUDA(cudaMemsetAsync(err, 0, 4, s));
+    const ListView v = list_view(c);
     c.lf_taylor.reserve(nl + 1);
     c.run_buf.reserve((size_t)nl * RUN_CAP + 1);
     c.lf_overflow.reserve(nl + 1);
@@ -382,22 +417,12 @@ void tree_lists(Ctx& c) {
     const int32_t nover = read_i32(c, n_over);
     if (nover > 0) {
         // leaves with more than RUN_CAP runs: write their runs with the per-leaf walk
-        k_walk<1, true><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_overflow.p, nullptr, nullptr,
-                                                         c.near_off.p, nullptr, c.near_run.p, nullptr, nullptr, nn,
-                                                         err, nullptr, 1);
+        k_walk<1><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_overflow.p, nullptr, nullptr,
+                                                  c.near_off.p, nullptr, c.near_run.p, nullptr, nn, err, 1);
         VV_LAUNCH_CHECK();
+        if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
     }
-    // far lists of the leaves that hold a segment centre (read by the SLAE right-hand side)
-    k_walk<0, true><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, nullptr, c.far_cnt.p,
-                                                     nullptr, nullptr, nullptr, nullptr, nullptr, nn, err, nullptr, 2);
-    VV_LAUNCH_CHECK();
-    exclusive_scan(c, c.far_cnt.p, c.far_off.p, nl);
-    c.n_far = read_i32(c, c.far_off.p + nl);
-    c.far_node.reserve(c.n_far + 1);
-    k_walk<1, true><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, nullptr, nullptr, nullptr,
-                                                     c.far_off.p, nullptr, c.far_node.p, nullptr, nn, err, nullptr, 2);
-    VV_LAUNCH_CHECK();
-    if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
+    c.lists_full = true;
     c.stats.near_runs = c.n_near_runs;
     c.taylor_precision = c.precision;
     unsigned long long ft = 0;

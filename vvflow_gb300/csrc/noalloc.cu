@@ -58,6 +58,9 @@ extern "C" int vvgpu_velocity_points_noalloc(vvgpu_ctx* h, int64_t n, const doub
                                                 std::to_string(VVGPU_NOALLOC_MAX_POINTS) + " points per call, got " +
                                                 std::to_string(n)};
         if (!c.built) throw ApiError{VVGPU_ERR_NOT_BUILT, "tree is not built"};
+        if (!c.lists_full)
+            throw ApiError{VVGPU_ERR_STATE, "near lists not built yet: call vvgpu_velocity_points (or vvgpu_eps, "
+                                            "vvgpu_convective, vvgpu_diffusive) after vvgpu_tree_build first"};
         VV_CUDA(cudaSetDevice(c.device));
         double* base = nullptr;
         VV_CUDA(scratch_address(c.device, &base));

@@ -7,8 +7,10 @@
 // (counted from the left) trades places with the k-th element with key < pivot inside
 // [f+L, l) (counted from the right).  Here every level of the tree is split at once:
 // one exclusive scan of the "low" flags gives every element its rank, the right-side lows
-// publish their positions in a table, and each left-side high performs its swap.  The
-// resulting permutation, node boxes and ranges are bit-identical to the reference.
+// publish their positions in a table, and each left-side high performs its swap.  Only the
+// keys (x, y) and a slot permutation move at each level; the rest of the vortex record
+// follows once, after the last level.  The resulting permutation, node boxes and ranges are
+// bit-identical to the reference.
 // Segment lists (bllist) are split stably (TSortedTree.cpp:139-148).
 //
 // All decision arithmetic uses explicitly rounded FP64 operations (no FMA contraction),
@@ -27,36 +29,42 @@ __device__ __forceinline__ void bbox_min_atomic(unsigned long long* slot, double
 __device__ __forceinline__ void bbox_max_atomic(unsigned long long* slot, double v) { atomicMax(slot, dkey(v)); }
 
 // Segmented (by node id, contiguous within the warp) min/max reduction, then one atomic
-// per segment head.  node < 0 marks lanes that do not contribute.
+// per segment head.  node < 0 marks lanes that do not contribute.  The reduction runs on
+// the order-preserving integer keys of the coordinates (dkey), so it stays on the integer
+// pipe (FP64 min/max would run on sm_103's narrow FP64 pipe).
 __device__ __forceinline__ void warp_bbox_update(int node, double px, double py, unsigned long long* bbox) {
     const int lane = threadIdx.x & 31;
-    double mnx = px, mny = py, mxx = px, mxy = py;
+    const unsigned long long kx = dkey(px), ky = dkey(py);
+    unsigned long long mnx = kx, mny = ky, mxx = kx, mxy = ky;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        int on = __shfl_down_sync(0xffffffffu, node, o);
-        double a = __shfl_down_sync(0xffffffffu, mnx, o);
-        double b = __shfl_down_sync(0xffffffffu, mny, o);
-        double cc = __shfl_down_sync(0xffffffffu, mxx, o);
-        double d = __shfl_down_sync(0xffffffffu, mxy, o);
+        const int on = __shfl_down_sync(0xffffffffu, node, o);
+        const unsigned long long a = __shfl_down_sync(0xffffffffu, mnx, o);
+        const unsigned long long b = __shfl_down_sync(0xffffffffu, mny, o);
+        const unsigned long long cc = __shfl_down_sync(0xffffffffu, mxx, o);
+        const unsigned long long d = __shfl_down_sync(0xffffffffu, mxy, o);
         if (lane + o < 32 && on == node) {
-            mnx = fmin(mnx, a); mny = fmin(mny, b); mxx = fmax(mxx, cc); mxy = fmax(mxy, d);
+            mnx = a < mnx ? a : mnx;
+            mny = b < mny ? b : mny;
+            mxx = cc > mxx ? cc : mxx;
+            mxy = d > mxy ? d : mxy;
         }
     }
-    int prev = __shfl_up_sync(0xffffffffu, node, 1);
-    bool head = (lane == 0) || (prev != node);
+    const int prev = __shfl_up_sync(0xffffffffu, node, 1);
+    const bool head = (lane == 0) || (prev != node);
     if (head && node >= 0) {
         unsigned long long* s = bbox + 4 * (size_t)node;
-        bbox_min_atomic(s + 0, mnx);
-        bbox_min_atomic(s + 1, mny);
-        bbox_max_atomic(s + 2, mxx);
-        bbox_max_atomic(s + 3, mxy);
+        atomicMin(s + 0, mnx);
+        atomicMin(s + 1, mny);
+        atomicMax(s + 2, mxx);
+        atomicMax(s + 3, mxy);
     }
 }
 
-__global__ void k_init_root(int32_t* node_of, int64_t n, int32_t* seg_order, int32_t* seg_node_of, int64_t m,
-                            unsigned long long* bbox) {
+__global__ void k_init_root(int32_t* node_of, int32_t* perm, int64_t n, int32_t* seg_order, int32_t* seg_node_of,
+                            int64_t m, unsigned long long* bbox) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) node_of[i] = 0;
+    if (i < n) { node_of[i] = 0; perm[i] = (int32_t)i; }
     if (i < m) { seg_order[i] = (int32_t)i; seg_node_of[i] = 0; }
     if (i == 0) {
         bbox[0] = dkey(DBL_MAX); bbox[1] = dkey(DBL_MAX);
@@ -180,7 +188,7 @@ __global__ void k_vswap(int64_t n, int64_t a, int64_t b, const int32_t* __restri
                         const int32_t* __restrict__ split, const int32_t* __restrict__ vf,
                         const int32_t* __restrict__ nlow, const int32_t* __restrict__ flags,
                         const int32_t* __restrict__ S, const int32_t* __restrict__ tab_rl, double* x,
-                        double* y, double* g, double* ie, double* vx, double* vy, int64_t* orig) {
+                        double* y, int32_t* perm) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int32_t k = node_of[i];
@@ -189,11 +197,40 @@ __global__ void k_vswap(int64_t n, int64_t a, int64_t b, const int32_t* __restri
     if (i >= f + L || flags[i]) return;
     int32_t kk = (int32_t)(i - f) - (S[i] - S[f]);  // highs to the left of i inside the node
     int64_t j = tab_rl[f + kk];
-    double t;
-#define SWP(arr) t = arr[i]; arr[i] = arr[j]; arr[j] = t;
-    SWP(x) SWP(y) SWP(g) SWP(ie) SWP(vx) SWP(vy)
-#undef SWP
-    int64_t o = orig[i]; orig[i] = orig[j]; orig[j] = o;
+    // the keys move at every level; the rest of the record follows once, through perm
+    const double tx = x[i], ty = y[i];
+    x[i] = x[j]; y[i] = y[j];
+    x[j] = tx; y[j] = ty;
+    const int32_t tp = perm[i];
+    perm[i] = perm[j];
+    perm[j] = tp;
+}
+
+// Applies the partition's permutation to the rest of the vortex record (two passes through
+// staging buffers, so the arrays keep their device addresses).
+__global__ void k_perm_gather(int64_t n, const int32_t* __restrict__ perm, const double* __restrict__ g,
+                              const double* __restrict__ ie, const double* __restrict__ vx,
+                              const double* __restrict__ vy, const int64_t* __restrict__ orig, double* tmp,
+                              int64_t* otmp) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t p = perm[i];
+    tmp[i] = g[p];
+    tmp[n + i] = ie[p];
+    tmp[2 * n + i] = vx[p];
+    tmp[3 * n + i] = vy[p];
+    otmp[i] = orig[p];
+}
+
+__global__ void k_perm_store(int64_t n, const double* __restrict__ tmp, const int64_t* __restrict__ otmp, double* g,
+                             double* ie, double* vx, double* vy, int64_t* orig) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    g[i] = tmp[i];
+    ie[i] = tmp[n + i];
+    vx[i] = tmp[2 * n + i];
+    vy[i] = tmp[3 * n + i];
+    orig[i] = otmp[i];
 }
 
 __global__ void k_vassign(int64_t n, int64_t a, int64_t b, int32_t* node_of, const int32_t* __restrict__ split,
@@ -210,6 +247,40 @@ __global__ void k_vassign(int64_t n, int64_t a, int64_t b, int32_t* node_of, con
             node_of[i] = node;
             px = x[i]; py = y[i];
         }
+    }
+    // A block whose elements all go to one child (the rule near the root, where children
+    // are large) reduces in shared memory and makes 4 atomics instead of 4 per warp.
+    __shared__ int s_node0;
+    __shared__ unsigned long long s_red[TB / 32][4];
+    if (threadIdx.x == 0) s_node0 = node;
+    __syncthreads();
+    if (__syncthreads_and(node == s_node0)) {
+        if (node < 0) return;
+        unsigned long long k0 = dkey(px), k1 = dkey(py), k2 = k0, k3 = k1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long a0 = __shfl_xor_sync(0xffffffffu, k0, o);
+            const unsigned long long a1 = __shfl_xor_sync(0xffffffffu, k1, o);
+            const unsigned long long a2 = __shfl_xor_sync(0xffffffffu, k2, o);
+            const unsigned long long a3 = __shfl_xor_sync(0xffffffffu, k3, o);
+            k0 = a0 < k0 ? a0 : k0; k1 = a1 < k1 ? a1 : k1;
+            k2 = a2 > k2 ? a2 : k2; k3 = a3 > k3 ? a3 : k3;
+        }
+        const int w = threadIdx.x >> 5;
+        if ((threadIdx.x & 31) == 0) { s_red[w][0] = k0; s_red[w][1] = k1; s_red[w][2] = k2; s_red[w][3] = k3; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
+                k0 = s_red[q][0] < k0 ? s_red[q][0] : k0; k1 = s_red[q][1] < k1 ? s_red[q][1] : k1;
+                k2 = s_red[q][2] > k2 ? s_red[q][2] : k2; k3 = s_red[q][3] > k3 ? s_red[q][3] : k3;
+            }
+            unsigned long long* sb = bbox + 4 * (size_t)node;
+            atomicMin(sb + 0, k0);
+            atomicMin(sb + 1, k1);
+            atomicMax(sb + 2, k2);
+            atomicMax(sb + 3, k3);
+        }
+        return;
     }
     warp_bbox_update(node, px, py, bbox);
 }
@@ -386,7 +457,9 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
     int32_t* err = (int32_t*)c.counters.p;
 
     int64_t nm = n > m ? n : m;
-    k_init_root<<<grid_for(nm, TB), TB, 0, s>>>(c.node_of.p, n, c.seg_order.p, c.seg_node_of.p, m, c.nd_bbox.p);
+    c.perm.reserve(n + 1);
+    k_init_root<<<grid_for(nm, TB), TB, 0, s>>>(c.node_of.p, c.perm.p, n, c.seg_order.p, c.seg_node_of.p, m,
+                                                c.nd_bbox.p);
     VV_LAUNCH_CHECK();
     if (n + m > 0) {
         k_root_bbox<<<grid_for(n + m, TB), TB, 0, s>>>(c.x.p, c.y.p, n, c.s_rx.p, c.s_ry.p, m, c.nd_bbox.p);
@@ -423,8 +496,7 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
                                                    c.flags.p, c.scan.p, c.nd_nlow.p, c.tab_rl.p);
             VV_LAUNCH_CHECK();
             k_vswap<<<grid_for(n, TB), TB, 0, s>>>(n, a, b, c.node_of.p, c.nd_split.p, c.nd_vf.p, c.nd_nlow.p,
-                                                   c.flags.p, c.scan.p, c.tab_rl.p, c.x.p, c.y.p, c.g.p, c.ie.p,
-                                                   c.vx.p, c.vy.p, c.orig.p);
+                                                   c.flags.p, c.scan.p, c.tab_rl.p, c.x.p, c.y.p, c.perm.p);
             VV_LAUNCH_CHECK();
             k_vassign<<<grid_for(n, TB), TB, 0, s>>>(n, a, b, c.node_of.p, c.nd_split.p, c.nd_vf.p, c.nd_nlow.p,
                                                      c.nd_ch1.p, c.x.p, c.y.p, c.nd_bbox.p);
@@ -451,6 +523,15 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
         c.nnodes = b + 2 * (int64_t)nsplit;
     }
     c.depth = (int64_t)c.level_begin.size() - 1;
+    if (n > 0) {
+        c.ptmp.reserve(4 * (size_t)n);
+        c.otmp.reserve(n);
+        k_perm_gather<<<grid_for(n, TB), TB, 0, s>>>(n, c.perm.p, c.g.p, c.ie.p, c.vx.p, c.vy.p, c.orig.p, c.ptmp.p,
+                                                     c.otmp.p);
+        VV_LAUNCH_CHECK();
+        k_perm_store<<<grid_for(n, TB), TB, 0, s>>>(n, c.ptmp.p, c.otmp.p, c.g.p, c.ie.p, c.vx.p, c.vy.p, c.orig.p);
+        VV_LAUNCH_CHECK();
+    }
     if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree deeper than supported"};
 
     // centroids bottom-up, leaf counts, then depth-first leaf order top-down

@@ -129,6 +129,7 @@ struct Ctx {
 
     // tree
     bool built = false;
+    bool lists_full = false;        // near runs of every leaf (else only of segment leaves)
     double far_criteria = 8, min_node = 0, max_node = 0;
     int64_t nnodes = 0, nleaves = 0, depth = 0;
     std::vector<int64_t> level_begin;
@@ -140,6 +141,9 @@ struct Ctx {
     DArr<double> nd_pivot;
     DArr<int32_t> nd_axis, nd_split, nd_nlow, nd_nlow_s, nd_lc, nd_dfs;
     DArr<int32_t> node_of, seg_node_of, seg_node_of2, flags, scan;
+    DArr<int32_t> perm;              // tree build: source slot of each slot (keys move, payload follows once)
+    DArr<double> ptmp;               // tree build: payload staging for the final permutation
+    DArr<int64_t> otmp;
     DArr<int32_t> tab_lh, tab_rl;
     DArr<int32_t> seg_order, seg_order2;
     DArr<int32_t> leaf_node;        // DFS order -> node id
@@ -166,7 +170,12 @@ struct Ctx {
     // epsilon / merge (fixed-point rounds; [2] = double buffer)
     DArr<int32_t> e_partner[2], e_zb, e_changed;
     DArr<double> e_x0, e_y0, e_g0, e_ox[2], e_oy[2], e_og[2], e_oie[2];
-    DArr<float4> e_rec0, e_recO;
+    DArr<float4> e_rec0, e_recO[2];
+    DArr<int32_t> e_vch, e_chg, e_nchg;  // per vortex: outcome changed; per leaf: changed near leaves
+    DArr<float> e_sr1, e_sr2;            // per vortex: search radii^2 of its last evaluation
+    DArr<float4> e_box_prev;             // per leaf: the last round's box
+    DArr<float> e_rreg;                  // per leaf: largest search radius^2 of its members
+    DArr<int32_t> e_flag, e_pos, e_list; // targets to evaluate in a round (flags, offsets, list)
     DArr<double> lf_mcs, lf_epr;
     DArr<int32_t> e_zb_prev, e_live, e_cand, e_ncand, e_dirty, e_lchanged;
     DArr<float> e_rlist, e_rnear;
@@ -178,6 +187,7 @@ struct Ctx {
     DArr<float> lf_rn;              // per leaf: extent of its near region in its frame
     DArr<float4> src32;             // per vortex: x, y in own leaf frame, g, eps^2
     DArr<float2> src_k;             // per vortex: anchor of its leaf
+    DArr<float> src_ie;             // per vortex: (float)_1_eps
     DArr<float4> lf_dbox;           // per leaf (diffusive): box of non-zero vortices and segment centres
 
     // SLAE
@@ -190,6 +200,7 @@ struct Ctx {
     int64_t neq_cached = 0;
     vvgpu_stats stats{};
     int64_t launches = 0;           // kernels launched by this context
+    int64_t eps_evaluations = 0;    // target evaluations over the rounds of the last epsilon pass
     bool count_pairs = true;        // count algorithmic near pairs before each convective pass
 
     cudaStream_t st() const { return stream; }
@@ -227,6 +238,49 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return v;
 }
 
+// Warp-cooperative iteration over the leaves of the near runs [r0, r1).  Every lane calls
+// f(q, valid) the same number of times, so f may use warp votes; q is a near leaf when
+// valid.  Runs are taken 32 at a time, their lengths prefix-summed across the lanes into s
+// (32 entries of per-warp shared memory), and each lane finds its run by binary search: all
+// lanes stay busy however short the runs are.  Leaves come in near-list order, 32 per call.
+template <class F>
+__device__ __forceinline__ void for_near_leaves(const int2* __restrict__ near_run, int32_t r0, int32_t r1, int2* s,
+                                                F&& f) {
+    const int lane = threadIdx.x & 31;
+    for (int32_t rb = r0; rb < r1; rb += 32) {
+        const int32_t rr = rb + lane;
+        int32_t first = 0, len = 0;
+        if (rr < r1) {
+            const int2 run = near_run[rr];
+            first = run.x;
+            len = run.y - run.x;
+        }
+        int32_t incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const int nrun = min(32, r1 - rb);
+        __syncwarp();
+        s[lane] = make_int2(incl - len, first);
+        __syncwarp();
+        for (int32_t kb = 0; kb < total; kb += 32) {
+            const int32_t k = kb + lane;
+            int lo = 0, hi = nrun - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s[mid].x <= k) lo = mid;
+                else hi = mid - 1;
+            }
+            const int2 e = s[lo];
+            f(e.y + (k - e.x), k < total);
+        }
+    }
+    __syncwarp();
+}
+
 inline unsigned grid_for(int64_t n, int block) {
     int64_t g = (n + block - 1) / block;
     if (g < 1) g = 1;
@@ -245,7 +299,11 @@ void ensure_vortex_capacity(Ctx& c, int64_t n, bool keep);
 // Leaf anchors (frame.cuh) and per-leaf FP32 boxes of the current vortex positions.
 void build_frames(Ctx& c);
 void tree_build(Ctx& c, double far_criteria, double min_node, double max_node);
+// Node frames plus the near runs and far lists of the leaves holding a segment centre
+// (all the SLAE right-hand side reads).
 void tree_lists(Ctx& c);
+// Near runs and far-field coefficients of every leaf, built once per tree on first use.
+void ensure_full_lists(Ctx& c);
 // Full far lists by an exact FP64 walk (inspection).
 void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t>& far_node);
 void eps_pass(Ctx& c, int merge, int64_t* merged);

@@ -179,6 +179,7 @@ class GpuSpace:
         self._ok(self.lib.vvgpu_get_stats(self.h, C.byref(s)), "get_stats")
         d = {k: getattr(s, k) for k, _ in Stats._fields_ if k != "reserved"}
         d["launches"] = int(s.reserved[0])
+        d["eps_evaluations"] = int(s.reserved[1])
         return d
 
     # -- state -----------------------------------------------------------------------
