@@ -8,13 +8,14 @@
 // reference, so whole near leaves farther than 8 eps from all targets of a leaf are
 // skipped: the warp tests boxes once per (target leaf, near leaf) in FP32 with a margin.
 //
-// One warp per target leaf: eight target slots times four source lanes.  FP64 path: every
-// pair in double precision
-// with the reference's formulas.  FP32 path: vortex pairs in local frames (frame.cuh) with
-// FP32 exp/sqrt; pairs whose cut-off or coincidence test falls within a rigorous bound of
+// One warp per target leaf in both paths.  FP64 path (k_diff64): eight target slots times
+// four source lanes, every pair in double precision with the reference's formulas.  FP32
+// path (k_diff32): four targets per lane, the 16 lanes of a half-warp stride over the
+// flattened sources of the candidate leaves; vortex pairs in local frames (frame.cuh) with
+// FP32 exp/rsqrt; pairs whose cut-off or coincidence test falls within a rigorous bound of
 // the FP32 error of its threshold are re-evaluated in FP64, so the set of contributing
-// pairs is the reference's.
-// Wall segments are always FP64.  Friction goes to TAtt::fric with FP64 atomics.
+// pairs is the reference's.  Wall segments are always FP64.  Friction goes to TAtt::fric
+// with FP64 atomics.
 #include <cfloat>
 
 #include "frame.cuh"
@@ -96,17 +97,11 @@ __device__ __forceinline__ void ff_add(float& ah, float& al, float bh, float bl)
     al = e - (ah - s);
 }
 
-// Warp per target leaf.  Lane = target slot (lane & 7) x source lane (lane >> 3): eight
-// targets per pass, the four source lanes split each candidate leaf's vortices.  Candidate
-// leaves come from a lane-parallel box test against the targets' box grown by 8 eps.
-//
-// FP32 path: targets come from the FP32 source records (own leaf frame), pair sums are
-// double-float pairs, and the final update runs in FP32 plus one FP64 addition per
-// coordinate.  FP64 (a narrow pipe on sm_103) is used only where a pair fell in the band
-// around a threshold or the leaf sees wall segments; a warp that met either takes the FP64
-// reduction and update for that group of targets.
-template <bool FP32>
-__global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
+// FP64 path.  Warp per target leaf.  Lane = target slot (lane & 7) x source lane
+// (lane >> 3): eight targets per pass, the four source lanes split each candidate leaf's
+// vortices.  Candidate leaves come from a lane-parallel box test against the targets' box
+// grown by 8 eps.  Every pair in double precision with the reference's formulas.
+__global__ void __launch_bounds__(DW * 32) k_diff64(DiffArgs a) {
     __shared__ int2 s_runs[DW][32];
     const int wq = threadIdx.x >> 5;
     const int64_t L = (int64_t)blockIdx.x * DW + wq;
@@ -120,31 +115,13 @@ __global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
     unsigned long long ncand = 0;
     for (int32_t c0 = v0; c0 < v1; c0 += 8) {
         const int32_t i = c0 + ts;
-        bool act = false;
+        const bool act = (i < v1) && (a.g[i] != 0.);
         double xi = 0, yi = 0, gi = 0, ie = 0;
-        float txf = 0, tyf = 0, ief = 0;
-        bool pos = false;
-        float reach = 0.f;
-        if (FP32) {
-            // g != 0 and its sign from the bit pattern (integer pipe)
-            const unsigned long long gb = (i < v1) ? (unsigned long long)__double_as_longlong(a.g[i]) : 0ull;
-            act = (gb << 1) != 0ull;
-            if (act) {
-                const float4 r4 = a.src32[i];
-                txf = r4.x; tyf = r4.y;
-                ief = a.src_ie[i];
-                pos = (gb >> 63) == 0ull;
-                reach = (8.f / ief) * (1.f + 1e-4f);
-                xi = a.x[i]; yi = a.y[i]; gi = a.g[i]; ie = a.ie[i];
-            }
-        } else {
-            act = (i < v1) && (a.g[i] != 0.);
-            if (act) {
-                xi = a.x[i]; yi = a.y[i]; gi = a.g[i]; ie = a.ie[i];
-                txf = (float)(xi - axL); tyf = (float)(yi - ayL);
-                pos = gi > 0;
-                reach = (float)(8.0 / ie) * (1.f + 1e-4f);
-            }
+        float txf = 0, tyf = 0, reach = 0.f;
+        if (act) {
+            xi = a.x[i]; yi = a.y[i]; gi = a.g[i]; ie = a.ie[i];
+            txf = (float)(xi - axL); tyf = (float)(yi - ayL);
+            reach = (float)(8.0 / ie) * (1.f + 1e-4f);
         }
         float bx0 = act ? txf : INFINITY, by0 = act ? tyf : INFINITY;
         float bx1 = act ? txf : -INFINITY, by1 = act ? tyf : -INFINITY;
@@ -159,10 +136,7 @@ __global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
         }
         if (!(bx0 <= bx1)) continue;  // no active target in this group (warp-uniform)
         const float pad = rmax + ldexpf(fabsf(bx0) + fabsf(bx1) + fabsf(by0) + fabsf(by1) + a.Gf, -16);
-        const float tmax = fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)), fmaxf(fabsf(by0), fabsf(by1)));
         double s2x = 0, s2y = 0, s3x = 0, s3y = 0, s1 = 0, s0 = 0;
-        float f2x = 0, f2y = 0, f1 = 0, c2x = 0, c2y = 0, c1 = 0;
-        bool used64 = false;  // this lane added an FP64 term
         for_near_leaves(a.near_run, r0, r1, s_runs[wq], [&](int32_t q, bool ok) {
             bool hit = false;
             if (ok) {
@@ -181,59 +155,18 @@ __global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
                 const int32_t j0 = a.lvf[qq], j1 = a.lvl[qq];
                 if (!act) continue;
                 if (sl == 0) ncand += (unsigned long long)(j1 - j0);
-                if (FP32) {
-                    const float2 sh = frame_shift(a.anchor[qq], kL, a.Gf);
-                    // Bound D on the FP32 error of |dr| for any pair of this leaf: each of
-                    // dx, dy carries at most 2^-24 (|t| + |s| + |s + sh| + |dx|) from the
-                    // roundings of the records, the shift and the subtraction (4x slack).
-                    // Pairs whose (|dr| / eps)^2 lies within the resulting band of the cut-off
-                    // 64, or whose |dx| + |dy| may be below the coincidence limit, are
-                    // evaluated in FP64.
-                    const float4 sb = a.box[qq];
-                    const float s4max = fmaxf(fmaxf(fabsf(sb.x), fabsf(sb.z)), fmaxf(fabsf(sb.y), fabsf(sb.w)));
-                    const float spmax = fmaxf(fmaxf(fabsf(sb.x + sh.x), fabsf(sb.z + sh.x)),
-                                              fmaxf(fabsf(sb.y + sh.y), fabsf(sb.w + sh.y)));
-                    const float D = ldexpf(2.f * tmax + s4max + 2.f * spmax, -21);
-                    const float band = 16.f * ief * D * (1.f + 1e-3f) + ldexpf(64.f, -19);
-                    const float tiny = 2.f * D + 1e-9f;
-                    float p2x = 0, p2y = 0, p1 = 0;
-                    for (int32_t j = j0 + sl; j < j1; j += 4) {
-                        const float4 s4 = a.src32[j];
-                        if (s4.z == 0.f || ((s4.z > 0.f) != pos)) continue;
-                        const float dx = txf - (s4.x + sh.x), dy = tyf - (s4.y + sh.y);
-                        const float r2 = dx * dx + dy * dy;
-                        const float u = r2 * ief * ief;  // (|dr| / eps)^2
-                        if (fabsf(u - 64.f) < band || (fabsf(dx) + fabsf(dy)) < tiny) {
-                            vortex_term64(xi, yi, gi, ie, a.x[j], a.y[j], a.g[j], s2x, s2y, s1);
-                            used64 = true;
-                            continue;
-                        }
-                        if (u > 64.f) continue;
-                        const float rs = rsqrtf(r2);
-                        const float t = s4.z * __expf(-(r2 * rs) * ief);
-                        const float qv = t * rs;
-                        p2x = fmaf(dx, qv, p2x);
-                        p2y = fmaf(dy, qv, p2y);
-                        p1 += t;
-                    }
-                    acc_add(f2x, c2x, p2x);
-                    acc_add(f2y, c2y, p2y);
-                    acc_add(f1, c1, p1);
-                } else {
-                    for (int32_t j = j0 + sl; j < j1; j += 4) {
-                        const double gj = a.g[j];
-                        if (gj == 0.) continue;
-                        vortex_term64(xi, yi, gi, ie, a.x[j], a.y[j], gj, s2x, s2y, s1);
-                    }
+                for (int32_t j = j0 + sl; j < j1; j += 4) {
+                    const double gj = a.g[j];
+                    if (gj == 0.) continue;
+                    vortex_term64(xi, yi, gi, ie, a.x[j], a.y[j], gj, s2x, s2y, s1);
                 }
-                // wall segments of this near leaf (segment_influence), FP64, split over source lanes
+                // wall segments of this near leaf (segment_influence), split over source lanes
                 for (int32_t qs = a.lsf[qq] + sl; qs < a.lsl[qq]; qs += 4) {
                     const int32_t sgm = a.seg_order[qs];
                     const double dx = xi - a.rx[sgm], dy = yi - a.ry[sgm];
                     const double dr2 = dx * dx + dy * dy;
                     const double dr = sqrt(dr2);
                     const double ea = -dr * ie;
-                    used64 = true;
                     if (ea < EXP_ARG_RESTRICTION) continue;
                     const double ex = exp(ea);
                     const double dsx = -a.dly[sgm], dsy = a.dlx[sgm];
@@ -243,29 +176,7 @@ __global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
                 }
             }
         });
-        if (FP32) {
-            // combine the four source lanes of each target slot as double-float pairs
-#pragma unroll
-            for (int o = 8; o < 32; o <<= 1) {
-                ff_add(f2x, c2x, __shfl_xor_sync(0xffffffffu, f2x, o), __shfl_xor_sync(0xffffffffu, c2x, o));
-                ff_add(f2y, c2y, __shfl_xor_sync(0xffffffffu, f2y, o), __shfl_xor_sync(0xffffffffu, c2y, o));
-                ff_add(f1, c1, __shfl_xor_sync(0xffffffffu, f1, o), __shfl_xor_sync(0xffffffffu, c1, o));
-            }
-            if (!__any_sync(0xffffffffu, used64)) {
-                if (act && sl == 0) {
-                    // MDiffusiveFast.cpp:41-45 with no wall term (s0 = s3 = 0), in FP32
-                    const float gif = (float)gi;
-                    float t1 = f1 + c1;
-                    if (((t1 > 0.f) - (t1 < 0.f)) != ((gif > 0.f) - (gif < 0.f)) || fabsf(t1) < fabsf(0.1f * gif))
-                        t1 = 0.1f * gif;
-                    const float f = ief / ((float)a.re * t1);
-                    a.vx[i] = a.vx[i] + (double)((f2x + c2x) * f);
-                    a.vy[i] = a.vy[i] + (double)((f2y + c2y) * f);
-                }
-                continue;
-            }
-        }
-        // combine the four source lanes of each target slot (FP64 terms)
+        // combine the four source lanes of each target slot
 #pragma unroll
         for (int o = 8; o < 32; o <<= 1) {
             s2x += __shfl_xor_sync(0xffffffffu, s2x, o);
@@ -276,11 +187,6 @@ __global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
             s0 += __shfl_xor_sync(0xffffffffu, s0, o);
         }
         if (act && sl == 0) {
-            if (FP32) {  // the FP32 pair sums, already combined over the source lanes
-                s2x += (double)f2x + (double)c2x;
-                s2y += (double)f2y + (double)c2y;
-                s1 += (double)f1 + (double)c1;
-            }
             if ((dsgn(s1) != dsgn(gi)) || (fabs(s1) < fabs(0.1 * gi))) s1 = 0.1 * gi;
             double f = ie / (a.re * s1);
             double vx = a.vx[i] + s2x * f, vy = a.vy[i] + s2y * f;
@@ -295,6 +201,281 @@ __global__ void __launch_bounds__(DW * 32) k_diff(DiffArgs a) {
     ncand = warp_sum_u64(ncand);
     if (lane == 0 && ncand) atomicAdd(a.cand, ncand);
 }
+
+// FP32 path.  Warp per target leaf, eight targets per chunk, split into 8 / DT lane groups
+// that each hold DT targets per lane in registers; the 4 DT lanes of a group stride over the
+// sources of the candidate leaves, taken as one flattened sequence per batch of up to 32
+// candidate leaves (so every source is loaded once per group and applied to DT targets).
+// Pair arithmetic is FP32 in local frames with compensated accumulation.  Pairs whose
+// cut-off or coincidence test falls within the rigorous FP32 error bound of its threshold,
+// and the wall-segment terms, are evaluated in FP64 into per-lane accumulators that are
+// reduced in a fixed order, so results are reproducible.
+template <int DT>
+__global__ void __launch_bounds__(DW * 32, 4) k_diff32(DiffArgs a) {
+    constexpr int LG = 4 * DT;  // lanes per group (source stride)
+    __shared__ int2 s_runs[DW][32];
+    __shared__ int4 s_hit[DW][32];     // flattened start, first vortex, shift x, shift y (bits)
+    __shared__ float2 s_hitb[DW][32];  // error bound D of the leaf, squared coincidence limit
+    __shared__ int32_t s_hitq[DW][32]; // leaf
+    // per lane FP64 accumulators (s2x, s2y, s1, s3x, s3y, s0 of its targets), touched only by
+    // band pairs and wall segments; lane-major so that lanes never share a bank row
+    __shared__ double s_d64[DW][DT * 6][32];
+    const int wq = threadIdx.x >> 5;
+    const int64_t L = (int64_t)blockIdx.x * DW + wq;
+    const int lane = threadIdx.x & 31;
+    if (L >= a.nl) return;
+    const int grp = lane / LG, sub = lane % LG;
+    const float2 kL = a.anchor[L];
+    const int32_t v0 = a.lvf[L], v1 = a.lvl[L];
+    const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
+    const float bandc = ldexpf(64.f, -19);
+    double(&d64)[DT * 6][32] = s_d64[wq];
+    unsigned long long ncand = 0;
+    for (int32_t c0 = v0; c0 < v1; c0 += 8) {
+        const int32_t tb = c0 + grp * DT;  // first target of this lane's group
+        float tx[DT], ty[DT], ief[DT], ie2[DT], b16[DT];
+        unsigned act = 0, pos = 0;  // bit t: target t active / positive
+        float bx0 = INFINITY, by0 = INFINITY, bx1 = -INFINITY, by1 = -INFINITY, rmax = 0.f;
+#pragma unroll
+        for (int t = 0; t < DT; t++) {
+            const int32_t i = tb + t;
+            const unsigned long long gb = (i < v1) ? (unsigned long long)__double_as_longlong(a.g[i]) : 0ull;
+            tx[t] = ty[t] = ief[t] = ie2[t] = b16[t] = 0.f;
+            if ((gb << 1) != 0ull) {  // g != 0 and its sign from the bit pattern (integer pipe)
+                act |= 1u << t;
+                if ((gb >> 63) == 0ull) pos |= 1u << t;
+                const float4 r4 = a.src32[i];
+                tx[t] = r4.x; ty[t] = r4.y;
+                ief[t] = a.src_ie[i];
+                ie2[t] = ief[t] * ief[t];
+                b16[t] = 16.f * ief[t] * (1.f + 1e-3f);
+                bx0 = fminf(bx0, r4.x); by0 = fminf(by0, r4.y);
+                bx1 = fmaxf(bx1, r4.x); by1 = fmaxf(by1, r4.y);
+                rmax = fmaxf(rmax, (8.f / ief[t]) * (1.f + 1e-4f));
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+            by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+            bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+            by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
+            rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+        }
+        if (!(bx0 <= bx1)) continue;  // no active target in this chunk (warp-uniform)
+        int nact = 0;
+#pragma unroll
+        for (int gg = 0; gg < 32 / LG; gg++) nact += __shfl_sync(0xffffffffu, __popc(act), gg * LG);
+        const float pad = rmax + ldexpf(fabsf(bx0) + fabsf(bx1) + fabsf(by0) + fabsf(by1) + a.Gf, -16);
+        const float tmax = fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)), fmaxf(fabsf(by0), fabsf(by1)));
+        float p2x[DT], p2y[DT], p1[DT], h2x[DT], l2x[DT], h2y[DT], l2y[DT], h1[DT], l1[DT];
+#pragma unroll
+        for (int t = 0; t < DT; t++) p2x[t] = p2y[t] = p1[t] = h2x[t] = l2x[t] = h2y[t] = l2y[t] = h1[t] = l1[t] = 0.f;
+        bool used64 = false;
+        int since = 0;
+        for_near_leaves(a.near_run, r0, r1, s_runs[wq], [&](int32_t q, bool ok) {
+            bool hit = false;
+            float4 b = make_float4(0.f, 0.f, -1.f, -1.f);
+            float2 sh = make_float2(0.f, 0.f);
+            if (ok) {
+                b = a.box[q];
+                if (b.x <= b.z) {
+                    sh = frame_shift(a.anchor[q], kL, a.Gf);
+                    const float dx = fmaxf(fmaxf(b.x + sh.x - bx1, bx0 - (b.z + sh.x)), 0.f);
+                    const float dy = fmaxf(fmaxf(b.y + sh.y - by1, by0 - (b.w + sh.y)), 0.f);
+                    hit = dx <= pad && dy <= pad && (dx * dx + dy * dy) <= pad * pad;
+                }
+            }
+            const unsigned mask = __ballot_sync(0xffffffffu, hit);
+            if (!mask) return;
+            int32_t j0 = 0, len = 0, segs = 0;
+            if (hit) {
+                j0 = a.lvf[q];
+                len = a.lvl[q] - j0;
+                segs = a.lsl[q] - a.lsf[q];
+            }
+            int32_t incl = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            const int nh = __popc(mask);
+            const bool any_seg = __any_sync(0xffffffffu, segs > 0);
+            __syncwarp();
+            if (hit) {
+                const int r = __popc(mask & ((1u << lane) - 1));
+                // Bound D on the FP32 error of |dr| for any pair of this leaf: each of dx, dy
+                // carries at most 2^-24 (|t| + |s| + |s + sh| + |dx|) from the roundings of the
+                // records, the shift and the subtraction (4x slack).
+                const float s4max = fmaxf(fmaxf(fabsf(b.x), fabsf(b.z)), fmaxf(fabsf(b.y), fabsf(b.w)));
+                const float spmax = fmaxf(fmaxf(fabsf(b.x + sh.x), fabsf(b.z + sh.x)),
+                                          fmaxf(fabsf(b.y + sh.y), fabsf(b.w + sh.y)));
+                const float D = ldexpf(2.f * tmax + s4max + 2.f * spmax, -21);
+                const float tiny = 2.f * D + 1e-9f;  // |dx| + |dy| below it may be under 1e-10
+                s_hit[wq][r] = make_int4(incl - len, j0, __float_as_int(sh.x), __float_as_int(sh.y));
+                s_hitb[wq][r] = make_float2(D, tiny * tiny);
+                s_hitq[wq][r] = q;
+            }
+            __syncwarp();
+            if (lane == 0) ncand += (unsigned long long)nact * (unsigned long long)total;
+            int cur = 0;
+            int32_t nextb = (nh > 1) ? s_hit[wq][1].x : total;
+            for (int32_t k = sub; k < total; k += LG) {
+                while (k >= nextb) {
+                    cur++;
+                    nextb = (cur + 1 < nh) ? s_hit[wq][cur + 1].x : total;
+                }
+                const int4 hc = s_hit[wq][cur];
+                const int32_t j = hc.y + (k - hc.x);
+                const float4 s4 = a.src32[j];
+                if (s4.z == 0.f) continue;
+                const float sx = s4.x + __int_as_float(hc.z), sy = s4.y + __int_as_float(hc.w);
+                // a target's pair with itself is excluded by the reference's coincidence rule
+                const int32_t jr = j - tb;
+                const unsigned self = (jr >= 0 && jr < DT) ? (1u << jr) : 0u;
+                const unsigned same = (s4.z > 0.f ? pos : ~pos) & act & ~self;
+                const float2 hb = s_hitb[wq][cur];
+                unsigned pend = 0;  // targets whose pair with this source goes to FP64
+#pragma unroll
+                for (int t = 0; t < DT; t++) {
+                    const float dx = tx[t] - sx, dy = ty[t] - sy;
+                    const float r2 = dx * dx + dy * dy;
+                    const float du = r2 * ie2[t] - 64.f;  // (|dr| / eps)^2 - 64
+                    const float bnd = fmaf(b16[t], hb.x, bandc);
+                    const bool sm = (same >> t) & 1u;
+                    if (sm && (fabsf(du) < bnd || r2 < hb.y)) pend |= 1u << t;
+                    const bool in = sm && du <= -bnd && r2 >= hb.y;
+                    const float r2c = in ? r2 : 1.f;
+                    const float rs = rsqrtf(r2c);
+                    const float tv = in ? s4.z * __expf(-(r2c * rs) * ief[t]) : 0.f;
+                    const float qv = tv * rs;
+                    p2x[t] = fmaf(dx, qv, p2x[t]);
+                    p2y[t] = fmaf(dy, qv, p2y[t]);
+                    p1[t] += tv;
+                }
+                if (pend) {  // rare: the reference's FP64 test and term
+                    if (!used64) {
+                        for (int w = 0; w < DT * 6; w++) d64[w][lane] = 0.;
+                        used64 = true;
+                    }
+                    for (int t = 0; t < DT; t++) {
+                        if (!((pend >> t) & 1u)) continue;
+                        const int32_t i = tb + t;
+                        vortex_term64(a.x[i], a.y[i], a.g[i], a.ie[i], a.x[j], a.y[j], a.g[j], d64[6 * t][lane],
+                                      d64[6 * t + 1][lane], d64[6 * t + 2][lane]);
+                    }
+                }
+                if (++since == 16) {
+                    since = 0;
+#pragma unroll
+                    for (int t = 0; t < DT; t++) {
+                        acc_add(h2x[t], l2x[t], p2x[t]); p2x[t] = 0.f;
+                        acc_add(h2y[t], l2y[t], p2y[t]); p2y[t] = 0.f;
+                        acc_add(h1[t], l1[t], p1[t]); p1[t] = 0.f;
+                    }
+                }
+            }
+            if (any_seg) {
+                // wall segments of the candidate leaves (segment_influence, MDiffusiveFast.cpp:108-123), FP64
+                for (int h = 0; h < nh; h++) {
+                    const int32_t qq = s_hitq[wq][h];
+                    const int32_t qs0 = a.lsf[qq], qs1 = a.lsl[qq];
+                    if (qs0 >= qs1) continue;
+                    if (!used64) {
+                        for (int w = 0; w < DT * 6; w++) d64[w][lane] = 0.;
+                        used64 = true;
+                    }
+                    for (int t = 0; t < DT; t++) {
+                        if (!((act >> t) & 1u)) continue;
+                        const int32_t i = tb + t;
+                        const double xi = a.x[i], yi = a.y[i], gi = a.g[i], ie = a.ie[i];
+                        for (int32_t qs = qs0 + sub; qs < qs1; qs += LG) {
+                            const int32_t sgm = a.seg_order[qs];
+                            const double dx = xi - a.rx[sgm], dy = yi - a.ry[sgm];
+                            const double dr2 = dx * dx + dy * dy;
+                            const double dr = sqrt(dr2);
+                            const double ea = -dr * ie;
+                            if (ea < EXP_ARG_RESTRICTION) continue;
+                            const double ex = exp(ea);
+                            const double dsx = -a.dly[sgm], dsy = a.dlx[sgm];
+                            d64[6 * t + 3][lane] += dsx * ex;
+                            d64[6 * t + 4][lane] += dsy * ex;
+                            d64[6 * t + 5][lane] += (dr * ie + 1) / dr2 * (dx * dsx + dy * dsy) * ex;
+                            atomicAdd(&a.fric[sgm], ie * ie * gi * ex * sqrt(dsx * dsx + dsy * dsy));
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+        });
+        // fold, then combine the LG source lanes of each group as double-float pairs
+#pragma unroll
+        for (int t = 0; t < DT; t++) {
+            acc_add(h2x[t], l2x[t], p2x[t]);
+            acc_add(h2y[t], l2y[t], p2y[t]);
+            acc_add(h1[t], l1[t], p1[t]);
+#pragma unroll
+            for (int o = LG / 2; o > 0; o >>= 1) {
+                ff_add(h2x[t], l2x[t], __shfl_xor_sync(0xffffffffu, h2x[t], o), __shfl_xor_sync(0xffffffffu, l2x[t], o));
+                ff_add(h2y[t], l2y[t], __shfl_xor_sync(0xffffffffu, h2y[t], o), __shfl_xor_sync(0xffffffffu, l2y[t], o));
+                ff_add(h1[t], l1[t], __shfl_xor_sync(0xffffffffu, h1[t], o), __shfl_xor_sync(0xffffffffu, l1[t], o));
+            }
+        }
+        const bool any64 = __any_sync(0xffffffffu, used64);
+        if (any64) {
+            if (!used64)
+                for (int w = 0; w < DT * 6; w++) d64[w][lane] = 0.;
+            __syncwarp();
+            // fixed-order sum over the LG lanes of each group into the group's first slot
+            for (int w = sub; w < DT * 6; w += LG) {
+                double acc = 0.;
+                for (int l2 = 0; l2 < LG; l2++) acc += d64[w][grp * LG + l2];
+                d64[w][grp * LG] = acc;
+            }
+            __syncwarp();
+        }
+        // lane sub == t of each group writes target t of its group
+#pragma unroll
+        for (int t = 0; t < DT; t++) {
+            if (sub != t || !((act >> t) & 1u)) continue;
+            const int32_t i = tb + t;
+            if (!any64) {
+                // MDiffusiveFast.cpp:41-45 with no wall term (s0 = s3 = 0), in FP32
+                const float gif = (float)a.g[i];
+                float t1 = h1[t] + l1[t];
+                if (((t1 > 0.f) - (t1 < 0.f)) != ((gif > 0.f) - (gif < 0.f)) || fabsf(t1) < fabsf(0.1f * gif))
+                    t1 = 0.1f * gif;
+                const float f = ief[t] / ((float)a.re * t1);
+                a.vx[i] = a.vx[i] + (double)((h2x[t] + l2x[t]) * f);
+                a.vy[i] = a.vy[i] + (double)((h2y[t] + l2y[t]) * f);
+            } else {
+                const double gi = a.g[i], ie = a.ie[i];
+                const double* dv = &d64[6 * t][grp * LG];
+                double s2x = dv[0 * 32] + ((double)h2x[t] + (double)l2x[t]);
+                double s2y = dv[1 * 32] + ((double)h2y[t] + (double)l2y[t]);
+                double s1 = dv[2 * 32] + ((double)h1[t] + (double)l1[t]);
+                double s0 = dv[5 * 32];
+                if ((dsgn(s1) != dsgn(gi)) || (fabs(s1) < fabs(0.1 * gi))) s1 = 0.1 * gi;
+                double f = ie / (a.re * s1);
+                double vx = a.vx[i] + s2x * f, vy = a.vy[i] + s2y * f;
+                if (s0 > C_PI) s0 = C_PI;
+                f = ie * ie / (a.re * (C_2PI - s0));
+                vx += dv[3 * 32] * f;
+                vy += dv[4 * 32] * f;
+                a.vx[i] = vx;
+                a.vy[i] = vy;
+            }
+        }
+    }
+    ncand = warp_sum_u64(ncand);
+    if (lane == 0 && ncand) atomicAdd(a.cand, ncand);
+}
+
+#ifndef DIFF32_DT
+#define DIFF32_DT 4
+#endif
 
 }  // namespace
 
@@ -319,8 +500,8 @@ void diffusive(Ctx& c) {
     VV_CUDA(cudaMemsetAsync(c.counters.p + 2, 0, 8, s));
     a.cand = c.counters.p + 2;
     unsigned grid = grid_for(nl, DW);
-    if (c.precision == VVGPU_FP32) k_diff<true><<<grid, DW * 32, 0, s>>>(a);
-    else k_diff<false><<<grid, DW * 32, 0, s>>>(a);
+    if (c.precision == VVGPU_FP32) k_diff32<DIFF32_DT><<<grid, DW * 32, 0, s>>>(a);
+    else k_diff64<<<grid, DW * 32, 0, s>>>(a);
     VV_LAUNCH_CHECK();
     unsigned long long cand = 0;
     VV_CUDA(cudaMemcpyAsync(&cand, c.counters.p + 2, 8, cudaMemcpyDeviceToHost, s));

@@ -42,13 +42,42 @@ constexpr int CHG_CAP = 48;      // changed near leaves kept per target leaf
 
 // MEpsilonFast::nearestBodySegment (MEpsilonFast.cpp:214-253) and the per-leaf merge
 // criterion / epsilon floor (MEpsilonFast.cpp:25-47).
+// Segment centres in FP32 relative to an exact per-body anchor (a float-representable
+// point), and the largest coordinate, for the FP32 filter of the fallback scan below.
+__global__ void k_seg_frame(int nbodies, const int64_t* __restrict__ body_first, const int64_t* __restrict__ body_count,
+                            const double* __restrict__ rx, const double* __restrict__ ry, float2* seg32,
+                            double2* banchor, float* brad) {
+    __shared__ float s_r[EB / 32];
+    const int b = blockIdx.x;
+    if (b >= nbodies) return;
+    const int64_t f = body_first[b], cnt = body_count[b];
+    const double ax = cnt > 0 ? (double)(float)rx[f] : 0., ay = cnt > 0 ? (double)(float)ry[f] : 0.;
+    float r = 0.f;
+    for (int64_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+        const float sx = (float)(rx[f + k] - ax), sy = (float)(ry[f + k] - ay);
+        seg32[f + k] = make_float2(sx, sy);
+        r = fmaxf(r, fmaxf(fabsf(sx), fabsf(sy)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
+    if ((threadIdx.x & 31) == 0) s_r[threadIdx.x >> 5] = r;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) r = fmaxf(r, s_r[w]);
+        banchor[b] = make_double2(ax, ay);
+        brad[b] = r;
+    }
+}
+
 __global__ void k_leaf_params(int64_t nl, const double4* __restrict__ lgeom, const int32_t* __restrict__ near_off,
                               const int2* __restrict__ near_run, const int32_t* __restrict__ lsf,
                               const int32_t* __restrict__ lsl, const int32_t* __restrict__ seg_order,
                               const double* __restrict__ rx, const double* __restrict__ ry,
                               const double* __restrict__ dlx, const double* __restrict__ dly,
                               const int64_t* __restrict__ body_first, const int64_t* __restrict__ body_count,
-                              int nbodies, int merge, double* mcs_out, double* epr_out) {
+                              const float2* __restrict__ seg32, const double2* __restrict__ banchor,
+                              const float* __restrict__ brad, int nbodies, int merge, double* mcs_out,
+                              double* epr_out) {
     int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= nl) return;
     double4 me = lgeom[L];
@@ -65,12 +94,36 @@ __global__ void k_leaf_params(int64_t nl, const double4* __restrict__ lgeom, con
         }
     }
     if (att < 0) {
+        // Every body's segments with the reference's skip rule.  Each comparison d < res is
+        // decided in FP32 when the two values differ by more than their error bounds
+        // (E <= 2^-19 R^2 with R bounding every coordinate involved), else in FP64 with the
+        // reference's operation order; the FP64 res is formed only when needed.
+        float resf = INFINITY, eres = 0.f;
+        bool rese_ok = true;
         for (int b = 0; b < nbodies; b++) {
-            int64_t f = body_first[b], cnt = body_count[b];
+            const int64_t f = body_first[b], cnt = body_count[b];
+            if (cnt <= 0) continue;
+            const double2 A = banchor[b];
+            const float pxg = (float)(px - A.x), pyg = (float)(py - A.y);
+            const float R = brad[b] + fabsf(pxg) + fabsf(pyg);
+            const float E = ldexpf(R * R, -19);
             for (int64_t k = 0; k < cnt; k++) {
-                int64_t s = f + k;
-                double d = dabs2(dsub(px, rx[s]), dsub(py, ry[s]));
-                if (d < res) { res = d; att = s; }
+                const int64_t s = f + k;
+                const float2 sp = seg32[s];
+                const float dx = pxg - sp.x, dy = pyg - sp.y;
+                const float df = dx * dx + dy * dy;
+                bool less, exact = false;
+                if (att < 0) less = true;  // res = DBL_MAX: any finite distance is smaller
+                else if (df < resf - (E + eres)) less = true;
+                else if (df > resf + (E + eres)) less = false;
+                else {
+                    if (!rese_ok) { res = dabs2(dsub(px, rx[att]), dsub(py, ry[att])); rese_ok = true; }
+                    const double d = dabs2(dsub(px, rx[s]), dsub(py, ry[s]));
+                    less = d < res;
+                    if (less) res = d;
+                    exact = true;
+                }
+                if (less) { resf = df; eres = E; att = s; rese_ok = exact; }
                 else k += 9;  // MEpsilonFast.cpp:248
             }
         }
@@ -652,18 +705,25 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
     // per-leaf merge criterion and epsilon floor
     c.lf_mcs.reserve(nl + 1);
     c.lf_epr.reserve(nl + 1);
-    std::vector<int64_t> bf(c.bodies.size() + 1), bc(c.bodies.size() + 1);
-    for (size_t b = 0; b < c.bodies.size(); b++) { bf[b] = c.bodies[b].first; bc[b] = c.bodies[b].count; }
-    DArr<int64_t> dbf, dbc;
-    dbf.reserve(bf.size());
-    dbc.reserve(bc.size());
-    VV_CUDA(cudaMemcpyAsync(dbf.p, bf.data(), bf.size() * 8, cudaMemcpyHostToDevice, s));
-    VV_CUDA(cudaMemcpyAsync(dbc.p, bc.data(), bc.size() * 8, cudaMemcpyHostToDevice, s));
+    const int nb = (int)c.bodies.size();
+    c.h_bfc.assign(2 * (size_t)nb + 2, 0);
+    for (int b = 0; b < nb; b++) { c.h_bfc[b] = c.bodies[b].first; c.h_bfc[nb + 1 + b] = c.bodies[b].count; }
+    c.e_bfc.reserve(c.h_bfc.size());
+    VV_CUDA(cudaMemcpyAsync(c.e_bfc.p, c.h_bfc.data(), c.h_bfc.size() * 8, cudaMemcpyHostToDevice, s));
+    const int64_t* dbf = c.e_bfc.p;
+    const int64_t* dbc = c.e_bfc.p + nb + 1;
+    c.e_seg32.reserve(c.m + 1);
+    c.e_banchor.reserve(nb + 1);
+    c.e_brad.reserve(nb + 1);
+    if (nb > 0) {
+        k_seg_frame<<<nb, EB, 0, s>>>(nb, dbf, dbc, c.s_rx.p, c.s_ry.p, c.e_seg32.p, c.e_banchor.p, c.e_brad.p);
+        VV_LAUNCH_CHECK();
+    }
     if (nl > 0) {
         k_leaf_params<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.lf_geom.p, c.near_off.p, c.near_run.p, c.lf_sf.p,
                                                       c.lf_sl.p, c.seg_order.p, c.s_rx.p, c.s_ry.p, c.s_dlx.p,
-                                                      c.s_dly.p, dbf.p, dbc.p, (int)c.bodies.size(), merge,
-                                                      c.lf_mcs.p, c.lf_epr.p);
+                                                      c.s_dly.p, dbf, dbc, c.e_seg32.p, c.e_banchor.p, c.e_brad.p,
+                                                      nb, merge, c.lf_mcs.p, c.lf_epr.p);
         VV_LAUNCH_CHECK();
     }
     if (n == 0) {

@@ -176,6 +176,11 @@ struct Ctx {
     DArr<float4> e_box_prev;             // per leaf: the last round's box
     DArr<float> e_rreg;                  // per leaf: largest search radius^2 of its members
     DArr<int32_t> e_flag, e_pos, e_list; // targets to evaluate in a round (flags, offsets, list)
+    std::vector<int64_t> h_bfc;          // body first segments, then counts
+    DArr<int64_t> e_bfc;
+    DArr<float2> e_seg32;                // segment centres in FP32 relative to their body's anchor
+    DArr<double2> e_banchor;
+    DArr<float> e_brad;
     DArr<double> lf_mcs, lf_epr;
     DArr<int32_t> e_zb_prev, e_live, e_cand, e_ncand, e_dirty, e_lchanged;
     DArr<float> e_rlist, e_rnear;
