@@ -363,6 +363,7 @@ struct EpsView {
     const int32_t* partner; const int32_t* zb;
     const double* ox; const double* oy; const double* og;
     double G; float Gf;
+    int first;  // first round: nobody is absorbed or merged yet (no state to look up)
 };
 
 // Candidate state as of the turn of target i.
@@ -374,6 +375,11 @@ __device__ __forceinline__ Cand cand_state(const EpsView& v, int32_t j, int32_t 
     Cand c;
     c.live = false;
     if (j == i || j == excl) return c;
+    if (v.first) {
+        c.rec = v.rec0[j];
+        c.live = c.rec.z != 0.f;
+        return c;
+    }
     if (v.zb[j] < i) return c;
     bool moved = (j < i) && (v.partner[j] >= 0);
     c.rec = moved ? v.recO[j] : v.rec0[j];
@@ -381,7 +387,7 @@ __device__ __forceinline__ Cand cand_state(const EpsView& v, int32_t j, int32_t 
     return c;
 }
 __device__ __forceinline__ void cand_exact(const EpsView& v, int32_t j, int32_t i, double& xj, double& yj, double& gj) {
-    bool moved = (j < i) && (v.partner[j] >= 0);
+    bool moved = !v.first && (j < i) && (v.partner[j] >= 0);
     xj = moved ? v.ox[j] : v.x0[j];
     yj = moved ? v.oy[j] : v.y0[j];
     gj = moved ? v.og[j] : v.g0[j];
@@ -795,7 +801,8 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
         EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.e_rnear.p,
                   (const float*)dmax_bits, c.near_off.p, c.near_run.p,
                   c.e_cand.p, c.e_ncand.p, c.e_rec0.p, c.e_recO[cur].p, c.e_x0.p, c.e_y0.p, c.e_g0.p,
-                  c.e_partner[cur].p, c.e_zb.p, c.e_ox[cur].p, c.e_oy[cur].p, c.e_og[cur].p, fr.G, fr.Gf};
+                  c.e_partner[cur].p, c.e_zb.p, c.e_ox[cur].p, c.e_oy[cur].p, c.e_og[cur].p, fr.G, fr.Gf,
+                  rounds == 1};
         const int nx = cur ^ 1;
         DirtyView dv{c.e_zb_prev.p, c.e_vch.p, c.e_chg.p, c.e_nchg.p, c.e_recO[nx].p, c.e_sr1.p, c.e_sr2.p};
         const int32_t* list = nullptr;

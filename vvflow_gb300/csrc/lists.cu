@@ -34,6 +34,7 @@ struct ListView {
     const float4* nf_cm;     // CMp x, y, CMm x, y (anchor frame)
     const float2* nf_g;      // CMp g, CMm g
     const double* cm;        // exact centroids (6 per node)
+    const float4* rec;       // packed per-node record (4 x float4, see k_node_frames)
     double fc;
     float fcf;
     float Gf;
@@ -46,10 +47,9 @@ __device__ __forceinline__ bool far_exact(const double4& tg, const double4& me, 
     return dabs2(dx, dy) > dmul(dmul(fc, hp), hp);
 }
 
-// FP32 filter, FP64 on the boundary.
-__device__ __forceinline__ bool far_test(const ListView& v, int32_t t, int32_t meN, float4 mg, float2 mk) {
-    float4 tg = v.nf_geo[t];
-    float2 tk = v.nf_k[t];
+// FP32 filter, FP64 on the boundary; node data given.
+__device__ __forceinline__ bool far_test_at(const ListView& v, float4 tg, float2 tk, int32_t t, int32_t meN, float4 mg,
+                                            float2 mk) {
     float dx = (tk.x - mk.x) + (tg.x - mg.x);
     float dy = (tk.y - mk.y) + (tg.y - mg.y);
     float lhs = dx * dx + dy * dy;
@@ -63,19 +63,45 @@ __device__ __forceinline__ bool far_test(const ListView& v, int32_t t, int32_t m
     return far_exact(v.geom[t], v.geom[meN], v.fc);
 }
 
+__device__ __forceinline__ bool far_test(const ListView& v, int32_t t, int32_t meN, float4 mg, float2 mk) {
+    return far_test_at(v, v.nf_geo[t], v.nf_k[t], t, meN, mg, mk);
+}
+
+// Packed node record: everything a walk reads about node t, in one 64-byte line.
+//   r0 = centre x, y (anchor frame), h + w, first child (int bits, -1 for a leaf)
+//   r1 = anchor x, y, depth-first leaf index (int bits, leaves only), 0
+//   r2 = CMp x, y, CMm x, y (anchor frame)      r3 = CMp g, CMm g, 0, 0
+struct NodeRec {
+    float4 r0, r1, r2, r3;
+};
+__device__ __forceinline__ NodeRec load_rec(const float4* __restrict__ rec, int32_t t) {
+    const float4* p = rec + 4 * (size_t)t;
+    return NodeRec{p[0], p[1], p[2], p[3]};
+}
+
 __global__ void k_node_frames(int64_t nn, const double4* __restrict__ geom, const double* __restrict__ cm, double G,
-                              float4* nf_geo, float2* nf_k, float4* nf_cm, float2* nf_g) {
+                              const int32_t* __restrict__ ch1, const int32_t* __restrict__ dfs, float4* nf_geo,
+                              float2* nf_k, float4* nf_cm, float2* nf_g, float4* rec) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nn) return;
     double4 gm = geom[k];
     double cx = isfinite(gm.x) ? gm.x : 0., cy = isfinite(gm.y) ? gm.y : 0.;
     float2 a = anchor_of(cx, cy, G);
     double ax = (double)a.x, ay = (double)a.y;
-    nf_geo[k] = make_float4((float)(gm.x - ax), (float)(gm.y - ay), (float)(gm.z + gm.w), 0.f);
+    const float4 g4 = make_float4((float)(gm.x - ax), (float)(gm.y - ay), (float)(gm.z + gm.w), 0.f);
+    nf_geo[k] = g4;
     nf_k[k] = a;
     const double* c = cm + 6 * k;
-    nf_cm[k] = make_float4((float)(c[0] - ax), (float)(c[1] - ay), (float)(c[3] - ax), (float)(c[4] - ay));
-    nf_g[k] = make_float2((float)c[2], (float)c[5]);
+    const float4 c4 = make_float4((float)(c[0] - ax), (float)(c[1] - ay), (float)(c[3] - ax), (float)(c[4] - ay));
+    const float2 gg = make_float2((float)c[2], (float)c[5]);
+    nf_cm[k] = c4;
+    nf_g[k] = gg;
+    const int32_t c1 = ch1[k];
+    float4* r = rec + 4 * (size_t)k;
+    r[0] = make_float4(g4.x, g4.y, g4.z, __int_as_float(c1));
+    r[1] = make_float4(a.x, a.y, __int_as_float(c1 < 0 ? dfs[k] : -1), 0.f);
+    r[2] = c4;
+    r[3] = make_float4(gg.x, gg.y, 0.f, 0.f);
 }
 
 // Marks the leaves that hold a segment centre (stree::findNode, TSortedTree.cpp:284-303).
@@ -110,7 +136,7 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
 // Per-leaf walk (one thread per leaf) for selected leaves only (sel[L] != 0).
 // PASS 0 counts, PASS 1 writes at the offsets.  Bit 1 of `what`: near runs (near_cnt /
 // near_off / near_run); bit 2: far nodes (far_cnt / far_off / far_node).  Unselected leaves
-// count zero.
+// are not touched.  Used for the leaves the warp-per-leaf walk could not hold.
 template <int PASS>
 __global__ void __launch_bounds__(LB) k_walk(int64_t nl, ListView v, const int32_t* __restrict__ leaf_node,
                                              const int32_t* __restrict__ sel, int32_t* near_cnt, int32_t* far_cnt,
@@ -120,11 +146,7 @@ __global__ void __launch_bounds__(LB) k_walk(int64_t nl, ListView v, const int32
     int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= nl) return;
     const bool want_near = what & 1, want_far = what & 2;
-    if (!sel[L]) {
-        if (PASS == 0 && want_near) near_cnt[L] = 0;
-        if (PASS == 0 && want_far) far_cnt[L] = 0;
-        return;
-    }
+    if (!sel[L]) return;
     const int32_t meN = leaf_node[L];
     const float4 mg = v.nf_geo[meN];
     const float2 mk = v.nf_k[meN];
@@ -165,6 +187,125 @@ __global__ void __launch_bounds__(LB) k_walk(int64_t nl, ListView v, const int32
     if (PASS == 0 && want_far) far_cnt[L] = nf;
 }
 
+// Warp-per-leaf walk for a list of selected leaves: the warp expands the tree level by
+// level (each lane tests one frontier node with the same far decision as every other walk),
+// so a leaf's walk takes one step per level instead of one per visited node.  Near leaves
+// are sorted (they come out level by level) and stored as runs; far nodes are stored in
+// level order.  PASS 0 counts, PASS 1 writes at the offsets; bit 1 of `what`: near runs,
+// bit 2: far nodes.  A leaf whose frontier or near set does not fit the shared buffers is
+// flagged in `fallback` (PASS 0) and left to the per-thread walk.
+constexpr int BW = 4;        // warps (leaves) per block
+constexpr int FCAP = 1024;   // frontier capacity per warp
+template <int PASS>
+__global__ void __launch_bounds__(BW * 32) k_walk_bfs(int64_t nsel, const int32_t* __restrict__ list, ListView v,
+                                                      const int32_t* __restrict__ leaf_node, int32_t* near_cnt,
+                                                      int32_t* far_cnt, const int32_t* __restrict__ near_off,
+                                                      const int32_t* __restrict__ far_off, int2* near_run,
+                                                      int32_t* far_node, int what, int32_t* fallback,
+                                                      int32_t* n_fallback) {
+    __shared__ int32_t s_f[BW][2][FCAP];
+    __shared__ int32_t s_near[BW][FCAP];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t idx = (int64_t)blockIdx.x * BW + w;
+    if (idx >= nsel) return;
+    const int32_t L = list[idx];
+    if (PASS == 1 && fallback[L]) return;
+    const bool want_near = what & 1, want_far = what & 2;
+    const int32_t meN = leaf_node[L];
+    const float4 mg = v.nf_geo[meN];
+    const float2 mk = v.nf_k[meN];
+    const unsigned lt = (1u << lane) - 1;
+    const int32_t fbase = (PASS && want_far) ? far_off[L] : 0;
+    int cur = 0, ncur = 1, nnear = 0, nfar = 0;
+    bool ovf = false;
+    if (lane == 0) s_f[w][0][0] = 0;
+    __syncwarp();
+    for (int depth = 0; ncur > 0; depth++) {
+        if (depth > MAX_DEPTH + 1) { ovf = true; break; }
+        int nnext = 0;
+        for (int base = 0; base < ncur; base += 32) {
+            const int k = base + lane;
+            int32_t t = -1, c1 = -1;
+            bool far = false, inner = false, leaf = false;
+            if (k < ncur) {
+                t = s_f[w][cur][k];
+                far = far_test(v, t, meN, mg, mk);
+                if (!far) {
+                    c1 = v.ch1[t];
+                    inner = c1 >= 0;
+                    leaf = !inner;
+                }
+            }
+            unsigned m = __ballot_sync(0xffffffffu, far);
+            if (far && PASS && want_far) far_node[fbase + nfar + __popc(m & lt)] = t;
+            nfar += __popc(m);
+            m = __ballot_sync(0xffffffffu, inner);
+            if (inner) {
+                const int pos = nnext + 2 * __popc(m & lt);
+                if (pos + 1 < FCAP) { s_f[w][cur ^ 1][pos] = c1; s_f[w][cur ^ 1][pos + 1] = c1 + 1; }
+            }
+            nnext += 2 * __popc(m);
+            m = __ballot_sync(0xffffffffu, leaf);
+            if (leaf) {
+                const int pos = nnear + __popc(m & lt);
+                if (pos < FCAP) s_near[w][pos] = v.dfs[t];
+            }
+            nnear += __popc(m);
+        }
+        if (nnext > FCAP || nnear > FCAP) { ovf = true; break; }
+        __syncwarp();
+        cur ^= 1;
+        ncur = nnext;
+    }
+    if (ovf) {
+        if (PASS == 0 && lane == 0) { fallback[L] = 1; atomicAdd(n_fallback, 1); }
+        return;
+    }
+    int32_t nr = 0, ne = 0;  // runs started, runs ended
+    if (want_near) {
+        // rank sort of the (distinct) near leaves into the free frontier buffer, then runs
+        int32_t* srt = s_f[w][cur];
+        __syncwarp();
+        for (int e = lane; e < nnear; e += 32) {
+            const int32_t x = s_near[w][e];
+            int r = 0;
+            for (int q = 0; q < nnear; q++) r += s_near[w][q] < x;
+            srt[r] = x;
+        }
+        __syncwarp();
+        const int32_t nbase = PASS ? near_off[L] : 0;
+        int32_t* out = reinterpret_cast<int32_t*>(near_run);
+        for (int base = 0; base < nnear; base += 32) {
+            const int p = base + lane;
+            bool st = false, en = false;
+            int32_t x = 0;
+            if (p < nnear) {
+                x = srt[p];
+                st = (p == 0) || (srt[p - 1] != x - 1);
+                en = (p == nnear - 1) || (srt[p + 1] != x + 1);
+            }
+            const unsigned ms = __ballot_sync(0xffffffffu, st), me = __ballot_sync(0xffffffffu, en);
+            if (PASS) {
+                if (st) out[2 * (size_t)(nbase + nr + __popc(ms & lt))] = x;
+                if (en) out[2 * (size_t)(nbase + ne + __popc(me & lt)) + 1] = x + 1;
+            }
+            nr += __popc(ms);
+            ne += __popc(me);
+        }
+    }
+    if (PASS == 0 && lane == 0) {
+        if (want_near) near_cnt[L] = nr;
+        if (want_far) far_cnt[L] = nfar;
+    }
+}
+
+// Indices of the flagged leaves, in order.
+__global__ void k_list_flags(int64_t nl, const int32_t* __restrict__ flag, const int32_t* __restrict__ pos,
+                             int32_t* list) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L < nl && flag[L]) list[pos[L]] = (int32_t)L;
+}
+
 // Far-field contribution of far node t to leaf (mg, mk | me), FP32 or FP64.
 template <bool FP32>
 struct Taylor {
@@ -197,6 +338,22 @@ struct Taylor {
             d3 += (fp2 * dpy * dpx + fm2 * dmy * dmx);
             d4 += (fp2 * (dpy * dpy - dpx * dpx) + fm2 * (dmy * dmy - dmx * dmx));
         }
+    }
+    // FP32 path with the node's record already loaded.
+    __device__ __forceinline__ void add_rec(const NodeRec& n, float4 mg, float2 mk) {
+        const float sx = mk.x - n.r1.x, sy = mk.y - n.r1.y;
+        const float4 c4 = n.r2;
+        const float gp = n.r3.x, gm = n.r3.y;
+        float dpx = sx + (mg.x - c4.x), dpy = sy + (mg.y - c4.y);
+        float dmx = sx + (mg.x - c4.z), dmy = sy + (mg.y - c4.w);
+        float ap = dpx * dpx + dpy * dpy, am = dmx * dmx + dmy * dmy;
+        float ip = rcp_approx(ap), im = rcp_approx(am);
+        float fp1 = gp * ip, fm1 = gm * im;
+        float fp2 = fp1 * ip, fm2 = fm1 * im;
+        two_sum_acc(h1, l1, -(fp1 * dpy + fm1 * dmy));
+        two_sum_acc(h2, l2, fp1 * dpx + fm1 * dmx);
+        two_sum_acc(h3, l3, fp2 * dpy * dpx + fm2 * dmy * dmx);
+        two_sum_acc(h4, l4, fp2 * (dpy * dpy - dpx * dpx) + fm2 * (dmy * dmy - dmx * dmx));
     }
     __device__ __forceinline__ double4 result() const {
         double a = d1, b = d2, cc = d3, d = d4;
@@ -234,34 +391,31 @@ __global__ void __launch_bounds__(WW * 32) k_walk_warp(int64_t nl, ListView v, c
     Taylor<FP32> tay;
     int32_t nr = 0, last = -2, rfirst = -1, nfar = 0;
     int2* myruns = run_buf + (size_t)(valid ? L : 0) * RUN_CAP;
-    if (lane == 0) { s_node[w][0] = 0; s_mask[w][0] = all; }
-    int sp = 1;
-    __syncwarp();
+    // The node being visited is held in registers with its record; the stack keeps the
+    // deferred right children.  The next node's record is requested before the far field of
+    // the current one is folded, so its latency overlaps that arithmetic.
+    int32_t t = 0;
+    uint32_t mask = all;
+    NodeRec cur = load_rec(v.rec, 0);
+    int sp = 0;
     int64_t guard = 0;
-    while (sp > 0) {
+    for (;;) {
         if (++guard > nodes_bound) { if (lane == 0) atomicExch(err, 2); break; }
-        sp--;
-        const int32_t t = s_node[w][sp];
-        const uint32_t mask = s_mask[w][sp];
-        __syncwarp();
         const bool act = (mask >> lane) & 1u;
-        const bool far = act && far_test(v, t, meN, mg, mk);
-        if (far) {
-            tay.add(v, t, mg, mk, me);
-            nfar++;
-        }
+        const bool far = act && far_test_at(v, cur.r0, make_float2(cur.r1.x, cur.r1.y), t, meN, mg, mk);
         const uint32_t rest = mask & ~__ballot_sync(0xffffffffu, far);
+        int32_t nt = -1;
+        uint32_t nmask = 0;
         if (rest) {
-            const int32_t c1 = v.ch1[t];
+            const int32_t c1 = __float_as_int(cur.r0.w);
             if (c1 >= 0) {
-                if (sp + 2 > MAX_DEPTH + 2) { if (lane == 0) atomicExch(err, 2); break; }
-                if (lane == 0) {
-                    s_node[w][sp] = c1 + 1; s_mask[w][sp] = rest;
-                    s_node[w][sp + 1] = c1; s_mask[w][sp + 1] = rest;
-                }
-                sp += 2;
+                if (sp + 1 > MAX_DEPTH + 2) { if (lane == 0) atomicExch(err, 2); break; }
+                if (lane == 0) { s_node[w][sp] = c1 + 1; s_mask[w][sp] = rest; }
+                sp++;
+                nt = c1;
+                nmask = rest;
             } else if ((rest >> lane) & 1u) {
-                const int32_t q = v.dfs[t];
+                const int32_t q = __float_as_int(cur.r1.z);
                 if (q == last + 1) {
                     last = q;
                 } else {
@@ -273,6 +427,23 @@ __global__ void __launch_bounds__(WW * 32) k_walk_warp(int64_t nl, ListView v, c
             }
         }
         __syncwarp();
+        if (nt < 0 && sp > 0) {
+            sp--;
+            nt = s_node[w][sp];
+            nmask = s_mask[w][sp];
+        }
+        NodeRec nxt;
+        if (nt >= 0) nxt = load_rec(v.rec, nt);
+        if (far) {
+            if (FP32) tay.add_rec(cur, mg, mk);
+            else tay.add(v, t, mg, mk, me);
+            nfar++;
+        }
+        if (nt < 0) break;
+        __syncwarp();
+        cur = nxt;
+        t = nt;
+        mask = nmask;
     }
     if (valid) {
         if (rfirst >= 0 && nr <= RUN_CAP) myruns[nr - 1] = make_int2(rfirst, last + 1);
@@ -336,9 +507,57 @@ __global__ void k_walk_exact(int64_t nl, const int32_t* __restrict__ leaf_node, 
 }  // namespace
 
 namespace {
+// Walks the leaves with sel[L] != 0: counts (count = true) into near_cnt / far_cnt, or
+// writes at near_off / far_off.  Counting keeps the list of selected leaves and flags the
+// leaves the warp-per-leaf walk could not hold; those take the per-thread walk.
+void walk_selected(Ctx& c, const ListView& v, const int32_t* sel, int what, bool count) {
+    cudaStream_t s = c.st();
+    const int64_t nl = c.nleaves, nn = c.nnodes;
+    int32_t* err = (int32_t*)c.counters.p + 1;
+    int32_t* nfb = (int32_t*)(c.counters.p + 15);
+    if (count || what == 1) {
+        c.sel_pos.reserve(nl + 2);
+        c.sel_list.reserve(nl + 1);
+        exclusive_scan(c, sel, c.sel_pos.p, nl);
+        c.n_sel = read_i32(c, c.sel_pos.p + nl);
+        k_list_flags<<<grid_for(nl, 256), 256, 0, s>>>(nl, sel, c.sel_pos.p, c.sel_list.p);
+        VV_LAUNCH_CHECK();
+        c.lf_fallback.reserve(nl + 1);
+        VV_CUDA(cudaMemsetAsync(c.lf_fallback.p, 0, (nl + 1) * 4, s));
+        VV_CUDA(cudaMemsetAsync(nfb, 0, 4, s));
+    }
+    if (c.n_sel == 0) return;
+    const unsigned g = grid_for(c.n_sel, BW);
+    if (count || what == 1) {
+        // the count pass (for `what == 1` the counts come from the warp walk; this pass only
+        // finds the leaves that need the per-thread walk)
+        k_walk_bfs<0><<<g, BW * 32, 0, s>>>(c.n_sel, c.sel_list.p, v, c.leaf_node.p,
+                                            count ? c.near_cnt.p : nullptr, c.far_cnt.p, nullptr, nullptr,
+                                            nullptr, nullptr, count ? what : 0, c.lf_fallback.p, nfb);
+        VV_LAUNCH_CHECK();
+        c.n_fallback = read_i32(c, nfb);
+        if (count && c.n_fallback > 0) {
+            k_walk<0><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_fallback.p, c.near_cnt.p,
+                                                      c.far_cnt.p, nullptr, nullptr, nullptr, nullptr, nn, err, what);
+            VV_LAUNCH_CHECK();
+        }
+    }
+    if (!count) {
+        k_walk_bfs<1><<<g, BW * 32, 0, s>>>(c.n_sel, c.sel_list.p, v, c.leaf_node.p, nullptr, nullptr, c.near_off.p,
+                                            c.far_off.p, c.near_run.p, c.far_node.p, what, c.lf_fallback.p, nfb);
+        VV_LAUNCH_CHECK();
+        if (c.n_fallback > 0) {
+            k_walk<1><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_fallback.p, nullptr, nullptr,
+                                                      c.near_off.p, c.far_off.p, c.near_run.p, c.far_node.p, nn, err,
+                                                      what);
+            VV_LAUNCH_CHECK();
+        }
+    }
+}
+
 ListView list_view(Ctx& c) {
     return ListView{c.nd_geom.p, c.nd_ch1.p, c.nd_dfs.p, c.nf_geo.p, c.nf_k.p, c.nf_cm.p, c.nf_g.p, c.nd_cm.p,
-                    c.far_criteria, (float)c.far_criteria, (float)c.frame_G};
+                    c.nf_rec.p, c.far_criteria, (float)c.far_criteria, (float)c.frame_G};
 }
 }  // namespace
 
@@ -354,8 +573,9 @@ void tree_lists(Ctx& c) {
     Frame fr = make_frame(std::fmax(std::fabs(root.x), std::fabs(root.y)) + std::fmax(root.z, root.w));
     c.frame_G = fr.G;
     c.nf_geo.reserve(nn); c.nf_k.reserve(nn); c.nf_cm.reserve(nn); c.nf_g.reserve(nn);
-    k_node_frames<<<grid_for(nn, 256), 256, 0, s>>>(nn, c.nd_geom.p, c.nd_cm.p, fr.G, c.nf_geo.p, c.nf_k.p,
-                                                    c.nf_cm.p, c.nf_g.p);
+    c.nf_rec.reserve(4 * (size_t)nn);
+    k_node_frames<<<grid_for(nn, 256), 256, 0, s>>>(nn, c.nd_geom.p, c.nd_cm.p, fr.G, c.nd_ch1.p, c.nd_dfs.p,
+                                                    c.nf_geo.p, c.nf_k.p, c.nf_cm.p, c.nf_g.p, c.nf_rec.p);
     VV_LAUNCH_CHECK();
     c.lf_flag.reserve(nl + 1);
     VV_CUDA(cudaMemsetAsync(c.lf_flag.p, 0, (nl + 1) * 4, s));
@@ -367,19 +587,17 @@ void tree_lists(Ctx& c) {
     const ListView v = list_view(c);
     c.near_cnt.reserve(nl + 1); c.far_cnt.reserve(nl + 1);
     c.near_off.reserve(nl + 2); c.far_off.reserve(nl + 2);
+    VV_CUDA(cudaMemsetAsync(c.near_cnt.p, 0, (nl + 1) * 4, s));
+    VV_CUDA(cudaMemsetAsync(c.far_cnt.p, 0, (nl + 1) * 4, s));
     // near runs and far lists of the leaves that hold a segment centre
-    k_walk<0><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, c.near_cnt.p, c.far_cnt.p, nullptr,
-                                              nullptr, nullptr, nullptr, nn, err, 3);
-    VV_LAUNCH_CHECK();
+    walk_selected(c, v, c.lf_flag.p, 3, /*count=*/true);
     exclusive_scan(c, c.near_cnt.p, c.near_off.p, nl);
     exclusive_scan(c, c.far_cnt.p, c.far_off.p, nl);
     c.n_near_runs = read_i32(c, c.near_off.p + nl);
     c.n_far = read_i32(c, c.far_off.p + nl);
     c.near_run.reserve(c.n_near_runs + 1);
     c.far_node.reserve(c.n_far + 1);
-    k_walk<1><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_flag.p, nullptr, nullptr, c.near_off.p,
-                                              c.far_off.p, c.near_run.p, c.far_node.p, nn, err, 3);
-    VV_LAUNCH_CHECK();
+    walk_selected(c, v, c.lf_flag.p, 3, /*count=*/false);
     if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
     c.lists_full = false;
     c.stats.near_runs = c.n_near_runs;
@@ -416,10 +634,8 @@ void ensure_full_lists(Ctx& c) {
     if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
     const int32_t nover = read_i32(c, n_over);
     if (nover > 0) {
-        // leaves with more than RUN_CAP runs: write their runs with the per-leaf walk
-        k_walk<1><<<grid_for(nl, LB), LB, 0, s>>>(nl, v, c.leaf_node.p, c.lf_overflow.p, nullptr, nullptr,
-                                                  c.near_off.p, nullptr, c.near_run.p, nullptr, nn, err, 1);
-        VV_LAUNCH_CHECK();
+        // leaves with more than RUN_CAP runs: write their runs with the warp-per-leaf walk
+        walk_selected(c, v, c.lf_overflow.p, 1, /*count=*/false);
         if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
     }
     c.lists_full = true;

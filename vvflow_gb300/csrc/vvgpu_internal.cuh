@@ -142,6 +142,8 @@ struct Ctx {
     DArr<int32_t> nd_axis, nd_split, nd_nlow, nd_nlow_s, nd_lc, nd_dfs;
     DArr<int32_t> node_of, seg_node_of, seg_node_of2, flags, scan;
     DArr<int32_t> perm;              // tree build: source slot of each slot (keys move, payload follows once)
+    DArr<int32_t> sel_pos, sel_list, lf_fallback;  // leaves walked one warp each
+    int64_t n_sel = 0, n_fallback = 0;
     DArr<double> ptmp;               // tree build: payload staging for the final permutation
     DArr<int64_t> otmp;
     DArr<int32_t> tab_lh, tab_rl;
@@ -160,6 +162,7 @@ struct Ctx {
     DArr<float4> nf_geo, nf_cm;     // per node, anchor frame: centre + (h+w); centroids
     DArr<float2> nf_k;              // per node anchor (FP32, exact)
     DArr<float2> nf_g;              // per node centroid circulations
+    DArr<float4> nf_rec;            // per node packed walk record (4 x float4)
     int64_t n_near_runs = 0, n_far = 0;
     DArr<int32_t> leaf_of;          // vortex -> leaf (DFS index)
 
