@@ -227,15 +227,33 @@ __global__ void __launch_bounds__(CW * 32, 4) k_conv32(ConvArgs a) {
             __syncwarp();
             int cur = 0;
             int32_t nextb = (nrun > 1) ? s_runs[wq][1].x : total;
-            for (int32_t k = sub; k < total; k += stride) {
-                while (k >= nextb) {
+            // the next source's record is requested before the current one is applied
+            float4 s4n = make_float4(0.f, 0.f, 0.f, 1.f);
+            float2 kkn = make_float2(0.f, 0.f);
+            if (sub < total) {
+                while (sub >= nextb) {
                     cur++;
                     nextb = (cur + 1 < nrun) ? s_runs[wq][cur + 1].x : total;
                 }
                 const int2 rc = s_runs[wq][cur];
-                const int32_t j = rc.y + (k - rc.x);
-                const float4 s4 = a.src32[j];
-                const float2 kk = a.src_k[j];
+                const int32_t j = rc.y + (sub - rc.x);
+                s4n = a.src32[j];
+                kkn = a.src_k[j];
+            }
+            for (int32_t k = sub; k < total; k += stride) {
+                const float4 s4 = s4n;
+                const float2 kk = kkn;
+                const int32_t kn = k + stride;
+                if (kn < total) {
+                    while (kn >= nextb) {
+                        cur++;
+                        nextb = (cur + 1 < nrun) ? s_runs[wq][cur + 1].x : total;
+                    }
+                    const int2 rc = s_runs[wq][cur];
+                    const int32_t j = rc.y + (kn - rc.x);
+                    s4n = a.src32[j];
+                    kkn = a.src_k[j];
+                }
                 const float sx = s4.x + (kk.x - kL.x);
                 const float sy = s4.y + (kk.y - kL.y);
 #pragma unroll

@@ -363,7 +363,6 @@ struct EpsView {
     const int32_t* partner; const int32_t* zb;
     const double* ox; const double* oy; const double* og;
     double G; float Gf;
-    int first;  // first round: nobody is absorbed or merged yet (no state to look up)
 };
 
 // Candidate state as of the turn of target i.
@@ -371,11 +370,13 @@ struct Cand {
     bool live;
     float4 rec;
 };
+// FIRST: the first round, where nobody is absorbed or merged yet (no state to look up).
+template <bool FIRST>
 __device__ __forceinline__ Cand cand_state(const EpsView& v, int32_t j, int32_t i, int32_t excl) {
     Cand c;
     c.live = false;
     if (j == i || j == excl) return c;
-    if (v.first) {
+    if (FIRST) {
         c.rec = v.rec0[j];
         c.live = c.rec.z != 0.f;
         return c;
@@ -386,8 +387,9 @@ __device__ __forceinline__ Cand cand_state(const EpsView& v, int32_t j, int32_t 
     c.live = c.rec.z != 0.f;
     return c;
 }
+template <bool FIRST>
 __device__ __forceinline__ void cand_exact(const EpsView& v, int32_t j, int32_t i, double& xj, double& yj, double& gj) {
-    bool moved = !v.first && (j < i) && (v.partner[j] >= 0);
+    bool moved = !FIRST && (j < i) && (v.partner[j] >= 0);
     xj = moved ? v.ox[j] : v.x0[j];
     yj = moved ? v.oy[j] : v.y0[j];
     gj = moved ? v.og[j] : v.g0[j];
@@ -428,14 +430,14 @@ struct NearBuf {
 };
 
 // Visits leaf q's live candidates for target i (shared by both passes).
-template <int PASS>
+template <int PASS, bool FIRST>
 __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, float2 aL, int32_t i, int32_t excl, float tx,
                                           float ty, double px, double py, float D, float& t1, float& t2,
                                           float& thr, Top2& best, NearBuf& buf) {
     float2 sh = frame_shift(v.anchor[q], aL, v.Gf);
     if (box_lb(v.box[q], sh, tx, ty) > thr) return;
     for (int32_t j = v.lvf[q]; j < v.lvl[q]; j++) {
-        Cand c = cand_state(v, j, i, excl);
+        Cand c = cand_state<FIRST>(v, j, i, excl);
         if (!c.live) continue;
         float dx = tx - (c.rec.x + sh.x), dy = ty - (c.rec.y + sh.y);
         float d = dx * dx + dy * dy;
@@ -445,7 +447,7 @@ __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, float2 aL
             if (d <= thr) buf.push(d, j, thr);
         } else if (d <= thr) {
             double xj, yj, gj;
-            cand_exact(v, j, i, xj, yj, gj);
+            cand_exact<FIRST>(v, j, i, xj, yj, gj);
             top2_push(best, dabs2(dsub(px, xj), dsub(py, yj)), j);
         }
     }
@@ -453,6 +455,7 @@ __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, float2 aL
 
 // Two nearest live candidates of target i (at exact position px,py) among leaf L's
 // candidate leaves, excluding slot excl.  Returns the exact FP64 top-2 of the reference.
+template <bool FIRST>
 __device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl, double px, double py,
                             bool use_list) {
     const float2 aL = v.anchor[L];
@@ -474,29 +477,29 @@ __device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl
                 for (int k = 0; k < buf.n; k++) {
                     if (!(buf.d[k] <= thr)) continue;
                     double xj, yj, gj;
-                    cand_exact(v, buf.j[k], i, xj, yj, gj);
+                    cand_exact<FIRST>(v, buf.j[k], i, xj, yj, gj);
                     top2_push(best, dabs2(dsub(px, xj), dsub(py, yj)), buf.j[k]);
                 }
                 break;
             }
         }
-        if (pass == 0) scan_leaf<0>(v, L, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
-        else scan_leaf<1>(v, L, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
+        if (pass == 0) scan_leaf<0, FIRST>(v, L, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
+        else scan_leaf<1, FIRST>(v, L, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
         if (nc >= 0) {
             const int32_t* cl = v.cand + (size_t)L * CAND_CAP;
             for (int32_t k = 0; k < nc; k++) {
                 int32_t q = cl[k];
                 if (q == L) continue;
-                if (pass == 0) scan_leaf<0>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
-                else scan_leaf<1>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
+                if (pass == 0) scan_leaf<0, FIRST>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
+                else scan_leaf<1, FIRST>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
             }
         } else {
             for (int32_t r = v.near_off[L]; r < v.near_off[L + 1]; r++) {
                 int2 run = v.near_run[r];
                 for (int32_t q = run.x; q < run.y; q++) {
                     if (q == L) continue;
-                    if (pass == 0) scan_leaf<0>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
-                    else scan_leaf<1>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
+                    if (pass == 0) scan_leaf<0, FIRST>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
+                    else scan_leaf<1, FIRST>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
                 }
             }
         }
@@ -577,18 +580,20 @@ __global__ void k_eps_compact(int64_t n, const int32_t* __restrict__ flag, const
     if (i < n && flag[i]) list[pos[i]] = (int32_t)i;
 }
 
-// Evaluates the targets list[0 .. *count) (every target when list is null; count = n).
+// Evaluates every target (FIRST: the first round) or the targets list[0 .. *count).
+template <bool FIRST>
 __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* __restrict__ list,
                             const int32_t* __restrict__ count, const int32_t* __restrict__ leaf_of,
                             const double* __restrict__ mcs_l, const double* __restrict__ epr_l,
                             const double* __restrict__ ie_in, const double* __restrict__ oie_old,
                             int32_t* partner_new, double* ox_new, double* oy_new, double* og_new, double* oie_new,
                             int32_t* changed, unsigned long long* evals) {
-    const int64_t cnt = list ? (int64_t)*count : n;
+    const int64_t cnt = FIRST ? n : (int64_t)*count;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(evals, (unsigned long long)cnt);
-    for (int64_t kk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; kk < cnt;
-         kk += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t i = list ? list[kk] : (int32_t)kk;
+    const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t kstep = FIRST ? cnt : (int64_t)gridDim.x * blockDim.x;  // FIRST: one target per thread
+    for (int64_t kk = k0; kk < cnt; kk += kstep) {
+        const int32_t i = FIRST ? (int32_t)kk : list[kk];
         const int32_t L = leaf_of[i];
         const double gi0 = v.g0[i];
         int32_t partner = SKIPPED;
@@ -596,7 +601,7 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
         float sr1 = -1.f, sr2 = -1.f;
         if (gi0 != 0 && !(v.zb[i] < i)) {
             const double mcs = mcs_l[L];
-            Top2 t = two_nearest(v, L, i, -1, px, py, true);
+            Top2 t = two_nearest<FIRST>(v, L, i, -1, px, py, true);
             sr1 = t.thr;
             double e;
             partner = -1;
@@ -605,8 +610,8 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
             else if (isnan(mcs)) e = __dsqrt_rn(t.r2);
             else {
                 double x1, y1, g1, x2, y2, g2;
-                cand_exact(v, t.l1, i, x1, y1, g1);
-                cand_exact(v, t.l2, i, x2, y2, g2);
+                cand_exact<FIRST>(v, t.l1, i, x1, y1, g1);
+                cand_exact<FIRST>(v, t.l2, i, x2, y2, g2);
                 if ((t.r1 < mcs) || ((dsgn(g1) == dsgn(g2)) && (dsgn(g1) != dsgn(gi)))) {
                     // MergeVortexes (MEpsilonFast.cpp:111-126)
                     if (dsgn(gi) == dsgn(g1)) {
@@ -621,7 +626,7 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
                     }
                     gi = dadd(gi, g1);
                     partner = t.l1;
-                    Top2 u = two_nearest(v, L, i, t.l1, px, py, false);
+                    Top2 u = two_nearest<FIRST>(v, L, i, t.l1, px, py, false);
                     sr2 = u.thr;
                     if (u.l1 == INT_MAX) e = DBL_MIN;
                     else if (u.l2 == INT_MAX) e = __dsqrt_rn(u.r1);
@@ -801,8 +806,7 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
         EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.e_rnear.p,
                   (const float*)dmax_bits, c.near_off.p, c.near_run.p,
                   c.e_cand.p, c.e_ncand.p, c.e_rec0.p, c.e_recO[cur].p, c.e_x0.p, c.e_y0.p, c.e_g0.p,
-                  c.e_partner[cur].p, c.e_zb.p, c.e_ox[cur].p, c.e_oy[cur].p, c.e_og[cur].p, fr.G, fr.Gf,
-                  rounds == 1};
+                  c.e_partner[cur].p, c.e_zb.p, c.e_ox[cur].p, c.e_oy[cur].p, c.e_og[cur].p, fr.G, fr.Gf};
         const int nx = cur ^ 1;
         DirtyView dv{c.e_zb_prev.p, c.e_vch.p, c.e_chg.p, c.e_nchg.p, c.e_recO[nx].p, c.e_sr1.p, c.e_sr2.p};
         const int32_t* list = nullptr;
@@ -816,10 +820,16 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
             VV_LAUNCH_CHECK();
             list = c.e_list.p;
         }
-        const unsigned eg = rounds > 1 ? std::min<unsigned>(grid_for(n, EB), 152u * 32u) : grid_for(n, EB);
-        k_eps_round<<<eg, EB, 0, s>>>(n, v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p,
-                                      c.e_oie[cur].p, c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p,
-                                      c.e_oie[nx].p, c.e_changed.p, c.counters.p + 14);
+        if (rounds == 1)
+            k_eps_round<true><<<grid_for(n, EB), EB, 0, s>>>(
+                n, v, dv, nullptr, nullptr, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
+                c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
+                c.counters.p + 14);
+        else
+            k_eps_round<false><<<std::min<unsigned>(grid_for(n, EB), 152u * 32u), EB, 0, s>>>(
+                n, v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
+                c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
+                c.counters.p + 14);
         VV_LAUNCH_CHECK();
         // new absorber table and merged records; leaves whose members changed
         k_zb_reset<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_zb.p, c.e_zb_prev.p, c.e_zb.p);

@@ -391,29 +391,35 @@ __global__ void __launch_bounds__(WW * 32) k_walk_warp(int64_t nl, ListView v, c
     Taylor<FP32> tay;
     int32_t nr = 0, last = -2, rfirst = -1, nfar = 0;
     int2* myruns = run_buf + (size_t)(valid ? L : 0) * RUN_CAP;
-    // The node being visited is held in registers with its record; the stack keeps the
-    // deferred right children.  The next node's record is requested before the far field of
-    // the current one is folded, so its latency overlaps that arithmetic.
-    int32_t t = 0;
-    uint32_t mask = all;
-    NodeRec cur = load_rec(v.rec, 0);
-    int sp = 0;
+    // Each visit reads the node's packed record (one 64-byte line) for the far test, the
+    // far field, the children and the leaf index.
+    if (lane == 0) { s_node[w][0] = 0; s_mask[w][0] = all; }
+    int sp = 1;
+    __syncwarp();
     int64_t guard = 0;
-    for (;;) {
+    while (sp > 0) {
         if (++guard > nodes_bound) { if (lane == 0) atomicExch(err, 2); break; }
+        sp--;
+        const int32_t t = s_node[w][sp];
+        const uint32_t mask = s_mask[w][sp];
+        __syncwarp();
         const bool act = (mask >> lane) & 1u;
+        const NodeRec cur = load_rec(v.rec, t);
         const bool far = act && far_test_at(v, cur.r0, make_float2(cur.r1.x, cur.r1.y), t, meN, mg, mk);
+        if (far) {
+            if (FP32) tay.add_rec(cur, mg, mk); else tay.add(v, t, mg, mk, me);
+            nfar++;
+        }
         const uint32_t rest = mask & ~__ballot_sync(0xffffffffu, far);
-        int32_t nt = -1;
-        uint32_t nmask = 0;
         if (rest) {
             const int32_t c1 = __float_as_int(cur.r0.w);
             if (c1 >= 0) {
-                if (sp + 1 > MAX_DEPTH + 2) { if (lane == 0) atomicExch(err, 2); break; }
-                if (lane == 0) { s_node[w][sp] = c1 + 1; s_mask[w][sp] = rest; }
-                sp++;
-                nt = c1;
-                nmask = rest;
+                if (sp + 2 > MAX_DEPTH + 2) { if (lane == 0) atomicExch(err, 2); break; }
+                if (lane == 0) {
+                    s_node[w][sp] = c1 + 1; s_mask[w][sp] = rest;
+                    s_node[w][sp + 1] = c1; s_mask[w][sp + 1] = rest;
+                }
+                sp += 2;
             } else if ((rest >> lane) & 1u) {
                 const int32_t q = __float_as_int(cur.r1.z);
                 if (q == last + 1) {
@@ -427,23 +433,6 @@ __global__ void __launch_bounds__(WW * 32) k_walk_warp(int64_t nl, ListView v, c
             }
         }
         __syncwarp();
-        if (nt < 0 && sp > 0) {
-            sp--;
-            nt = s_node[w][sp];
-            nmask = s_mask[w][sp];
-        }
-        NodeRec nxt;
-        if (nt >= 0) nxt = load_rec(v.rec, nt);
-        if (far) {
-            if (FP32) tay.add_rec(cur, mg, mk);
-            else tay.add(v, t, mg, mk, me);
-            nfar++;
-        }
-        if (nt < 0) break;
-        __syncwarp();
-        cur = nxt;
-        t = nt;
-        mask = nmask;
     }
     if (valid) {
         if (rfirst >= 0 && nr <= RUN_CAP) myruns[nr - 1] = make_int2(rfirst, last + 1);
