@@ -239,6 +239,12 @@ def gpu_arm(args):
     stp = S.stats()
     v32 = S.vortices()
     S.tree_destroy()
+    # MFlowmove::move_and_clean, the caller-side step after the path (not part of a step)
+    t0 = time.perf_counter()
+    moved_out = S.move_and_clean(True)
+    torch.cuda.synchronize()
+    phases["move_and_clean_after_step"] = round((time.perf_counter() - t0) * 1e3, 3)
+    phases["move_and_clean_erased_in_body"] = moved_out
 
     # ---- e2e through the C ABI with host buffers ----------------------------------------
     hx = torch.from_numpy(wl.x).pin_memory()

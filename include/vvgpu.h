@@ -24,6 +24,8 @@
  *                                             (libvvhd/headers/MDiffusiveFast.hpp:10,
  *                                              libvvhd/src/MDiffusiveFast.cpp:8-48)
  *   vvgpu_vortex_shed                      <- MFlowmove::vortex_shed()
+ *   vvgpu_move_and_clean                   <- MFlowmove::move_and_clean()
+ *   vvgpu_calc_forces, vvgpu_zero_forces   <- Space::calc_forces(), Space::zero_forces()
  *                                             (libvvhd/headers/MFlowmove.hpp:12,
  *                                              libvvhd/src/MFlowmove.cpp:217-235)
  *   vvgpu_gsum                             <- Space::gsum() (libvvhd/headers/TSpace.hpp:93-99)
@@ -190,6 +192,24 @@ int vvgpu_velocity_points_noalloc(vvgpu_ctx* ctx, int64_t n, const double* px, c
  * are in scope (VVGPU_ERR_UNSUPPORTED otherwise). */
 int vvgpu_slae(vvgpu_ctx* ctx, vvgpu_body_out* out);
 int vvgpu_vortex_shed(vvgpu_ctx* ctx);
+/* MFlowmove::move_and_clean(remove, &collision, &cleaned) (libvvhd/src/MFlowmove.cpp:11-215)
+ * for rigid bodies at rest (no collision): r += v dt, erasing |g| < 1e-10 and, with
+ * remove != 0, the vortices inside a body with the dead-vortex bookkeeping (TBody::fdt_dead,
+ * g_dead, TAtt::gsum), v = 0, and the dead-segment bookkeeping.  The list order is kept.
+ * `cleaned` receives the number erased inside bodies.  Call with the tree destroyed. */
+int vvgpu_move_and_clean(vvgpu_ctx* ctx, int remove, int64_t* cleaned);
+/* Current TBody state of body `body` (g_dead and fdt_dead change in move_and_clean,
+ * friction_prev in zero_forces). */
+int vvgpu_get_body_params(vvgpu_ctx* ctx, int body, vvgpu_body_params* out);
+/* Space::calc_forces (libvvhd/src/TSpace.cpp:94-117): adds to each segment's TAtt::Cp, Fr,
+ * Nu and computes each body's friction and nusselt, written to out4[4 b .. 4 b + 3]
+ * (friction x, y, o, nusselt; out4 may be NULL).  No heat: hsum = 0, Prandtl number 0. */
+int vvgpu_calc_forces(vvgpu_ctx* ctx, double* out4);
+/* Space::zero_forces (TSpace.cpp:122-142): TAtt::gsum = fric = 0; per body friction_prev =
+ * friction, then friction, fdt_dead, g_dead and nusselt = 0. */
+int vvgpu_zero_forces(vvgpu_ctx* ctx);
+/* TAtt::Cp, Fr, Nu of every segment (the calc_forces accumulators). */
+int vvgpu_get_segment_forces(vvgpu_ctx* ctx, double* cp, double* fr, double* nu);
 int vvgpu_gsum(vvgpu_ctx* ctx, double* out);
 
 /* ---- inspection (parity tests; same meaning as the oracle's exports) -------------- */

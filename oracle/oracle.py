@@ -106,6 +106,13 @@ def _load(kind: str):
         "slae_export": (C.c_int, [H, _D, _D, _D]),
         "vortex_shed": (C.c_int, [H]),
         "gsum": (C.c_double, [H]),
+        "set_velocities": (C.c_int, [H, _D, _D]),
+        "move_and_clean": (C.c_int, [H, C.c_int, C.POINTER(C.c_int64)]),
+        "get_body_params": (C.c_int, [H, C.c_int, C.POINTER(BodyParams)]),
+        "set_segment_state": (C.c_int, [H, _D, _D, _D]),
+        "calc_forces": (C.c_int, [H, _D]),
+        "zero_forces": (C.c_int, [H]),
+        "get_segment_forces": (C.c_int, [H, _D, _D, _D]),
     }
     if kind == "port":
         sig["direct_velocity"] = (C.c_int, [H, C.c_int64, _D, _D, _D, _D])
@@ -309,6 +316,42 @@ class OracleSpace:
 
     def gsum(self):
         return float(self.f["gsum"](self.h))
+
+    def set_velocities(self, vx, vy):
+        vx = np.ascontiguousarray(vx, dtype=np.float64)
+        vy = np.ascontiguousarray(vy, dtype=np.float64)
+        self._ok(self.f["set_velocities"](self.h, _p(vx), _p(vy)), "set_velocities")
+
+    def move_and_clean(self, remove: bool = True) -> int:
+        """MFlowmove::move_and_clean (MFlowmove.cpp:11-215); returns the number of vortices
+        removed inside bodies."""
+        n = C.c_int64(0)
+        self._ok(self.f["move_and_clean"](self.h, 1 if remove else 0, C.byref(n)), "move_and_clean")
+        return int(n.value)
+
+    def body_params(self, b: int = 0) -> dict:
+        bp = BodyParams()
+        self._ok(self.f["get_body_params"](self.h, int(b), C.byref(bp)), "get_body_params")
+        return {k: getattr(bp, k) for k, _ in BodyParams._fields_}
+
+    def set_segment_state(self, g=None, fric=None, gsum=None):
+        arr = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (g, fric, gsum)]
+        self._ok(self.f["set_segment_state"](self.h, *(_p(a) for a in arr)), "set_segment_state")
+
+    def calc_forces(self) -> np.ndarray:
+        """Space::calc_forces (TSpace.cpp:94-117); per body [friction x, y, o, nusselt]."""
+        out = np.zeros((self.nbodies, 4))
+        self._ok(self.f["calc_forces"](self.h, _p(out)), "calc_forces")
+        return out
+
+    def zero_forces(self):
+        self._ok(self.f["zero_forces"](self.h), "zero_forces")
+
+    def segment_forces(self) -> dict:
+        out = {k: np.empty(self.m) for k in ("cp", "fr", "nu")}
+        self._ok(self.f["get_segment_forces"](self.h, _p(out["cp"]), _p(out["fr"]), _p(out["nu"])),
+                 "get_segment_forces")
+        return out
 
     def set_sample(self, stride: int):
         self._ok(self.f["set_sample"](self.h, int(stride)), "set_sample")

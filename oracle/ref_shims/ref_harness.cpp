@@ -431,4 +431,100 @@ int vvr_vortex_shed(void* h) {
 
 double vvr_gsum(void* h) { return ((Handle*)h)->S.gsum(); }
 
+int vvr_set_velocities(void* h, const double* vx, const double* vy) {
+    Handle* H = (Handle*)h;
+    size_t i = 0;
+    for (auto& o : H->S.VortexList) { o.v = TVec(vx[i], vy[i]); i++; }
+    return 0;
+}
+
+// MFlowmove::move_and_clean.  The original index of each surviving vortex is carried
+// through the call in TObj::_1_eps (which move_and_clean does not read) and restored after.
+int vvr_move_and_clean(void* h, int remove, int64_t* cleaned) {
+    Handle* H = (Handle*)h;
+    if (H->built) return -2;
+    std::vector<double> ie;
+    size_t k = 0;
+    for (auto& o : H->S.VortexList) { ie.push_back(o._1_eps); o._1_eps = (double)k++; }
+    MFlowmove fm(&H->S);
+    const void* collision = nullptr;
+    size_t nc = 0;
+    fm.move_and_clean(remove != 0, &collision, &nc);
+    std::vector<int64_t> orig;
+    for (auto& o : H->S.VortexList) {
+        const size_t slot = (size_t)o._1_eps;
+        orig.push_back(H->orig[slot]);
+        o._1_eps = ie[slot];
+    }
+    H->orig = orig;
+    if (cleaned) *cleaned = (int64_t)nc;
+    return collision ? -5 : 0;
+}
+
+int vvr_set_segment_state(void* h, const double* g, const double* fric, const double* gsum) {
+    Handle* H = (Handle*)h;
+    int64_t k = 0;
+    for (auto& b : H->S.BodyList)
+        for (auto& a : b->alist) {
+            if (g) a.g = g[k];
+            if (fric) a.fric = fric[k];
+            if (gsum) a.gsum = gsum[k];
+            k++;
+        }
+    return 0;
+}
+
+int vvr_calc_forces(void* h, double* out4) {
+    Handle* H = (Handle*)h;
+    H->S.calc_forces();
+    int bi = 0;
+    for (auto& b : H->S.BodyList) {
+        if (out4) {
+            out4[4 * bi + 0] = b->friction.r.x; out4[4 * bi + 1] = b->friction.r.y;
+            out4[4 * bi + 2] = b->friction.o; out4[4 * bi + 3] = b->nusselt;
+        }
+        bi++;
+    }
+    return 0;
+}
+
+int vvr_zero_forces(void* h) {
+    ((Handle*)h)->S.zero_forces();
+    return 0;
+}
+
+int vvr_get_segment_forces(void* h, double* cp, double* fr, double* nu) {
+    Handle* H = (Handle*)h;
+    int64_t k = 0;
+    for (auto& b : H->S.BodyList)
+        for (auto& a : b->alist) {
+            if (cp) cp[k] = a.Cp;
+            if (fr) fr[k] = a.Fr;
+            if (nu) nu[k] = a.Nu;
+            k++;
+        }
+    return 0;
+}
+
+int vvr_get_body_params(void* h, int bi, vvo_body_params* out) {
+    Handle* H = (Handle*)h;
+    if (bi < 0 || bi >= (int)H->S.BodyList.size() || !out) return -1;
+    const TBody& b = *H->S.BodyList[bi];
+    memset(out, 0, sizeof *out);
+    out->holder_x = b.holder.r.x; out->holder_y = b.holder.r.y; out->holder_o = b.holder.o;
+    out->dpos_x = b.dpos.r.x; out->dpos_y = b.dpos.r.y; out->dpos_o = b.dpos.o;
+    out->speed_slae_x = b.speed_slae.r.x; out->speed_slae_y = b.speed_slae.r.y; out->speed_slae_o = b.speed_slae.o;
+    out->speed_slae_prev_x = b.speed_slae_prev.r.x; out->speed_slae_prev_y = b.speed_slae_prev.r.y;
+    out->speed_slae_prev_o = b.speed_slae_prev.o;
+    out->friction_prev_x = b.friction_prev.r.x; out->friction_prev_y = b.friction_prev.r.y;
+    out->friction_prev_o = b.friction_prev.o;
+    out->fdt_dead_x = b.fdt_dead.r.x; out->fdt_dead_y = b.fdt_dead.r.y; out->fdt_dead_o = b.fdt_dead.o;
+    out->g_dead = b.g_dead;
+    out->density = b.density;
+    out->kspring_x = b.kspring.r.x; out->kspring_y = b.kspring.r.y; out->kspring_o = b.kspring.o;
+    out->special_segment_no = b.special_segment_no;
+    out->bc_kutta = b.boundary_condition == bc_t::kutta;
+    return 0;
+}
+
 }  // extern "C"

@@ -1,13 +1,23 @@
-// Project-written stand-in for the Space constructor of libvvhd/src/TSpace.cpp, whose
-// translation unit needs HDF5 (absent here). TEST INFRASTRUCTURE ONLY.
-// Field defaults follow TSpace.cpp:14-36.
+// Project-written stand-ins for the HDF5 entry points that libvvhd/src/TSpace.cpp names
+// (declared in hdf5_stub/hdf5.h) and for the members of Space whose translation units need
+// HDF5 (TSpace_save_hdf.cpp, TSpace_load_hdf.cpp, TSpace_load_v13.cpp).  TSpace.cpp itself
+// is compiled unmodified, so Space's constructor, calc_forces and zero_forces are the
+// reference's own.  Snapshot I/O is not part of the oracle: these report failure.
+// TEST INFRASTRUCTURE ONLY.
+#include <stdexcept>
+#include <string>
+
 #include "TSpace.hpp"
+#include "hdf5.h"
 
-#include <limits>
+herr_t H5Eset_auto(hid_t, void*, void*) { return -1; }
+htri_t H5Fis_hdf5(const char*) { return -1; }
+hid_t H5Fopen(const char*, unsigned, hid_t) { return -1; }
+hid_t H5Fcreate(const char*, unsigned, hid_t, hid_t) { return -1; }
+herr_t H5Fclose(hid_t) { return -1; }
 
-static const double shim_inf = std::numeric_limits<double>::infinity();
+void h5_throw(std::string fn, std::string arg) { throw std::runtime_error(fn + " " + arg + ": no HDF5 in the oracle"); }
 
-Space::Space()
-    : caption(), re(shim_inf), pr(0), inf_g(), inf_vx(), inf_vy(), inf_marker(), gravity(),
-      time(), dt(1, 1), dt_save(), dt_streak(), dt_profile(), finish(shim_inf), BodyList(),
-      VortexList(), HeatList(), SourceList(), StreakSourceList(), StreakList() {}
+void Space::save_hdf(int64_t) { throw std::runtime_error("Space::save_hdf: no HDF5 in the oracle"); }
+void Space::load_hdf(int64_t, metainfo_t*) { throw std::runtime_error("Space::load_hdf: no HDF5 in the oracle"); }
+void Space::load_v13(const char*) { throw std::runtime_error("Space::load_v13: not in the oracle"); }

@@ -53,6 +53,7 @@ typedef struct {
     int64_t first, count;
     vvo_body_params p;
     double slen, area, cofm_x, cofm_y, moi_cofm;
+    double friction_x, friction_y, friction_o, nusselt;  /* TBody::friction, nusselt */
 } obody;
 
 struct vvo_space {
@@ -64,6 +65,7 @@ struct vvo_space {
     /* all TAtt of all bodies, concatenated */
     int64_t m, mcap;
     double *cx, *cy, *rx, *ry, *dlx, *dly, *sie, *sg, *fric, *gsum;
+    double *cp, *fr, *nu;  /* TAtt::Cp, Fr, Nu (Space::calc_forces accumulators) */
     uint32_t* slip;
     int nb, nbcap;
     obody* bodies;
@@ -120,6 +122,7 @@ void vvo_destroy(vvo_space* S) {
     free(S->x); free(S->y); free(S->g); free(S->ie); free(S->vx); free(S->vy); free(S->orig);
     free(S->cx); free(S->cy); free(S->rx); free(S->ry); free(S->dlx); free(S->dly);
     free(S->sie); free(S->sg); free(S->fric); free(S->gsum); free(S->slip);
+    free(S->cp); free(S->fr); free(S->nu);
     free(S->bodies);
     free(S->snk_x); free(S->snk_y); free(S->snk_g);
     free(S->mat); free(S->rhs); free(S->sol);
@@ -188,12 +191,14 @@ int vvo_add_body(vvo_space* S, int64_t nseg, const double* corner_x, const doubl
         S->dlx = xrealloc(S->dlx, d); S->dly = xrealloc(S->dly, d);
         S->sie = xrealloc(S->sie, d); S->sg = xrealloc(S->sg, d);
         S->fric = xrealloc(S->fric, d); S->gsum = xrealloc(S->gsum, d);
+        S->cp = xrealloc(S->cp, d); S->fr = xrealloc(S->fr, d); S->nu = xrealloc(S->nu, d);
         S->slip = xrealloc(S->slip, sizeof(uint32_t) * (size_t)m);
     }
     for (int64_t k = 0; k < nseg; k++) {
         int64_t i = S->m + k;
         S->cx[i] = corner_x[k]; S->cy[i] = corner_y[k];
         S->sg[i] = 0; S->fric[i] = 0; S->gsum[i] = 0;
+        S->cp[i] = 0; S->fr[i] = 0; S->nu[i] = 0;
         S->slip[i] = slip ? slip[k] : 0;
     }
     if (S->nb == S->nbcap) {
@@ -1261,6 +1266,201 @@ int vvo_slae_export(const vvo_space* S, double* matrix, double* rhs, double* sol
     if (matrix) memcpy(matrix, S->mat, sizeof(double) * (size_t)(n * n));
     if (rhs) memcpy(rhs, S->rhs, sizeof(double) * (size_t)n);
     if (solution) memcpy(solution, S->sol, sizeof(double) * (size_t)n);
+    return 0;
+}
+
+/* TBody::isPointInvalid -> isPointInContour over the body's corners (TBody.cpp:217-280):
+ * the bounding rectangle / disc of doFillProperties (TBody.cpp:327-342) as a pre-check
+ * unless the body is inverted (area <= 0), then crossing-number parity, then the segment
+ * whose centre is nearest (first minimum in list order).  Returns the global segment index
+ * or -1. */
+static int64_t point_invalid(const vvo_space* S, const obody* b, double px, double py) {
+    const int64_t f = b->first, n = b->count;
+    int in = (b->area <= 0);
+    double r2max = 0, blx = INFINITY, bly = INFINITY, trx = -INFINITY, try_ = -INFINITY;
+    for (int64_t k = 0; k < n; k++) {
+        const double cx = S->cx[f + k], cy = S->cy[f + k];
+        const double r2 = abs2(cx - b->cofm_x, cy - b->cofm_y);
+        if (r2 > r2max) r2max = r2;
+        if (cx > trx) trx = cx;
+        if (cy > try_) try_ = cy;
+        if (cx < blx) blx = cx;
+        if (cy < bly) bly = cy;
+    }
+    if (!in && (px < blx || py < bly || px > trx || py > try_ || abs2(px - b->cofm_x, py - b->cofm_y) > r2max))
+        return -1;
+    for (int64_t i = 0, j = n - 1; i < n; j = i++) {
+        const double vix = S->cx[f + i], viy = S->cy[f + i], vjx = S->cx[f + j], vjy = S->cy[f + j];
+        if (((viy < vjy) && (viy < py) && (py <= vjy) && ((vjy - viy) * (px - vix) > (vjx - vix) * (py - viy))) ||
+            ((viy > vjy) && (viy > py) && (py >= vjy) && ((vjy - viy) * (px - vix) < (vjx - vix) * (py - viy))))
+            in = !in;
+    }
+    if (!in) return -1;
+    int64_t best = -1;
+    double bd = DBL_MAX;
+    for (int64_t k = 0; k < n; k++) {
+        const double d = abs2(S->rx[f + k] - px, S->ry[f + k] - py);
+        if (d < bd) { bd = d; best = f + k; }
+    }
+    return best;
+}
+
+/* MFlowmove::move_and_clean (MFlowmove.cpp:11-215) for rigid bodies at rest: with no
+ * spring there is no collision (current_dt = dt) and the bodies do not move (a SLAE speed
+ * below 1e-10, the solver's round-off of zero, is not applied), so only the vortex part and
+ * the bookkeeping remain.  The order of every FP64 accumulation follows
+ * the reference (list order for the removed vortices, body and segment order after). */
+int vvo_move_and_clean(vvo_space* S, int remove, int64_t* cleaned) {
+    if (S->built) return -2;
+    for (int bi = 0; bi < S->nb; bi++) {
+        const vvo_body_params* p = &S->bodies[bi].p;
+        if (!is_rigid(p->kspring_x) || !is_rigid(p->kspring_y) || !is_rigid(p->kspring_o)) return -4;
+        if (p->speed_x != 0 || p->speed_y != 0 || p->speed_o != 0 ||
+            !(fabs(p->speed_slae_x) + fabs(p->speed_slae_y) + fabs(p->speed_slae_o) < 1E-10))
+            return -4;
+    }
+    const double dt = S->dt;
+    int64_t nc = 0;
+    /* r += v * dt (MFlowmove.cpp:104) */
+    for (int64_t i = 0; i < S->n; i++) {
+        S->x[i] = S->x[i] + S->vx[i] * dt;
+        S->y[i] = S->y[i] + S->vy[i] * dt;
+    }
+    /* erase |g| < remove_eps (:110-114), keeping the order */
+    int64_t w = 0;
+    for (int64_t i = 0; i < S->n; i++) {
+        if (fabs(S->g[i]) < REMOVE_EPS) continue;
+        S->x[w] = S->x[i]; S->y[w] = S->y[i]; S->g[w] = S->g[i]; S->ie[w] = S->ie[i];
+        S->vx[w] = S->vx[i]; S->vy[w] = S->vy[i]; S->orig[w] = S->orig[i];
+        w++;
+    }
+    S->n = w;
+    if (remove) {
+        /* erase vortices inside a body, with the dead-vortex bookkeeping (:121-143) */
+        w = 0;
+        for (int64_t i = 0; i < S->n; i++) {
+            int64_t seg = -1;
+            int bad = -1;
+            for (int bi = 0; bi < S->nb; bi++) {
+                seg = point_invalid(S, &S->bodies[bi], S->x[i], S->y[i]);
+                if (seg >= 0) { bad = bi; break; }
+            }
+            if (bad < 0) {
+                S->x[w] = S->x[i]; S->y[w] = S->y[i]; S->g[w] = S->g[i]; S->ie[w] = S->ie[i];
+                S->vx[w] = S->vx[i]; S->vy[w] = S->vy[i]; S->orig[w] = S->orig[i];
+                w++;
+                continue;
+            }
+            vvo_body_params* p = &S->bodies[bad].p;
+            const double gi = S->g[i], px = S->x[i], py = S->y[i];
+            p->fdt_dead_x += (-py) * gi;
+            p->fdt_dead_y += px * gi;
+            p->fdt_dead_o += abs2(px - body_axis_x(&S->bodies[bad]), py - body_axis_y(&S->bodies[bad])) * gi;
+            S->gsum[seg] -= gi;
+            p->g_dead += gi;
+            nc++;
+        }
+        S->n = w;
+    }
+    /* v = 0 (:192-197) */
+    for (int64_t i = 0; i < S->n; i++) { S->vx[i] = 0; S->vy[i] = 0; }
+    /* dead segments: |g| < remove_eps or slip (:199-214) */
+    for (int bi = 0; bi < S->nb; bi++) {
+        obody* b = &S->bodies[bi];
+        const double ax = body_axis_x(b), ay = body_axis_y(b);
+        for (int64_t k = 0; k < b->count; k++) {
+            const int64_t s = b->first + k;
+            if (fabs(S->sg[s]) < REMOVE_EPS || S->slip[s]) {
+                const double gs = S->sg[s];
+                b->p.fdt_dead_x += (-S->cy[s]) * gs;
+                b->p.fdt_dead_y += S->cx[s] * gs;
+                b->p.fdt_dead_o += abs2(S->cx[s] - ax, S->cy[s] - ay) * gs;
+                S->gsum[s] -= gs;
+                b->p.g_dead += gs;
+            }
+        }
+    }
+    if (cleaned) *cleaned = nc;
+    return 0;
+}
+
+int vvo_set_segment_state(vvo_space* S, const double* g, const double* fric, const double* gsum) {
+    for (int64_t i = 0; i < S->m; i++) {
+        if (g) S->sg[i] = g[i];
+        if (fric) S->fric[i] = fric[i];
+        if (gsum) S->gsum[i] = gsum[i];
+    }
+    return 0;
+}
+
+/* Space::calc_forces (TSpace.cpp:94-117).  No heat here: hsum = 0 and Space::pr = 0, the
+ * reference's defaults, are kept in the formulas so that Nu and nusselt match it. */
+int vvo_calc_forces(vvo_space* S, double* out4) {
+    const double pr = 0., hsum = 0.;
+    const double c_nyudt_pi = S->dt / (C_PI * S->re);
+    const double c_nyu_pi = 1. / (C_PI * S->re);
+    for (int bi = 0; bi < S->nb; bi++) {
+        obody* b = &S->bodies[bi];
+        double tmp_gsum = 0;
+        b->friction_x = b->friction_y = b->friction_o = 0;
+        for (int64_t k = 0; k < b->count; k++) {
+            const int64_t s = b->first + k;
+            const double dlabs = sqrt(abs2(S->dlx[s], S->dly[s]));
+            tmp_gsum += S->gsum[s];
+            S->cp[s] += tmp_gsum;
+            S->fr[s] += S->fric[s] * c_nyudt_pi;
+            S->nu[s] += hsum * (S->re * pr / dlabs);
+            const double f = S->fric[s] * c_nyu_pi / dlabs;
+            b->friction_x -= S->dlx[s] * f;
+            b->friction_y -= S->dly[s] * f;
+            b->friction_o -= ((-S->ry[s]) * S->dlx[s] + S->rx[s] * S->dly[s]) * f;
+            b->nusselt += hsum * (S->re * pr);
+        }
+        b->nusselt /= S->dt;
+        if (out4) {
+            out4[4 * bi + 0] = b->friction_x; out4[4 * bi + 1] = b->friction_y;
+            out4[4 * bi + 2] = b->friction_o; out4[4 * bi + 3] = b->nusselt;
+        }
+    }
+    return 0;
+}
+
+/* Space::zero_forces (TSpace.cpp:122-142); force_hydro/force_holder are not kept here. */
+int vvo_zero_forces(vvo_space* S) {
+    for (int bi = 0; bi < S->nb; bi++) {
+        obody* b = &S->bodies[bi];
+        for (int64_t k = 0; k < b->count; k++) {
+            const int64_t s = b->first + k;
+            S->gsum[s] = 0; S->fric[s] = 0;
+        }
+        b->p.friction_prev_x = b->friction_x;
+        b->p.friction_prev_y = b->friction_y;
+        b->p.friction_prev_o = b->friction_o;
+        b->friction_x = b->friction_y = b->friction_o = 0;
+        b->p.fdt_dead_x = b->p.fdt_dead_y = b->p.fdt_dead_o = 0;
+        b->p.g_dead = 0;
+        b->nusselt = 0;
+    }
+    return 0;
+}
+
+int vvo_get_segment_forces(const vvo_space* S, double* cp, double* fr, double* nu) {
+    for (int64_t i = 0; i < S->m; i++) {
+        if (cp) cp[i] = S->cp[i];
+        if (fr) fr[i] = S->fr[i];
+        if (nu) nu[i] = S->nu[i];
+    }
+    return 0;
+}
+
+int vvo_set_velocities(vvo_space* S, const double* vx, const double* vy) {
+    for (int64_t i = 0; i < S->n; i++) { S->vx[i] = vx[i]; S->vy[i] = vy[i]; }
+    return 0;
+}
+
+int vvo_get_body_params(const vvo_space* S, int b, vvo_body_params* out) {
+    if (b < 0 || b >= S->nb || !out) return -1;
+    *out = S->bodies[b].p;
     return 0;
 }
 

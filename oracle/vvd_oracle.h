@@ -131,6 +131,22 @@ int vvo_last_timings(const vvo_space* S, double* out3);
 int vvo_slae_rhs_step(vvo_space* S, double* rhs_out);
 /* MFlowmove::vortex_shed (MFlowmove.cpp:217-235). */
 int vvo_vortex_shed(vvo_space* S);
+/* MFlowmove::move_and_clean(remove, &collision, &cleaned) (MFlowmove.cpp:11-215) for rigid
+ * bodies at rest (no collision): r += v dt, removal of |g| < 1e-10 and (remove != 0) of
+ * vortices inside a body with its circulation bookkeeping, v = 0, dead segment terms.
+ * Returns -2 with the tree built, -4 for moving or spring-mounted bodies. */
+int vvo_move_and_clean(vvo_space* S, int remove, int64_t* cleaned);
+int vvo_get_body_params(const vvo_space* S, int b, vvo_body_params* out);
+/* TObj::v of every vortex (as left by the convective and diffusive passes). */
+int vvo_set_velocities(vvo_space* S, const double* vx, const double* vy);
+/* TAtt::g, fric and gsum of every segment. */
+int vvo_set_segment_state(vvo_space* S, const double* g, const double* fric, const double* gsum);
+/* Space::calc_forces (TSpace.cpp:94-117): per-segment Cp, Fr, Nu accumulation and each
+ * body's friction (x, y, o) and nusselt, written to out4[4 b .. 4 b + 3]. */
+int vvo_calc_forces(vvo_space* S, double* out4);
+/* Space::zero_forces (TSpace.cpp:122-142). */
+int vvo_zero_forces(vvo_space* S);
+int vvo_get_segment_forces(const vvo_space* S, double* cp, double* fr, double* nu);
 /* Space::gsum (TSpace.hpp:93-99). */
 double vvo_gsum(const vvo_space* S);
 

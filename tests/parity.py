@@ -13,11 +13,25 @@ GOLDEN_EXACT_PREFIXES = ("t1_", "t2_")
 EXACT_KEYS = ("merged", "n_after_shed", "eps_x", "eps_y", "eps_g", "eps_inv_eps", "eps_orig")
 
 
-def golden_cases(folder):
+def golden_cases(folder, prefix=None):
+    """Fixture names in ``folder``: the one-step fixtures (no prefix), or those whose name
+    starts with ``prefix`` (e.g. "move_")."""
     import glob
     import os
-    return sorted(os.path.splitext(os.path.basename(p))[0]
-                  for p in glob.glob(os.path.join(folder, "*.npz")))
+    names = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(folder, "*.npz")))
+    if prefix is None:
+        return [n for n in names if not n.startswith(("move_", "forces_"))]
+    return [n for n in names if n.startswith(prefix)]
+
+
+def check_move(got: dict, d: dict, prefix: str):
+    """MFlowmove::move_and_clean outputs: every array bit-exact (the FP64 bookkeeping sums
+    run in the reference's order)."""
+    for k, v in got.items():
+        ref = d[prefix + k]
+        assert np.asarray(v).shape == ref.shape, (prefix + k, np.asarray(v).shape, ref.shape)
+        eq_nan = np.asarray(v).dtype.kind == "f"
+        assert np.array_equal(np.asarray(v), ref, equal_nan=eq_nan), prefix + k
 
 
 def load_workload(path):

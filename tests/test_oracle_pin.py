@@ -55,3 +55,45 @@ def test_port_matches_reference_live(seed):
     b = _run("port", wl, True)
     bad = check_step(a, b, vel_tol=0, diff_tol=0, fric_tol=0, slae_tol=0)
     assert not bad, bad
+
+
+# ---- MFlowmove::move_and_clean -------------------------------------------------------
+from move_cases import cases as move_cases, run_move  # noqa: E402
+from parity import check_move  # noqa: E402
+
+
+@pytest.mark.parametrize("case", golden_cases(GOLDEN, prefix="move_"))
+def test_port_move_matches_golden(case):
+    d = dict(np.load(os.path.join(GOLDEN, case + ".npz")))
+    c = move_cases()[case[len("move_"):]]
+    for remove in (True, False):
+        S = oracle.OracleSpace("port")
+        got = run_move(S, c, remove, oracle.default_body_params)
+        S.close()
+        check_move(got, d, "rm_" if remove else "keep_")
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference sources not present")
+def test_port_move_matches_reference_live():
+    rng = np.random.default_rng(99)
+    c = move_cases()["cyl"]
+    c = dict(c, vx=rng.normal(0, 3.0, len(c["x"])), vy=rng.normal(0, 3.0, len(c["x"])))
+    outs = []
+    for kind in ("port", "ref"):
+        S = oracle.OracleSpace(kind)
+        outs.append(run_move(S, c, True, oracle.default_body_params))
+        S.close()
+    check_move(outs[0], {"rm_" + k: v for k, v in outs[1].items()}, "rm_")
+
+
+# ---- Space::calc_forces / zero_forces -----------------------------------------------
+from move_cases import forces_cases, run_forces  # noqa: E402
+
+
+@pytest.mark.parametrize("case", golden_cases(GOLDEN, prefix="forces_"))
+def test_port_forces_match_golden(case):
+    d = dict(np.load(os.path.join(GOLDEN, case + ".npz")))
+    S = oracle.OracleSpace("port")
+    got = run_forces(S, forces_cases()[case[len("forces_"):]], oracle.default_body_params)
+    S.close()
+    check_move(got, d, "")

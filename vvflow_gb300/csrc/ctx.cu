@@ -261,9 +261,11 @@ int vvgpu_add_body(vvgpu_ctx* h, int64_t nseg, const double* cx, const double* c
     c.s_g.reserve(m, true, m0, s);
     c.s_fric.reserve(m, true, m0, s);
     c.s_gsum.reserve(m, true, m0, s);
-    VV_CUDA(cudaMemsetAsync(c.s_g.p + m0, 0, nseg * sizeof(double), s));
-    VV_CUDA(cudaMemsetAsync(c.s_fric.p + m0, 0, nseg * sizeof(double), s));
-    VV_CUDA(cudaMemsetAsync(c.s_gsum.p + m0, 0, nseg * sizeof(double), s));
+    c.s_cp.reserve(m, true, m0, s);
+    c.s_fr.reserve(m, true, m0, s);
+    c.s_nu.reserve(m, true, m0, s);
+    for (auto* a : {&c.s_g, &c.s_fric, &c.s_gsum, &c.s_cp, &c.s_fr, &c.s_nu})
+        VV_CUDA(cudaMemsetAsync(a->p + m0, 0, nseg * sizeof(double), s));
     c.segs_dirty = true;
     c.lu_valid = false;
     API_END
@@ -484,6 +486,42 @@ int vvgpu_vortex_shed(vvgpu_ctx* h) {
     API_BEGIN(h)
     if (c.built) throw ApiError{VVGPU_ERR_STATE, "shed with the tree built"};
     vortex_shed(c);
+    API_END
+}
+
+int vvgpu_move_and_clean(vvgpu_ctx* h, int remove, int64_t* cleaned) {
+    API_BEGIN(h)
+    if (c.built) throw ApiError{VVGPU_ERR_STATE, "move_and_clean with the tree built"};
+    move_and_clean(c, remove, cleaned);
+    API_END
+}
+
+int vvgpu_calc_forces(vvgpu_ctx* h, double* out4) {
+    API_BEGIN(h)
+    calc_forces(c, out4);
+    API_END
+}
+
+int vvgpu_zero_forces(vvgpu_ctx* h) {
+    API_BEGIN(h)
+    zero_forces(c);
+    API_END
+}
+
+int vvgpu_get_segment_forces(vvgpu_ctx* h, double* cp, double* fr, double* nu) {
+    API_BEGIN(h)
+    cudaStream_t s = c.st();
+    d2h(cp, c.s_cp.p, c.m, s);
+    d2h(fr, c.s_fr.p, c.m, s);
+    d2h(nu, c.s_nu.p, c.m, s);
+    VV_CUDA(cudaStreamSynchronize(s));
+    API_END
+}
+
+int vvgpu_get_body_params(vvgpu_ctx* h, int body, vvgpu_body_params* out) {
+    API_BEGIN(h)
+    if (body < 0 || body >= (int)c.bodies.size() || !out) throw ApiError{VVGPU_ERR_ARG, "bad body index"};
+    *out = c.bodies[body].p;
     API_END
 }
 

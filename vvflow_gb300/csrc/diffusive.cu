@@ -26,6 +26,7 @@ namespace vvgpu {
 namespace {
 
 constexpr int DW = 4;
+constexpr int SRC_CAP = 256;  // FP32 path: sources staged per warp at a time
 
 // Box of non-zero vortices and segment centres of each leaf, FP32 in the leaf's own frame.
 __global__ void k_dbox(int64_t nl, const int32_t* __restrict__ lvf, const int32_t* __restrict__ lvl,
@@ -215,7 +216,8 @@ __global__ void __launch_bounds__(DW * 32, 4) k_diff32(DiffArgs a) {
     constexpr int LG = 4 * DT;  // lanes per group (source stride)
     __shared__ int2 s_runs[DW][32];
     __shared__ int4 s_hit[DW][32];     // flattened start, first vortex, shift x, shift y (bits)
-    __shared__ float2 s_hitb[DW][32];  // error bound D of the leaf, squared coincidence limit
+    __shared__ float2 s_hitb[DW][32];  // error bound D of the leaf
+    __shared__ float4 s_src[DW][SRC_CAP];  // staged sources: x, y in L's frame, g, index (bits)
     __shared__ int32_t s_hitq[DW][32]; // leaf
     // per lane FP64 accumulators (s2x, s2y, s1, s3x, s3y, s0 of its targets), touched only by
     // band pairs and wall segments; lane-major so that lanes never share a bank row
@@ -313,69 +315,83 @@ __global__ void __launch_bounds__(DW * 32, 4) k_diff32(DiffArgs a) {
                 const float spmax = fmaxf(fmaxf(fabsf(b.x + sh.x), fabsf(b.z + sh.x)),
                                           fmaxf(fabsf(b.y + sh.y), fabsf(b.w + sh.y)));
                 const float D = ldexpf(2.f * tmax + s4max + 2.f * spmax, -21);
-                const float tiny = 2.f * D + 1e-9f;  // |dx| + |dy| below it may be under 1e-10
                 s_hit[wq][r] = make_int4(incl - len, j0, __float_as_int(sh.x), __float_as_int(sh.y));
-                s_hitb[wq][r] = make_float2(D, tiny * tiny);
+                s_hitb[wq][r] = make_float2(D, 0.f);
                 s_hitq[wq][r] = q;
             }
             __syncwarp();
             if (lane == 0) ncand += (unsigned long long)nact * (unsigned long long)total;
-            int cur = 0;
-            int32_t nextb = (nh > 1) ? s_hit[wq][1].x : total;
-            for (int32_t k = sub; k < total; k += LG) {
-                while (k >= nextb) {
-                    cur++;
-                    nextb = (cur + 1 < nh) ? s_hit[wq][cur + 1].x : total;
-                }
-                const int4 hc = s_hit[wq][cur];
-                const int32_t j = hc.y + (k - hc.x);
-                const float4 s4 = a.src32[j];
-                if (s4.z == 0.f) continue;
-                const float sx = s4.x + __int_as_float(hc.z), sy = s4.y + __int_as_float(hc.w);
-                // a target's pair with itself is excluded by the reference's coincidence rule
-                const int32_t jr = j - tb;
-                const unsigned self = (jr >= 0 && jr < DT) ? (1u << jr) : 0u;
-                const unsigned same = (s4.z > 0.f ? pos : ~pos) & act & ~self;
-                const float2 hb = s_hitb[wq][cur];
-                unsigned pend = 0;  // targets whose pair with this source goes to FP64
-#pragma unroll
-                for (int t = 0; t < DT; t++) {
-                    const float dx = tx[t] - sx, dy = ty[t] - sy;
-                    const float r2 = dx * dx + dy * dy;
-                    const float du = r2 * ie2[t] - 64.f;  // (|dr| / eps)^2 - 64
-                    const float bnd = fmaf(b16[t], hb.x, bandc);
-                    const bool sm = (same >> t) & 1u;
-                    if (sm && (fabsf(du) < bnd || r2 < hb.y)) pend |= 1u << t;
-                    const bool in = sm && du <= -bnd && r2 >= hb.y;
-                    const float r2c = in ? r2 : 1.f;
-                    const float rs = rsqrtf(r2c);
-                    const float tv = in ? s4.z * __expf(-(r2c * rs) * ief[t]) : 0.f;
-                    const float qv = tv * rs;
-                    p2x[t] = fmaf(dx, qv, p2x[t]);
-                    p2y[t] = fmaf(dy, qv, p2y[t]);
-                    p1[t] += tv;
-                }
-                if (pend) {  // rare: the reference's FP64 test and term
-                    if (!used64) {
-                        for (int w = 0; w < DT * 6; w++) d64[w][lane] = 0.;
-                        used64 = true;
+            // band parameters of this batch: the largest error bound D of its leaves
+            float Dm = 0.f;
+            for (int h = 0; h < nh; h++) Dm = fmaxf(Dm, s_hitb[wq][h].x);
+            const float tiny = 2.f * Dm + 1e-9f, tiny2 = tiny * tiny;
+            for (int32_t kb = 0; kb < total; kb += SRC_CAP) {
+                const int32_t nst = min(SRC_CAP, total - kb);
+                // stage the sources (shifted into L's frame) once per warp
+                for (int32_t k = lane; k < nst; k += 32) {
+                    const int32_t kk = kb + k;
+                    int lo = 0, hi = nh - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (s_hit[wq][mid].x <= kk) lo = mid;
+                        else hi = mid - 1;
                     }
-                    for (int t = 0; t < DT; t++) {
-                        if (!((pend >> t) & 1u)) continue;
-                        const int32_t i = tb + t;
-                        vortex_term64(a.x[i], a.y[i], a.g[i], a.ie[i], a.x[j], a.y[j], a.g[j], d64[6 * t][lane],
-                                      d64[6 * t + 1][lane], d64[6 * t + 2][lane]);
-                    }
+                    const int4 hc = s_hit[wq][lo];
+                    const int32_t j = hc.y + (kk - hc.x);
+                    const float4 s4 = a.src32[j];
+                    s_src[wq][k] = make_float4(s4.x + __int_as_float(hc.z), s4.y + __int_as_float(hc.w), s4.z,
+                                               __int_as_float(j));
                 }
-                if (++since == 16) {
-                    since = 0;
+                __syncwarp();
+                for (int32_t k = sub; k < nst; k += LG) {
+                    const float4 sv = s_src[wq][k];
+                    if (sv.z == 0.f) continue;
+                    const int32_t j = __float_as_int(sv.w);
+                    // a target's pair with itself is excluded by the reference's coincidence rule
+                    const int32_t jr = j - tb;
+                    const unsigned self = (jr >= 0 && jr < DT) ? (1u << jr) : 0u;
+                    const unsigned same = (sv.z > 0.f ? pos : ~pos) & act & ~self;
+                    unsigned pend = 0;  // targets whose pair with this source goes to FP64
 #pragma unroll
                     for (int t = 0; t < DT; t++) {
-                        acc_add(h2x[t], l2x[t], p2x[t]); p2x[t] = 0.f;
-                        acc_add(h2y[t], l2y[t], p2y[t]); p2y[t] = 0.f;
-                        acc_add(h1[t], l1[t], p1[t]); p1[t] = 0.f;
+                        const float dx = tx[t] - sv.x, dy = ty[t] - sv.y;
+                        const float r2 = dx * dx + dy * dy;
+                        const float du = r2 * ie2[t] - 64.f;  // (|dr| / eps)^2 - 64
+                        const float bnd = fmaf(b16[t], Dm, bandc);
+                        const bool sm = (same >> t) & 1u;
+                        if (sm && (fabsf(du) < bnd || r2 < tiny2)) pend |= 1u << t;
+                        const bool in = sm && du <= -bnd && r2 >= tiny2;
+                        const float r2c = in ? r2 : 1.f;
+                        const float rs = rsqrtf(r2c);
+                        const float tv = in ? sv.z * __expf(-(r2c * rs) * ief[t]) : 0.f;
+                        const float qv = tv * rs;
+                        p2x[t] = fmaf(dx, qv, p2x[t]);
+                        p2y[t] = fmaf(dy, qv, p2y[t]);
+                        p1[t] += tv;
+                    }
+                    if (pend) {  // rare: the reference's FP64 test and term
+                        if (!used64) {
+                            for (int w = 0; w < DT * 6; w++) d64[w][lane] = 0.;
+                            used64 = true;
+                        }
+                        for (int t = 0; t < DT; t++) {
+                            if (!((pend >> t) & 1u)) continue;
+                            const int32_t i = tb + t;
+                            vortex_term64(a.x[i], a.y[i], a.g[i], a.ie[i], a.x[j], a.y[j], a.g[j], d64[6 * t][lane],
+                                          d64[6 * t + 1][lane], d64[6 * t + 2][lane]);
+                        }
+                    }
+                    if (++since == 16) {
+                        since = 0;
+#pragma unroll
+                        for (int t = 0; t < DT; t++) {
+                            acc_add(h2x[t], l2x[t], p2x[t]); p2x[t] = 0.f;
+                            acc_add(h2y[t], l2y[t], p2y[t]); p2y[t] = 0.f;
+                            acc_add(h1[t], l1[t], p1[t]); p1[t] = 0.f;
+                        }
                     }
                 }
+                __syncwarp();
             }
             if (any_seg) {
                 // wall segments of the candidate leaves (segment_influence, MDiffusiveFast.cpp:108-123), FP64

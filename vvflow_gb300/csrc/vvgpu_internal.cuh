@@ -98,6 +98,7 @@ struct BodyHost {
     int64_t first, count;
     vvgpu_body_params p;
     double slen, area, cofm_x, cofm_y, moi_cofm;
+    double friction_x = 0, friction_y = 0, friction_o = 0, nusselt = 0;  // TBody::friction, nusselt
 };
 
 struct Ctx {
@@ -121,6 +122,9 @@ struct Ctx {
     std::vector<uint32_t> h_slip;
     std::vector<BodyHost> bodies;
     DArr<double> s_cx, s_cy, s_rx, s_ry, s_dlx, s_dly, s_ie, s_g, s_fric, s_gsum;
+    DArr<double> s_cp, s_fr, s_nu;  // TAtt::Cp, Fr, Nu (Space::calc_forces accumulators)
+    DArr<int64_t> f_fc;
+    DArr<double> f_out;
     DArr<uint32_t> s_slip;
     bool segs_dirty = true;
     // sinks
@@ -179,6 +183,10 @@ struct Ctx {
     DArr<float4> e_box_prev;             // per leaf: the last round's box
     DArr<float> e_rreg;                  // per leaf: largest search radius^2 of its members
     DArr<int32_t> e_flag, e_pos, e_list; // targets to evaluate in a round (flags, offsets, list)
+    // move_and_clean
+    DArr<double> mv_bodies, mv_acc;      // per body inside-test geometry; bookkeeping sums
+    DArr<int32_t> mv_dead, mv_dpos, mv_list;
+    DArr<int2> mv_at;
     std::vector<int64_t> h_bfc;          // body first segments, then counts
     DArr<int64_t> e_bfc;
     DArr<float2> e_seg32;                // segment centres in FP32 relative to their body's anchor
@@ -322,6 +330,9 @@ void diffusive(Ctx& c);
 void slae(Ctx& c, vvgpu_body_out* out);
 void upload_segments(Ctx& c);
 void vortex_shed(Ctx& c);
+void move_and_clean(Ctx& c, int remove, int64_t* cleaned);
+void calc_forces(Ctx& c, double* out4);
+void zero_forces(Ctx& c);
 double gsum(Ctx& c);
 
 }  // namespace vvgpu

@@ -102,6 +102,11 @@ SIGNATURES = {
     "vvgpu_velocity_points_noalloc": (C.c_int, [_H, C.c_int64, _D, _D, _D, _D]),
     "vvgpu_slae": (C.c_int, [_H, C.POINTER(BodyOut)]),
     "vvgpu_vortex_shed": (C.c_int, [_H]),
+    "vvgpu_move_and_clean": (C.c_int, [_H, C.c_int, C.POINTER(C.c_int64)]),
+    "vvgpu_get_body_params": (C.c_int, [_H, C.c_int, C.POINTER(BodyParams)]),
+    "vvgpu_calc_forces": (C.c_int, [_H, _D]),
+    "vvgpu_zero_forces": (C.c_int, [_H]),
+    "vvgpu_get_segment_forces": (C.c_int, [_H, _D, _D, _D]),
     "vvgpu_gsum": (C.c_int, [_H, _D]),
     "vvgpu_tree_sizes": (C.c_int, [_H, _I64, _I64, _I64, _I64]),
     "vvgpu_tree_leaves": (C.c_int, [_H, _D, _D, _D, _D, _I64, _I64, _I32, _I64, _I64, _I64]),
@@ -198,6 +203,10 @@ class GpuSpace:
         g = np.ascontiguousarray(g, np.float64)
         self._ok(self.lib.vvgpu_set_segment_g(self.h, _p(g)), "set_segment_g")
 
+    def set_segment_state(self, g=None, fric=None, gsum=None):
+        arr = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (g, fric, gsum)]
+        self._ok(self.lib.vvgpu_set_segment_state(self.h, *(_p(a) for a in arr)), "set_segment_state")
+
     def set_vortices(self, x, y, g, inv_eps=None):
         x, y, g = (np.ascontiguousarray(a, np.float64) for a in (x, y, g))
         ie = None if inv_eps is None else np.ascontiguousarray(inv_eps, np.float64)
@@ -286,6 +295,40 @@ class GpuSpace:
         v = C.c_double()
         self._ok(self.lib.vvgpu_gsum(self.h, C.byref(v)), "gsum")
         return v.value
+
+    def set_velocities(self, vx, vy):
+        """TObj::v of every vortex (host arrays of the current list length)."""
+        vx = np.ascontiguousarray(vx, dtype=np.float64)
+        vy = np.ascontiguousarray(vy, dtype=np.float64)
+        self._ok(self.lib.vvgpu_set_velocities(self.h, _p(vx), _p(vy)), "set_velocities")
+
+    def move_and_clean(self, remove: bool = True) -> int:
+        """MFlowmove::move_and_clean (MFlowmove.cpp:11-215); returns the number of vortices
+        erased inside bodies."""
+        n = C.c_int64(0)
+        self._ok(self.lib.vvgpu_move_and_clean(self.h, 1 if remove else 0, C.byref(n)), "move_and_clean")
+        return int(n.value)
+
+    def body_params(self, b: int = 0) -> dict:
+        bp = BodyParams()
+        self._ok(self.lib.vvgpu_get_body_params(self.h, int(b), C.byref(bp)), "get_body_params")
+        return {k: getattr(bp, k) for k, _ in BodyParams._fields_}
+
+    def calc_forces(self) -> np.ndarray:
+        """Space::calc_forces (TSpace.cpp:94-117); per body [friction x, y, o, nusselt]."""
+        out = np.zeros((self.nbodies, 4))
+        self._ok(self.lib.vvgpu_calc_forces(self.h, _p(out)), "calc_forces")
+        return out
+
+    def zero_forces(self):
+        self._ok(self.lib.vvgpu_zero_forces(self.h), "zero_forces")
+
+    def segment_forces(self) -> dict:
+        m = self.m
+        out = {k: np.empty(m) for k in ("cp", "fr", "nu")}
+        self._ok(self.lib.vvgpu_get_segment_forces(self.h, _p(out["cp"]), _p(out["fr"]), _p(out["nu"])),
+                 "get_segment_forces")
+        return out
 
     def set_stream(self, stream_ptr: int | None):
         """Queues all work on the caller's CUDA stream (cudaStream_t as an integer)."""
