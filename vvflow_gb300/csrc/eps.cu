@@ -219,15 +219,30 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
                            const int32_t* __restrict__ live, float Gf, int32_t* cand, int32_t* ncand, float* rn,
                            float* rlist, float* rnear, const int32_t* __restrict__ leaf_changed, int32_t* dirty,
                            int32_t* chg, int32_t* nchg, const float4* __restrict__ box_prev,
-                           const float* __restrict__ rreg, int first_round, const float* __restrict__ dmax_p) {
+                           const float* __restrict__ rreg, const int32_t* __restrict__ chg_pre, int first_round,
+                           const float* __restrict__ dmax_p) {
     __shared__ int2 s_runs[EB / 32][32];
     const int wq = threadIdx.x >> 5;
     const int64_t L = (int64_t)blockIdx.x * (blockDim.x / 32) + wq;
     const int lane = threadIdx.x & 31;
     if (L >= nl) return;
+    const int32_t r0 = near_off[L], r1 = near_off[L + 1];
+    if (!first_round) {
+        // No near leaf changed in the last round (prefix sums of the changed flags over each
+        // near run): the boxes the list was checked against are unchanged, so the list stays
+        // valid and no target of L needs a new evaluation.
+        bool any = false;
+        for (int32_t r = r0 + lane; r < r1; r += 32) {
+            const int2 run = near_run[r];
+            any = any || chg_pre[run.y] != chg_pre[run.x];
+        }
+        if (!__any_sync(0xffffffffu, any)) {
+            if (lane == 0) { dirty[L] = 0; nchg[L] = 0; }
+            return;
+        }
+    }
     const float4 bL = box[L];
     const float2 aL = anchor[L];
-    const int32_t r0 = near_off[L], r1 = near_off[L + 1];
     const float dmax = first_round ? 0.f : *dmax_p;
     // upper bound on every target's second-nearest distance (squared)
     float R2 = INFINITY;
@@ -761,6 +776,7 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
     c.e_chg.reserve((size_t)nl * CHG_CAP + 1);
     c.e_nchg.reserve(nl + 1);
     c.e_box_prev.reserve(nl + 1);
+    c.e_lchg_pre.reserve(nl + 2);
     c.e_flag.reserve(n + 1);
     c.e_pos.reserve(n + 2);
     c.e_list.reserve(n + 1);
@@ -800,7 +816,8 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                        c.lf_box32.p, c.e_live.p, fr.Gf, c.e_cand.p, c.e_ncand.p,
                                                        c.lf_rn.p, c.e_rlist.p, c.e_rnear.p, c.e_lchanged.p,
                                                        c.e_dirty.p, c.e_chg.p, c.e_nchg.p, c.e_box_prev.p,
-                                                       c.e_rreg.p, rounds == 1, (const float*)dmax_bits);
+                                                       c.e_rreg.p, c.e_lchg_pre.p, rounds == 1,
+                                                       (const float*)dmax_bits);
         VV_LAUNCH_CHECK();
         VV_CUDA(cudaMemsetAsync(c.e_changed.p, 0, 4, s));
         EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.e_rnear.p,
@@ -845,6 +862,7 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                       c.e_og[cur].p, c.e_og[nx].p, c.e_zb_prev.p, c.e_zb.p,
                                                       c.e_lchanged.p, c.e_vch.p);
         VV_LAUNCH_CHECK();
+        exclusive_scan(c, c.e_lchanged.p, c.e_lchg_pre.p, nl);
         cur = nx;
         int32_t changed = read_i32(c, c.e_changed.p);
         if (!changed) break;

@@ -182,6 +182,7 @@ struct Ctx {
     DArr<float> e_sr1, e_sr2;            // per vortex: search radii^2 of its last evaluation
     DArr<float4> e_box_prev;             // per leaf: the last round's box
     DArr<float> e_rreg;                  // per leaf: largest search radius^2 of its members
+    DArr<int32_t> e_lchg_pre;            // exclusive prefix sums of the changed-leaf flags
     DArr<int32_t> e_flag, e_pos, e_list; // targets to evaluate in a round (flags, offsets, list)
     // move_and_clean
     DArr<double> mv_bodies, mv_acc;      // per body inside-test geometry; bookkeeping sums
