@@ -10,8 +10,9 @@
 //
 // One warp per target leaf in both paths.  FP64 path (k_diff64): eight target slots times
 // four source lanes, every pair in double precision with the reference's formulas.  FP32
-// path (k_diff32): four targets per lane, the 16 lanes of a half-warp stride over the
-// flattened sources of the candidate leaves; vortex pairs in local frames (frame.cuh) with
+// path (k_diff32): two targets per lane in four lane groups, the eight lanes of a group
+// stride over the sources of the candidate leaves (staged in shared memory per batch);
+// vortex pairs in local frames (frame.cuh) with
 // FP32 exp/rsqrt; pairs whose cut-off or coincidence test falls within a rigorous bound of
 // the FP32 error of its threshold are re-evaluated in FP64, so the set of contributing
 // pairs is the reference's.  Wall segments are always FP64.  Friction goes to TAtt::fric
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__(DW * 32) k_diff64(DiffArgs a) {
 // and the wall-segment terms, are evaluated in FP64 into per-lane accumulators that are
 // reduced in a fixed order, so results are reproducible.
 template <int DT>
-__global__ void __launch_bounds__(DW * 32, 4) k_diff32(DiffArgs a) {
+__global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
     constexpr int LG = 4 * DT;  // lanes per group (source stride)
     __shared__ int2 s_runs[DW][32];
     __shared__ int4 s_hit[DW][32];     // flattened start, first vortex, shift x, shift y (bits)
@@ -489,8 +490,10 @@ __global__ void __launch_bounds__(DW * 32, 4) k_diff32(DiffArgs a) {
     if (lane == 0 && ncand) atomicAdd(a.cand, ncand);
 }
 
+// two targets per lane, four lane groups: measured faster than four targets per lane at 4M
+// (11.0 vs 11.9 ms), the smaller register footprint allowing six blocks per SM
 #ifndef DIFF32_DT
-#define DIFF32_DT 4
+#define DIFF32_DT 2
 #endif
 
 }  // namespace
