@@ -5,9 +5,11 @@
 // (DistributeContent, TSortedTree.cpp:81-99).  That loop is a set of disjoint swaps: with
 // L = #{key < pivot} in the slice [f, l), the k-th element with key >= pivot inside [f, f+L)
 // (counted from the left) trades places with the k-th element with key < pivot inside
-// [f+L, l) (counted from the right).  Here every level of the tree is split at once:
-// one exclusive scan of the "low" flags gives every element its rank, the right-side lows
-// publish their positions in a table, and each left-side high performs its swap.  Only the
+// [f+L, l) (counted from the right).  Here every level of the tree is split at once: nodes
+// of at most 64 vortices by one warp each (ballots give the ranks, the swap goes through
+// shared memory), larger ones by blocks over 1024-vortex chunks (counts per chunk, one
+// exclusive scan, then each vortex's rank; the lows of the right part and the highs of the
+// left part publish their positions in two tables by rank, and one thread per pair swaps).  Only the
 // keys (x, y) and a slot permutation move at each level; the rest of the vortex record
 // follows once, after the last level.  The resulting permutation, node boxes and ranges are
 // bit-identical to the reference.
@@ -28,43 +30,10 @@ constexpr int TB = 256;
 __device__ __forceinline__ void bbox_min_atomic(unsigned long long* slot, double v) { atomicMin(slot, dkey(v)); }
 __device__ __forceinline__ void bbox_max_atomic(unsigned long long* slot, double v) { atomicMax(slot, dkey(v)); }
 
-// Segmented (by node id, contiguous within the warp) min/max reduction, then one atomic
-// per segment head.  node < 0 marks lanes that do not contribute.  The reduction runs on
-// the order-preserving integer keys of the coordinates (dkey), so it stays on the integer
-// pipe (FP64 min/max would run on sm_103's narrow FP64 pipe).
-__device__ __forceinline__ void warp_bbox_update(int node, double px, double py, unsigned long long* bbox) {
-    const int lane = threadIdx.x & 31;
-    const unsigned long long kx = dkey(px), ky = dkey(py);
-    unsigned long long mnx = kx, mny = ky, mxx = kx, mxy = ky;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int on = __shfl_down_sync(0xffffffffu, node, o);
-        const unsigned long long a = __shfl_down_sync(0xffffffffu, mnx, o);
-        const unsigned long long b = __shfl_down_sync(0xffffffffu, mny, o);
-        const unsigned long long cc = __shfl_down_sync(0xffffffffu, mxx, o);
-        const unsigned long long d = __shfl_down_sync(0xffffffffu, mxy, o);
-        if (lane + o < 32 && on == node) {
-            mnx = a < mnx ? a : mnx;
-            mny = b < mny ? b : mny;
-            mxx = cc > mxx ? cc : mxx;
-            mxy = d > mxy ? d : mxy;
-        }
-    }
-    const int prev = __shfl_up_sync(0xffffffffu, node, 1);
-    const bool head = (lane == 0) || (prev != node);
-    if (head && node >= 0) {
-        unsigned long long* s = bbox + 4 * (size_t)node;
-        atomicMin(s + 0, mnx);
-        atomicMin(s + 1, mny);
-        atomicMax(s + 2, mxx);
-        atomicMax(s + 3, mxy);
-    }
-}
-
-__global__ void k_init_root(int32_t* node_of, int32_t* perm, int64_t n, int32_t* seg_order, int32_t* seg_node_of,
-                            int64_t m, unsigned long long* bbox) {
+__global__ void k_init_root(int32_t* perm, int64_t n, int32_t* seg_order, int32_t* seg_node_of, int64_t m,
+                            unsigned long long* bbox) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) { node_of[i] = 0; perm[i] = (int32_t)i; }
+    if (i < n) perm[i] = (int32_t)i;
     if (i < m) { seg_order[i] = (int32_t)i; seg_node_of[i] = 0; }
     if (i == 0) {
         bbox[0] = dkey(DBL_MAX); bbox[1] = dkey(DBL_MAX);
@@ -72,16 +41,49 @@ __global__ void k_init_root(int32_t* node_of, int32_t* perm, int64_t n, int32_t*
     }
 }
 
-// Root box over all segment centres and all vortices (snode::Stretch, TSortedTree.cpp:101-137).
+// Root box over all segment centres and all vortices (snode::Stretch, TSortedTree.cpp:101-137):
+// grid-stride, one set of atomics per block.  Boxes are reduced on the order-preserving
+// integer keys of the coordinates (dkey), on the integer pipe rather than sm_103's narrow
+// FP64 pipe.
 __global__ void k_root_bbox(const double* __restrict__ x, const double* __restrict__ y, int64_t n,
                             const double* __restrict__ rx, const double* __restrict__ ry, int64_t m,
                             unsigned long long* bbox) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int node = -1;
-    double px = 0, py = 0;
-    if (i < n) { node = 0; px = x[i]; py = y[i]; }
-    else if (i - n < m && i >= n) { node = 0; px = rx[i - n]; py = ry[i - n]; }
-    warp_bbox_update(node, px, py, bbox);
+    __shared__ unsigned long long s_b[TB / 32][4];
+    unsigned long long b[4] = {dkey(DBL_MAX), dkey(DBL_MAX), dkey(-DBL_MAX), dkey(-DBL_MAX)};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n + m; i += (int64_t)gridDim.x * blockDim.x) {
+        const double px = i < n ? x[i] : rx[i - n], py = i < n ? y[i] : ry[i - n];
+        const unsigned long long kx = dkey(px), ky = dkey(py);
+        b[0] = kx < b[0] ? kx : b[0];
+        b[1] = ky < b[1] ? ky : b[1];
+        b[2] = kx > b[2] ? kx : b[2];
+        b[3] = ky > b[3] ? ky : b[3];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long u[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) u[e] = __shfl_xor_sync(0xffffffffu, b[e], o);
+        b[0] = u[0] < b[0] ? u[0] : b[0];
+        b[1] = u[1] < b[1] ? u[1] : b[1];
+        b[2] = u[2] > b[2] ? u[2] : b[2];
+        b[3] = u[3] > b[3] ? u[3] : b[3];
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int e = 0; e < 4; e++) s_b[w][e] = b[e];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < TB / 32; q++) {
+            b[0] = s_b[q][0] < b[0] ? s_b[q][0] : b[0];
+            b[1] = s_b[q][1] < b[1] ? s_b[q][1] : b[1];
+            b[2] = s_b[q][2] > b[2] ? s_b[q][2] : b[2];
+            b[3] = s_b[q][3] > b[3] ? s_b[q][3] : b[3];
+        }
+        atomicMin(bbox + 0, b[0]);
+        atomicMin(bbox + 1, b[1]);
+        atomicMax(bbox + 2, b[2]);
+        atomicMax(bbox + 3, b[3]);
+    }
 }
 
 // Box -> (x, y, h, w) exactly as Stretch: x = (bl+tr).x*0.5, h = (tr-bl).y, w = (tr-bl).x
@@ -152,62 +154,6 @@ __device__ __forceinline__ bool in_level_split(int32_t k, int64_t a, int64_t b, 
     return k >= a && k < b && split[k];
 }
 
-__global__ void k_vclass(int64_t n, int64_t a, int64_t b, const int32_t* __restrict__ node_of,
-                         const int32_t* __restrict__ split, const int32_t* __restrict__ axis,
-                         const double* __restrict__ pivot, const double* __restrict__ x,
-                         const double* __restrict__ y, int32_t* flags) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int32_t k = node_of[i];
-    int f = 0;
-    if (in_level_split(k, a, b, split)) {
-        double key = axis[k] ? x[i] : y[i];
-        f = key < pivot[k];
-    }
-    flags[i] = f;
-}
-
-__global__ void k_vrank(int64_t n, int64_t a, int64_t b, const int32_t* __restrict__ node_of,
-                        const int32_t* __restrict__ split, const int32_t* __restrict__ vf,
-                        const int32_t* __restrict__ vl, const int32_t* __restrict__ flags,
-                        const int32_t* __restrict__ S, int32_t* nlow, int32_t* tab_rl) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int32_t k = node_of[i];
-    if (!in_level_split(k, a, b, split)) return;
-    int32_t f = vf[k], l = vl[k];
-    int32_t L = S[l] - S[f];
-    if (i == f) nlow[k] = L;
-    if (i >= f + L && flags[i]) {
-        int32_t r = S[l] - S[i + 1];  // lows strictly to the right of i inside the node
-        tab_rl[f + r] = (int32_t)i;
-    }
-}
-
-__global__ void k_vswap(int64_t n, int64_t a, int64_t b, const int32_t* __restrict__ node_of,
-                        const int32_t* __restrict__ split, const int32_t* __restrict__ vf,
-                        const int32_t* __restrict__ nlow, const int32_t* __restrict__ flags,
-                        const int32_t* __restrict__ S, const int32_t* __restrict__ tab_rl, double* x,
-                        double* y, int32_t* perm) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int32_t k = node_of[i];
-    if (!in_level_split(k, a, b, split)) return;
-    int32_t f = vf[k], L = nlow[k];
-    if (i >= f + L || flags[i]) return;
-    int32_t kk = (int32_t)(i - f) - (S[i] - S[f]);  // highs to the left of i inside the node
-    int64_t j = tab_rl[f + kk];
-    // the keys move at every level; the rest of the record follows once, through perm
-    const double tx = x[i], ty = y[i];
-    x[i] = x[j]; y[i] = y[j];
-    x[j] = tx; y[j] = ty;
-    const int32_t tp = perm[i];
-    perm[i] = perm[j];
-    perm[j] = tp;
-}
-
-// Applies the partition's permutation to the rest of the vortex record (two passes through
-// staging buffers, so the arrays keep their device addresses).
 __global__ void k_perm_gather(int64_t n, const int32_t* __restrict__ perm, const double* __restrict__ g,
                               const double* __restrict__ ie, const double* __restrict__ vx,
                               const double* __restrict__ vy, const int64_t* __restrict__ orig, double* tmp,
@@ -233,56 +179,308 @@ __global__ void k_perm_store(int64_t n, const double* __restrict__ tmp, const in
     orig[i] = otmp[i];
 }
 
-__global__ void k_vassign(int64_t n, int64_t a, int64_t b, int32_t* node_of, const int32_t* __restrict__ split,
-                          const int32_t* __restrict__ vf, const int32_t* __restrict__ nlow,
-                          const int32_t* __restrict__ ch1, const double* __restrict__ x,
-                          const double* __restrict__ y, unsigned long long* bbox) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int node = -1;
-    double px = 0, py = 0;
-    if (i < n) {
-        int32_t k = node_of[i];
-        if (in_level_split(k, a, b, split)) {
-            node = ch1[k] + ((i >= vf[k] + nlow[k]) ? 1 : 0);
-            node_of[i] = node;
-            px = x[i]; py = y[i];
-        }
+// Every split node's vortices are partitioned by one of two routes, chosen by size: one warp
+// per node of at most SMALL_N vortices, or blocks over chunks of CH vortices of the larger
+// nodes (count, scan, place, swap).  Both give the pairing of the swap loop of
+// TSortedTree.cpp:81-99: the kk-th high of the left part (kk = highs to its left) trades
+// places with the low of the right part that has kk lows to its right.  Segments are
+// partitioned by their own passes whatever the route.
+constexpr int SMALL_N = 64;
+constexpr int SW = 4;          // warps per block in k_small_split
+constexpr int CT = 256;        // threads per chunk block
+constexpr int CE = 4;          // vortices per thread in a chunk
+constexpr int CH = CT * CE;    // vortices per chunk
+constexpr int CNW = CT / 32;
+
+// k_route: counts[0] = warp-route nodes (listed in small_list), counts[1] = chunks; chunk c
+// belongs to node chunk_node[c], and node k's chunks are cbase[k] .. cbase[k] + nch - 1 in
+// position order.
+__global__ void k_route(int64_t a, int64_t cnt, const int32_t* __restrict__ split, const int32_t* __restrict__ vf,
+                        const int32_t* __restrict__ vl, int32_t* counts, int32_t* small_list, int32_t* cbase,
+                        int32_t* chunk_node) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t k = (int32_t)(a + t);
+    bool small = false;
+    int nch = 0;
+    if (t < cnt && split[k]) {
+        const int32_t nv = vl[k] - vf[k];
+        if (nv <= SMALL_N) small = true;
+        else nch = (nv + CH - 1) / CH;
     }
-    // A block whose elements all go to one child (the rule near the root, where children
-    // are large) reduces in shared memory and makes 4 atomics instead of 4 per warp.
-    __shared__ int s_node0;
-    __shared__ unsigned long long s_red[TB / 32][4];
-    if (threadIdx.x == 0) s_node0 = node;
-    __syncthreads();
-    if (__syncthreads_and(node == s_node0)) {
-        if (node < 0) return;
-        unsigned long long k0 = dkey(px), k1 = dkey(py), k2 = k0, k3 = k1;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1;
+    const unsigned ms = __ballot_sync(0xffffffffu, small);
+    if (ms) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(counts, __popc(ms));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (small) small_list[base + __popc(ms & below)] = k;
+    }
+    int incl = nch;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long a0 = __shfl_xor_sync(0xffffffffu, k0, o);
-            const unsigned long long a1 = __shfl_xor_sync(0xffffffffu, k1, o);
-            const unsigned long long a2 = __shfl_xor_sync(0xffffffffu, k2, o);
-            const unsigned long long a3 = __shfl_xor_sync(0xffffffffu, k3, o);
-            k0 = a0 < k0 ? a0 : k0; k1 = a1 < k1 ? a1 : k1;
-            k2 = a2 > k2 ? a2 : k2; k3 = a3 > k3 ? a3 : k3;
-        }
-        const int w = threadIdx.x >> 5;
-        if ((threadIdx.x & 31) == 0) { s_red[w][0] = k0; s_red[w][1] = k1; s_red[w][2] = k2; s_red[w][3] = k3; }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
-                k0 = s_red[q][0] < k0 ? s_red[q][0] : k0; k1 = s_red[q][1] < k1 ? s_red[q][1] : k1;
-                k2 = s_red[q][2] > k2 ? s_red[q][2] : k2; k3 = s_red[q][3] > k3 ? s_red[q][3] : k3;
-            }
-            unsigned long long* sb = bbox + 4 * (size_t)node;
-            atomicMin(sb + 0, k0);
-            atomicMin(sb + 1, k1);
-            atomicMax(sb + 2, k2);
-            atomicMax(sb + 3, k3);
-        }
-        return;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
     }
-    warp_bbox_update(node, px, py, bbox);
+    const int tot = __shfl_sync(0xffffffffu, incl, 31);
+    if (tot == 0) return;  // warp-uniform
+    int wbase = 0;
+    if (lane == 0) wbase = atomicAdd(counts + 1, tot);
+    wbase = __shfl_sync(0xffffffffu, wbase, 0);
+    const int cb = wbase + incl - nch;
+    if (nch) cbase[k] = cb;
+    unsigned mm = __ballot_sync(0xffffffffu, nch > 0);
+    while (mm) {  // the warp writes each node's chunk entries together
+        const int src = __ffs(mm) - 1;
+        mm &= mm - 1;
+        const int b = __shfl_sync(0xffffffffu, cb, src), nc = __shfl_sync(0xffffffffu, nch, src);
+        const int32_t kk = __shfl_sync(0xffffffffu, k, src);
+        for (int j = lane; j < nc; j += 32) chunk_node[b + j] = kk;
+    }
+}
+
+__device__ __forceinline__ void bbox_acc(unsigned long long* b, double px, double py) {
+    const unsigned long long kx = dkey(px), ky = dkey(py);
+    b[0] = kx < b[0] ? kx : b[0];
+    b[1] = ky < b[1] ? ky : b[1];
+    b[2] = kx > b[2] ? kx : b[2];
+    b[3] = ky > b[3] ? ky : b[3];
+}
+__device__ __forceinline__ void bbox_merge(unsigned long long* b, const unsigned long long* u) {
+    b[0] = u[0] < b[0] ? u[0] : b[0];
+    b[1] = u[1] < b[1] ? u[1] : b[1];
+    b[2] = u[2] > b[2] ? u[2] : b[2];
+    b[3] = u[3] > b[3] ? u[3] : b[3];
+}
+__device__ __forceinline__ void bbox_warp_reduce(unsigned long long* b) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long u[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) u[e] = __shfl_xor_sync(0xffffffffu, b[e], o);
+        bbox_merge(b, u);
+    }
+}
+__device__ __forceinline__ void bbox_init(unsigned long long* b) {
+    b[0] = b[1] = dkey(DBL_MAX);
+    b[2] = b[3] = dkey(-DBL_MAX);
+}
+// The children's boxes take atomics: other blocks and the segment passes merge into them.
+__device__ __forceinline__ void bbox_commit(unsigned long long* dst, const unsigned long long* b) {
+    atomicMin(dst + 0, b[0]);
+    atomicMin(dst + 1, b[1]);
+    atomicMax(dst + 2, b[2]);
+    atomicMax(dst + 3, b[3]);
+}
+
+// One warp per node of at most SMALL_N vortices.  Every vortex is loaded to registers before
+// any is stored, so the in-place scatter to the paired destinations needs no staging.
+__global__ void __launch_bounds__(SW * 32) k_small_split(const int32_t* __restrict__ list, int64_t nlist,
+                                                         const int32_t* __restrict__ vf, const int32_t* __restrict__ vl,
+                                                         const int32_t* __restrict__ axis,
+                                                         const double* __restrict__ pivot,
+                                                         const int32_t* __restrict__ ch1, double* x, double* y,
+                                                         int32_t* perm, int32_t* nlow, unsigned long long* bbox) {
+    __shared__ int32_t s_tr[SW][SMALL_N], s_tl[SW][SMALL_N];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t t = (int64_t)blockIdx.x * SW + w;
+    if (t >= nlist) return;
+    const int32_t k = list[t];
+    const int32_t f = vf[k], n = vl[k] - f;
+    const bool byx = axis[k] != 0;
+    const double pv = pivot[k];
+    double ex[2], ey[2];
+    int32_t ep[2];
+    bool val[2], low[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int q = lane + 32 * h;
+        val[h] = q < n;
+        ex[h] = val[h] ? x[f + q] : 0.;
+        ey[h] = val[h] ? y[f + q] : 0.;
+        ep[h] = val[h] ? perm[f + q] : 0;
+        low[h] = val[h] && ((byx ? ex[h] : ey[h]) < pv);
+    }
+    const unsigned m0 = __ballot_sync(0xffffffffu, low[0]), m1 = __ballot_sync(0xffffffffu, low[1]);
+    const int L = __popc(m0) + __popc(m1);
+    const unsigned below = (1u << lane) - 1;
+    const int lb[2] = {__popc(m0 & below), __popc(m0) + __popc(m1 & below)};  // lows before q
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int q = lane + 32 * h;
+        if (val[h] && q >= L && low[h]) s_tr[w][L - lb[h] - 1] = q;
+        if (val[h] && q < L && !low[h]) s_tl[w][q - lb[h]] = q;
+    }
+    __syncwarp();
+    const int32_t c1 = ch1[k];
+    unsigned long long b0[4], b1[4];
+    bbox_init(b0);
+    bbox_init(b1);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        if (!val[h]) continue;
+        const int q = lane + 32 * h;
+        int dq = q;
+        if (q < L && !low[h]) dq = s_tr[w][q - lb[h]];
+        if (q >= L && low[h]) dq = s_tl[w][L - lb[h] - 1];
+        x[f + dq] = ex[h];
+        y[f + dq] = ey[h];
+        perm[f + dq] = ep[h];
+        if (low[h]) bbox_acc(b0, ex[h], ey[h]);
+        else bbox_acc(b1, ex[h], ey[h]);
+    }
+    bbox_warp_reduce(b0);
+    bbox_warp_reduce(b1);
+    if (lane == 0) {
+        if (L > 0) bbox_commit(bbox + 4 * (size_t)c1, b0);
+        if (L < n) bbox_commit(bbox + 4 * (size_t)(c1 + 1), b1);
+        nlow[k] = L;
+    }
+}
+
+struct ChunkPos {
+    int32_t k, f, n, j, cb, nch;  // node, its first vortex, its size, chunk index, first chunk, chunks
+};
+__device__ __forceinline__ ChunkPos chunk_pos(int c, const int32_t* chunk_node, const int32_t* cbase,
+                                              const int32_t* vf, const int32_t* vl) {
+    ChunkPos p;
+    p.k = chunk_node[c];
+    p.cb = cbase[p.k];
+    p.j = c - p.cb;
+    p.f = vf[p.k];
+    p.n = vl[p.k] - p.f;
+    p.nch = (p.n + CH - 1) / CH;
+    return p;
+}
+
+// Lows (key < pivot) in each chunk.
+__global__ void __launch_bounds__(CT) k_chunk_count(const int32_t* __restrict__ chunk_node,
+                                                    const int32_t* __restrict__ cbase, const int32_t* __restrict__ vf,
+                                                    const int32_t* __restrict__ vl, const int32_t* __restrict__ axis,
+                                                    const double* __restrict__ pivot, const double* __restrict__ x,
+                                                    const double* __restrict__ y, int32_t* chunk_cnt) {
+    __shared__ int s_c[CNW];
+    const ChunkPos p = chunk_pos(blockIdx.x, chunk_node, cbase, vf, vl);
+    const double* key = axis[p.k] ? x : y;
+    const double pv = pivot[p.k];
+    int cl = 0;
+#pragma unroll
+    for (int e = 0; e < CE; e++) {
+        const int q = p.j * CH + e * CT + threadIdx.x;
+        cl += __popc(__ballot_sync(0xffffffffu, q < p.n && key[p.f + q] < pv));
+    }
+    if ((threadIdx.x & 31) == 0) s_c[threadIdx.x >> 5] = cl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int w = 0; w < CNW; w++) tot += s_c[w];
+        chunk_cnt[blockIdx.x] = tot;
+    }
+}
+
+// Ranks every vortex of a chunk among the node's lows and highs (pre = exclusive scan of the
+// chunk counts), publishes the pairing tables (tab_tr[f + r] = right-part low with r lows to
+// its right, tab_tl[f + kk] = left-part high with kk highs to its left), the number of pairs
+// npair[k], the split count nlow[k], and the children's boxes.  Reads the keys only.
+__global__ void __launch_bounds__(CT) k_chunk_place(const int32_t* __restrict__ chunk_node,
+                                                    const int32_t* __restrict__ cbase, const int32_t* __restrict__ vf,
+                                                    const int32_t* __restrict__ vl, const int32_t* __restrict__ axis,
+                                                    const double* __restrict__ pivot, const int32_t* __restrict__ ch1,
+                                                    const double* __restrict__ x, const double* __restrict__ y,
+                                                    const int32_t* __restrict__ pre, int32_t* tab_tr, int32_t* tab_tl,
+                                                    int32_t* npair, int32_t* nlow, unsigned long long* bbox) {
+    __shared__ int s_cnt[CE * CNW], s_pre[CE * CNW];
+    __shared__ unsigned long long s_b[CNW][8];
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const ChunkPos p = chunk_pos(blockIdx.x, chunk_node, cbase, vf, vl);
+    const bool byx = axis[p.k] != 0;
+    const double pv = pivot[p.k];
+    const int L = pre[p.cb + p.nch] - pre[p.cb];
+    const int before = pre[blockIdx.x] - pre[p.cb];  // lows in the node's earlier chunks
+    double ex[CE], ey[CE];
+    unsigned lowm[CE];
+#pragma unroll
+    for (int e = 0; e < CE; e++) {
+        const int q = p.j * CH + e * CT + tid;
+        const bool v = q < p.n;
+        ex[e] = v ? x[p.f + q] : 0.;
+        ey[e] = v ? y[p.f + q] : 0.;
+        lowm[e] = __ballot_sync(0xffffffffu, v && ((byx ? ex[e] : ey[e]) < pv));
+        if (lane == 0) s_cnt[e * CNW + w] = __popc(lowm[e]);
+    }
+    __syncthreads();
+    if (w == 0) {  // exclusive prefix over (row e, warp w) in position order; CE * CNW = 32
+        const int c0 = s_cnt[lane];
+        int incl = c0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        s_pre[lane] = incl - c0;
+    }
+    __syncthreads();
+    const unsigned below = (1u << lane) - 1;
+    unsigned long long b0[4], b1[4];
+    bbox_init(b0);
+    bbox_init(b1);
+    const int32_t k = p.k, f = p.f;
+    if (p.j == 0 && tid == 0) {
+        nlow[k] = L;
+        if (L == 0) npair[k] = 0;
+    }
+#pragma unroll
+    for (int e = 0; e < CE; e++) {
+        const int q = p.j * CH + e * CT + tid;
+        if (q >= p.n) continue;
+        const bool low = (lowm[e] >> lane) & 1u;
+        const int lb = before + s_pre[e * CNW + w] + __popc(lowm[e] & below);  // lows before q
+        if (q >= L && low) tab_tr[f + L - lb - 1] = q;
+        if (q < L && !low) tab_tl[f + q - lb] = q;
+        if (q == L - 1) npair[k] = L - lb - (low ? 1 : 0);  // highs in the left part
+        if (low) bbox_acc(b0, ex[e], ey[e]);
+        else bbox_acc(b1, ex[e], ey[e]);
+    }
+    bbox_warp_reduce(b0);
+    bbox_warp_reduce(b1);
+    if (lane == 0) {
+#pragma unroll
+        for (int e = 0; e < 4; e++) { s_b[w][e] = b0[e]; s_b[w][4 + e] = b1[e]; }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int q = 1; q < CNW; q++) {
+            bbox_merge(b0, &s_b[q][0]);
+            bbox_merge(b1, &s_b[q][4]);
+        }
+        int lows = 0;
+        for (int q = 0; q < CE * CNW; q++) lows += s_cnt[q];
+        const int lo = p.j * CH, hi = min(p.n, lo + CH);
+        const int32_t c1 = ch1[k];
+        if (lows > 0) bbox_commit(bbox + 4 * (size_t)c1, b0);
+        if (lows < hi - lo) bbox_commit(bbox + 4 * (size_t)(c1 + 1), b1);
+    }
+}
+
+// Swaps the pairs p = j * CH .. of the chunk's node: tab_tl[f + p] <-> tab_tr[f + p].
+__global__ void __launch_bounds__(CT) k_chunk_swap(const int32_t* __restrict__ chunk_node,
+                                                   const int32_t* __restrict__ cbase, const int32_t* __restrict__ vf,
+                                                   const int32_t* __restrict__ vl, const int32_t* __restrict__ npair,
+                                                   const int32_t* __restrict__ tab_tr,
+                                                   const int32_t* __restrict__ tab_tl, double* x, double* y,
+                                                   int32_t* perm) {
+    const ChunkPos p = chunk_pos(blockIdx.x, chunk_node, cbase, vf, vl);
+    const int H = npair[p.k];
+#pragma unroll
+    for (int e = 0; e < CE; e++) {
+        const int q = p.j * CH + e * CT + threadIdx.x;
+        if (q >= H) break;
+        const int64_t i = p.f + tab_tl[p.f + q], j = p.f + tab_tr[p.f + q];
+        const double tx = x[i], ty = y[i];
+        const int32_t tp = perm[i];
+        x[i] = x[j]; y[i] = y[j]; perm[i] = perm[j];
+        x[j] = tx; y[j] = ty; perm[j] = tp;
+    }
 }
 
 __global__ void k_sclass(int64_t m, int64_t a, int64_t b, const int32_t* __restrict__ seg_node_of,
@@ -443,13 +641,15 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
         c.nd_pivot.reserve(need, true, keep, s);
         c.nd_axis.reserve(need, true, keep, s); c.nd_split.reserve(need, true, keep, s);
         c.nd_nlow.reserve(need, true, keep, s); c.nd_nlow_s.reserve(need, true, keep, s);
+        c.nd_cbase.reserve(need, true, keep, s); c.nd_npair.reserve(need, true, keep, s);
     };
+    c.lvl_cnt.reserve(4);
     c.nnodes = 1;
     ensure_nodes(cap_nodes);
-    c.node_of.reserve(n + 1);
     c.flags.reserve(n + m + 2);
     c.scan.reserve(n + m + 2);
     c.tab_rl.reserve(n + 1);
+    c.tab_lh.reserve(n + 1);
     c.seg_order.reserve(m + 1); c.seg_order2.reserve(m + 1);
     c.seg_node_of.reserve(m + 1); c.seg_node_of2.reserve(m + 1);
     c.counters.reserve(16);
@@ -458,11 +658,11 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
 
     int64_t nm = n > m ? n : m;
     c.perm.reserve(n + 1);
-    k_init_root<<<grid_for(nm, TB), TB, 0, s>>>(c.node_of.p, c.perm.p, n, c.seg_order.p, c.seg_node_of.p, m,
+    k_init_root<<<grid_for(nm, TB), TB, 0, s>>>(c.perm.p, n, c.seg_order.p, c.seg_node_of.p, m,
                                                 c.nd_bbox.p);
     VV_LAUNCH_CHECK();
     if (n + m > 0) {
-        k_root_bbox<<<grid_for(n + m, TB), TB, 0, s>>>(c.x.p, c.y.p, n, c.s_rx.p, c.s_ry.p, m, c.nd_bbox.p);
+        k_root_bbox<<<std::min<int64_t>(grid_for(n + m, TB), 152 * 8), TB, 0, s>>>(c.x.p, c.y.p, n, c.s_rx.p, c.s_ry.p, m, c.nd_bbox.p);
         VV_LAUNCH_CHECK();
     }
     k_finalize_root<<<1, 1, 0, s>>>(c.nd_geom.p, c.nd_bbox.p, c.nd_vf.p, c.nd_vl.p, c.nd_sf.p, c.nd_sl.p,
@@ -485,21 +685,39 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
         k_children<<<grid_for(cnt, TB), TB, 0, s>>>(a, b, cnt, c.nd_split.p, c.scan.p, c.nd_ch1.p, c.nd_depth.p,
                                                     c.nd_path.p, c.nd_bbox.p, c.nd_nlow.p, c.nd_nlow_s.p);
         VV_LAUNCH_CHECK();
-        int32_t nsplit = read_i32(c, c.scan.p + cnt);
+        // partition the vortices of each split node: one warp per small node, chunk blocks
+        // over the larger ones
+        c.lvl_list.reserve((size_t)cnt + 1);
+        c.chunk_node.reserve((size_t)cnt + (size_t)(n / CH) + 2);
+        VV_CUDA(cudaMemsetAsync(c.lvl_cnt.p, 0, 2 * sizeof(int32_t), s));
+        k_route<<<grid_for(cnt, TB), TB, 0, s>>>(a, cnt, c.nd_split.p, c.nd_vf.p, c.nd_vl.p, c.lvl_cnt.p,
+                                                 c.lvl_list.p, c.nd_cbase.p, c.chunk_node.p);
+        VV_LAUNCH_CHECK();
+        int32_t hc[3];
+        VV_CUDA(cudaMemcpyAsync(hc, c.scan.p + cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        VV_CUDA(cudaMemcpyAsync(hc + 1, c.lvl_cnt.p, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        VV_CUDA(cudaStreamSynchronize(s));
+        const int32_t nsplit = hc[0], nsmall = hc[1], nchunk = hc[2];
         if (nsplit == 0) break;
-        if (n > 0) {
-            k_vclass<<<grid_for(n, TB), TB, 0, s>>>(n, a, b, c.node_of.p, c.nd_split.p, c.nd_axis.p, c.nd_pivot.p,
-                                                    c.x.p, c.y.p, c.flags.p);
+        if (nsmall > 0) {
+            k_small_split<<<grid_for(nsmall, SW), SW * 32, 0, s>>>(c.lvl_list.p, nsmall, c.nd_vf.p, c.nd_vl.p,
+                                                                   c.nd_axis.p, c.nd_pivot.p, c.nd_ch1.p, c.x.p,
+                                                                   c.y.p, c.perm.p, c.nd_nlow.p, c.nd_bbox.p);
             VV_LAUNCH_CHECK();
-            exclusive_scan(c, c.flags.p, c.scan.p, n);
-            k_vrank<<<grid_for(n, TB), TB, 0, s>>>(n, a, b, c.node_of.p, c.nd_split.p, c.nd_vf.p, c.nd_vl.p,
-                                                   c.flags.p, c.scan.p, c.nd_nlow.p, c.tab_rl.p);
+        }
+        if (nchunk > 0) {
+            c.chunk_cnt.reserve((size_t)nchunk + 1);
+            c.chunk_pre.reserve((size_t)nchunk + 1);
+            k_chunk_count<<<nchunk, CT, 0, s>>>(c.chunk_node.p, c.nd_cbase.p, c.nd_vf.p, c.nd_vl.p, c.nd_axis.p,
+                                                c.nd_pivot.p, c.x.p, c.y.p, c.chunk_cnt.p);
             VV_LAUNCH_CHECK();
-            k_vswap<<<grid_for(n, TB), TB, 0, s>>>(n, a, b, c.node_of.p, c.nd_split.p, c.nd_vf.p, c.nd_nlow.p,
-                                                   c.flags.p, c.scan.p, c.tab_rl.p, c.x.p, c.y.p, c.perm.p);
+            exclusive_scan(c, c.chunk_cnt.p, c.chunk_pre.p, nchunk);
+            k_chunk_place<<<nchunk, CT, 0, s>>>(c.chunk_node.p, c.nd_cbase.p, c.nd_vf.p, c.nd_vl.p, c.nd_axis.p,
+                                                c.nd_pivot.p, c.nd_ch1.p, c.x.p, c.y.p, c.chunk_pre.p, c.tab_rl.p,
+                                                c.tab_lh.p, c.nd_npair.p, c.nd_nlow.p, c.nd_bbox.p);
             VV_LAUNCH_CHECK();
-            k_vassign<<<grid_for(n, TB), TB, 0, s>>>(n, a, b, c.node_of.p, c.nd_split.p, c.nd_vf.p, c.nd_nlow.p,
-                                                     c.nd_ch1.p, c.x.p, c.y.p, c.nd_bbox.p);
+            k_chunk_swap<<<nchunk, CT, 0, s>>>(c.chunk_node.p, c.nd_cbase.p, c.nd_vf.p, c.nd_vl.p, c.nd_npair.p,
+                                               c.tab_rl.p, c.tab_lh.p, c.x.p, c.y.p, c.perm.p);
             VV_LAUNCH_CHECK();
         }
         if (m > 0) {

@@ -144,8 +144,12 @@ struct Ctx {
     DArr<unsigned long long> nd_bbox;  // 4 per node: encoded min x, min y, max x, max y
     DArr<double> nd_pivot;
     DArr<int32_t> nd_axis, nd_split, nd_nlow, nd_nlow_s, nd_lc, nd_dfs;
-    DArr<int32_t> node_of, seg_node_of, seg_node_of2, flags, scan;
+    DArr<int32_t> seg_node_of, seg_node_of2, flags, scan;
     DArr<int32_t> perm;              // tree build: source slot of each slot (keys move, payload follows once)
+    DArr<int32_t> nd_cbase, nd_npair;  // tree build: node's first chunk, pairs swapped in its split
+    DArr<int32_t> lvl_cnt;           // tree build: per-level counts of warp-split nodes and of chunks
+    DArr<int32_t> lvl_list;          // tree build: per-level list of warp-split nodes
+    DArr<int32_t> chunk_node, chunk_cnt, chunk_pre;  // tree build: per-level chunks of the larger nodes
     DArr<int32_t> sel_pos, sel_list, lf_fallback;  // leaves walked one warp each
     int64_t n_sel = 0, n_fallback = 0;
     DArr<double> ptmp;               // tree build: payload staging for the final permutation
