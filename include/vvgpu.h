@@ -29,6 +29,11 @@
  *                                             (libvvhd/headers/MFlowmove.hpp:12,
  *                                              libvvhd/src/MFlowmove.cpp:217-235)
  *   vvgpu_gsum                             <- Space::gsum() (libvvhd/headers/TSpace.hpp:93-99)
+ *   vvgpu_field_velocity, _streamfunction, <- XVelocity, XStreamfunction, XVorticity:
+ *   _vorticity                                constructor + mode/ref_frame/eps_mult +
+ *                                             evaluate() + XField::map
+ *                                             (libvvhd/headers/XVelocity.hpp:10-28,
+ *                                              XStreamfunction.hpp:9-29, XVorticity.hpp:7-21)
  *
  * The Space state crosses the boundary as structure-of-arrays of doubles
  * (TObj r.x, r.y, g, _1_eps, v.x, v.y; libvvhd/headers/TObj.hpp:10-35) and body corners
@@ -211,6 +216,29 @@ int vvgpu_zero_forces(vvgpu_ctx* ctx);
 /* TAtt::Cp, Fr, Nu of every segment (the calc_forces accumulators). */
 int vvgpu_get_segment_forces(vvgpu_ctx* ctx, double* cp, double* fr, double* nu);
 int vvgpu_gsum(vvgpu_ctx* ctx, double* out);
+
+/* ---- grid fields (libvvhd/src/XVelocity.cpp, XStreamfunction.cpp, XVorticity.cpp) ---- */
+/* An xres x yres grid p = (xmin, ymin) + dxdy * (xi, yj), with xmin, ymin and dxdy rounded
+ * to float as XField stores them (XField.hpp:47); out[yj * xres + xi] as XField::map.
+ * The reference evaluates each field on a private copy of Space: the context's vortex
+ * list, epsilon and segment gsum are left as they were.  No tree may be built on entry
+ * (VVGPU_ERR_STATE) and none is left.  VVGPU_ERR_ARG where XField/X* throw
+ * std::invalid_argument (xres or yres <= 1, dxdy not finite or <= 0, eps_mult <= 0, bad
+ * mode or ref_frame), VVGPU_ERR_UNSUPPORTED for moving bodies.
+ * velocity: tree (8, 20 dl, 0.1), epsilon without merging, then
+ *   MConvectiveFast::velocity(p) - frame speed; mode 'x'|'y'; ref_frame 'o' (none),
+ *   'f' (free stream), 'b' (first body's speed_slae).  dl = Space::average_segment_length().
+ * streamfunction: tree (8, 10 dl, 20 dl); the grid cells (p, p + dxdy] that hold a sink are
+ *   reported in grid order: at most gap_cap of them written to gap_xi/gap_yj/gap, their
+ *   number in *ngaps (may be NULL).
+ * vorticity: vortex_shed, tree (8, 20 dl); 0 inside a body. */
+int vvgpu_field_velocity(vvgpu_ctx* ctx, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                         char mode, char ref_frame, float* out);
+int vvgpu_field_streamfunction(vvgpu_ctx* ctx, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                               double eps_mult, char ref_frame, float* out, int64_t gap_cap, uint16_t* gap_xi,
+                               uint16_t* gap_yj, float* gap, int64_t* ngaps);
+int vvgpu_field_vorticity(vvgpu_ctx* ctx, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                          double eps_mult, float* out);
 
 /* ---- inspection (parity tests; same meaning as the oracle's exports) -------------- */
 int vvgpu_tree_sizes(vvgpu_ctx* ctx, int64_t* nnodes, int64_t* nleaves, int64_t* nnear,

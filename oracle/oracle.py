@@ -70,6 +70,8 @@ _D = C.POINTER(C.c_double)
 _I64 = C.POINTER(C.c_int64)
 _I32 = C.POINTER(C.c_int32)
 _U32 = C.POINTER(C.c_uint32)
+_U16 = C.POINTER(C.c_uint16)
+_F = C.POINTER(C.c_float)
 
 
 def _load(kind: str):
@@ -113,6 +115,12 @@ def _load(kind: str):
         "calc_forces": (C.c_int, [H, _D]),
         "zero_forces": (C.c_int, [H]),
         "get_segment_forces": (C.c_int, [H, _D, _D, _D]),
+        "field_velocity": (C.c_int, [H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                     C.c_char, C.c_char, _F]),
+        "field_streamfunction": (C.c_int, [H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                           C.c_double, C.c_char, _F, C.c_int64, _U16, _U16, _F, _I64]),
+        "field_vorticity": (C.c_int, [H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                      C.c_double, _F]),
     }
     if kind == "port":
         sig["direct_velocity"] = (C.c_int, [H, C.c_int64, _D, _D, _D, _D])
@@ -176,6 +184,10 @@ class OracleSpace:
     def set_segment_g(self, g):
         g = np.ascontiguousarray(g, np.float64)
         self._ok(self.f["set_segment_g"](self.h, _p(g)), "set_segment_g")
+
+    def set_sinks(self, x, y, g):
+        x, y, g = (np.ascontiguousarray(a, np.float64) for a in (x, y, g))
+        self._ok(self.f["set_sinks"](self.h, len(x), _p(x), _p(y), _p(g)), "set_sinks")
 
     def set_vortices(self, x, y, g, inv_eps=None):
         x, y, g = (np.ascontiguousarray(a, np.float64) for a in (x, y, g))
@@ -351,6 +363,32 @@ class OracleSpace:
         out = {k: np.empty(self.m) for k in ("cp", "fr", "nu")}
         self._ok(self.f["get_segment_forces"](self.h, _p(out["cp"]), _p(out["fr"]), _p(out["nu"])),
                  "get_segment_forces")
+        return out
+
+    # grid fields (XVelocity.cpp, XStreamfunction.cpp, XVorticity.cpp); out[yj, xi] float32
+    def field_velocity(self, xmin, ymin, dxdy, xres, yres, mode="x", ref_frame="o"):
+        out = np.zeros((yres, xres), np.float32)
+        self._ok(self.f["field_velocity"](self.h, xmin, ymin, dxdy, xres, yres, mode.encode(),
+                                          ref_frame.encode(), _p(out, C.c_float)), "field_velocity")
+        return out
+
+    def field_streamfunction(self, xmin, ymin, dxdy, xres, yres, eps_mult=1.0, ref_frame="o", gap_cap=4096):
+        out = np.zeros((yres, xres), np.float32)
+        gx = np.zeros(gap_cap, np.uint16)
+        gy = np.zeros(gap_cap, np.uint16)
+        gv = np.zeros(gap_cap, np.float32)
+        ng = C.c_int64(0)
+        self._ok(self.f["field_streamfunction"](self.h, xmin, ymin, dxdy, xres, yres, eps_mult,
+                                                ref_frame.encode(), _p(out, C.c_float), gap_cap,
+                                                _p(gx, C.c_uint16), _p(gy, C.c_uint16), _p(gv, C.c_float),
+                                                C.byref(ng)), "field_streamfunction")
+        k = min(int(ng.value), gap_cap)
+        return out, (gx[:k].copy(), gy[:k].copy(), gv[:k].copy())
+
+    def field_vorticity(self, xmin, ymin, dxdy, xres, yres, eps_mult=1.0):
+        out = np.zeros((yres, xres), np.float32)
+        self._ok(self.f["field_vorticity"](self.h, xmin, ymin, dxdy, xres, yres, eps_mult,
+                                           _p(out, C.c_float)), "field_vorticity")
         return out
 
     def set_sample(self, stride: int):

@@ -6,6 +6,7 @@
 // the same Python wrapper drives the reference and the C restatement. The harness
 // reads tree internals for export, so it opens the classes' private sections for this
 // translation unit only (the class layout is unchanged).
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <complex>
@@ -27,6 +28,11 @@
 #include "MFlowmove.hpp"
 #include "TSortedTree.hpp"
 #include "TSpace.hpp"
+#define protected public
+#include "XStreamfunction.hpp"
+#include "XVelocity.hpp"
+#include "XVorticity.hpp"
+#undef protected
 #undef private
 
 #include "../vvd_oracle.h"
@@ -525,6 +531,70 @@ int vvr_get_body_params(void* h, int bi, vvo_body_params* out) {
     out->special_segment_no = b.special_segment_no;
     out->bc_kutta = b.boundary_condition == bc_t::kutta;
     return 0;
+}
+
+// Grid fields: the reference's XVelocity / XStreamfunction / XVorticity constructed on the
+// handle's Space (each copies it), evaluated, and XField::map copied out.
+static int field_out(XField& f, int32_t xres, int32_t yres, float* out) {
+    for (int32_t yj = 0; yj < yres; yj++)
+        for (int32_t xi = 0; xi < xres; xi++) out[(int64_t)yj * xres + xi] = f.at(xi, yj);
+    return 0;
+}
+
+int vvr_field_velocity(void* h, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres, char mode,
+                       char ref_frame, float* out) {
+    Handle* H = (Handle*)h;
+    if (H->built) return -2;
+    try {
+        XVelocity f(H->S, xmin, ymin, dxdy, xres, yres);
+        f.mode = mode;
+        f.ref_frame = ref_frame;
+        f.evaluate();
+        return field_out(f, xres, yres, out);
+    } catch (std::invalid_argument&) {
+        return -1;
+    }
+}
+
+int vvr_field_streamfunction(void* h, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                             double eps_mult, char ref_frame, float* out, int64_t gap_cap, uint16_t* gap_xi,
+                             uint16_t* gap_yj, float* gap, int64_t* ngaps) {
+    Handle* H = (Handle*)h;
+    if (H->built) return -2;
+    try {
+        XStreamfunction f(H->S, xmin, ymin, dxdy, xres, yres);
+        f.eps_mult = eps_mult;
+        f.ref_frame = ref_frame;
+        f.evaluate();
+        // gaps come in thread order: sort into grid order
+        std::vector<TGap> gs(f.gaps.begin(), f.gaps.end());
+        std::sort(gs.begin(), gs.end(), [](const TGap& a, const TGap& b) {
+            return a.yj != b.yj ? a.yj < b.yj : a.xi < b.xi;
+        });
+        int64_t k = 0;
+        for (const TGap& gp : gs) {
+            if (k < gap_cap) { gap_xi[k] = gp.xi; gap_yj[k] = gp.yj; gap[k] = gp.gap; }
+            k++;
+        }
+        if (ngaps) *ngaps = k;
+        return field_out(f, xres, yres, out);
+    } catch (std::invalid_argument&) {
+        return -1;
+    }
+}
+
+int vvr_field_vorticity(void* h, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                        double eps_mult, float* out) {
+    Handle* H = (Handle*)h;
+    if (H->built) return -2;
+    try {
+        XVorticity f(H->S, xmin, ymin, dxdy, xres, yres);
+        f.eps_mult = eps_mult;
+        f.evaluate();
+        return field_out(f, xres, yres, out);
+    } catch (std::invalid_argument&) {
+        return -1;
+    }
 }
 
 }  // extern "C"

@@ -23,6 +23,7 @@ static double now_s(void) {
 #define C_PI    3.14159265358979323846
 #define C_2PI   (2. * C_PI)
 #define C_1_2PI (1. / (2. * C_PI))
+#define C_1_4PI (1. / (4. * C_PI))
 #define C_1_PI  (1. / C_PI)
 
 /* Tree_MaxListSize, libvvhd/src/TSortedTree.cpp:10 */
@@ -724,13 +725,17 @@ static void near_influence(const vvo_space* S, int64_t L, double px, double py,
     *oy = ry * C_1_2PI;
 }
 
+/* The reference writes abs(src.g) without std:: and without a global abs(double) in scope
+ * (MConvectiveFast.cpp:166), so C's int abs(int) runs on the circulation truncated to int. */
+static double int_abs_of(double g) { return (double)abs((int)g); }
+
 /* sink_list_influence (MConvectiveFast.cpp:153-170). */
 static void sink_influence(const vvo_space* S, double px, double py, double* ox, double* oy) {
     double rx = 0, ry = 0;
     const double e2 = S->dt * C_1_PI;
     for (int64_t k = 0; k < S->ns; k++) {
         double dx = px - S->snk_x[k], dy = py - S->snk_y[k];
-        double s = S->snk_g[k] / (abs2(dx, dy) + e2 * fabs(S->snk_g[k]));
+        double s = S->snk_g[k] / (abs2(dx, dy) + e2 * int_abs_of(S->snk_g[k]));
         rx += dx * s; ry += dy * s;
     }
     *ox = rx * C_1_2PI;
@@ -815,10 +820,11 @@ int vvo_velocity_points(vvo_space* S, int64_t n, const double* px, const double*
                         double* vx, double* vy) {
     if (!S->built) return -3;
     if (!bodies_at_rest(S)) return -4;
+    int32_t* pos = (int32_t*)xrealloc(NULL, sizeof(int32_t) * (size_t)(S->nnodes ? S->nnodes : 1));
+    for (int64_t k = 0; k < S->nnodes; k++) pos[k] = -1;
+    for (int64_t t = 0; t < S->nleaves; t++) pos[S->leaves[t]] = (int32_t)t;
     for (int64_t q = 0; q < n; q++) {
-        int32_t k = find_node(S, px[q], py[q]);
-        int64_t L = -1;
-        for (int64_t t = 0; t < S->nleaves; t++) if (S->leaves[t] == k) { L = t; break; }
+        const int64_t L = pos[find_node(S, px[q], py[q])];
         double rx = 0, ry = 0, ax, ay;
         if (L >= 0) {
             near_influence(S, L, px[q], py[q], &ax, &ay); rx += ax; ry += ay;
@@ -839,6 +845,7 @@ int vvo_velocity_points(vvo_space* S, int64_t n, const double* px, const double*
         }
         vx[q] = rx; vy[q] = ry;
     }
+    free(pos);
     return 0;
 }
 
@@ -1481,4 +1488,266 @@ int vvo_vortex_shed(vvo_space* S) {
         }
     }
     return 0;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Grid fields (libvvhd/src/XVelocity.cpp, XStreamfunction.cpp, XVorticity.cpp)          */
+/* ------------------------------------------------------------------------------------ */
+
+/* The reference evaluates every field on a private copy of Space (XVelocity.hpp:23 and
+ * the others); the copy's vortex list, epsilon and attached-segment sums are saved here
+ * and put back afterwards. */
+typedef struct {
+    int64_t n;
+    double *x, *y, *g, *ie, *vx, *vy, *gsum;
+    int64_t* orig;
+} osnap;
+
+static double* dup_d(const double* a, int64_t n) {
+    double* r = (double*)xrealloc(NULL, sizeof(double) * (size_t)(n ? n : 1));
+    if (n) memcpy(r, a, sizeof(double) * (size_t)n);
+    return r;
+}
+
+static void snap_save(const vvo_space* S, osnap* q) {
+    q->n = S->n;
+    q->x = dup_d(S->x, S->n); q->y = dup_d(S->y, S->n); q->g = dup_d(S->g, S->n);
+    q->ie = dup_d(S->ie, S->n); q->vx = dup_d(S->vx, S->n); q->vy = dup_d(S->vy, S->n);
+    q->orig = (int64_t*)xrealloc(NULL, sizeof(int64_t) * (size_t)(S->n ? S->n : 1));
+    if (S->n) memcpy(q->orig, S->orig, sizeof(int64_t) * (size_t)S->n);
+    q->gsum = dup_d(S->gsum, S->m);
+}
+
+static void snap_restore(vvo_space* S, osnap* q) {
+    free_tree(S);
+    S->n = q->n;
+    size_t d = sizeof(double) * (size_t)q->n;
+    if (q->n) {
+        memcpy(S->x, q->x, d); memcpy(S->y, q->y, d); memcpy(S->g, q->g, d);
+        memcpy(S->ie, q->ie, d); memcpy(S->vx, q->vx, d); memcpy(S->vy, q->vy, d);
+        memcpy(S->orig, q->orig, sizeof(int64_t) * (size_t)q->n);
+    }
+    if (S->m) memcpy(S->gsum, q->gsum, sizeof(double) * (size_t)S->m);
+    free(q->x); free(q->y); free(q->g); free(q->ie); free(q->vx); free(q->vy); free(q->orig); free(q->gsum);
+}
+
+/* Space::average_segment_length (TSpace.hpp:119-129): of the first body. */
+static double avg_seg_len(const vvo_space* S) {
+    if (!S->nb) return 0;
+    const obody* b = &S->bodies[0];
+    if (b->count <= 1) return 0;
+    return b->slen / (double)(b->count - 1);
+}
+
+/* XField::XField (XField.cpp:8-24): the grid origin and spacing are stored as float. */
+static int field_grid(double xmin, double ymin, double dxdy, int32_t xres, int32_t yres, float* fx, float* fy,
+                      float* fd) {
+    *fx = (float)xmin; *fy = (float)ymin; *fd = (float)dxdy;
+    if (xres <= 1 || yres <= 1) return 0;
+    if (!isfinite(*fd) || *fd <= 0) return 0;
+    return 1;
+}
+
+/* leaf index (DFS) of every node id that is a leaf */
+static int32_t* leaf_pos(const vvo_space* S) {
+    int32_t* pos = (int32_t*)xrealloc(NULL, sizeof(int32_t) * (size_t)(S->nnodes ? S->nnodes : 1));
+    for (int64_t L = 0; L < S->nleaves; L++) pos[S->leaves[L]] = (int32_t)L;
+    return pos;
+}
+
+/* MEpsilonFast::eps2h (MEpsilonFast.cpp:66-92): squared distance to the second nearest
+ * vortex (any circulation, coincident points skipped) over the near leaves of leaf L. */
+static double eps2h(const vvo_space* S, int64_t L, double px, double py) {
+    double res1 = INFINITY, res2 = INFINITY;
+    for (int64_t t = S->near_off[L]; t < S->near_off[L + 1]; t++) {
+        const onode* nn = &S->nodes[S->near_list[t]];
+        for (int64_t j = nn->vf; j < nn->vl; j++) {
+            const double d = abs2(px - S->x[j], py - S->y[j]);
+            if (!d) continue;
+            else if (d < res1) { res2 = res1; res1 = d; }
+            else if (d < res2) res2 = d;
+        }
+    }
+    if (isfinite(res2)) return res2;
+    if (isfinite(res1)) return res1;
+    return -DBL_MAX;
+}
+
+static int ref_speed(const vvo_space* S, char ref_frame, double* rx, double* ry) {
+    switch (ref_frame) {
+    case 'o': *rx = 0; *ry = 0; return 1;
+    case 'f': *rx = S->inf_vx; *ry = S->inf_vy; return 1;
+    case 'b':
+        if (!S->nb) return 0;
+        *rx = S->bodies[0].p.speed_slae_x; *ry = S->bodies[0].p.speed_slae_y;
+        return 1;
+    default: return 0;
+    }
+}
+
+/* XVelocity::evaluate (XVelocity.cpp:24-73): tree (8, 20 dl, 0.1), epsilon without merging,
+ * then MConvectiveFast::velocity at every node of the grid minus the frame speed. */
+int vvo_field_velocity(vvo_space* S, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                       char mode, char ref_frame, float* out) {
+    float fx, fy, fd;
+    if (!field_grid(xmin, ymin, dxdy, xres, yres, &fx, &fy, &fd)) return -1;
+    double rfx, rfy;
+    if (!ref_speed(S, ref_frame, &rfx, &rfy)) return -1;
+    if (mode != 'x' && mode != 'y') return -1;
+    if (S->built) return -2;
+    if (!bodies_at_rest(S)) return -4;
+    osnap q;
+    snap_save(S, &q);
+    const double dl = avg_seg_len(S);
+    int rc = vvo_tree_build(S, 8, dl * 20, 0.1);
+    int64_t merged;
+    if (!rc) rc = vvo_eps(S, 0, &merged);
+    if (!rc) {
+        const int64_t np = (int64_t)xres * yres;
+        double* px = (double*)xrealloc(NULL, sizeof(double) * 4 * (size_t)np);
+        double *py = px + np, *vx = px + 2 * np, *vy = px + 3 * np;
+        for (int32_t yj = 0; yj < yres; yj++)
+            for (int32_t xi = 0; xi < xres; xi++) {
+                px[(int64_t)yj * xres + xi] = (double)fx + (double)fd * xi;
+                py[(int64_t)yj * xres + xi] = (double)fy + (double)fd * yj;
+            }
+        rc = vvo_velocity_points(S, np, px, py, vx, vy);
+        for (int64_t k = 0; !rc && k < np; k++) out[k] = (float)(mode == 'x' ? vx[k] - rfx : vy[k] - rfy);
+        free(px);
+    }
+    snap_restore(S, &q);
+    return rc;
+}
+
+/* XStreamfunction::evaluate and streamfunction(node, p, gap) (XStreamfunction.cpp:47-212):
+ * tree (8, 10 dl, 20 dl); every vortex gets eps^2 = eps_mult^2 max(eps2h / 4, (0.2 dl)^2);
+ * psi = [sum over segments, far-node centroids and near vortices of -g log(r^2 + e^2)] / 4pi
+ * + [sum over sinks of q atan2] / 2pi + p . rotl(V_inf - V_frame).  Sinks inside the cell
+ * (p, p + dxdy] give gap entries, in grid order. */
+int vvo_field_streamfunction(vvo_space* S, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                             double eps_mult, char ref_frame, float* out, int64_t gap_cap, uint16_t* gap_xi,
+                             uint16_t* gap_yj, float* gap, int64_t* ngaps) {
+    float fx, fy, fd;
+    if (!field_grid(xmin, ymin, dxdy, xres, yres, &fx, &fy, &fd)) return -1;
+    if (eps_mult <= 0) return -1;
+    double rfx, rfy;
+    if (!ref_speed(S, ref_frame, &rfx, &rfy)) return -1;
+    if (S->built) return -2;
+    if (!bodies_at_rest(S)) return -4;
+    osnap q;
+    snap_save(S, &q);
+    const double dl = avg_seg_len(S);
+    const double rd2 = sqr(0.2 * dl);
+    int rc = vvo_tree_build(S, 8, dl > 0 ? dl * 10 : 0, dl > 0 ? dl * 20 : INFINITY);
+    int64_t ng = 0;
+    if (!rc) {
+        double* e2 = (double*)xrealloc(NULL, sizeof(double) * (size_t)(S->n ? S->n : 1));
+        for (int64_t L = 0; L < S->nleaves; L++) {
+            const onode* nd = &S->nodes[S->leaves[L]];
+            for (int64_t i = nd->vf; i < nd->vl; i++)
+                e2[i] = sqr(eps_mult) * smax(eps2h(S, L, S->x[i], S->y[i]) * 0.25, sqr(0.2 * dl));
+        }
+        int32_t* pos = leaf_pos(S);
+        const double vfx = S->inf_vx - rfx, vfy = S->inf_vy - rfy;
+        for (int32_t yj = 0; yj < yres; yj++)
+            for (int32_t xi = 0; xi < xres; xi++) {
+                const double px = (double)fx + (double)fd * xi, py = (double)fy + (double)fd * yj;
+                const int64_t L = pos[find_node(S, px, py)];
+                double t4 = 0, t2 = 0, pgap = 0;
+                for (int64_t s = 0; s < S->m; s++) t4 += -S->sg[s] * log(abs2(px - S->rx[s], py - S->ry[s]) + rd2);
+                for (int64_t s = 0; s < S->ns; s++) {
+                    t2 += S->snk_g[s] * atan2(py - S->snk_y[s], px - S->snk_x[s]);
+                    if (px < S->snk_x[s] && S->snk_x[s] <= px + (double)fd && py < S->snk_y[s] &&
+                        S->snk_y[s] <= py + (double)fd)
+                        pgap += S->snk_g[s];
+                }
+                for (int64_t t = S->far_off[L]; t < S->far_off[L + 1]; t++) {
+                    const onode* fn = &S->nodes[S->far_list[t]];
+                    t4 += -fn->cmp_g * log(abs2(px - fn->cmp_x, py - fn->cmp_y) + rd2);
+                    t4 += -fn->cmm_g * log(abs2(px - fn->cmm_x, py - fn->cmm_y) + rd2);
+                }
+                for (int64_t t = S->near_off[L]; t < S->near_off[L + 1]; t++) {
+                    const onode* nn = &S->nodes[S->near_list[t]];
+                    for (int64_t j = nn->vf; j < nn->vl; j++)
+                        t4 += -S->g[j] * log(abs2(px - S->x[j], py - S->y[j]) + e2[j]);
+                }
+                out[(int64_t)yj * xres + xi] = (float)(t4 * C_1_4PI + t2 * C_1_2PI + (px * (-vfy) + py * vfx));
+                if (pgap) {
+                    if (ng < gap_cap) {
+                        gap_xi[ng] = (uint16_t)xi; gap_yj[ng] = (uint16_t)yj; gap[ng] = (float)pgap;
+                    }
+                    ng++;
+                }
+            }
+        free(pos);
+        free(e2);
+    }
+    if (ngaps) *ngaps = ng;
+    snap_restore(S, &q);
+    return rc;
+}
+
+/* XVorticity::evaluate and vorticity(node, p) (XVorticity.cpp:26-94): vortex_shed, tree
+ * (8, 20 dl, DBL_MAX); every vortex gets a = 1 / (eps_mult^2 max(eps2h, (0.6 dl)^2));
+ * omega = 0 inside a body, else [sum over near vortices of g a exp(-a r^2), cut at
+ * -a r^2 <= -6] / pi + (erfarg < 3 ? (1 - erf(erfarg)) / 2 : 0) with erfarg = (squared
+ * distance to the nearest segment centre of the near leaves) / (dl eps_mult)^2. */
+int vvo_field_vorticity(vvo_space* S, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                        double eps_mult, float* out) {
+    float fx, fy, fd;
+    if (!field_grid(xmin, ymin, dxdy, xres, yres, &fx, &fy, &fd)) return -1;
+    if (eps_mult <= 0) return -1;
+    if (S->built) return -2;
+    if (!bodies_at_rest(S)) return -4;
+    osnap q;
+    snap_save(S, &q);
+    const double dl = avg_seg_len(S);
+    int rc = vvo_vortex_shed(S);
+    if (!rc) rc = vvo_tree_build(S, 8, dl * 20, DBL_MAX);
+    if (!rc) {
+        double* a = (double*)xrealloc(NULL, sizeof(double) * 2 * (size_t)(S->n ? S->n : 1));
+        double* ag = a + S->n;
+        for (int64_t L = 0; L < S->nleaves; L++) {
+            const onode* nd = &S->nodes[S->leaves[L]];
+            for (int64_t i = nd->vf; i < nd->vl; i++) {
+                a[i] = 1. / (sqr(eps_mult) * smax(eps2h(S, L, S->x[i], S->y[i]), sqr(0.6 * dl)));
+                ag[i] = a[i] * S->g[i];
+            }
+        }
+        int32_t* pos = leaf_pos(S);
+        const double e2 = sqr(dl * eps_mult);
+        for (int32_t yj = 0; yj < yres; yj++)
+            for (int32_t xi = 0; xi < xres; xi++) {
+                const double px = (double)fx + (double)fd * xi, py = (double)fy + (double)fd * yj;
+                int inside = 0;
+                for (int b = 0; b < S->nb && !inside; b++) inside = point_invalid(S, &S->bodies[b], px, py) >= 0;
+                double res = 0;
+                if (!inside) {
+                    const int64_t L = pos[find_node(S, px, py)];
+                    double h2 = INFINITY;
+                    for (int64_t t = S->near_off[L]; t < S->near_off[L + 1]; t++) {
+                        const onode* nn = &S->nodes[S->near_list[t]];
+                        for (int64_t j = nn->vf; j < nn->vl; j++) {
+                            const double exparg = -abs2(px - S->x[j], py - S->y[j]) * a[j];
+                            res += (exparg > -6) ? ag[j] * exp(exparg) : 0;
+                        }
+                    }
+                    res *= C_1_PI;
+                    for (int64_t t = S->near_off[L]; t < S->near_off[L + 1]; t++) {
+                        const onode* nn = &S->nodes[S->near_list[t]];
+                        for (int64_t k = nn->sf; k < nn->sl; k++) {
+                            const int64_t sg = S->seg_order[k];
+                            h2 = smin(h2, abs2(px - S->rx[sg], py - S->ry[sg]));
+                        }
+                    }
+                    const double erfarg = h2 / e2;
+                    res += (erfarg < 3) ? 0.5 * (1 - erf(erfarg)) : 0;
+                }
+                out[(int64_t)yj * xres + xi] = (float)res;
+            }
+        free(pos);
+        free(a);
+    }
+    snap_restore(S, &q);
+    return rc;
 }

@@ -150,6 +150,21 @@ int vvo_get_segment_forces(const vvo_space* S, double* cp, double* fr, double* n
 /* Space::gsum (TSpace.hpp:93-99). */
 double vvo_gsum(const vvo_space* S);
 
+/* Grid fields of libvvhd (XVelocity.cpp, XStreamfunction.cpp, XVorticity.cpp): an
+ * xres x yres grid p = (xmin, ymin) + dxdy (xi, yj) with xmin, ymin, dxdy rounded to float
+ * (XField.hpp:47), out[yj * xres + xi] as XField::map.  Each evaluates on a private copy of
+ * the space (the vortex list, epsilon and segment sums are restored).  Return -1 for
+ * arguments the reference rejects with std::invalid_argument, -2 with a tree built, -4 for
+ * moving bodies.  The stream function also reports the grid cells that hold a sink (gap
+ * entries, grid order, at most gap_cap written; *ngaps = their number). */
+int vvo_field_velocity(vvo_space* S, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                       char mode, char ref_frame, float* out);
+int vvo_field_streamfunction(vvo_space* S, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                             double eps_mult, char ref_frame, float* out, int64_t gap_cap, uint16_t* gap_xi,
+                             uint16_t* gap_yj, float* gap, int64_t* ngaps);
+int vvo_field_vorticity(vvo_space* S, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                        double eps_mult, float* out);
+
 /* FP64 direct sums (no tree) used to measure the tree's own error:
  * convective velocity of every non-zero vortex at the given points, with each source's
  * own smoothing radius (biot_savart, MConvectiveFast.cpp:116-120), plus inf_speed. */

@@ -15,12 +15,12 @@ EXACT_KEYS = ("merged", "n_after_shed", "eps_x", "eps_y", "eps_g", "eps_inv_eps"
 
 def golden_cases(folder, prefix=None):
     """Fixture names in ``folder``: the one-step fixtures (no prefix), or those whose name
-    starts with ``prefix`` (e.g. "move_")."""
+    starts with ``prefix`` (e.g. "move_", "field_")."""
     import glob
     import os
     names = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(folder, "*.npz")))
     if prefix is None:
-        return [n for n in names if not n.startswith(("move_", "forces_"))]
+        return [n for n in names if not n.startswith(("move_", "forces_", "field_"))]
     return [n for n in names if n.startswith(prefix)]
 
 
@@ -114,4 +114,29 @@ def check_step(ref, got, *, vel_tol, diff_tol, fric_tol, slae_tol, exact=True, p
         e = rel_err(got[p + "slae_x"], ref[p + "slae_x"])
         if not e <= slae_tol * 100:
             bad.append(f"{p}slae solution rel err {e:.3e}")
+    return bad
+
+
+def check_fields(got: dict, ref: dict, rel_tol: float):
+    """Grid fields (XField::map, float32).  Exact: the stream function's gap lists.  Within
+    ``rel_tol`` of the field's largest magnitude: every map value (the FP64 sums run in a
+    different order and CUDA's log/exp/erf/atan2 differ from the C library's in the last
+    bits before the rounding to float).  Returns failure strings."""
+    bad = []
+    for k, b in ref.items():
+        if k.startswith("in_"):
+            continue
+        a = np.asarray(got[k])
+        b = np.asarray(b)
+        if a.shape != b.shape:
+            bad.append(f"{k}: shape {a.shape} != {b.shape}")
+            continue
+        if "_gap" in k:
+            if not np.array_equal(a, b):
+                bad.append(f"{k}: gap lists differ")
+            continue
+        d = np.abs(a.astype(np.float64) - b.astype(np.float64))
+        scale = float(np.max(np.abs(b))) if b.size else 0.0
+        if not np.all(np.isfinite(a)) or (b.size and d.max() > rel_tol * scale):
+            bad.append(f"{k}: max |d| {d.max():.3g} > {rel_tol:.0e} x {scale:.3g}")
     return bad

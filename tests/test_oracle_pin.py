@@ -97,3 +97,64 @@ def test_port_forces_match_golden(case):
     got = run_forces(S, forces_cases()[case[len("forces_"):]], oracle.default_body_params)
     S.close()
     check_move(got, d, "")
+
+
+# ---- grid fields: XVelocity / XStreamfunction / XVorticity ---------------------------
+import field_cases as FC  # noqa: E402
+
+
+@pytest.mark.parametrize("case", golden_cases(GOLDEN, prefix="field_"))
+def test_port_fields_match_golden(case):
+    """The restatement's fields are bit-identical to the reference's (same operation order
+    and the same C library), the gap lists included; the space is left as it was."""
+    d = dict(np.load(os.path.join(GOLDEN, case + ".npz")))
+    c = FC.case_from_fixture(d)
+    S = oracle.OracleSpace("port")
+    FC.load(S, c)
+    before = S.vortices()
+    got = FC.run_fields(S, c)
+    after = S.vortices()
+    S.close()
+    for k, v in got.items():
+        assert np.array_equal(v, d[k]), k
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference sources not present")
+def test_port_fields_match_reference_live():
+    """A case the fixtures do not hold: two sinks in one cell, a finer grid over the body."""
+    c = dict(FC.cases()["cyl"])
+    c["sinks"] = (np.array([0.71, 0.72, -1.3]), np.array([0.41, 0.42, 0.2]), np.array([0.5, -1.7, 3.2]))
+    c["grid"] = (-1.0, -0.8, 0.05, 41, 33)
+    outs = []
+    for kind in ("port", "ref"):
+        S = oracle.OracleSpace(kind)
+        FC.load(S, c)
+        outs.append(FC.run_fields(S, c))
+        S.close()
+    for k in outs[1]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
+def test_port_fields_reject_bad_arguments():
+    """XField / X* throw std::invalid_argument (XField.cpp:17-23, XVelocity.cpp:42-44,
+    XStreamfunction.cpp:49-50, XVorticity.cpp:28-29); with the tree built the oracle says so."""
+    c = FC.cases()["no_vortices"]
+    S = oracle.OracleSpace("port")
+    FC.load(S, c)
+    for kw in (dict(xres=1), dict(yres=0), dict(dxdy=0.0), dict(dxdy=float("inf"))):
+        a = dict(xmin=-1.0, ymin=-1.0, dxdy=0.1, xres=8, yres=8)
+        a.update(kw)
+        with pytest.raises(oracle.OracleError):
+            S.field_vorticity(a["xmin"], a["ymin"], a["dxdy"], a["xres"], a["yres"])
+    with pytest.raises(oracle.OracleError):
+        S.field_velocity(-1.0, -1.0, 0.1, 8, 8, mode="z")
+    with pytest.raises(oracle.OracleError):
+        S.field_velocity(-1.0, -1.0, 0.1, 8, 8, ref_frame="q")
+    with pytest.raises(oracle.OracleError):
+        S.field_streamfunction(-1.0, -1.0, 0.1, 8, 8, eps_mult=0.0)
+    S.tree_build(8, 0.1, 1.0)
+    with pytest.raises(oracle.OracleError):
+        S.field_vorticity(-1.0, -1.0, 0.1, 8, 8)
+    S.close()

@@ -91,7 +91,7 @@ __device__ __forceinline__ void extra_terms(const ConvArgs& a, double px, double
     double rx = 0, ry = 0;
     for (int64_t k = 0; k < a.ns; k++) {
         double dx = px - a.kx[k], dy = py - a.ky[k];
-        double s = a.kg[k] / (dx * dx + dy * dy + a.sink_e2 * fabs(a.kg[k]));
+        double s = a.kg[k] / (dx * dx + dy * dy + a.sink_e2 * sink_abs(a.kg[k]));
         rx += dx * s; ry += dy * s;
     }
     double bx = 0, by = 0;
@@ -455,6 +455,8 @@ ConvArgs make_args(Ctx& c) {
     return a;
 }
 
+}  // namespace
+
 void check_bodies_at_rest(Ctx& c) {
     for (auto& b : c.bodies) {
         const vvgpu_body_params& p = b.p;
@@ -462,8 +464,6 @@ void check_bodies_at_rest(Ctx& c) {
             throw ApiError{VVGPU_ERR_UNSUPPORTED, "moving bodies (attached sheets) are not supported"};
     }
 }
-
-}  // namespace
 
 void build_frames(Ctx& c) {
     cudaStream_t s = c.st();

@@ -525,6 +525,33 @@ int vvgpu_get_body_params(vvgpu_ctx* h, int body, vvgpu_body_params* out) {
     API_END
 }
 
+int vvgpu_field_velocity(vvgpu_ctx* h, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                         char mode, char ref_frame, float* out) {
+    API_BEGIN(h)
+    if (!out) throw ApiError{VVGPU_ERR_ARG, "null pointer"};
+    field_velocity(c, xmin, ymin, dxdy, xres, yres, mode, ref_frame, out);
+    API_END
+}
+
+int vvgpu_field_streamfunction(vvgpu_ctx* h, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                               double eps_mult, char ref_frame, float* out, int64_t gap_cap, uint16_t* gap_xi,
+                               uint16_t* gap_yj, float* gap, int64_t* ngaps) {
+    API_BEGIN(h)
+    if (!out || gap_cap < 0 || (gap_cap > 0 && (!gap_xi || !gap_yj || !gap)))
+        throw ApiError{VVGPU_ERR_ARG, "bad output arrays"};
+    field_streamfunction(c, xmin, ymin, dxdy, xres, yres, eps_mult, ref_frame, out, gap_cap, gap_xi, gap_yj, gap,
+                         ngaps);
+    API_END
+}
+
+int vvgpu_field_vorticity(vvgpu_ctx* h, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                          double eps_mult, float* out) {
+    API_BEGIN(h)
+    if (!out) throw ApiError{VVGPU_ERR_ARG, "null pointer"};
+    field_vorticity(c, xmin, ymin, dxdy, xres, yres, eps_mult, out);
+    API_END
+}
+
 int vvgpu_gsum(vvgpu_ctx* h, double* out) {
     API_BEGIN(h)
     if (!out) throw ApiError{VVGPU_ERR_ARG, "null pointer"};

@@ -13,49 +13,17 @@
 // list order, then each body's segments); everything else is one thread per vortex.
 #include <cfloat>
 
+#include "body_test.cuh"
 #include "vvgpu_internal.cuh"
 
 namespace vvgpu {
 
 namespace {
 
-struct MoveBody {
-    double blx, bly, trx, try_, cofx, cofy, r2max, axx, axy;
-    int64_t first, count;
-    int inverted;  // area <= 0: TBody::isInsideValid
-};
-
-// TBody::isPointInContour over the corners, exact FP64 (no contraction).  Returns the
-// global index of the segment whose centre is nearest, or -1.
-__device__ int64_t point_invalid(const MoveBody& b, const double* __restrict__ cx, const double* __restrict__ cy,
-                                 const double* __restrict__ rx, const double* __restrict__ ry, double px, double py) {
-    bool in = b.inverted != 0;
-    if (!in && (px < b.blx || py < b.bly || px > b.trx || py > b.try_ ||
-                dabs2(dsub(px, b.cofx), dsub(py, b.cofy)) > b.r2max))
-        return -1;
-    const int64_t f = b.first, n = b.count;
-    for (int64_t i = 0, j = n - 1; i < n; j = i++) {
-        const double vix = cx[f + i], viy = cy[f + i], vjx = cx[f + j], vjy = cy[f + j];
-        const double lhs = dmul(dsub(vjy, viy), dsub(px, vix));
-        const double rhs = dmul(dsub(vjx, vix), dsub(py, viy));
-        if (((viy < vjy) && (viy < py) && (py <= vjy) && (lhs > rhs)) ||
-            ((viy > vjy) && (viy > py) && (py >= vjy) && (lhs < rhs)))
-            in = !in;
-    }
-    if (!in) return -1;
-    int64_t best = -1;
-    double bd = DBL_MAX;
-    for (int64_t k = 0; k < n; k++) {
-        const double d = dabs2(dsub(rx[f + k], px), dsub(ry[f + k], py));
-        if (d < bd) { bd = d; best = f + k; }
-    }
-    return best;
-}
-
 // Move, then classify: keep (1), erase as small (0, seg = -1), erase inside body b at
 // segment seg (0, seg >= 0).
 __global__ void k_move_classify(int64_t n, double dt, int remove, double* x, double* y, const double* __restrict__ vx,
-                                const double* __restrict__ vy, const double* __restrict__ g, const MoveBody* bodies,
+                                const double* __restrict__ vy, const double* __restrict__ g, const BodyTest* bodies,
                                 int nb, const double* __restrict__ cx, const double* __restrict__ cy,
                                 const double* __restrict__ rx, const double* __restrict__ ry, int32_t* keep,
                                 int32_t* dead, int2* dead_at) {
@@ -118,7 +86,7 @@ __global__ void k_dead_list(int64_t n, const int32_t* __restrict__ dead, const i
 __global__ void k_move_bookkeep(const int32_t* __restrict__ list, const int32_t* __restrict__ count,
                                 const int2* __restrict__ dead_at, const double* __restrict__ x,
                                 const double* __restrict__ y, const double* __restrict__ g,
-                                const MoveBody* bodies, int nb, const double* __restrict__ cx,
+                                const BodyTest* bodies, int nb, const double* __restrict__ cx,
                                 const double* __restrict__ cy, const double* __restrict__ sg,
                                 const uint32_t* __restrict__ slip, double* gsum, double* acc) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
@@ -126,7 +94,7 @@ __global__ void k_move_bookkeep(const int32_t* __restrict__ list, const int32_t*
     for (int32_t k = 0; k < nd; k++) {
         const int32_t i = list[k];
         const int2 at = dead_at[i];
-        const MoveBody& b = bodies[at.x];
+        const BodyTest& b = bodies[at.x];
         const double gi = g[i], px = x[i], py = y[i];
         double* a = acc + 4 * at.x;
         a[0] = dadd(a[0], dmul(-py, gi));
@@ -136,7 +104,7 @@ __global__ void k_move_bookkeep(const int32_t* __restrict__ list, const int32_t*
         a[3] = dadd(a[3], gi);
     }
     for (int bi = 0; bi < nb; bi++) {
-        const MoveBody& b = bodies[bi];
+        const BodyTest& b = bodies[bi];
         double* a = acc + 4 * bi;
         for (int64_t q = 0; q < b.count; q++) {
             const int64_t s = b.first + q;
@@ -171,42 +139,22 @@ void move_and_clean(Ctx& c, int remove, int64_t* cleaned) {
     const int64_t n = c.n;
     const int nb = (int)c.bodies.size();
     // per-body inside-test geometry (TBody::doFillProperties, TBody.cpp:327-342)
-    std::vector<MoveBody> hb(nb + 1);
+    std::vector<BodyTest> hb(nb + 1);
     std::vector<double> hacc(4 * (size_t)nb + 4, 0.);
     for (int bi = 0; bi < nb; bi++) {
         const BodyHost& b = c.bodies[bi];
-        MoveBody mb{};
-        mb.blx = mb.bly = INFINITY;
-        mb.trx = mb.try_ = -INFINITY;
-        mb.r2max = 0;
-        mb.cofx = b.cofm_x;
-        mb.cofy = b.cofm_y;
-        for (int64_t k = 0; k < b.count; k++) {
-            const double px = c.h_cx[b.first + k], py = c.h_cy[b.first + k];
-            const double dx = px - b.cofm_x, dy = py - b.cofm_y;
-            const double r2 = dx * dx + dy * dy;
-            if (r2 > mb.r2max) mb.r2max = r2;
-            if (px > mb.trx) mb.trx = px;
-            if (py > mb.try_) mb.try_ = py;
-            if (px < mb.blx) mb.blx = px;
-            if (py < mb.bly) mb.bly = py;
-        }
-        mb.axx = b.p.holder_x + b.p.dpos_x;
-        mb.axy = b.p.holder_y + b.p.dpos_y;
-        mb.first = b.first;
-        mb.count = b.count;
-        mb.inverted = b.area <= 0;
+        const BodyTest mb = body_test_of(c, b);
         hb[bi] = mb;
         hacc[4 * bi + 0] = b.p.fdt_dead_x;
         hacc[4 * bi + 1] = b.p.fdt_dead_y;
         hacc[4 * bi + 2] = b.p.fdt_dead_o;
         hacc[4 * bi + 3] = b.p.g_dead;
     }
-    c.mv_bodies.reserve(hb.size() * sizeof(MoveBody) / sizeof(double) + 1);
+    c.mv_bodies.reserve(hb.size() * sizeof(BodyTest) / sizeof(double) + 1);
     c.mv_acc.reserve(hacc.size());
-    VV_CUDA(cudaMemcpyAsync(c.mv_bodies.p, hb.data(), hb.size() * sizeof(MoveBody), cudaMemcpyHostToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(c.mv_bodies.p, hb.data(), hb.size() * sizeof(BodyTest), cudaMemcpyHostToDevice, s));
     VV_CUDA(cudaMemcpyAsync(c.mv_acc.p, hacc.data(), hacc.size() * 8, cudaMemcpyHostToDevice, s));
-    const MoveBody* dbodies = reinterpret_cast<const MoveBody*>(c.mv_bodies.p);
+    const BodyTest* dbodies = reinterpret_cast<const BodyTest*>(c.mv_bodies.p);
     int32_t new_n = 0, ndead = 0;
     if (n > 0) {
         c.flags.reserve(n + 1);

@@ -132,7 +132,7 @@ __global__ void k_slip_rows(FillArgs a) {
         double kxs = 0, kys = 0;
         for (int64_t q = 0; q < a.ns; q++) {
             double dx = srx - a.kx[q], dy = sry - a.ky[q];
-            double f = a.kg[q] / (dx * dx + dy * dy + a.sink_e2 * fabs(a.kg[q]));
+            double f = a.kg[q] / (dx * dx + dy * dy + a.sink_e2 * sink_abs(a.kg[q]));
             kxs += dx * f; kys += dy * f;
         }
         kxs *= C_1_2PI; kys *= C_1_2PI;

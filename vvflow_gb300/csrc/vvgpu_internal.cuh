@@ -94,6 +94,11 @@ struct DArr {
     }
 };
 
+// The smoothing of a sink scales with abs(src.g), written in MConvectiveFast.cpp:166 without
+// std:: and without a global abs(double) in scope: C's int abs(int) runs on the circulation
+// truncated to int, so sinks with |g| < 1 are unsmoothed.
+__host__ __device__ __forceinline__ double sink_abs(double g) { return (double)abs((int)g); }
+
 struct BodyHost {
     int64_t first, count;
     vvgpu_body_params p;
@@ -331,6 +336,16 @@ void eps_pass(Ctx& c, int merge, int64_t* merged);
 void convective(Ctx& c);
 void velocity_points(Ctx& c, int64_t n, const double* px, const double* py, double* vx, double* vy);
 void velocity_points_on_device(Ctx& c, int64_t n, const double* dpx, const double* dpy, double* dvx, double* dvy);
+// TVec3D::iszero of every body's speed_slae (TVec3D.hpp:17), else VVGPU_ERR_UNSUPPORTED.
+void check_bodies_at_rest(Ctx& c);
+// grid fields (fields.cu)
+void field_velocity(Ctx& c, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres, char mode,
+                    char ref_frame, float* out);
+void field_streamfunction(Ctx& c, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres,
+                          double eps_mult, char ref_frame, float* out, int64_t gap_cap, uint16_t* gap_xi,
+                          uint16_t* gap_yj, float* gap, int64_t* ngaps);
+void field_vorticity(Ctx& c, double xmin, double ymin, double dxdy, int32_t xres, int32_t yres, double eps_mult,
+                     float* out);
 void diffusive(Ctx& c);
 void slae(Ctx& c, vvgpu_body_out* out);
 void upload_segments(Ctx& c);

@@ -66,6 +66,8 @@ _D = C.POINTER(C.c_double)
 _I64 = C.POINTER(C.c_int64)
 _I32 = C.POINTER(C.c_int32)
 _U32 = C.POINTER(C.c_uint32)
+_U16 = C.POINTER(C.c_uint16)
+_F = C.POINTER(C.c_float)
 _H = C.c_void_p
 
 # name -> (restype, argtypes); the same list is the ABI surface checked by the tests
@@ -108,6 +110,12 @@ SIGNATURES = {
     "vvgpu_zero_forces": (C.c_int, [_H]),
     "vvgpu_get_segment_forces": (C.c_int, [_H, _D, _D, _D]),
     "vvgpu_gsum": (C.c_int, [_H, _D]),
+    "vvgpu_field_velocity": (C.c_int, [_H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                       C.c_char, C.c_char, _F]),
+    "vvgpu_field_streamfunction": (C.c_int, [_H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                             C.c_double, C.c_char, _F, C.c_int64, _U16, _U16, _F, _I64]),
+    "vvgpu_field_vorticity": (C.c_int, [_H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                        C.c_double, _F]),
     "vvgpu_tree_sizes": (C.c_int, [_H, _I64, _I64, _I64, _I64]),
     "vvgpu_tree_leaves": (C.c_int, [_H, _D, _D, _D, _D, _I64, _I64, _I32, _I64, _I64, _I64]),
     "vvgpu_tree_nodes": (C.c_int, [_H, _D, _D, _D, _D, _I64, _I64, _I32, _I64] + [_D] * 6),
@@ -207,6 +215,10 @@ class GpuSpace:
         arr = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (g, fric, gsum)]
         self._ok(self.lib.vvgpu_set_segment_state(self.h, *(_p(a) for a in arr)), "set_segment_state")
 
+    def set_sinks(self, x, y, g):
+        x, y, g = (np.ascontiguousarray(a, np.float64) for a in (x, y, g))
+        self._ok(self.lib.vvgpu_set_sinks(self.h, len(x), _p(x), _p(y), _p(g)), "set_sinks")
+
     def set_vortices(self, x, y, g, inv_eps=None):
         x, y, g = (np.ascontiguousarray(a, np.float64) for a in (x, y, g))
         ie = None if inv_eps is None else np.ascontiguousarray(inv_eps, np.float64)
@@ -290,6 +302,32 @@ class GpuSpace:
 
     def vortex_shed(self):
         self._ok(self.lib.vvgpu_vortex_shed(self.h), "vortex_shed")
+
+    # -- grid fields (XVelocity, XStreamfunction, XVorticity); out[yj, xi] float32 ------
+    def field_velocity(self, xmin, ymin, dxdy, xres, yres, mode="x", ref_frame="o"):
+        out = np.zeros((yres, xres), np.float32)
+        self._ok(self.lib.vvgpu_field_velocity(self.h, xmin, ymin, dxdy, xres, yres, mode.encode(),
+                                               ref_frame.encode(), _p(out, C.c_float)), "field_velocity")
+        return out
+
+    def field_streamfunction(self, xmin, ymin, dxdy, xres, yres, eps_mult=1.0, ref_frame="o", gap_cap=4096):
+        out = np.zeros((yres, xres), np.float32)
+        gx = np.zeros(gap_cap, np.uint16)
+        gy = np.zeros(gap_cap, np.uint16)
+        gv = np.zeros(gap_cap, np.float32)
+        ng = C.c_int64(0)
+        self._ok(self.lib.vvgpu_field_streamfunction(self.h, xmin, ymin, dxdy, xres, yres, eps_mult,
+                                                     ref_frame.encode(), _p(out, C.c_float), gap_cap,
+                                                     _p(gx, C.c_uint16), _p(gy, C.c_uint16),
+                                                     _p(gv, C.c_float), C.byref(ng)), "field_streamfunction")
+        k = min(int(ng.value), gap_cap)
+        return out, (gx[:k].copy(), gy[:k].copy(), gv[:k].copy())
+
+    def field_vorticity(self, xmin, ymin, dxdy, xres, yres, eps_mult=1.0):
+        out = np.zeros((yres, xres), np.float32)
+        self._ok(self.lib.vvgpu_field_vorticity(self.h, xmin, ymin, dxdy, xres, yres, eps_mult,
+                                                _p(out, C.c_float)), "field_vorticity")
+        return out
 
     def gsum(self):
         v = C.c_double()
