@@ -53,6 +53,10 @@ def parse():
                     help="run the warm-up, then exactly one step between cudaProfilerStart/Stop and exit "
                          "(for `ncu --profile-from-start off`)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="path used by --profile")
+    ap.add_argument("--config", default="wake4m", choices=["wake4m", "batched"],
+                    help="wake4m: the 4M-vortex ellipse wake (default); batched: the sweep of independent "
+                         "cylinder simulations advanced together (vvgpu_batch_step)")
+    ap.add_argument("--instances", type=int, default=256, help="--config batched: number of simulations")
     return ap.parse_args()
 
 
@@ -488,10 +492,74 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------------------
+# batched sweep: many independent cylinder simulations per step
+def batched_arm(args):
+    import torch
+
+    from vvflow_gb300 import build as B
+    from vvflow_gb300 import workloads as W
+    from vvflow_gb300.vvgpu import VVGPU_FP32, Batch, GpuSpace
+
+    rank, world, local = dist_env()
+    B.build()
+    torch.cuda.set_device(local)
+    wls = W.batched_cylinders(args.instances, seed=5 + rank)
+    spaces = []
+    for wl in wls:
+        S = GpuSpace(VVGPU_FP32, device=local, reserve=wl.n + 4 * wl.m)
+        S.set_params(wl.re, wl.dt, wl.inf_vx, wl.inf_vy, 0.0, 0.0)
+        for cx, cy in wl.bodies:
+            S.add_body(cx, cy)
+        S.set_vortices(wl.x, wl.y, wl.g)
+        spaces.append(S)
+    batch = Batch(spaces, 8.0, [wl.node_sizes() for wl in wls], merge=True, move=True)
+    # warm-up: one step, then the autotuner's steps (one per host pool size)
+    batch.step(nthreads=16)
+    cands = (2, 4, 8, 16, 32)
+    nt, _ = batch.autotune(cands)
+    for _ in range(max(0, args.warmup - 1 - len(cands))):
+        batch.step()
+    clk = Clocks()
+    per = []
+    vsteps = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vsteps += sum(S.n for S in spaces)
+        per.append(batch.step())
+    torch.cuda.synchronize()
+    T = time.perf_counter() - t0
+    clocks = clk.stop()
+    per = np.concatenate(per)
+    total_n = sum(S.n for S in spaces)
+    out = {
+        "metric": "vortex-steps/s (batched sweep of independent cylinder simulations)",
+        "value": vsteps / T, "unit": "vortex-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": 1 + len(cands) + max(0, args.warmup - 1 - len(cands)),
+        "ms_per_step": 1e3 * T / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded cylinder wakes)",
+        "config": {"workload": f"batched_cylinders x{args.instances}: N log-uniform 5e3..2e5, "
+                               "nu log-uniform 1/2000..1/100, M 200..1000, FP32 pairwise, merge on, "
+                               "move_and_clean each step", "instances": args.instances,
+                   "total_vortices_end": int(total_n), "host_threads": nt, "autotune_candidates": list(cands),
+                   "timing": "host wall clock between device-wide synchronisations (instances run on "
+                             "their own streams)"},
+        "instance_step_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
+                             "max": float(per.max())},
+        "clocks": clocks,
+    }
+    print(json.dumps(out))
+    for S in spaces:
+        S.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.config == "batched":
+        batched_arm(args)
     else:
         gpu_arm(args)
 

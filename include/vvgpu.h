@@ -217,6 +217,27 @@ int vvgpu_zero_forces(vvgpu_ctx* ctx);
 int vvgpu_get_segment_forces(vvgpu_ctx* ctx, double* cp, double* fr, double* nu);
 int vvgpu_gsum(vvgpu_ctx* ctx, double* out);
 
+/* ---- batched sweep: many independent simulations advanced by one call ------------------ */
+/* One simulate() step (utils/vvflow/vvflow.cpp:214-255: tree build, calc_circulation, tree
+ * destroy, vortex_shed, tree build, CalcEpsilonFast(merge), process_all_lists,
+ * process_vort_list, tree destroy), then, with move != 0, MFlowmove::move_and_clean(true). */
+typedef struct vvgpu_step_cfg {
+    double far_criteria, min_node, max_node;   /* stree(S, farCriteria, minNode, maxNode) */
+    int32_t merge;                             /* CalcEpsilonFast(merge)                 */
+    int32_t move;                              /* move_and_clean after the velocities    */
+} vvgpu_step_cfg;
+/* Advances each of count independent contexts by one step with cfgs[i]: a pool of nthreads
+ * host threads (<= 0: one per host core) takes the instances largest first and drives each
+ * on its own stream.  Each instance computes exactly what the same calls compute alone.
+ * step_ms[i] (may be NULL) = instance i's wall time, its stream synchronised; status[i]
+ * (may be NULL) = its return code.  Returns the first non-zero status, else 0. */
+int vvgpu_batch_step(vvgpu_ctx* const* ctxs, int64_t count, const vvgpu_step_cfg* cfgs, int32_t nthreads,
+                     double* step_ms, int32_t* status);
+/* Runs one batched step per candidate pool size (these steps advance the instances) and
+ * returns the fastest in *best (its wall time in *best_ms, may be NULL). */
+int vvgpu_batch_autotune(vvgpu_ctx* const* ctxs, int64_t count, const vvgpu_step_cfg* cfgs,
+                         const int32_t* candidates, int32_t ncand, int32_t* best, double* best_ms);
+
 /* ---- grid fields (libvvhd/src/XVelocity.cpp, XStreamfunction.cpp, XVorticity.cpp) ---- */
 /* An xres x yres grid p = (xmin, ymin) + dxdy * (xi, yj), with xmin, ymin and dxdy rounded
  * to float as XField stores them (XField.hpp:47); out[yj * xres + xi] as XField::map.

@@ -7,10 +7,6 @@
 
 using namespace vvgpu;
 
-struct vvgpu_ctx {
-    Ctx c;
-};
-
 namespace {
 
 int fail(Ctx& c, int code, const std::string& msg) {

@@ -18,10 +18,6 @@
 
 #include "vvgpu_internal.cuh"
 
-struct vvgpu_ctx {
-    vvgpu::Ctx c;
-};
-
 namespace {
 
 __device__ __align__(256) double g_point_scratch[4 * VVGPU_NOALLOC_MAX_POINTS];

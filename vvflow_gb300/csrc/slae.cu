@@ -379,9 +379,9 @@ __global__ void k_gemv(int64_t n, const T* __restrict__ M, const double* __restr
     if (lane == 0) y[row] = add ? y[row] + acc : acc;
 }
 
-// r = b - A x, and |r|^2, |b|^2 accumulated in acc[0], acc[1]
+// r = b - A x; sq[row] = r^2, sq[n + row] = b^2 (summed deterministically afterwards)
 __global__ void k_residual(int64_t n, const double* __restrict__ A, const double* __restrict__ x,
-                           const double* __restrict__ b, double* r, double* acc) {
+                           const double* __restrict__ b, double* r, double* sq) {
     int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (row >= n) return;
@@ -393,9 +393,28 @@ __global__ void k_residual(int64_t n, const double* __restrict__ A, const double
     if (lane == 0) {
         double rr = b[row] - s;
         r[row] = rr;
-        atomicAdd(&acc[0], rr * rr);
-        atomicAdd(&acc[1], b[row] * b[row]);
+        sq[row] = rr * rr;
+        sq[n + row] = b[row] * b[row];
     }
+}
+
+// Deterministic sums (the same bits on every run, unlike atomics across blocks): SUM_BLOCKS
+// fixed blocks reduce fixed grid-stride slices, then one block adds their partials.
+constexpr int SUM_BLOCKS = 304;
+__global__ void k_sum_stage1(int64_t n, const double* __restrict__ v, double* part) {
+    __shared__ double sh[32];
+    double t = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        t += v[i];
+    t = block_sum(t, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+__global__ void k_sum_stage2(int nparts, const double* __restrict__ part, double* out) {
+    __shared__ double sh[32];
+    double t = 0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) t += part[i];
+    t = block_sum(t, sh);
+    if (threadIdx.x == 0) *out = t;
 }
 
 __global__ void k_scatter_solution(int64_t nb, const int32_t* col_seg0, const int32_t* body_first,
@@ -406,15 +425,6 @@ __global__ void k_scatter_solution(int64_t nb, const int32_t* col_seg0, const in
     }
 }
 
-__global__ void k_gsum(int64_t n, const double* __restrict__ g, double* out) {
-    __shared__ double sh[32];
-    double v = 0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        v += g[i];
-    double t = block_sum(v, sh);
-    if (threadIdx.x == 0) atomicAdd(out, t);
-}
-
 }  // namespace
 
 double gsum(Ctx& c) {
@@ -423,7 +433,10 @@ double gsum(Ctx& c) {
     double* out = (double*)(c.counters.p + 4);
     VV_CUDA(cudaMemsetAsync(out, 0, 8, s));
     if (c.n) {
-        k_gsum<<<304, 256, 0, s>>>(c.n, c.g.p, out);
+        c.sum_part.reserve(SUM_BLOCKS);
+        k_sum_stage1<<<SUM_BLOCKS, 256, 0, s>>>(c.n, c.g.p, c.sum_part.p);
+        VV_LAUNCH_CHECK();
+        k_sum_stage2<<<1, 256, 0, s>>>(SUM_BLOCKS, c.sum_part.p, out);
         VV_LAUNCH_CHECK();
     }
     double v = 0;
@@ -557,8 +570,10 @@ void slae(Ctx& c, vvgpu_body_out* out) {
         c.neq_cached = n;
     }
     // x = inv b, then FP64 iterative refinement
-    DArr<double> r;
+    DArr<double> r, sq;
     r.reserve(n);
+    sq.reserve(2 * (size_t)n);
+    c.sum_part.reserve(2 * SUM_BLOCKS);
     double* acc = (double*)(c.counters.p + 8);
     const unsigned gg = grid_for(n, 8);
     auto apply_inv = [&](const double* v, double* y, bool add) {
@@ -568,9 +583,14 @@ void slae(Ctx& c, vvgpu_body_out* out) {
     };
     apply_inv(c.B.p, c.X.p, false);
     for (int it = 0; it < 12; it++) {
-        VV_CUDA(cudaMemsetAsync(acc, 0, 16, s));
-        k_residual<<<gg, 256, 0, s>>>(n, c.A.p, c.X.p, c.B.p, r.p, acc);
+        k_residual<<<gg, 256, 0, s>>>(n, c.A.p, c.X.p, c.B.p, r.p, sq.p);
         VV_LAUNCH_CHECK();
+        for (int k = 0; k < 2; k++) {
+            k_sum_stage1<<<SUM_BLOCKS, 256, 0, s>>>(n, sq.p + k * n, c.sum_part.p + k * SUM_BLOCKS);
+            VV_LAUNCH_CHECK();
+            k_sum_stage2<<<1, 256, 0, s>>>(SUM_BLOCKS, c.sum_part.p + k * SUM_BLOCKS, acc + k);
+            VV_LAUNCH_CHECK();
+        }
         double h[2];
         VV_CUDA(cudaMemcpyAsync(h, acc, 16, cudaMemcpyDeviceToHost, s));
         VV_CUDA(cudaStreamSynchronize(s));

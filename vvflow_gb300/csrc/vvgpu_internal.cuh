@@ -181,6 +181,7 @@ struct Ctx {
 
     // scratch for reductions / counters
     DArr<unsigned long long> counters;
+    DArr<double> sum_part;          // partial sums of the deterministic reductions
     DArr<int32_t> scan_tmp;
 
     // epsilon / merge (fixed-point rounds; [2] = double buffer)
@@ -356,3 +357,8 @@ void zero_forces(Ctx& c);
 double gsum(Ctx& c);
 
 }  // namespace vvgpu
+
+// The opaque handle of include/vvgpu.h.
+struct vvgpu_ctx {
+    vvgpu::Ctx c;
+};

@@ -50,6 +50,11 @@ class BodyOut(C.Structure):
         "force_holder_x", "force_holder_y", "force_holder_o")]
 
 
+class StepCfg(C.Structure):
+    _fields_ = [("far_criteria", C.c_double), ("min_node", C.c_double), ("max_node", C.c_double),
+                ("merge", C.c_int32), ("move", C.c_int32)]
+
+
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "n_vortices", "n_segments", "n_nodes", "n_leaves", "tree_depth", "near_pairs", "far_pairs",
@@ -110,6 +115,9 @@ SIGNATURES = {
     "vvgpu_zero_forces": (C.c_int, [_H]),
     "vvgpu_get_segment_forces": (C.c_int, [_H, _D, _D, _D]),
     "vvgpu_gsum": (C.c_int, [_H, _D]),
+    "vvgpu_batch_step": (C.c_int, [C.POINTER(_H), C.c_int64, C.POINTER(StepCfg), C.c_int32, _D, _I32]),
+    "vvgpu_batch_autotune": (C.c_int, [C.POINTER(_H), C.c_int64, C.POINTER(StepCfg), _I32, C.c_int32, _I32,
+                                       C.POINTER(C.c_double)]),
     "vvgpu_field_velocity": (C.c_int, [_H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
                                        C.c_char, C.c_char, _F]),
     "vvgpu_field_streamfunction": (C.c_int, [_H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
@@ -435,3 +443,48 @@ class GpuSpace:
                                            _p(d["near_path"], C.c_int64), _p(d["far_off"], C.c_int64),
                                            _p(d["far_depth"], C.c_int32), _p(d["far_path"], C.c_int64)), "tree_lists")
         return d
+
+
+class Batch:
+    """Many independent GpuSpace instances advanced together (vvgpu_batch_step): each step
+    is simulate()'s step (tree build, SLAE, destroy, shed, tree build, eps, convective,
+    diffusive, destroy), optionally followed by move_and_clean, per instance with its own
+    tree sizes."""
+
+    def __init__(self, spaces, far_criteria, node_sizes, merge=True, move=True):
+        self.lib = load_library()
+        self.spaces = list(spaces)
+        n = len(self.spaces)
+        self.handles = (_H * n)(*[S.h for S in self.spaces])
+        self.cfgs = (StepCfg * n)()
+        for i, (mn, mx) in enumerate(node_sizes):
+            fc = far_criteria[i] if hasattr(far_criteria, "__len__") else far_criteria
+            self.cfgs[i] = StepCfg(fc, mn, mx, 1 if merge else 0, 1 if move else 0)
+        self.nthreads = 0
+
+    def step(self, nthreads=None):
+        """One batched step; returns each instance's wall time in ms (stream synchronised)."""
+        n = len(self.spaces)
+        ms = np.zeros(n)
+        st = np.zeros(n, np.int32)
+        nt = self.nthreads if nthreads is None else nthreads
+        rc = self.lib.vvgpu_batch_step(self.handles, n, self.cfgs, nt, _p(ms), _p(st, C.c_int32))
+        if rc != 0:
+            bad = [i for i in range(n) if st[i] != 0]
+            i = bad[0] if bad else 0
+            msg = self.lib.vvgpu_last_error(self.spaces[i].h)
+            raise VVGpuError(rc, f"batch_step (instance {i})", msg.decode() if msg else "")
+        return ms
+
+    def autotune(self, candidates=(1, 2, 4, 8, 16)):
+        """Times one batched step per pool size (the steps advance the instances) and keeps
+        the fastest; returns (pool size, ms)."""
+        cand = np.asarray(candidates, np.int32)
+        best = C.c_int32(0)
+        bms = C.c_double(0)
+        rc = self.lib.vvgpu_batch_autotune(self.handles, len(self.spaces), self.cfgs, _p(cand, C.c_int32),
+                                          len(cand), C.byref(best), C.byref(bms))
+        if rc != 0:
+            raise VVGpuError(rc, "batch_autotune")
+        self.nthreads = int(best.value)
+        return self.nthreads, float(bms.value)

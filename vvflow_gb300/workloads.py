@@ -183,3 +183,20 @@ def ellipse_wake(n: int = 4_000_000, m: int = 4000, seed: int = 3, angle_deg: fl
     x, y, g = wake_cloud(n, 0.5, 80.0, body=(cx, cy), seed=seed)
     return Workload("ellipse_wake", [(cx, cy)], x, y, g, re=1e4, dt=0.002,
                     far_criteria=far_criteria)
+
+
+def batched_cylinders(count: int = 256, n_lo: int = 5_000, n_hi: int = 200_000, m_lo: int = 200,
+                      m_hi: int = 1_000, seed: int = 5) -> list:
+    """Independent cylinder simulations for the batched sweep: per instance N log-uniform in
+    [n_lo, n_hi], nu = 1/re log-uniform in [1/2000, 1/100], M uniform in [m_lo, m_hi], a wake
+    cloud (x in 0.5..20) seeded per instance."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+        nu = math.exp(rng.uniform(math.log(1 / 2000), math.log(1 / 100)))
+        m = int(rng.integers(m_lo, m_hi + 1))
+        cx, cy = cylinder_corners(0.5, m)
+        x, y, g = wake_cloud(n, 0.5, 20.0, body=(cx, cy), seed=seed * 100003 + k)
+        out.append(Workload(f"cylinder_{k}", [(cx, cy)], x, y, g, re=1.0 / nu, dt=0.002))
+    return out
