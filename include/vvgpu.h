@@ -238,6 +238,44 @@ int vvgpu_batch_step(vvgpu_ctx* const* ctxs, int64_t count, const vvgpu_step_cfg
 int vvgpu_batch_autotune(vvgpu_ctx* const* ctxs, int64_t count, const vvgpu_step_cfg* cfgs,
                          const int32_t* candidates, int32_t ncand, int32_t* best, double* best_ms);
 
+/* ---- learned far-field correction (no counterpart in the reference) ------------------- */
+/* An MLP 20 -> 64 -> 64 -> 2 (tanh-GELU, BF16 weights and activations, FP32 accumulation on
+ * the tensor cores) that predicts, for one far cell of the tree and one target point, the
+ * residual of the cell's exact velocity beyond the reference's two-monopole far field
+ * (MConvectiveFast.cpp:139-151).  Samples are (target, far cell) pairs of a built tree with
+ * FP64 direct-sum labels.  Parameters: W1[64][32] (inputs 20..31 unused), b1[64],
+ * W2[64][64], b2[64], W3[2][64], b3[2] as one float vector of vvgpu_mlp_num_params(). */
+typedef struct vvgpu_mlp vvgpu_mlp;
+int vvgpu_mlp_create(int device, uint64_t seed, vvgpu_mlp** out);
+int vvgpu_mlp_destroy(vvgpu_mlp* m);
+const char* vvgpu_mlp_last_error(const vvgpu_mlp* m);
+int64_t vvgpu_mlp_num_params(void);
+int vvgpu_mlp_get_params(vvgpu_mlp* m, float* out);
+int vvgpu_mlp_set_params(vvgpu_mlp* m, const float* in);
+/* standardisation, 42 floats: network input k = (feature k - norm[k]) * norm[20 + k], label o
+ * = network output o * norm[40 + o] (default: identity); fit_norm sets it from the samples
+ * (means, 1 / standard deviations, label root mean squares) */
+int vvgpu_mlp_set_norm(vvgpu_mlp* m, const float* norm);
+int vvgpu_mlp_get_norm(vvgpu_mlp* m, float* norm);
+int vvgpu_mlp_fit_norm(vvgpu_mlp* m);
+/* samples: features [n][20] and labels [n][2] (float) */
+int vvgpu_mlp_set_samples(vvgpu_mlp* m, int64_t n, const float* feat, const float* lab);
+int64_t vvgpu_mlp_num_samples(const vvgpu_mlp* m);
+int vvgpu_mlp_get_samples(vvgpu_mlp* m, int64_t first, int64_t n, float* feat, float* lab);
+/* appends the (target, far cell) pairs of np points in ctx's built tree, labelled by the
+ * FP64 direct sum over each cell; *added = pairs appended */
+int vvgpu_mlp_add_samples(vvgpu_mlp* m, vvgpu_ctx* ctx, int64_t np, const double* px, const double* py,
+                          int64_t* added);
+/* gradient (and loss) of (1/n) sum |y - t|^2 over the first n samples; weights unchanged */
+int vvgpu_mlp_gradient(vvgpu_mlp* m, int64_t n, float* grad, float* loss);
+/* Adam over all samples, mini-batches of `batch` (a multiple of 128), reshuffled each epoch */
+int vvgpu_mlp_train(vvgpu_mlp* m, int64_t epochs, int64_t batch, float lr, uint64_t seed, float* loss_per_epoch);
+int vvgpu_mlp_forward(vvgpu_mlp* m, int64_t n, const float* feat, float* y);
+/* MConvectiveFast::velocity(p) of ctx's built tree plus the learned correction of each far
+ * cell of p's leaf; *npairs = cells evaluated (may be NULL) */
+int vvgpu_velocity_points_learned(vvgpu_ctx* ctx, vvgpu_mlp* m, int64_t np, const double* px, const double* py,
+                                  double* vx, double* vy, int64_t* npairs);
+
 /* ---- grid fields (libvvhd/src/XVelocity.cpp, XStreamfunction.cpp, XVorticity.cpp) ---- */
 /* An xres x yres grid p = (xmin, ymin) + dxdy * (xi, yj), with xmin, ymin and dxdy rounded
  * to float as XField stores them (XField.hpp:47); out[yj * xres + xi] as XField::map.

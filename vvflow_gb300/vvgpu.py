@@ -118,6 +118,23 @@ SIGNATURES = {
     "vvgpu_batch_step": (C.c_int, [C.POINTER(_H), C.c_int64, C.POINTER(StepCfg), C.c_int32, _D, _I32]),
     "vvgpu_batch_autotune": (C.c_int, [C.POINTER(_H), C.c_int64, C.POINTER(StepCfg), _I32, C.c_int32, _I32,
                                        C.POINTER(C.c_double)]),
+    "vvgpu_mlp_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(_H)]),
+    "vvgpu_mlp_destroy": (C.c_int, [_H]),
+    "vvgpu_mlp_last_error": (C.c_char_p, [_H]),
+    "vvgpu_mlp_num_params": (C.c_int64, []),
+    "vvgpu_mlp_get_params": (C.c_int, [_H, _F]),
+    "vvgpu_mlp_set_params": (C.c_int, [_H, _F]),
+    "vvgpu_mlp_set_norm": (C.c_int, [_H, _F]),
+    "vvgpu_mlp_get_norm": (C.c_int, [_H, _F]),
+    "vvgpu_mlp_fit_norm": (C.c_int, [_H]),
+    "vvgpu_mlp_set_samples": (C.c_int, [_H, C.c_int64, _F, _F]),
+    "vvgpu_mlp_num_samples": (C.c_int64, [_H]),
+    "vvgpu_mlp_get_samples": (C.c_int, [_H, C.c_int64, C.c_int64, _F, _F]),
+    "vvgpu_mlp_add_samples": (C.c_int, [_H, _H, C.c_int64, _D, _D, _I64]),
+    "vvgpu_mlp_gradient": (C.c_int, [_H, C.c_int64, _F, _F]),
+    "vvgpu_mlp_train": (C.c_int, [_H, C.c_int64, C.c_int64, C.c_float, C.c_uint64, _F]),
+    "vvgpu_mlp_forward": (C.c_int, [_H, C.c_int64, _F, _F]),
+    "vvgpu_velocity_points_learned": (C.c_int, [_H, _H, C.c_int64, _D, _D, _D, _D, _I64]),
     "vvgpu_field_velocity": (C.c_int, [_H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
                                        C.c_char, C.c_char, _F]),
     "vvgpu_field_streamfunction": (C.c_int, [_H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
@@ -488,3 +505,113 @@ class Batch:
             raise VVGpuError(rc, "batch_autotune")
         self.nthreads = int(best.value)
         return self.nthreads, float(bms.value)
+
+
+class Mlp:
+    """The learned far-field correction (vvgpu_mlp_*): an MLP 20 -> 64 -> 64 -> 2 trained on
+    (target, far cell) pairs of a built tree with FP64 direct-sum labels."""
+
+    NF = 20
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        self.lib = load_library()
+        h = _H()
+        rc = self.lib.vvgpu_mlp_create(device, seed, C.byref(h))
+        if rc != 0:
+            raise VVGpuError(rc, "vvgpu_mlp_create", "(needs a CUDA device)")
+        self.h = h
+        self.nparam = int(self.lib.vvgpu_mlp_num_params())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vvgpu_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc, what):
+        if rc != 0:
+            msg = self.lib.vvgpu_mlp_last_error(self.h)
+            raise VVGpuError(rc, what, msg.decode() if msg else "")
+
+    def params(self):
+        out = np.empty(self.nparam, np.float32)
+        self._ok(self.lib.vvgpu_mlp_get_params(self.h, _p(out, C.c_float)), "mlp_get_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.nparam
+        self._ok(self.lib.vvgpu_mlp_set_params(self.h, _p(p, C.c_float)), "mlp_set_params")
+
+    def norm(self):
+        out = np.empty(2 * self.NF + 2, np.float32)
+        self._ok(self.lib.vvgpu_mlp_get_norm(self.h, _p(out, C.c_float)), "mlp_get_norm")
+        return out
+
+    def set_norm(self, nrm):
+        nrm = np.ascontiguousarray(nrm, np.float32)
+        self._ok(self.lib.vvgpu_mlp_set_norm(self.h, _p(nrm, C.c_float)), "mlp_set_norm")
+
+    def fit_norm(self):
+        self._ok(self.lib.vvgpu_mlp_fit_norm(self.h), "mlp_fit_norm")
+        return self.norm()
+
+    def set_samples(self, feat, lab):
+        feat = np.ascontiguousarray(feat, np.float32)
+        lab = np.ascontiguousarray(lab, np.float32)
+        self._ok(self.lib.vvgpu_mlp_set_samples(self.h, len(feat), _p(feat, C.c_float), _p(lab, C.c_float)),
+                 "mlp_set_samples")
+
+    @property
+    def nsamples(self):
+        return int(self.lib.vvgpu_mlp_num_samples(self.h))
+
+    def samples(self, first=0, n=None):
+        n = self.nsamples - first if n is None else n
+        f = np.empty((n, self.NF), np.float32)
+        lab = np.empty((n, 2), np.float32)
+        self._ok(self.lib.vvgpu_mlp_get_samples(self.h, first, n, _p(f, C.c_float), _p(lab, C.c_float)),
+                 "mlp_get_samples")
+        return f, lab
+
+    def add_samples(self, space, px, py):
+        px = np.ascontiguousarray(px, np.float64)
+        py = np.ascontiguousarray(py, np.float64)
+        n = C.c_int64(0)
+        self._ok(self.lib.vvgpu_mlp_add_samples(self.h, space.h, len(px), _p(px), _p(py), C.byref(n)),
+                 "mlp_add_samples")
+        return int(n.value)
+
+    def gradient(self, n=None):
+        n = self.nsamples if n is None else n
+        g = np.empty(self.nparam, np.float32)
+        loss = C.c_float(0)
+        self._ok(self.lib.vvgpu_mlp_gradient(self.h, n, _p(g, C.c_float), C.byref(loss)), "mlp_gradient")
+        return g, float(loss.value)
+
+    def train(self, epochs, batch=8192, lr=1e-3, seed=1):
+        out = np.empty(epochs, np.float32)
+        self._ok(self.lib.vvgpu_mlp_train(self.h, epochs, batch, lr, seed, _p(out, C.c_float)), "mlp_train")
+        return out
+
+    def forward(self, feat):
+        feat = np.ascontiguousarray(feat, np.float32)
+        y = np.empty((len(feat), 2), np.float32)
+        self._ok(self.lib.vvgpu_mlp_forward(self.h, len(feat), _p(feat, C.c_float), _p(y, C.c_float)), "mlp_forward")
+        return y
+
+    def velocity_points(self, space, px, py):
+        """velocity(p) of the space's built tree plus the learned correction."""
+        px = np.ascontiguousarray(px, np.float64)
+        py = np.ascontiguousarray(py, np.float64)
+        vx = np.empty(len(px))
+        vy = np.empty(len(px))
+        n = C.c_int64(0)
+        self._ok(self.lib.vvgpu_velocity_points_learned(space.h, self.h, len(px), _p(px), _p(py), _p(vx), _p(vy),
+                                                         C.byref(n)), "velocity_points_learned")
+        return vx, vy, int(n.value)
