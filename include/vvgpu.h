@@ -217,6 +217,11 @@ int vvgpu_zero_forces(vvgpu_ctx* ctx);
 int vvgpu_get_segment_forces(vvgpu_ctx* ctx, double* cp, double* fr, double* nu);
 int vvgpu_gsum(vvgpu_ctx* ctx, double* out);
 
+/* FP64 direct sum (no tree) at n points: every vortex with its own epsilon (biot_savart,
+ * MConvectiveFast.cpp:116-120) plus the sink, slip-segment and free-stream terms of
+ * velocity(p).  The reference of the tree's own approximation error. */
+int vvgpu_direct_velocity(vvgpu_ctx* ctx, int64_t n, const double* px, const double* py, double* vx, double* vy);
+
 /* ---- batched sweep: many independent simulations advanced by one call ------------------ */
 /* One simulate() step (utils/vvflow/vvflow.cpp:214-255: tree build, calc_circulation, tree
  * destroy, vortex_shed, tree build, CalcEpsilonFast(merge), process_all_lists,

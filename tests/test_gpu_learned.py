@@ -156,3 +156,31 @@ def test_gpu_mlp_training_lowers_tree_error():
     e_learn = np.hypot(lx - dx, ly - dy)
     assert npairs > 0
     assert np.mean(e_learn) < 0.5 * np.mean(e_plain), (np.mean(e_learn), np.mean(e_plain))
+
+
+@pytest.mark.gpu
+def test_gpu_direct_sum_matches_oracle():
+    """vvgpu_direct_velocity (no tree, each source's epsilon, sinks, free stream) against the
+    restatement's direct sum, FP64 within 1e-12 of the largest velocity."""
+    import oracle
+    from vvflow_gb300 import workloads as W
+    from vvflow_gb300.vvgpu import VVGPU_FP64, GpuSpace
+    wl = W.cylinder_annulus(5000, 200, seed=8)
+    rng = np.random.default_rng(8)
+    ie = rng.uniform(5.0, 50.0, wl.n)
+    ie[::17] = 0.0
+    px = rng.uniform(-3, 3, 300)
+    py = rng.uniform(-3, 3, 300)
+    sinks = (np.array([0.8, -1.5]), np.array([0.2, 1.1]), np.array([0.3, -2.5]))
+    out = []
+    for S in (GpuSpace(VVGPU_FP64), oracle.OracleSpace("port")):
+        S.set_params(wl.re, wl.dt, 1.0, 0.2)
+        for cx, cy in wl.bodies:
+            S.add_body(cx, cy)
+        S.set_sinks(*sinks)
+        S.set_vortices(wl.x, wl.y, wl.g, ie)
+        out.append(S.direct_velocity(px, py))
+        S.close()
+    (gx, gy), (rx, ry) = out
+    scale = np.abs(np.concatenate([rx, ry])).max()
+    assert np.abs(gx - rx).max() <= 1e-12 * scale and np.abs(gy - ry).max() <= 1e-12 * scale

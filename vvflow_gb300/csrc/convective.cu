@@ -414,6 +414,45 @@ __global__ void k_points(int64_t np, const double* __restrict__ qx, const double
     ovy[q] = ry * C_1_2PI + fy * C_1_2PI + ey + a.inf_vy;
 }
 
+// FP64 direct sum over every vortex (no tree), each source with its own epsilon (biot_savart,
+// MConvectiveFast.cpp:116-120), plus the sink, slip-segment and free-stream terms of
+// velocity(p): the tree's own approximation error is measured against it.  One block per
+// target, fixed-order reduction.
+constexpr int DIRECT_TB = 256;
+__global__ void __launch_bounds__(DIRECT_TB) k_direct(int64_t n, const double* __restrict__ qx,
+                                                     const double* __restrict__ qy, ConvArgs a, double* ovx,
+                                                     double* ovy) {
+    __shared__ double sh[2][DIRECT_TB / 32];
+    const int64_t q = blockIdx.x;
+    const double px = qx[q], py = qy[q];
+    double rx = 0, ry = 0;
+    for (int64_t j = threadIdx.x; j < n; j += DIRECT_TB) {
+        const double gj = a.g[j];
+        if (gj == 0.) continue;
+        const double dx = px - a.x[j], dy = py - a.y[j];
+        const double e = 1. / a.ie[j];
+        const double s = gj / (dx * dx + dy * dy + e * e);
+        rx -= dy * s;
+        ry += dx * s;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        rx += __shfl_xor_sync(0xffffffffu, rx, o);
+        ry += __shfl_xor_sync(0xffffffffu, ry, o);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { sh[0][w] = rx; sh[1][w] = ry; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sx = 0, sy = 0;
+        for (int k = 0; k < DIRECT_TB / 32; k++) { sx += sh[0][k]; sy += sh[1][k]; }
+        double ex, ey;
+        extra_terms(a, px, py, ex, ey);
+        ovx[q] = sx * C_1_2PI + ex + a.inf_vx;
+        ovy[q] = sy * C_1_2PI + ey + a.inf_vy;
+    }
+}
+
 // Algorithmic near-pair count: sum over leaves of (non-zero targets) x (non-zero sources
 // in the near runs).
 __global__ void k_leaf_nz(int64_t nl, const int32_t* __restrict__ lvf, const int32_t* __restrict__ lvl,
@@ -537,6 +576,27 @@ void velocity_points(Ctx& c, int64_t np, const double* px, const double* py, dou
     k_points<<<grid_for(np, 128), 128, 0, s>>>(np, q.p, q.p + np, c.nd_geom.p, c.nd_ch1.p, c.nd_dfs.p, a,
                                               q.p + 2 * np, q.p + 3 * np);
     VV_LAUNCH_CHECK();
+    VV_CUDA(cudaMemcpyAsync(vx, q.p + 2 * np, np * 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaMemcpyAsync(vy, q.p + 3 * np, np * 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+}
+
+void direct_velocity(Ctx& c, int64_t np, const double* px, const double* py, double* vx, double* vy) {
+    check_bodies_at_rest(c);
+    if (np == 0) return;
+    upload_segments(c);
+    cudaStream_t s = c.st();
+    DArr<double> q;
+    q.reserve(4 * np);
+    VV_CUDA(cudaMemcpyAsync(q.p, px, np * 8, cudaMemcpyHostToDevice, s));
+    VV_CUDA(cudaMemcpyAsync(q.p + np, py, np * 8, cudaMemcpyHostToDevice, s));
+    ConvArgs a = make_args(c);
+    for (int64_t b = 0; b < np; b += 65535) {
+        const int64_t cnt = std::min<int64_t>(65535, np - b);
+        k_direct<<<(unsigned)cnt, DIRECT_TB, 0, s>>>(c.n, q.p + b, q.p + np + b, a, q.p + 2 * np + b,
+                                                     q.p + 3 * np + b);
+        VV_LAUNCH_CHECK();
+    }
     VV_CUDA(cudaMemcpyAsync(vx, q.p + 2 * np, np * 8, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaMemcpyAsync(vy, q.p + 3 * np, np * 8, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));

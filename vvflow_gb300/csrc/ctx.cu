@@ -443,6 +443,7 @@ int vvgpu_eps(vvgpu_ctx* h, int merge, int64_t* merged) {
     if (!c.built) throw ApiError{VVGPU_ERR_NOT_BUILT, "tree is not built"};
     ensure_full_lists(c);
     eps_pass(c, merge, merged);
+    c.mom_valid = false;  // merges move circulation
     API_END
 }
 
@@ -518,6 +519,13 @@ int vvgpu_get_body_params(vvgpu_ctx* h, int body, vvgpu_body_params* out) {
     API_BEGIN(h)
     if (body < 0 || body >= (int)c.bodies.size() || !out) throw ApiError{VVGPU_ERR_ARG, "bad body index"};
     *out = c.bodies[body].p;
+    API_END
+}
+
+int vvgpu_direct_velocity(vvgpu_ctx* h, int64_t n, const double* px, const double* py, double* vx, double* vy) {
+    API_BEGIN(h)
+    if (n < 0 || (n && (!px || !py || !vx || !vy))) throw ApiError{VVGPU_ERR_ARG, "bad point arrays"};
+    direct_velocity(c, n, px, py, vx, vy);
     API_END
 }
 

@@ -522,42 +522,85 @@ __global__ void k_loss_sum(int ntiles, const float* __restrict__ part, float* ou
 
 // Per node, the complex moments about its +/- centroids (nd_cm): M_k = sum g (z - c)^k,
 // k = 2, 3, 4, over the node's vortices of that sign; mom[12 k ..] = M2+, M3+, M4+, M2-,
-// M3-, M4- (re, im).  One warp per node, fixed-order reduction.
-__global__ void k_node_moments(int64_t nn, const int32_t* __restrict__ vf, const int32_t* __restrict__ vl,
-                               const double* __restrict__ cm, const double* __restrict__ x,
-                               const double* __restrict__ y, const double* __restrict__ g, double* mom) {
-    const int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (k >= nn) return;
+// M3-, M4- (re, im).  Leaves sum their vortices; inner nodes, level by level from the
+// bottom, shift their children's moments to their own centroid (binomial expansion of
+// (z - c)^k = ((z - c') + d)^k, d = c' - c, with M_0 = the child's circulation and M_1 = 0
+// about the child's own centroid).
+__device__ __forceinline__ void cmul(double ax, double ay, double bx, double by, double& rx, double& ry) {
+    rx = ax * bx - ay * by;
+    ry = ax * by + ay * bx;
+}
+
+__global__ void k_leaf_moments(int64_t nn, const int32_t* __restrict__ ch1, const int32_t* __restrict__ vf,
+                               const int32_t* __restrict__ vl, const double* __restrict__ cm,
+                               const double* __restrict__ x, const double* __restrict__ y,
+                               const double* __restrict__ g, double* mom) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nn || ch1[k] >= 0) return;
     const double* c = cm + 6 * k;
     double a[12];
 #pragma unroll
     for (int q = 0; q < 12; q++) a[q] = 0.;
-    for (int32_t j = vf[k] + lane; j < vl[k]; j += 32) {
+    for (int32_t j = vf[k]; j < vl[k]; j++) {
         const double gj = g[j];
         if (gj == 0.) continue;
         const int o = gj > 0 ? 0 : 6;
         const double wx = x[j] - (gj > 0 ? c[0] : c[3]), wy = y[j] - (gj > 0 ? c[1] : c[4]);
-        double px = wx * wx - wy * wy, py = 2. * wx * wy;  // w^2
+        double px, py;
+        cmul(wx, wy, wx, wy, px, py);
 #pragma unroll
         for (int e = 0; e < 3; e++) {
             a[o + 2 * e] += gj * px;
             a[o + 2 * e + 1] += gj * py;
-            const double nx = px * wx - py * wy, ny = px * wy + py * wx;
+            double nx, ny;
+            cmul(px, py, wx, wy, nx, ny);
             px = nx;
             py = ny;
         }
     }
 #pragma unroll
-    for (int q = 0; q < 12; q++) {
-        double v = a[q];
+    for (int q = 0; q < 12; q++) mom[12 * k + q] = a[q];
+}
+
+__global__ void k_inner_moments(int64_t a0, int64_t cnt, const int32_t* __restrict__ ch1,
+                                const double* __restrict__ cm, double* mom) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    const int64_t k = a0 + t;
+    const int32_t c1 = ch1[k];
+    if (c1 < 0) return;
+    double out[12];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        a[q] = v;
+    for (int q = 0; q < 12; q++) out[q] = 0.;
+    for (int sgn = 0; sgn < 2; sgn++) {
+        const double cx = cm[6 * k + 3 * sgn], cy = cm[6 * k + 3 * sgn + 1];
+        for (int h = 0; h < 2; h++) {
+            const int64_t u = c1 + h;
+            const double G = cm[6 * u + 3 * sgn + 2];
+            if (G == 0.) continue;
+            const double dx = cm[6 * u + 3 * sgn] - cx, dy = cm[6 * u + 3 * sgn + 1] - cy;
+            const double* m = mom + 12 * u + 6 * sgn;  // M2', M3', M4'
+            double d2x, d2y, d3x, d3y, d4x, d4y;
+            cmul(dx, dy, dx, dy, d2x, d2y);
+            cmul(d2x, d2y, dx, dy, d3x, d3y);
+            cmul(d3x, d3y, dx, dy, d4x, d4y);
+            double tx, ty, ux, uy, vx, vy;
+            // M2 = M2' + G d^2
+            out[6 * sgn + 0] += m[0] + G * d2x;
+            out[6 * sgn + 1] += m[1] + G * d2y;
+            // M3 = M3' + 3 M2' d + G d^3
+            cmul(m[0], m[1], dx, dy, tx, ty);
+            out[6 * sgn + 2] += m[2] + 3. * tx + G * d3x;
+            out[6 * sgn + 3] += m[3] + 3. * ty + G * d3y;
+            // M4 = M4' + 4 M3' d + 6 M2' d^2 + G d^4
+            cmul(m[2], m[3], dx, dy, ux, uy);
+            cmul(m[0], m[1], d2x, d2y, vx, vy);
+            out[6 * sgn + 4] += m[4] + 4. * ux + 6. * vx + G * d4x;
+            out[6 * sgn + 5] += m[5] + 4. * uy + 6. * vy + G * d4y;
+        }
     }
-    if (lane == 0)
 #pragma unroll
-        for (int q = 0; q < 12; q++) mom[12 * k + q] = a[q];
+    for (int q = 0; q < 12; q++) mom[12 * k + q] = out[q];
 }
 
 struct WalkView {
@@ -826,8 +869,27 @@ struct PairSet {
     int64_t npairs = 0;
     DArr<int64_t> off;
     DArr<int32_t> node, target;
-    DArr<double> pts, back, mom;
+    DArr<double> pts, back;
 };
+
+// the moments of every node of the built tree, once per tree
+void ensure_moments(Ctx& c) {
+    if (c.mom_valid) return;
+    cudaStream_t s = c.st();
+    const int64_t nn = c.nnodes;
+    c.nd_mom.reserve(12 * (size_t)nn + 12);
+    k_leaf_moments<<<grid_for(nn, 128), 128, 0, s>>>(nn, c.nd_ch1.p, c.nd_vf.p, c.nd_vl.p, c.nd_cm.p, c.x.p, c.y.p,
+                                                     c.g.p, c.nd_mom.p);
+    VV_LAUNCH_CHECK();
+    const int64_t nlev = (int64_t)c.level_begin.size() - 1;
+    for (int64_t lv = nlev - 1; lv >= 0; lv--) {
+        const int64_t a = c.level_begin[lv], b = std::min<int64_t>(c.level_begin[lv + 1], nn);
+        if (b <= a) continue;
+        k_inner_moments<<<grid_for(b - a, 128), 128, 0, s>>>(a, b - a, c.nd_ch1.p, c.nd_cm.p, c.nd_mom.p);
+        VV_LAUNCH_CHECK();
+    }
+    c.mom_valid = true;
+}
 
 // far pairs of np points (device arrays dpx, dpy) in the context's built tree, with features
 // (and labels) into feat/lab (device, grown as needed)
@@ -835,10 +897,7 @@ void make_pairs(Ctx& c, int64_t np, const double* dpx, const double* dpy, PairSe
                 DArr<float>& lab, int64_t feat_off, bool with_label) {
     cudaStream_t s = c.st();
     const int64_t nn = c.nnodes;
-    ps.mom.reserve(12 * (size_t)nn + 12);
-    k_node_moments<<<grid_for(32 * nn, 256), 256, 0, s>>>(nn, c.nd_vf.p, c.nd_vl.p, c.nd_cm.p, c.x.p, c.y.p, c.g.p,
-                                                          ps.mom.p);
-    VV_LAUNCH_CHECK();
+    ensure_moments(c);
     WalkView wv{c.nd_geom.p, c.nd_ch1.p, c.far_criteria, nn};
     DArr<int32_t> cnt;
     cnt.reserve((size_t)np + 1);
@@ -862,7 +921,7 @@ void make_pairs(Ctx& c, int64_t np, const double* dpx, const double* dpy, PairSe
     lab.reserve((size_t)need * 2 + 1, true, (size_t)feat_off * 2, s);
     if (ps.npairs > 0) {
         k_pair_samples<<<grid_for(ps.npairs, 128), 128, 0, s>>>(
-            ps.npairs, ps.node.p, ps.target.p, dpx, dpy, c.nd_geom.p, c.nd_cm.p, ps.mom.p, c.nd_vf.p, c.nd_vl.p,
+            ps.npairs, ps.node.p, ps.target.p, dpx, dpy, c.nd_geom.p, c.nd_cm.p, c.nd_mom.p, c.nd_vf.p, c.nd_vl.p,
             c.x.p, c.y.p, c.g.p, feat.p + feat_off * NF, lab.p + feat_off * 2, ps.back.p, with_label ? 1 : 0);
         VV_LAUNCH_CHECK();
     }
@@ -977,15 +1036,20 @@ int vvgpu_mlp_get_norm(vvgpu_mlp* m, float* norm) {
     MLP_END
 }
 
-// standardisation from the samples: per-feature mean and 1 / standard deviation (1 where
-// the deviation is 0), per-output root mean square of the labels
+// standardisation from the samples (every k-th sample, at most FIT_MAX of them): per-feature
+// mean and 1 / standard deviation (1 where the deviation is 0), per-output root mean square
+// of the labels
+constexpr int64_t FIT_MAX = 4000000;
 int vvgpu_mlp_fit_norm(vvgpu_mlp* m) {
     MLP_BEGIN(m)
-    const int64_t n = M.nsamples;
-    if (n <= 0) throw ApiError{VVGPU_ERR_ARG, "no samples"};
+    const int64_t total = M.nsamples;
+    if (total <= 0) throw ApiError{VVGPU_ERR_ARG, "no samples"};
+    const int64_t stride = (total + FIT_MAX - 1) / FIT_MAX;
+    const int64_t n = (total + stride - 1) / stride;
     std::vector<float> f((size_t)n * NF), l((size_t)n * 2);
-    VV_CUDA(cudaMemcpyAsync(f.data(), M.feat.p, f.size() * 4, cudaMemcpyDeviceToHost, M.stream));
-    VV_CUDA(cudaMemcpyAsync(l.data(), M.lab.p, l.size() * 4, cudaMemcpyDeviceToHost, M.stream));
+    VV_CUDA(cudaMemcpy2DAsync(f.data(), NF * 4, M.feat.p, stride * NF * 4, NF * 4, n, cudaMemcpyDeviceToHost,
+                              M.stream));
+    VV_CUDA(cudaMemcpy2DAsync(l.data(), 2 * 4, M.lab.p, stride * 2 * 4, 2 * 4, n, cudaMemcpyDeviceToHost, M.stream));
     VV_CUDA(cudaStreamSynchronize(M.stream));
     std::vector<double> s1(NF, 0.), s2(NF, 0.), ls(2, 0.);
     for (int64_t i = 0; i < n; i++) {

@@ -787,6 +787,7 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
     VV_LAUNCH_CHECK();
     tree_lists(c);
     c.built = true;
+    c.mom_valid = false;
     c.stats.n_vortices = n;
     c.stats.n_segments = m;
     c.stats.n_nodes = nn;

@@ -182,6 +182,8 @@ struct Ctx {
     // scratch for reductions / counters
     DArr<unsigned long long> counters;
     DArr<double> sum_part;          // partial sums of the deterministic reductions
+    DArr<double> nd_mom;            // learned correction: per node complex moments M2..M4 of each sign
+    bool mom_valid = false;
     DArr<int32_t> scan_tmp;
 
     // epsilon / merge (fixed-point rounds; [2] = double buffer)
@@ -337,6 +339,7 @@ void eps_pass(Ctx& c, int merge, int64_t* merged);
 void convective(Ctx& c);
 void velocity_points(Ctx& c, int64_t n, const double* px, const double* py, double* vx, double* vy);
 void velocity_points_on_device(Ctx& c, int64_t n, const double* dpx, const double* dpy, double* dvx, double* dvy);
+void direct_velocity(Ctx& c, int64_t n, const double* px, const double* py, double* vx, double* vy);
 // TVec3D::iszero of every body's speed_slae (TVec3D.hpp:17), else VVGPU_ERR_UNSUPPORTED.
 void check_bodies_at_rest(Ctx& c);
 // grid fields (fields.cu)

@@ -115,6 +115,7 @@ SIGNATURES = {
     "vvgpu_zero_forces": (C.c_int, [_H]),
     "vvgpu_get_segment_forces": (C.c_int, [_H, _D, _D, _D]),
     "vvgpu_gsum": (C.c_int, [_H, _D]),
+    "vvgpu_direct_velocity": (C.c_int, [_H, C.c_int64, _D, _D, _D, _D]),
     "vvgpu_batch_step": (C.c_int, [C.POINTER(_H), C.c_int64, C.POINTER(StepCfg), C.c_int32, _D, _I32]),
     "vvgpu_batch_autotune": (C.c_int, [C.POINTER(_H), C.c_int64, C.POINTER(StepCfg), _I32, C.c_int32, _I32,
                                        C.POINTER(C.c_double)]),
@@ -327,6 +328,15 @@ class GpuSpace:
 
     def vortex_shed(self):
         self._ok(self.lib.vvgpu_vortex_shed(self.h), "vortex_shed")
+
+    def direct_velocity(self, px, py):
+        """FP64 direct sum over every vortex (no tree) at the points."""
+        px = np.ascontiguousarray(px, np.float64)
+        py = np.ascontiguousarray(py, np.float64)
+        vx = np.empty_like(px)
+        vy = np.empty_like(px)
+        self._ok(self.lib.vvgpu_direct_velocity(self.h, len(px), _p(px), _p(py), _p(vx), _p(vy)), "direct_velocity")
+        return vx, vy
 
     # -- grid fields (XVelocity, XStreamfunction, XVorticity); out[yj, xi] float32 ------
     def field_velocity(self, xmin, ymin, dxdy, xres, yres, mode="x", ref_frame="o"):
