@@ -35,6 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "vortex-steps/s @4M vortices: learned/FP32 vs plain FP64 GPU at ≤1e-5 rel err"
+CONV32_DRAM_BYTES_4M = 444.3e6 + 54.1e6
 L2_BYTES = 129 * 2**20
 
 
@@ -352,7 +353,10 @@ def gpu_arm(args):
     peak = measure_fp32_peak(torch, dev)
     roof = {"bound": "fp32", "kernel": "k_conv32 (convective near field)",
             "achieved": flops / (conv_ms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
-            "frac": flops / (conv_ms / 1e3) / 1e12 / peak, "traffic": None,
+            "frac": flops / (conv_ms / 1e3) / 1e12 / peak,
+            # DRAM bytes read + written by one k_conv32 launch of this workload, from one ncu
+            # capture (profiles/step_dram_ellipse_wake_4M.md); other sizes were not captured
+            "traffic": CONV32_DRAM_BYTES_4M if (args.n, args.m) == (4_000_000, 4000) else None,
             "algorithmic_flops_per_launch": flops,
             "near_pairs": stp["near_pairs"], "far_pairs": stp["far_pairs"],
             "launch_ms": conv_ms,
