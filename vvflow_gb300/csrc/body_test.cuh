@@ -17,6 +17,15 @@ struct BodyTest {
     int inverted;  // area <= 0: TBody::isInsideValid
 };
 
+// Order-preserving integer key of a double: a < b (IEEE) <=> ykey(a) < ykey(b), with -0 and
+// +0 one key (as they compare equal); not for NaN.
+__device__ __forceinline__ int64_t ykey(double v) {
+    uint64_t u = (uint64_t)__double_as_longlong(v);
+    if ((u << 1) == 0) u = 0;
+    const uint64_t k = (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+    return (int64_t)(k ^ 0x8000000000000000ull);
+}
+
 // TBody::isPointInContour over the corners, exact FP64 (no contraction).  Returns the
 // global index of the segment whose centre is nearest, or -1.
 __device__ __forceinline__ int64_t point_invalid(const BodyTest& b, const double* __restrict__ cx, const double* __restrict__ cy,
@@ -25,14 +34,25 @@ __device__ __forceinline__ int64_t point_invalid(const BodyTest& b, const double
     if (!in && (px < b.blx || py < b.bly || px > b.trx || py > b.try_ ||
                 dabs2(dsub(px, b.cofx), dsub(py, b.cofy)) > b.r2max))
         return -1;
+    // The y-range conditions of an edge are exact comparisons of doubles, made here on
+    // order-preserving integer keys (integer pipe); only the few edges whose range holds py
+    // take the FP64 products.
     const int64_t f = b.first, n = b.count;
-    for (int64_t i = 0, j = n - 1; i < n; j = i++) {
-        const double vix = cx[f + i], viy = cy[f + i], vjx = cx[f + j], vjy = cy[f + j];
-        const double lhs = dmul(dsub(vjy, viy), dsub(px, vix));
-        const double rhs = dmul(dsub(vjx, vix), dsub(py, viy));
-        if (((viy < vjy) && (viy < py) && (py <= vjy) && (lhs > rhs)) ||
-            ((viy > vjy) && (viy > py) && (py >= vjy) && (lhs < rhs)))
-            in = !in;
+    if (n > 0) {
+        const int64_t kpy = ykey(py);
+        int64_t kjy = ykey(cy[f + n - 1]);
+        for (int64_t i = 0, j = n - 1; i < n; j = i++) {
+            const int64_t kiy = ykey(cy[f + i]);
+            const bool up = (kiy < kjy) && (kiy < kpy) && (kpy <= kjy);
+            const bool down = (kiy > kjy) && (kiy > kpy) && (kpy >= kjy);
+            if (up || down) {
+                const double vix = cx[f + i], viy = cy[f + i], vjx = cx[f + j], vjy = cy[f + j];
+                const double lhs = dmul(dsub(vjy, viy), dsub(px, vix));
+                const double rhs = dmul(dsub(vjx, vix), dsub(py, viy));
+                if ((up && lhs > rhs) || (down && lhs < rhs)) in = !in;
+            }
+            kjy = kiy;
+        }
     }
     if (!in) return -1;
     int64_t best = -1;
