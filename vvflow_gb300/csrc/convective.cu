@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(CW * 32) k_conv64(ConvArgs a) {
 // FP32 near field.  Eight targets per lane.  A leaf with at most 8 targets uses all 32
 // lanes over its sources; with 9..16 targets each half-warp takes 8 targets and strides
 // over the sources by 16 (larger leaves loop in groups of 16).  Each lane keeps plain FP32
-// partial sums for up to 16 sources and then folds them into a TwoSum-compensated pair.
+// partial sums for up to 32 sources and then folds them into a TwoSum-compensated pair.
 constexpr int TC32 = 8;
 
 __global__ void __launch_bounds__(CW * 32, 4) k_conv32(ConvArgs a) {
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(CW * 32, 4) k_conv32(ConvArgs a) {
                     px[t] = fmaf(-dy, q, px[t]);
                     py[t] = fmaf(dx, q, py[t]);
                 }
-                if (++since == 16) {
+                if (++since == 32) {
                     since = 0;
 #pragma unroll
                     for (int t = 0; t < TC32; t++) {
