@@ -1,5 +1,6 @@
 // Device-wide exclusive prefix sum over int32 (used by the tree partition and list builds).
-// Three passes: per-block totals, a one-block scan of the totals, per-block rescan + offset.
+// Three passes: per-block totals, a one-block scan of the totals, per-block rescan + offset;
+// inputs of at most four tiles take a single one-block pass.
 #include "vvgpu_internal.cuh"
 
 namespace vvgpu {
@@ -83,9 +84,42 @@ __global__ void k_tile_scan(const int32_t* __restrict__ in, int64_t n, const int
     }
 }
 
+// Short inputs (at most SMALL_TILES tiles): one block walks the tiles in order, carrying the
+// running total, so the scan is one launch instead of three.
+constexpr int SMALL_TILES = 4;
+__global__ void k_scan_small(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ out) {
+    __shared__ int32_t wt[SCAN_BLOCK / 32];
+    int32_t carry = 0;
+    for (int64_t t0 = 0; t0 < n; t0 += SCAN_TILE) {
+        const int64_t base = t0 + (int64_t)threadIdx.x * SCAN_ITEMS;
+        int32_t v[SCAN_ITEMS];
+        int32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++) {
+            v[k] = (base + k < n) ? in[base + k] : 0;
+            s += v[k];
+        }
+        int32_t total;
+        const int32_t inc = block_inclusive(s, wt, total);
+        int32_t run = carry + inc - s;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++) {
+            if (base + k < n) out[base + k] = run;
+            run += v[k];
+        }
+        carry += total;
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
 }  // namespace
 
 void exclusive_scan(Ctx& c, const int32_t* in, int32_t* out, int64_t n) {
+    if (n <= (int64_t)SMALL_TILES * SCAN_TILE) {
+        k_scan_small<<<1, SCAN_BLOCK, 0, c.st()>>>(in, n, out);
+        VV_LAUNCH_CHECK();
+        return;
+    }
     int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (nb < 1) nb = 1;
     c.scan_tmp.reserve((size_t)nb);
