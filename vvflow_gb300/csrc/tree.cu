@@ -109,9 +109,10 @@ __global__ void k_finalize_root(double4* geom, const unsigned long long* bbox, i
 __global__ void k_decide(int64_t a, int64_t cnt, const double4* __restrict__ geom, const int32_t* __restrict__ vf,
                          const int32_t* __restrict__ vl, const int32_t* __restrict__ sf, const int32_t* __restrict__ sl,
                          const int32_t* __restrict__ depth, double min_node, double max_node, int32_t* split,
-                         int32_t* flags, double* pivot, int32_t* axis, int32_t* err) {
+                         int32_t* flags, double* pivot, int32_t* axis, int32_t* err, int32_t* counts) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= cnt) return;
+    if (t == 0) counts[0] = counts[1] = 0;  // the route's counters of this level
     int64_t k = a + t;
     double4 gm = geom[k];
     double h = gm.z, w = gm.w;
@@ -128,14 +129,9 @@ __global__ void k_decide(int64_t a, int64_t cnt, const double4* __restrict__ geo
     pivot[k] = byx ? gm.x : gm.y;
 }
 
-__global__ void k_children(int64_t a, int64_t b, int64_t cnt, const int32_t* __restrict__ split,
-                           const int32_t* __restrict__ lscan, int32_t* ch1, int32_t* depth, int64_t* path,
-                           unsigned long long* bbox, int32_t* nlow, int32_t* nlow_s) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= cnt) return;
-    int64_t k = a + t;
-    if (!split[k]) { ch1[k] = -1; return; }
-    int64_t c1 = b + 2 * (int64_t)lscan[t];
+__device__ __forceinline__ void make_children(int64_t k, int64_t c1, int32_t* ch1, int32_t* depth, int64_t* path,
+                                              int32_t* parent, unsigned long long* bbox, int32_t* nlow,
+                                              int32_t* nlow_s) {
     ch1[k] = (int32_t)c1;
     nlow[k] = 0;
     nlow_s[k] = 0;
@@ -144,6 +140,7 @@ __global__ void k_children(int64_t a, int64_t b, int64_t cnt, const int32_t* __r
         ch1[c] = -1;
         depth[c] = depth[k] + 1;
         path[c] = path[k] * 2 + q;
+        parent[c] = (int32_t)k;
         unsigned long long* s = bbox + 4 * c;
         s[0] = dkey(DBL_MAX); s[1] = dkey(DBL_MAX);
         s[2] = dkey(-DBL_MAX); s[3] = dkey(-DBL_MAX);
@@ -195,11 +192,20 @@ constexpr int CNW = CT / 32;
 // k_route: counts[0] = warp-route nodes (listed in small_list), counts[1] = chunks; chunk c
 // belongs to node chunk_node[c], and node k's chunks are cbase[k] .. cbase[k] + nch - 1 in
 // position order.
-__global__ void k_route(int64_t a, int64_t cnt, const int32_t* __restrict__ split, const int32_t* __restrict__ vf,
+// Creates the children of the level's split nodes (ids b + 2 * rank among the split
+// nodes), then routes each split node.  counts[2] = the level's split count.
+__global__ void k_route(int64_t a, int64_t b, int64_t cnt, const int32_t* __restrict__ split,
+                        const int32_t* __restrict__ lscan, const int32_t* __restrict__ vf,
                         const int32_t* __restrict__ vl, int32_t* counts, int32_t* small_list, int32_t* cbase,
-                        int32_t* chunk_node) {
+                        int32_t* chunk_node, int32_t* ch1, int32_t* depth, int64_t* path, int32_t* parent,
+                        unsigned long long* bbox, int32_t* nlow, int32_t* nlow_s) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int32_t k = (int32_t)(a + t);
+    if (t == 0) counts[2] = lscan[cnt];
+    if (t < cnt) {
+        if (split[k]) make_children(k, b + 2 * (int64_t)lscan[t], ch1, depth, path, parent, bbox, nlow, nlow_s);
+        else ch1[k] = -1;
+    }
     bool small = false;
     int nch = 0;
     if (t < cnt && split[k]) {
@@ -579,32 +585,53 @@ __device__ __forceinline__ void combine_cm(const double* a, const double* b, dou
     } else { out[0] = nx; out[1] = ny; out[2] = 0; }
 }
 
-__global__ void k_inner_cm(int64_t a, int64_t cnt, const int32_t* __restrict__ ch1, const double4* __restrict__ geom,
-                           double* cm, int32_t* lc) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= cnt) return;
-    int64_t k = a + t;
-    int32_t c1 = ch1[k];
-    if (c1 < 0) return;
-    double4 gm = geom[k];
-    const double* A = cm + 6 * (size_t)c1;
-    const double* B = cm + 6 * (size_t)(c1 + 1);
-    double* o = cm + 6 * k;
-    combine_cm(A, B, o, gm.x, gm.y);
-    combine_cm(A + 3, B + 3, o + 3, gm.x, gm.y);
-    lc[k] = lc[c1] + lc[c1 + 1];
+// All inner centroids in one pass: each leaf's thread climbs towards the root, and at each
+// node the second child to arrive combines both children (always in the order ch1, ch1 + 1,
+// so the result does not depend on which arrives last) and climbs on.
+__global__ void k_tree_cm(int64_t nn, const int32_t* __restrict__ ch1, const int32_t* __restrict__ parent,
+                          const double4* __restrict__ geom, double* cm, int32_t* lc, int32_t* arrive) {
+    const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k0 >= nn || ch1[k0] >= 0) return;
+    int32_t k = (int32_t)k0;
+    for (int it = 0; it <= MAX_DEPTH; it++) {
+        const int32_t p = parent[k];
+        if (p < 0) return;
+        __threadfence();  // this subtree's results before the arrival
+        if (atomicAdd(&arrive[p], 1) == 0) return;  // the sibling combines
+        __threadfence();
+        const int32_t c1 = ch1[p];
+        const double4 gm = geom[p];
+        double A[6], B[6], o[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            A[q] = __ldcg(cm + 6 * (size_t)c1 + q);
+            B[q] = __ldcg(cm + 6 * (size_t)(c1 + 1) + q);
+        }
+        combine_cm(A, B, o, gm.x, gm.y);
+        combine_cm(A + 3, B + 3, o + 3, gm.x, gm.y);
+#pragma unroll
+        for (int q = 0; q < 6; q++) cm[6 * (size_t)p + q] = o[q];
+        lc[p] = __ldcg(lc + c1) + __ldcg(lc + c1 + 1);
+        k = p;
+    }
 }
 
-__global__ void k_dfs(int64_t a, int64_t cnt, const int32_t* __restrict__ ch1, const int32_t* __restrict__ lc,
-                      int32_t* dfs, int32_t* leaf_node) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= cnt) return;
-    int64_t k = a + t;
-    if (k == 0) dfs[0] = 0;
-    int32_t c1 = ch1[k];
-    if (c1 < 0) { leaf_node[dfs[k]] = (int32_t)k; return; }
-    dfs[c1] = dfs[k];
-    dfs[c1 + 1] = dfs[k] + lc[c1];
+// Depth-first leaf index of every node (its first leaf): the leaves of the left siblings on
+// the way up to the root, summed; leaf_node[dfs] = node for the leaves.
+__global__ void k_tree_dfs(int64_t nn, const int32_t* __restrict__ ch1, const int32_t* __restrict__ parent,
+                           const int32_t* __restrict__ lc, int32_t* dfs, int32_t* leaf_node) {
+    const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k0 >= nn) return;
+    int32_t k = (int32_t)k0, d = 0;
+    for (int it = 0; it <= MAX_DEPTH; it++) {
+        const int32_t p = parent[k];
+        if (p < 0) break;
+        const int32_t c1 = ch1[p];
+        if (k != c1) d += lc[c1];
+        k = p;
+    }
+    dfs[k0] = d;
+    if (ch1[k0] < 0) leaf_node[d] = (int32_t)k0;
 }
 
 __global__ void k_leaf_arrays(int64_t nl, const int32_t* __restrict__ leaf_node, const int32_t* __restrict__ vf,
@@ -642,6 +669,7 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
         c.nd_axis.reserve(need, true, keep, s); c.nd_split.reserve(need, true, keep, s);
         c.nd_nlow.reserve(need, true, keep, s); c.nd_nlow_s.reserve(need, true, keep, s);
         c.nd_cbase.reserve(need, true, keep, s); c.nd_npair.reserve(need, true, keep, s);
+        c.nd_parent.reserve(need, true, keep, s);
     };
     c.lvl_cnt.reserve(4);
     c.nnodes = 1;
@@ -665,6 +693,7 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
         k_root_bbox<<<std::min<int64_t>(grid_for(n + m, TB), 152 * 8), TB, 0, s>>>(c.x.p, c.y.p, n, c.s_rx.p, c.s_ry.p, m, c.nd_bbox.p);
         VV_LAUNCH_CHECK();
     }
+    VV_CUDA(cudaMemsetAsync(c.nd_parent.p, 0xff, sizeof(int32_t), s));  // the root has none
     k_finalize_root<<<1, 1, 0, s>>>(c.nd_geom.p, c.nd_bbox.p, c.nd_vf.p, c.nd_vl.p, c.nd_sf.p, c.nd_sl.p,
                                     c.nd_ch1.p, c.nd_depth.p, c.nd_path.p, n, m);
     VV_LAUNCH_CHECK();
@@ -677,27 +706,24 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
         ensure_nodes(b + 2 * cnt);
         c.flags.reserve(cnt + 1);
         c.scan.reserve(cnt + 2);
-        k_decide<<<grid_for(cnt, TB), TB, 0, s>>>(a, cnt, c.nd_geom.p, c.nd_vf.p, c.nd_vl.p, c.nd_sf.p, c.nd_sl.p,
-                                                  c.nd_depth.p, min_node, max_node, c.nd_split.p, c.flags.p,
-                                                  c.nd_pivot.p, c.nd_axis.p, err);
-        VV_LAUNCH_CHECK();
-        exclusive_scan(c, c.flags.p, c.scan.p, cnt);
-        k_children<<<grid_for(cnt, TB), TB, 0, s>>>(a, b, cnt, c.nd_split.p, c.scan.p, c.nd_ch1.p, c.nd_depth.p,
-                                                    c.nd_path.p, c.nd_bbox.p, c.nd_nlow.p, c.nd_nlow_s.p);
-        VV_LAUNCH_CHECK();
-        // partition the vortices of each split node: one warp per small node, chunk blocks
-        // over the larger ones
         c.lvl_list.reserve((size_t)cnt + 1);
         c.chunk_node.reserve((size_t)cnt + (size_t)(n / CH) + 2);
-        VV_CUDA(cudaMemsetAsync(c.lvl_cnt.p, 0, 2 * sizeof(int32_t), s));
-        k_route<<<grid_for(cnt, TB), TB, 0, s>>>(a, cnt, c.nd_split.p, c.nd_vf.p, c.nd_vl.p, c.lvl_cnt.p,
-                                                 c.lvl_list.p, c.nd_cbase.p, c.chunk_node.p);
+        k_decide<<<grid_for(cnt, TB), TB, 0, s>>>(a, cnt, c.nd_geom.p, c.nd_vf.p, c.nd_vl.p, c.nd_sf.p, c.nd_sl.p,
+                                                  c.nd_depth.p, min_node, max_node, c.nd_split.p, c.flags.p,
+                                                  c.nd_pivot.p, c.nd_axis.p, err, c.lvl_cnt.p);
+        VV_LAUNCH_CHECK();
+        exclusive_scan(c, c.flags.p, c.scan.p, cnt);
+        // children of the split nodes, then the partition route of each: one warp per small
+        // node, chunk blocks over the larger ones
+        k_route<<<grid_for(cnt, TB), TB, 0, s>>>(a, b, cnt, c.nd_split.p, c.scan.p, c.nd_vf.p, c.nd_vl.p,
+                                                 c.lvl_cnt.p, c.lvl_list.p, c.nd_cbase.p, c.chunk_node.p,
+                                                 c.nd_ch1.p, c.nd_depth.p, c.nd_path.p, c.nd_parent.p, c.nd_bbox.p,
+                                                 c.nd_nlow.p, c.nd_nlow_s.p);
         VV_LAUNCH_CHECK();
         int32_t hc[3];
-        VV_CUDA(cudaMemcpyAsync(hc, c.scan.p + cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        VV_CUDA(cudaMemcpyAsync(hc + 1, c.lvl_cnt.p, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        VV_CUDA(cudaMemcpyAsync(hc, c.lvl_cnt.p, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         VV_CUDA(cudaStreamSynchronize(s));
-        const int32_t nsplit = hc[0], nsmall = hc[1], nchunk = hc[2];
+        const int32_t nsmall = hc[0], nchunk = hc[1], nsplit = hc[2];
         if (nsplit == 0) break;
         if (nsmall > 0) {
             k_small_split<<<grid_for(nsmall, SW), SW * 32, 0, s>>>(c.lvl_list.p, nsmall, c.nd_vf.p, c.nd_vl.p,
@@ -757,27 +783,19 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
     c.nd_cm.reserve(6 * nn);
     c.nd_lc.reserve(nn);
     c.nd_dfs.reserve(nn);
+    c.nd_arrive.reserve(nn);
+    VV_CUDA(cudaMemsetAsync(c.nd_arrive.p, 0, nn * sizeof(int32_t), s));
     k_leaf_cm<<<grid_for(nn, TB), TB, 0, s>>>(nn, c.nd_ch1.p, c.nd_vf.p, c.nd_vl.p, c.nd_geom.p, c.x.p, c.y.p,
                                               c.g.p, c.nd_cm.p, c.nd_lc.p);
     VV_LAUNCH_CHECK();
-    const int64_t nlev = (int64_t)c.level_begin.size() - 1;
-    for (int64_t lv = nlev - 1; lv >= 0; lv--) {
-        int64_t a = c.level_begin[lv], b = c.level_begin[lv + 1];
-        if (b > nn) b = nn;
-        if (b <= a) continue;
-        k_inner_cm<<<grid_for(b - a, TB), TB, 0, s>>>(a, b - a, c.nd_ch1.p, c.nd_geom.p, c.nd_cm.p, c.nd_lc.p);
-        VV_LAUNCH_CHECK();
-    }
+    k_tree_cm<<<grid_for(nn, TB), TB, 0, s>>>(nn, c.nd_ch1.p, c.nd_parent.p, c.nd_geom.p, c.nd_cm.p, c.nd_lc.p,
+                                              c.nd_arrive.p);
+    VV_LAUNCH_CHECK();
     int32_t nl = read_i32(c, c.nd_lc.p);
     c.nleaves = nl;
     c.leaf_node.reserve(nl + 1);
-    for (int64_t lv = 0; lv < nlev; lv++) {
-        int64_t a = c.level_begin[lv], b = c.level_begin[lv + 1];
-        if (b > nn) b = nn;
-        if (b <= a) continue;
-        k_dfs<<<grid_for(b - a, TB), TB, 0, s>>>(a, b - a, c.nd_ch1.p, c.nd_lc.p, c.nd_dfs.p, c.leaf_node.p);
-        VV_LAUNCH_CHECK();
-    }
+    k_tree_dfs<<<grid_for(nn, TB), TB, 0, s>>>(nn, c.nd_ch1.p, c.nd_parent.p, c.nd_lc.p, c.nd_dfs.p, c.leaf_node.p);
+    VV_LAUNCH_CHECK();
     c.lf_vf.reserve(nl + 1); c.lf_vl.reserve(nl + 1); c.lf_sf.reserve(nl + 1); c.lf_sl.reserve(nl + 1);
     c.lf_geom.reserve(nl + 1);
     c.leaf_of.reserve(n + 1);

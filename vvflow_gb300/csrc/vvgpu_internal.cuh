@@ -152,6 +152,7 @@ struct Ctx {
     DArr<int32_t> seg_node_of, seg_node_of2, flags, scan;
     DArr<int32_t> perm;              // tree build: source slot of each slot (keys move, payload follows once)
     DArr<int32_t> nd_cbase, nd_npair;  // tree build: node's first chunk, pairs swapped in its split
+    DArr<int32_t> nd_parent, nd_arrive;  // tree build: parent node; children arrived (bottom-up pass)
     DArr<int32_t> lvl_cnt;           // tree build: per-level counts of warp-split nodes and of chunks
     DArr<int32_t> lvl_list;          // tree build: per-level list of warp-split nodes
     DArr<int32_t> chunk_node, chunk_cnt, chunk_pre;  // tree build: per-level chunks of the larger nodes
