@@ -516,7 +516,7 @@ def batched_arm(args):
     batch = Batch(spaces, 8.0, [wl.node_sizes() for wl in wls], merge=True, move=True)
     # warm-up: one step, then the autotuner's steps (one per host pool size)
     batch.step(nthreads=16)
-    cands = (2, 4, 8, 16, 32)
+    cands = (4, 8, 16, 32, 64)
     nt, _ = batch.autotune(cands)
     for _ in range(max(0, args.warmup - 1 - len(cands))):
         batch.step()
