@@ -106,14 +106,13 @@ __global__ void k_finalize_root(double4* geom, const unsigned long long* bbox, i
 }
 
 // snode::DivideNode leaf rules (TSortedTree.cpp:36-56).
-__global__ void k_decide(int64_t a, int64_t cnt, const double4* __restrict__ geom, const int32_t* __restrict__ vf,
-                         const int32_t* __restrict__ vl, const int32_t* __restrict__ sf, const int32_t* __restrict__ sl,
-                         const int32_t* __restrict__ depth, double min_node, double max_node, int32_t* split,
-                         int32_t* flags, double* pivot, int32_t* axis, int32_t* err, int32_t* counts) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= cnt) return;
-    if (t == 0) counts[0] = counts[1] = 0;  // the route's counters of this level
-    int64_t k = a + t;
+// DivideNode's test (TSortedTree.cpp:36-79): split unless small enough; the split is at the
+// box midpoint across the longer side.  Returns the flag.
+__device__ __forceinline__ int decide_node(int64_t k, const double4* __restrict__ geom, const int32_t* __restrict__ vf,
+                                           const int32_t* __restrict__ vl, const int32_t* __restrict__ sf,
+                                           const int32_t* __restrict__ sl, const int32_t* __restrict__ depth,
+                                           double min_node, double max_node, int32_t* split, double* pivot,
+                                           int32_t* axis, int32_t* err) {
     double4 gm = geom[k];
     double h = gm.z, w = gm.w;
     double mx = smax(h, w), mn = smin(h, w);
@@ -123,10 +122,21 @@ __global__ void k_decide(int64_t a, int64_t cnt, const double4* __restrict__ geo
     int s = leaf ? 0 : 1;
     if (s && depth[k] >= MAX_DEPTH) { s = 0; atomicExch(err, 1); }
     split[k] = s;
-    flags[t] = s;
     bool byx = h < w;
     axis[k] = byx ? 1 : 0;
     pivot[k] = byx ? gm.x : gm.y;
+    return s;
+}
+
+__global__ void k_decide(int64_t a, int64_t cnt, const double4* __restrict__ geom, const int32_t* __restrict__ vf,
+                         const int32_t* __restrict__ vl, const int32_t* __restrict__ sf, const int32_t* __restrict__ sl,
+                         const int32_t* __restrict__ depth, double min_node, double max_node, int32_t* split,
+                         int32_t* flags, double* pivot, int32_t* axis, int32_t* err, int32_t* counts) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    if (t == 0) counts[0] = counts[1] = 0;  // the route's counters of this level
+    const int64_t k = a + t;
+    flags[t] = decide_node(k, geom, vf, vl, sf, sl, depth, min_node, max_node, split, pivot, axis, err);
 }
 
 __device__ __forceinline__ void make_children(int64_t k, int64_t c1, int32_t* ch1, int32_t* depth, int64_t* path,
@@ -537,11 +547,98 @@ __global__ void k_sscatter(int64_t m, int64_t a, int64_t b, const int32_t* __res
     bbox_max_atomic(bb + 3, ry[s]);
 }
 
-__global__ void k_finalize(int64_t a, int64_t cnt, const int32_t* __restrict__ split, const int32_t* __restrict__ ch1,
-                           const int32_t* __restrict__ nlow, const int32_t* __restrict__ nlow_s, int32_t* vf,
-                           int32_t* vl, int32_t* sf, int32_t* sl, double4* geom, const unsigned long long* bbox) {
+// The segment split of one level in one block (m <= SEG1_MAX): classify, scan in shared
+// memory, then the same stable scatter as k_sscatter.
+constexpr int SEG1_MAX = 8192;
+constexpr int SEG1_TB = 1024;
+__global__ void __launch_bounds__(SEG1_TB) k_seg_level(int64_t m, int64_t a, int64_t b,
+                                                      const int32_t* __restrict__ seg_node_of,
+                                                      const int32_t* __restrict__ seg_order,
+                                                      const int32_t* __restrict__ split, const int32_t* __restrict__ axis,
+                                                      const double* __restrict__ pivot, const int32_t* __restrict__ sf,
+                                                      const int32_t* __restrict__ sl, const int32_t* __restrict__ ch1,
+                                                      int32_t* nlow_s, int32_t* seg_order2, int32_t* seg_node_of2,
+                                                      const double* __restrict__ rx, const double* __restrict__ ry,
+                                                      unsigned long long* bbox) {
+    __shared__ int32_t S[SEG1_MAX + 1];
+    __shared__ int32_t wsum[SEG1_TB / 32];
+    __shared__ int32_t carry_s;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) carry_s = 0;
+    __syncthreads();
+    for (int64_t q0 = 0; q0 < m; q0 += SEG1_TB) {
+        const int64_t q = q0 + tid;
+        int f = 0;
+        if (q < m) {
+            const int32_t k = seg_node_of[q];
+            if (in_level_split(k, a, b, split)) {
+                const int32_t sg = seg_order[q];
+                const double key = axis[k] ? rx[sg] : ry[sg];
+                f = key < pivot[k];
+            }
+        }
+        int v = f;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
+        }
+        if (lane == 31) wsum[w] = v;
+        __syncthreads();
+        if (w == 0) {
+            int x = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += u;
+            }
+            wsum[lane] = x;
+        }
+        __syncthreads();
+        const int carry = carry_s;
+        if (q < m) S[q] = carry + (w ? wsum[w - 1] : 0) + v - f;  // exclusive
+        __syncthreads();
+        if (tid == 0) carry_s = carry + wsum[SEG1_TB / 32 - 1];
+        __syncthreads();
+    }
+    if (tid == 0) S[m] = carry_s;
+    __syncthreads();
+    for (int64_t q = tid; q < m; q += SEG1_TB) {
+        const int32_t k = seg_node_of[q];
+        const int32_t sg = seg_order[q];
+        if (!in_level_split(k, a, b, split)) {
+            seg_order2[q] = sg;
+            seg_node_of2[q] = k;
+            continue;
+        }
+        const int32_t f = sf[k], l = sl[k];
+        const int32_t nl = S[l] - S[f];
+        if (q == f) nlow_s[k] = nl;
+        const int32_t before = S[q] - S[f];
+        const bool low = (S[q + 1] - S[q]) != 0;
+        const int32_t nq = low ? f + before : f + nl + ((int32_t)(q - f) - before);
+        const int32_t child = ch1[k] + (low ? 0 : 1);
+        seg_order2[nq] = sg;
+        seg_node_of2[nq] = child;
+        unsigned long long* bb = bbox + 4 * (size_t)child;
+        bbox_min_atomic(bb + 0, rx[sg]);
+        bbox_min_atomic(bb + 1, ry[sg]);
+        bbox_max_atomic(bb + 2, rx[sg]);
+        bbox_max_atomic(bb + 3, ry[sg]);
+    }
+}
+
+// Ranges and boxes of the level's children, then their split decisions: the next level's
+// nodes are [b, b + 2 nsplit) and their flags go to flags[c - b] for its scan.
+__global__ void k_finalize(int64_t a, int64_t b, int64_t cnt, const int32_t* split,
+                           const int32_t* __restrict__ ch1, const int32_t* __restrict__ nlow,
+                           const int32_t* __restrict__ nlow_s, int32_t* vf, int32_t* vl, int32_t* sf, int32_t* sl,
+                           double4* geom, const unsigned long long* bbox, const int32_t* __restrict__ depth,
+                           double min_node, double max_node, int32_t* nsplit_flag, double* pivot, int32_t* axis,
+                           int32_t* err, int32_t* flags, int32_t* counts) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= cnt) return;
+    if (t == 0) counts[0] = counts[1] = 0;  // the next level's route counters
     int64_t k = a + t;
     if (!split[k]) return;
     int32_t c1 = ch1[k], c2 = c1 + 1;
@@ -551,6 +648,10 @@ __global__ void k_finalize(int64_t a, int64_t cnt, const int32_t* __restrict__ s
     sf[c2] = sf[k] + nlow_s[k]; sl[c2] = sl[k];
     geom[c1] = geom_from_bbox(bbox + 4 * (size_t)c1);
     geom[c2] = geom_from_bbox(bbox + 4 * (size_t)c2);
+    for (int q = 0; q < 2; q++) {
+        const int64_t c = c1 + q;
+        flags[c - b] = decide_node(c, geom, vf, vl, sf, sl, depth, min_node, max_node, nsplit_flag, pivot, axis, err);
+    }
 }
 
 // ---- centroids (snode::CalculateCMass, TSortedTree.cpp:150-197) and depth-first order ----
@@ -704,14 +805,18 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
         int64_t a = c.level_begin[d], b = c.level_begin[d + 1], cnt = b - a;
         if (cnt <= 0) break;
         ensure_nodes(b + 2 * cnt);
-        c.flags.reserve(cnt + 1);
+        // this level's flags come from the previous level's k_finalize (kept); the next
+        // level's (up to 2 cnt) are written by this level's
+        c.flags.reserve(2 * cnt + 2, true, cnt + 1, s);
         c.scan.reserve(cnt + 2);
         c.lvl_list.reserve((size_t)cnt + 1);
         c.chunk_node.reserve((size_t)cnt + (size_t)(n / CH) + 2);
-        k_decide<<<grid_for(cnt, TB), TB, 0, s>>>(a, cnt, c.nd_geom.p, c.nd_vf.p, c.nd_vl.p, c.nd_sf.p, c.nd_sl.p,
-                                                  c.nd_depth.p, min_node, max_node, c.nd_split.p, c.flags.p,
-                                                  c.nd_pivot.p, c.nd_axis.p, err, c.lvl_cnt.p);
-        VV_LAUNCH_CHECK();
+        if (d == 0) {
+            k_decide<<<grid_for(cnt, TB), TB, 0, s>>>(a, cnt, c.nd_geom.p, c.nd_vf.p, c.nd_vl.p, c.nd_sf.p, c.nd_sl.p,
+                                                      c.nd_depth.p, min_node, max_node, c.nd_split.p, c.flags.p,
+                                                      c.nd_pivot.p, c.nd_axis.p, err, c.lvl_cnt.p);
+            VV_LAUNCH_CHECK();
+        }
         exclusive_scan(c, c.flags.p, c.scan.p, cnt);
         // children of the split nodes, then the partition route of each: one warp per small
         // node, chunk blocks over the larger ones
@@ -746,7 +851,14 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
                                                c.tab_rl.p, c.tab_lh.p, c.x.p, c.y.p, c.perm.p);
             VV_LAUNCH_CHECK();
         }
-        if (m > 0) {
+        if (m > 0 && m <= SEG1_MAX) {
+            k_seg_level<<<1, SEG1_TB, 0, s>>>(m, a, b, c.seg_node_of.p, c.seg_order.p, c.nd_split.p, c.nd_axis.p,
+                                              c.nd_pivot.p, c.nd_sf.p, c.nd_sl.p, c.nd_ch1.p, c.nd_nlow_s.p,
+                                              c.seg_order2.p, c.seg_node_of2.p, c.s_rx.p, c.s_ry.p, c.nd_bbox.p);
+            VV_LAUNCH_CHECK();
+            std::swap(c.seg_order, c.seg_order2);
+            std::swap(c.seg_node_of, c.seg_node_of2);
+        } else if (m > 0) {
             k_sclass<<<grid_for(m, TB), TB, 0, s>>>(m, a, b, c.seg_node_of.p, c.seg_order.p, c.nd_split.p,
                                                     c.nd_axis.p, c.nd_pivot.p, c.s_rx.p, c.s_ry.p, c.flags.p);
             VV_LAUNCH_CHECK();
@@ -759,9 +871,10 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
             std::swap(c.seg_order, c.seg_order2);
             std::swap(c.seg_node_of, c.seg_node_of2);
         }
-        k_finalize<<<grid_for(cnt, TB), TB, 0, s>>>(a, cnt, c.nd_split.p, c.nd_ch1.p, c.nd_nlow.p, c.nd_nlow_s.p,
+        k_finalize<<<grid_for(cnt, TB), TB, 0, s>>>(a, b, cnt, c.nd_split.p, c.nd_ch1.p, c.nd_nlow.p, c.nd_nlow_s.p,
                                                     c.nd_vf.p, c.nd_vl.p, c.nd_sf.p, c.nd_sl.p, c.nd_geom.p,
-                                                    c.nd_bbox.p);
+                                                    c.nd_bbox.p, c.nd_depth.p, min_node, max_node, c.nd_split.p,
+                                                    c.nd_pivot.p, c.nd_axis.p, err, c.flags.p, c.lvl_cnt.p);
         VV_LAUNCH_CHECK();
         c.level_begin.push_back(b + 2 * (int64_t)nsplit);
         c.nnodes = b + 2 * (int64_t)nsplit;
