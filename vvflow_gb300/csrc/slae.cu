@@ -582,6 +582,9 @@ void slae(Ctx& c, vvgpu_body_out* out) {
         VV_LAUNCH_CHECK();
     };
     apply_inv(c.B.p, c.X.p, false);
+    // refine until |r|^2 <= 1e-26 |b|^2, or until a correction stops paying (the residual
+    // falls by less than 4x: it has reached the rounding floor of its own FP64 evaluation)
+    double r2_prev = INFINITY;
     for (int it = 0; it < 12; it++) {
         k_residual<<<gg, 256, 0, s>>>(n, c.A.p, c.X.p, c.B.p, r.p, sq.p);
         VV_LAUNCH_CHECK();
@@ -595,6 +598,8 @@ void slae(Ctx& c, vvgpu_body_out* out) {
         VV_CUDA(cudaMemcpyAsync(h, acc, 16, cudaMemcpyDeviceToHost, s));
         VV_CUDA(cudaStreamSynchronize(s));
         if (!(h[0] > 1e-26 * h[1])) break;
+        if (!(h[0] < 0.25 * r2_prev)) break;
+        r2_prev = h[0];
         apply_inv(r.p, c.X.p, true);
     }
     int64_t maxcnt = 0;
