@@ -236,14 +236,14 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
     unsigned long long ncand = 0;
     for (int32_t c0 = v0; c0 < v1; c0 += 8) {
         const int32_t tb = c0 + grp * DT;  // first target of this lane's group
-        float tx[DT], ty[DT], ief[DT], ie2[DT], b16[DT];
+        float tx[DT], ty[DT], ief[DT], ie2[DT], b16[DT], iefl[DT];
         unsigned act = 0, pos = 0;  // bit t: target t active / positive
         float bx0 = INFINITY, by0 = INFINITY, bx1 = -INFINITY, by1 = -INFINITY, rmax = 0.f;
 #pragma unroll
         for (int t = 0; t < DT; t++) {
             const int32_t i = tb + t;
             const unsigned long long gb = (i < v1) ? (unsigned long long)__double_as_longlong(a.g[i]) : 0ull;
-            tx[t] = ty[t] = ief[t] = ie2[t] = b16[t] = 0.f;
+            tx[t] = ty[t] = ief[t] = ie2[t] = b16[t] = iefl[t] = 0.f;
             if ((gb << 1) != 0ull) {  // g != 0 and its sign from the bit pattern (integer pipe)
                 act |= 1u << t;
                 if ((gb >> 63) == 0ull) pos |= 1u << t;
@@ -251,6 +251,7 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
                 tx[t] = r4.x; ty[t] = r4.y;
                 ief[t] = a.src_ie[i];
                 ie2[t] = ief[t] * ief[t];
+                iefl[t] = ief[t] * 1.4426950408889634f;  // log2(e) / eps
                 b16[t] = 16.f * ief[t] * (1.f + 1e-3f);
                 bx0 = fminf(bx0, r4.x); by0 = fminf(by0, r4.y);
                 bx1 = fmaxf(bx1, r4.x); by1 = fmaxf(by1, r4.y);
@@ -326,6 +327,9 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
             float Dm = 0.f;
             for (int h = 0; h < nh; h++) Dm = fmaxf(Dm, s_hitb[wq][h].x);
             const float tiny = 2.f * Dm + 1e-9f, tiny2 = tiny * tiny;
+            float bndv[DT];  // each target's band half-width for this batch
+#pragma unroll
+            for (int t = 0; t < DT; t++) bndv[t] = fmaf(b16[t], Dm, bandc);
             for (int32_t kb = 0; kb < total; kb += SRC_CAP) {
                 const int32_t nst = min(SRC_CAP, total - kb);
                 // stage the sources (shifted into L's frame) once per warp
@@ -358,13 +362,16 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
                         const float dx = tx[t] - sv.x, dy = ty[t] - sv.y;
                         const float r2 = dx * dx + dy * dy;
                         const float du = r2 * ie2[t] - 64.f;  // (|dr| / eps)^2 - 64
-                        const float bnd = fmaf(b16[t], Dm, bandc);
+                        const float bnd = bndv[t];
                         const bool sm = (same >> t) & 1u;
                         if (sm && (fabsf(du) < bnd || r2 < tiny2)) pend |= 1u << t;
                         const bool in = sm && du <= -bnd && r2 >= tiny2;
                         const float r2c = in ? r2 : 1.f;
                         const float rs = rsqrtf(r2c);
-                        const float tv = in ? sv.z * __expf(-(r2c * rs) * ief[t]) : 0.f;
+                        // exp(-|dr| / eps) as 2^(-|dr| (log2(e) / eps)), one MUFU ex2
+                        float ex2v;
+                        asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex2v) : "f"(-(r2c * rs) * iefl[t]));
+                        const float tv = in ? sv.z * ex2v : 0.f;
                         const float qv = tv * rs;
                         p2x[t] = fmaf(dx, qv, p2x[t]);
                         p2y[t] = fmaf(dy, qv, p2y[t]);
