@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
                                           d64[6 * t + 1][lane], d64[6 * t + 2][lane]);
                         }
                     }
-                    if (++since == 16) {
+                    if (++since == 32) {
                         since = 0;
 #pragma unroll
                         for (int t = 0; t < DT; t++) {
