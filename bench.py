@@ -77,44 +77,113 @@ def workload(n, m, rank):
 # ---------------------------------------------------------------------------------------
 # clocks
 class Clocks:
+    """SM clock, power and clock-event reasons sampled while the timed region runs.
+
+    A background thread polls NVML (libnvidia-ml through ctypes; read-only queries) every
+    10 ms, so even a sub-second timed region gets tens of samples; when NVML cannot be
+    loaded, `nvidia-smi -lms 100` is polled instead.  `device` is the CUDA ordinal (the
+    NVML handle is looked up by the device's UUID, which CUDA_VISIBLE_DEVICES does not
+    renumber)."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits
+    REASON_BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+                   0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
-    def __init__(self, bus_id=None):
+    def __init__(self, device=None):
+        self.rows = []  # (sm_mhz, max_mhz, power_w, reason_bits)
+        self.p = None
+        self.thread = None
+        self.source = "unavailable"
+        if self._start_nvml(device):
+            return
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
-        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
-        if bus_id:
-            cmd += ["-i", bus_id]
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100"]
         try:
             self.p = subprocess.Popen(cmd, stdout=self.f, stderr=subprocess.DEVNULL)
+            self.source = "nvidia-smi -lms 100"
         except OSError:
             self.p = None
 
+    def _start_nvml(self, device):
+        import ctypes
+        import threading
+        try:
+            import torch
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return False
+            h = ctypes.c_void_p()
+            dev = torch.cuda.current_device() if device is None else device
+            uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+            if lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(h)) != 0:
+                return False
+            reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        except Exception:
+            return False
+        self.stop_flag = threading.Event()
+
+        def run():
+            clk, mx, pw, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+            while not self.stop_flag.is_set():
+                ok = lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0  # NVML_CLOCK_SM
+                ok = ok and lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0
+                ok = ok and reasons(h, ctypes.byref(rs)) == 0
+                if ok:
+                    p = pw.value / 1e3 if lib.nvmlDeviceGetPowerUsage(h, ctypes.byref(pw)) == 0 else float("nan")
+                    self.rows.append((float(clk.value), float(mx.value), p, int(rs.value)))
+                self.stop_flag.wait(0.01)
+
+        self.thread = threading.Thread(target=run, daemon=True)
+        self.thread.start()
+        self.source = "NVML every 10 ms"
+        return True
+
     def stop(self):
+        if self.thread is not None:
+            self.stop_flag.set()
+            self.thread.join(5)
+            return self.summary(self.rows, self.source)
+        rows = []
         if self.p:
             self.p.terminate()
             try:
                 self.p.wait(5)
             except Exception:
                 self.p.kill()
-        self.f.flush()
-        rows = []
-        try:
-            for line in open(self.f.name):
-                parts = [x.strip() for x in line.split(",")]
-                if len(parts) >= 9:
-                    rows.append(parts)
-        finally:
-            os.unlink(self.f.name)
+            self.f.flush()
+            try:
+                for line in open(self.f.name):
+                    parts = [x.strip() for x in line.split(",")]
+                    if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                        bits = 0
+                        for k, b in enumerate((0x8, 0x40, 0x20, 0x4)):
+                            if "Active" in parts[5 + k] and "Not" not in parts[5 + k]:
+                                bits |= b
+                        mx = float(parts[2]) if parts[2].replace(".", "").isdigit() else float("nan")
+                        try:
+                            pw = float(parts[3])
+                        except ValueError:
+                            pw = float("nan")
+                        rows.append((float(parts[1]), mx, pw, bits))
+            finally:
+                os.unlink(self.f.name)
+        return self.summary(rows, self.source)
+
+    @classmethod
+    def summary(cls, rows, source):
         if not rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k] and "Not" not in r[5 + k]})
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0,
+                    "source": source}
+        sm = np.array([r[0] for r in rows])
+        mx = [r[1] for r in rows if r[1] == r[1]]
+        pw = [r[2] for r in rows if r[2] == r[2]]
+        reasons = sorted({name for r in rows for bit, name in cls.REASON_BITS.items() if r[3] & bit})
+        return {"sm_mhz": float(np.median(sm)), "sm_min_mhz": float(sm.min()),
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows),
+                "power_w_median": round(float(np.median(pw)), 1) if pw else None, "source": source}
 
 
 # ---------------------------------------------------------------------------------------
@@ -208,13 +277,7 @@ def gpu_arm(args):
     st0 = S.stats()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    bus = None
-    try:
-        bus = torch.cuda.get_device_properties(local).pci_bus_id if hasattr(
-            torch.cuda.get_device_properties(local), "pci_bus_id") else None
-    except Exception:
-        bus = None
-    clk = Clocks(None)
+    clk = Clocks(local)
     barrier()
     torch.cuda.synchronize()
     e0.record()

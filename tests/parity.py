@@ -84,8 +84,12 @@ def check_exact(ref, got, keys=None, prefix=""):
     return bad
 
 
-def check_step(ref, got, *, vel_tol, diff_tol, fric_tol, slae_tol, exact=True, prefix=""):
-    """Returns a list of failure strings (empty = pass)."""
+def check_step(ref, got, *, vel_tol, diff_tol, fric_tol, slae_tol, slae_rhs_tol=None, slae_x_tol=None, exact=True,
+               prefix=""):
+    """Returns a list of failure strings (empty = pass).  The SLAE right-hand side and
+    solution default to 10x and 100x the matrix tolerance."""
+    slae_rhs_tol = slae_tol * 10 if slae_rhs_tol is None else slae_rhs_tol
+    slae_x_tol = slae_tol * 100 if slae_x_tol is None else slae_x_tol
     bad = []
     if exact:
         keys = [k[len(prefix):] for k in ref if k.startswith(prefix)
@@ -109,11 +113,11 @@ def check_step(ref, got, *, vel_tol, diff_tol, fric_tol, slae_tol, exact=True, p
         if not e <= slae_tol:
             bad.append(f"{p}slae matrix rel err {e:.3e}")
         e = rel_err(got[p + "slae_b"], ref[p + "slae_b"])
-        if not e <= slae_tol * 10:
-            bad.append(f"{p}slae rhs rel err {e:.3e}")
+        if not e <= slae_rhs_tol:
+            bad.append(f"{p}slae rhs rel err {e:.3e} > {slae_rhs_tol:.1e}")
         e = rel_err(got[p + "slae_x"], ref[p + "slae_x"])
-        if not e <= slae_tol * 100:
-            bad.append(f"{p}slae solution rel err {e:.3e}")
+        if not e <= slae_x_tol:
+            bad.append(f"{p}slae solution rel err {e:.3e} > {slae_x_tol:.1e}")
     return bad
 
 

@@ -264,6 +264,7 @@ int vvgpu_add_body(vvgpu_ctx* h, int64_t nseg, const double* cx, const double* c
         VV_CUDA(cudaMemsetAsync(a->p + m0, 0, nseg * sizeof(double), s));
     c.segs_dirty = true;
     c.lu_valid = false;
+    c.seg_version++;
     API_END
 }
 
@@ -296,6 +297,7 @@ int vvgpu_clear_bodies(vvgpu_ctx* h) {
     c.h_slip.clear();
     c.segs_dirty = true;
     c.lu_valid = false;
+    c.seg_version++;
     API_END
 }
 

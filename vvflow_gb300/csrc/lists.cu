@@ -126,13 +126,6 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return r;
 }
 
-__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
-    float s = hi + v;
-    float bp = s - hi;
-    lo += (hi - (s - bp)) + (v - bp);
-    hi = s;
-}
-
 // Per-leaf walk (one thread per leaf) for selected leaves only (sel[L] != 0).
 // PASS 0 counts, PASS 1 writes at the offsets.  Bit 1 of `what`: near runs (near_cnt /
 // near_off / near_run); bit 2: far nodes (far_cnt / far_off / far_node).  Unselected leaves

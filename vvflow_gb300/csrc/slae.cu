@@ -15,6 +15,7 @@
 // FP64; FP32 mode inverts in FP32.  Either way x = inv b is refined with FP64 residuals
 // r = b - A x until |r| / |b| < 1e-13 (at most 12 sweeps).
 #include <cfloat>
+#include <cstring>
 
 #include "vvgpu_internal.cuh"
 
@@ -94,7 +95,21 @@ struct FillArgs {
     bool rhs_only;
 };
 
+// 0.5 log(dr2 / dr1) in FP32 for a point clear of both smoothing discs; d = point - corner
+// 1, dr2 - dr1 = |dl|^2 - 2 d.dl exactly, so a ratio near 1 goes through log1p of that
+// difference instead of a cancelling quotient.
+__device__ __forceinline__ float half_log_ratio(float dr1, float dr2, float dx, float dy, float dlx, float dly,
+                                                float dl2) {
+    const float q = dr2 / dr1;
+    if (q > 0.5f && q < 2.f) return 0.5f * log1pf((dl2 - 2.f * (dx * dlx + dy * dly)) / dr1);
+    return 0.5f * logf(q);
+}
+
 // One block per slip row: RHS through the tree, then (unless rhs_only) the M + 3 nb cells.
+// F32: the RHS pairs clear of both smoothing discs (the reference's log branch, decided
+// with a 1e-4 margin) and the far centroids run in FP32 with compensated sums; every other
+// pair takes the FP64 formula.  The matrix cells are FP64 in both modes.
+template <bool F32>
 __global__ void k_slip_rows(FillArgs a) {
     __shared__ double sh[32];
     const int64_t ri = blockIdx.x;
@@ -112,20 +127,52 @@ __global__ void k_slip_rows(FillArgs a) {
     }
     const int32_t L = a.dfs[k];
     double part = 0;
+    const double c1x = a.S.cx[s], c1y = a.S.cy[s], c2x = c1x + dlx, c2y = c1y + dly;
+    const float dlxf = (float)dlx, dlyf = (float)dly, dl2f = (float)(dlx * dlx + dly * dly);
+    float ph = 0.f, pl = 0.f;
     for (int32_t r = a.near_off[L]; r < a.near_off[L + 1]; r++) {
         int2 run = a.near_run[r];
         for (int32_t j = a.lvf[run.x] + threadIdx.x; j < a.lvl[run.y - 1]; j += blockDim.x) {
             double gj = a.g[j];
             if (gj == 0.) continue;
-            part += xi_g(a.S, a.x[j], a.y[j], s, 1. / a.ie[j]) * gj;
+            if (F32) {
+                const double xj = a.x[j], yj = a.y[j], iej = a.ie[j];
+                const float dx = (float)(xj - c1x), dy = (float)(yj - c1y);
+                const float ex = dx - dlxf, ey = dy - dlyf;
+                const float dr1 = dx * dx + dy * dy, dr2 = ex * ex + ey * ey;
+                const float ie2 = (float)iej * (float)iej;
+                if (dr1 * ie2 > 1.0001f && dr2 * ie2 > 1.0001f) {  // false for NaN
+                    two_sum_acc(ph, pl, half_log_ratio(dr1, dr2, dx, dy, dlxf, dlyf, dl2f) * (float)gj);
+                    continue;
+                }
+                part += xi_g(a.S, xj, yj, s, 1. / iej) * gj;
+            } else {
+                part += xi_g(a.S, a.x[j], a.y[j], s, 1. / a.ie[j]) * gj;
+            }
         }
     }
-    const double c1x = a.S.cx[s], c1y = a.S.cy[s], c2x = c1x + dlx, c2y = c1y + dly;
     for (int32_t t = a.far_off[L] + threadIdx.x; t < a.far_off[L + 1]; t += blockDim.x) {
         const double* c = a.cm + 6 * (size_t)a.far_node[t];
-        part += xi_g_dist(c[0], c[1], c1x, c1y, c2x, c2y) * c[2];
-        part += xi_g_dist(c[3], c[4], c1x, c1y, c2x, c2y) * c[5];
+        if (F32) {
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const double px = c[3 * h], py = c[3 * h + 1], g = c[3 * h + 2];
+                const float dx = (float)(px - c1x), dy = (float)(py - c1y);
+                const float ex = dx - dlxf, ey = dy - dlyf;
+                const float dr1 = dx * dx + dy * dy, dr2 = ex * ex + ey * ey;
+                if (dr1 > 1e-30f && dr2 > 1e-30f && dr1 < 1e30f && dr2 < 1e30f) {
+                    // a finite log times g: an empty sign (g = 0) adds exactly 0
+                    if (g != 0.) two_sum_acc(ph, pl, half_log_ratio(dr1, dr2, dx, dy, dlxf, dlyf, dl2f) * (float)g);
+                } else {
+                    part += xi_g_dist(px, py, c1x, c1y, c2x, c2y) * g;
+                }
+            }
+        } else {
+            part += xi_g_dist(c[0], c[1], c1x, c1y, c2x, c2y) * c[2];
+            part += xi_g_dist(c[3], c[4], c1x, c1y, c2x, c2y) * c[5];
+        }
     }
+    if (F32) part += (double)ph + (double)pl;
     double node_inf = block_sum(part, sh);
     if (threadIdx.x == 0) {
         double rhs = (-a.inf_vy) * dlx + a.inf_vx * dly;
@@ -489,10 +536,26 @@ void slae(Ctx& c, vvgpu_body_out* out) {
             d.special = b.p.special_segment_no; d.kutta = b.p.bc_kutta;
         }
     }
-    DArr<int32_t> dmaps;
+    int inf_body = -1;
+    for (int bi = 0; bi < nb; bi++)
+        if (!c.bodies[bi].p.bc_kutta) { inf_body = bi; break; }
+    // Everything the matrix cells depend on.  While it is unchanged and the inverse is
+    // cached, only the right-hand side is filled (the reference likewise refills just its
+    // right column once the body matrix and its inverse are in place,
+    // MConvectiveFast.cpp:245-246).
+    std::vector<double> sig{(double)n, (double)nb, (double)c.precision, c.dt, (double)inf_body,
+                            (double)c.seg_version};
+    for (int bi = 0; bi < nb; bi++) {
+        const BodyDev& d = bd[bi];
+        sig.insert(sig.end(), {(double)bfirst[bi], (double)bcount[bi], d.area, d.cofx, d.cofy, d.axx, d.axy, d.moi,
+                               d.dens, (double)d.special, (double)d.kutta});
+    }
+    const bool rhs_only = c.lu_valid && c.lu_precision == c.precision && c.neq_cached == n &&
+                          sig.size() == c.slae_sig.size() &&
+                          std::memcmp(sig.data(), c.slae_sig.data(), sig.size() * sizeof(double)) == 0;
     const size_t nsl = slip_rows.size();
-    dmaps.reserve(3 * nb + 2 * n + nsl + 1);
-    int32_t* d_col0 = dmaps.p;
+    c.slae_maps.reserve(3 * nb + 2 * n + nsl + 1);
+    int32_t* d_col0 = c.slae_maps.p;
     int32_t* d_bfirst = d_col0 + nb;
     int32_t* d_bcount = d_bfirst + nb;
     int32_t* d_rowseg = d_bcount + nb;
@@ -504,14 +567,14 @@ void slae(Ctx& c, vvgpu_body_out* out) {
     VV_CUDA(cudaMemcpyAsync(d_rowseg, row_seg.data(), n * 4, cudaMemcpyHostToDevice, s));
     VV_CUDA(cudaMemcpyAsync(d_rowbody, row_body.data(), n * 4, cudaMemcpyHostToDevice, s));
     if (nsl) VV_CUDA(cudaMemcpyAsync(d_slip, slip_rows.data(), nsl * 4, cudaMemcpyHostToDevice, s));
-    DArr<BodyDev> dbd;
-    dbd.reserve(nb);
-    VV_CUDA(cudaMemcpyAsync(dbd.p, bd.data(), nb * sizeof(BodyDev), cudaMemcpyHostToDevice, s));
+    c.slae_bodies.reserve((nb * sizeof(BodyDev) + sizeof(double) - 1) / sizeof(double));
+    BodyDev* dbd = reinterpret_cast<BodyDev*>(c.slae_bodies.p);
+    VV_CUDA(cudaMemcpyAsync(dbd, bd.data(), nb * sizeof(BodyDev), cudaMemcpyHostToDevice, s));
 
     c.A.reserve(n * n);
     c.B.reserve(n);
     c.X.reserve(n);
-    VV_CUDA(cudaMemsetAsync(c.A.p, 0, n * n * sizeof(double), s));
+    if (!rhs_only) VV_CUDA(cudaMemsetAsync(c.A.p, 0, n * n * sizeof(double), s));
     VV_CUDA(cudaMemsetAsync(c.B.p, 0, n * sizeof(double), s));
     FillArgs fa{};
     fa.n = n; fa.A = c.A.p; fa.B = c.B.p;
@@ -524,22 +587,20 @@ void slae(Ctx& c, vvgpu_body_out* out) {
     fa.x = c.x.p; fa.y = c.y.p; fa.g = c.g.p; fa.ie = c.ie.p;
     fa.ns = c.ns; fa.kx = c.k_x.p; fa.ky = c.k_y.p; fa.kg = c.k_g.p; fa.sink_e2 = c.dt * C_1_PI;
     fa.inf_vx = c.inf_vx; fa.inf_vy = c.inf_vy;
-    fa.rhs_only = false;
+    fa.rhs_only = rhs_only;
     if (nsl) {
-        k_slip_rows<<<(unsigned)nsl, 256, 0, s>>>(fa);
+        if (c.precision == VVGPU_FP32) k_slip_rows<true><<<(unsigned)nsl, 256, 0, s>>>(fa);
+        else k_slip_rows<false><<<(unsigned)nsl, 256, 0, s>>>(fa);
         VV_LAUNCH_CHECK();
     }
-    int inf_body = -1;
-    for (int bi = 0; bi < nb; bi++)
-        if (!c.bodies[bi].p.bc_kutta) { inf_body = bi; break; }
-    k_body_rows<<<nb, 256, 0, s>>>(n, c.A.p, c.B.p, dbd.p, nb, d_col0, d_bcount, c.s_cy.p, c.s_cx.p, d_bfirst, c.dt,
-                                   gs, c.inf_g, c.grav_x, c.grav_y, inf_body, false);
+    k_body_rows<<<nb, 256, 0, s>>>(n, c.A.p, c.B.p, dbd, nb, d_col0, d_bcount, c.s_cy.p, c.s_cx.p, d_bfirst, c.dt,
+                                   gs, c.inf_g, c.grav_x, c.grav_y, inf_body, rhs_only);
     VV_LAUNCH_CHECK();
 
     // reuse the cached inverse while the matrix bytes are unchanged
-    bool same = false;
+    bool same = rhs_only;
     int32_t* singular = (int32_t*)(c.counters.p + 6);
-    if (c.lu_valid && c.lu_precision == c.precision && c.neq_cached == n) {
+    if (!rhs_only && c.lu_valid && c.lu_precision == c.precision && c.neq_cached == n) {
         int32_t* diff = (int32_t*)(c.counters.p + 7);
         VV_CUDA(cudaMemsetAsync(diff, 0, 4, s));
         k_differs<<<grid_for(n * n, 256), 256, 0, s>>>(n * n, (const unsigned long long*)c.A.p,
@@ -569,10 +630,12 @@ void slae(Ctx& c, vvgpu_body_out* out) {
         c.lu_precision = c.precision;
         c.neq_cached = n;
     }
+    c.slae_sig = std::move(sig);
     // x = inv b, then FP64 iterative refinement
-    DArr<double> r, sq;
-    r.reserve(n);
-    sq.reserve(2 * (size_t)n);
+    c.slae_r.reserve(n);
+    c.slae_sq.reserve(2 * (size_t)n);
+    DArr<double>& r = c.slae_r;
+    DArr<double>& sq = c.slae_sq;
     c.sum_part.reserve(2 * SUM_BLOCKS);
     double* acc = (double*)(c.counters.p + 8);
     const unsigned gg = grid_for(n, 8);

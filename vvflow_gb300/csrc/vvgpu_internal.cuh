@@ -228,6 +228,11 @@ struct Ctx {
     bool lu_valid = false;
     int lu_precision = 0;
     int64_t neq_cached = 0;
+    std::vector<double> slae_sig;   // inputs of the matrix in A (A is reused while they are equal)
+    uint64_t seg_version = 0;       // bumped whenever the segment geometry changes
+    DArr<int32_t> slae_maps;        // column / row maps of the system
+    DArr<double> slae_bodies;       // per-body row data
+    DArr<double> slae_r, slae_sq;   // refinement residual and its squared terms
     vvgpu_stats stats{};
     int64_t launches = 0;           // kernels launched by this context
     int64_t eps_evaluations = 0;    // target evaluations over the rounds of the last epsilon pass
@@ -246,6 +251,13 @@ __device__ __forceinline__ double dabs2(double x, double y) { return dadd(dmul(x
 __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
 __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double dsgn(double v) { return (v > 0) ? 1. : ((v < 0) ? -1. : 0.); }
+// Compensated FP32 accumulation (Knuth's TwoSum): hi + lo carries the running sum.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
+    float s = hi + v;
+    float bp = s - hi;
+    lo += (hi - (s - bp)) + (v - bp);
+    hi = s;
+}
 
 // Order-preserving map double -> uint64 for atomicMin/atomicMax on doubles.
 __device__ __forceinline__ unsigned long long dkey(double v) {

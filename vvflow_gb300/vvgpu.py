@@ -387,6 +387,16 @@ class GpuSpace:
         self._ok(self.lib.vvgpu_get_body_params(self.h, int(b), C.byref(bp)), "get_body_params")
         return {k: getattr(bp, k) for k, _ in BodyParams._fields_}
 
+    def set_body_params(self, b: int = 0, **changes):
+        """Updates the named fields of body b's parameters (vvgpu_body_params)."""
+        bp = BodyParams()
+        self._ok(self.lib.vvgpu_get_body_params(self.h, int(b), C.byref(bp)), "get_body_params")
+        for k, v in changes.items():
+            if k not in dict(BodyParams._fields_):
+                raise KeyError(k)
+            setattr(bp, k, v)
+        self._ok(self.lib.vvgpu_set_body_params(self.h, int(b), C.byref(bp)), "set_body_params")
+
     def calc_forces(self) -> np.ndarray:
         """Space::calc_forces (TSpace.cpp:94-117); per body [friction x, y, o, nusselt]."""
         out = np.zeros((self.nbodies, 4))
