@@ -180,9 +180,14 @@ int vvgpu_ctx_destroy(vvgpu_ctx* h) {
     Ctx& c = h->c;
     cudaSetDevice(c.device);
     cudaStreamSynchronize(c.stream);
-    cudaStream_t own = c.own_stream;
+    if (c.side) cudaStreamSynchronize(c.side);
+    cudaStream_t own = c.own_stream, side = c.side;
+    cudaEvent_t e1 = c.ev_fork, e2 = c.ev_join;
     delete h;  // device arrays are released by their destructors
     if (own) cudaStreamDestroy(own);
+    if (side) cudaStreamDestroy(side);
+    if (e1) cudaEventDestroy(e1);
+    if (e2) cudaEventDestroy(e2);
     return VVGPU_OK;
 }
 

@@ -800,6 +800,7 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
     VV_LAUNCH_CHECK();
 
     c.level_begin.assign({0, 1});
+    cudaStream_t side = side_stream(c);
     int64_t d = 0;
     for (;; d++) {
         int64_t a = c.level_begin[d], b = c.level_begin[d + 1], cnt = b - a;
@@ -825,17 +826,43 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
                                                  c.nd_ch1.p, c.nd_depth.p, c.nd_path.p, c.nd_parent.p, c.nd_bbox.p,
                                                  c.nd_nlow.p, c.nd_nlow_s.p);
         VV_LAUNCH_CHECK();
+        // The segment split and the warp-per-node splits touch other data than the chunk
+        // partition (other nodes' ranges; the children's boxes only through atomic min/max),
+        // so they run on the side stream, joined before k_finalize.
+        const bool seg1 = m > 0 && m <= SEG1_MAX;
+        if (seg1) {
+            VV_CUDA(cudaEventRecord(c.ev_fork, s));
+            VV_CUDA(cudaStreamWaitEvent(side, c.ev_fork, 0));
+            k_seg_level<<<1, SEG1_TB, 0, side>>>(m, a, b, c.seg_node_of.p, c.seg_order.p, c.nd_split.p,
+                                                 c.nd_axis.p, c.nd_pivot.p, c.nd_sf.p, c.nd_sl.p, c.nd_ch1.p,
+                                                 c.nd_nlow_s.p, c.seg_order2.p, c.seg_node_of2.p, c.s_rx.p, c.s_ry.p,
+                                                 c.nd_bbox.p);
+            VV_LAUNCH_CHECK();
+            std::swap(c.seg_order, c.seg_order2);
+            std::swap(c.seg_node_of, c.seg_node_of2);
+        }
         int32_t hc[3];
         VV_CUDA(cudaMemcpyAsync(hc, c.lvl_cnt.p, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         VV_CUDA(cudaStreamSynchronize(s));
         const int32_t nsmall = hc[0], nchunk = hc[1], nsplit = hc[2];
-        if (nsplit == 0) break;
+        if (nsplit == 0) {
+            if (seg1) {  // nothing split: the side stream's copy of the segment order is unchanged
+                VV_CUDA(cudaEventRecord(c.ev_join, side));
+                VV_CUDA(cudaStreamWaitEvent(s, c.ev_join, 0));
+            }
+            break;
+        }
         if (nsmall > 0) {
-            k_small_split<<<grid_for(nsmall, SW), SW * 32, 0, s>>>(c.lvl_list.p, nsmall, c.nd_vf.p, c.nd_vl.p,
-                                                                   c.nd_axis.p, c.nd_pivot.p, c.nd_ch1.p, c.x.p,
-                                                                   c.y.p, c.perm.p, c.nd_nlow.p, c.nd_bbox.p);
+            if (!seg1) {
+                VV_CUDA(cudaEventRecord(c.ev_fork, s));
+                VV_CUDA(cudaStreamWaitEvent(side, c.ev_fork, 0));
+            }
+            k_small_split<<<grid_for(nsmall, SW), SW * 32, 0, side>>>(c.lvl_list.p, nsmall, c.nd_vf.p, c.nd_vl.p,
+                                                                      c.nd_axis.p, c.nd_pivot.p, c.nd_ch1.p, c.x.p,
+                                                                      c.y.p, c.perm.p, c.nd_nlow.p, c.nd_bbox.p);
             VV_LAUNCH_CHECK();
         }
+        const bool forked = seg1 || nsmall > 0;
         if (nchunk > 0) {
             c.chunk_cnt.reserve((size_t)nchunk + 1);
             c.chunk_pre.reserve((size_t)nchunk + 1);
@@ -851,14 +878,7 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
                                                c.tab_rl.p, c.tab_lh.p, c.x.p, c.y.p, c.perm.p);
             VV_LAUNCH_CHECK();
         }
-        if (m > 0 && m <= SEG1_MAX) {
-            k_seg_level<<<1, SEG1_TB, 0, s>>>(m, a, b, c.seg_node_of.p, c.seg_order.p, c.nd_split.p, c.nd_axis.p,
-                                              c.nd_pivot.p, c.nd_sf.p, c.nd_sl.p, c.nd_ch1.p, c.nd_nlow_s.p,
-                                              c.seg_order2.p, c.seg_node_of2.p, c.s_rx.p, c.s_ry.p, c.nd_bbox.p);
-            VV_LAUNCH_CHECK();
-            std::swap(c.seg_order, c.seg_order2);
-            std::swap(c.seg_node_of, c.seg_node_of2);
-        } else if (m > 0) {
+        if (m > SEG1_MAX) {
             k_sclass<<<grid_for(m, TB), TB, 0, s>>>(m, a, b, c.seg_node_of.p, c.seg_order.p, c.nd_split.p,
                                                     c.nd_axis.p, c.nd_pivot.p, c.s_rx.p, c.s_ry.p, c.flags.p);
             VV_LAUNCH_CHECK();
@@ -870,6 +890,10 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
             VV_LAUNCH_CHECK();
             std::swap(c.seg_order, c.seg_order2);
             std::swap(c.seg_node_of, c.seg_node_of2);
+        }
+        if (forked) {
+            VV_CUDA(cudaEventRecord(c.ev_join, side));
+            VV_CUDA(cudaStreamWaitEvent(s, c.ev_join, 0));
         }
         k_finalize<<<grid_for(cnt, TB), TB, 0, s>>>(a, b, cnt, c.nd_split.p, c.nd_ch1.p, c.nd_nlow.p, c.nd_nlow_s.p,
                                                     c.nd_vf.p, c.nd_vl.p, c.nd_sf.p, c.nd_sl.p, c.nd_geom.p,

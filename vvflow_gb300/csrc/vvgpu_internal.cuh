@@ -111,6 +111,10 @@ struct Ctx {
     int precision = VVGPU_FP64;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
+    // second stream for work that runs beside the main stream's kernels within one call
+    // (forked and joined through the two events); created on first use
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string last_error;
 
     double re = 1.0 / 0.0, dt = 1.0, inf_vx = 0, inf_vy = 0, inf_g = 0, time = 0, grav_x = 0, grav_y = 0;
@@ -240,6 +244,16 @@ struct Ctx {
 
     cudaStream_t st() const { return stream; }
 };
+
+// The context's side stream (and its fork / join events), created on first use.
+inline cudaStream_t side_stream(Ctx& c) {
+    if (!c.side) {
+        VV_CUDA(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
+        VV_CUDA(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
+        VV_CUDA(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming));
+    }
+    return c.side;
+}
 
 // ---- exact FP64 arithmetic (no FMA contraction: the reference is built without FMA) ----
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
