@@ -562,13 +562,8 @@ __global__ void k_leaf_moments(int64_t nn, const int32_t* __restrict__ ch1, cons
     for (int q = 0; q < 12; q++) mom[12 * k + q] = a[q];
 }
 
-__global__ void k_inner_moments(int64_t a0, int64_t cnt, const int32_t* __restrict__ ch1,
-                                const double* __restrict__ cm, double* mom) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= cnt) return;
-    const int64_t k = a0 + t;
-    const int32_t c1 = ch1[k];
-    if (c1 < 0) return;
+// Moments of inner node k from its two children's (binomial shift to k's centroids).
+__device__ void inner_moments(int64_t k, int32_t c1, const double* __restrict__ cm, double* mom) {
     double out[12];
 #pragma unroll
     for (int q = 0; q < 12; q++) out[q] = 0.;
@@ -579,7 +574,9 @@ __global__ void k_inner_moments(int64_t a0, int64_t cnt, const int32_t* __restri
             const double G = cm[6 * u + 3 * sgn + 2];
             if (G == 0.) continue;
             const double dx = cm[6 * u + 3 * sgn] - cx, dy = cm[6 * u + 3 * sgn + 1] - cy;
-            const double* m = mom + 12 * u + 6 * sgn;  // M2', M3', M4'
+            double m[6];  // M2', M3', M4' (written by another thread: read through L2)
+#pragma unroll
+            for (int q = 0; q < 6; q++) m[q] = __ldcg(mom + 12 * u + 6 * sgn + q);
             double d2x, d2y, d3x, d3y, d4x, d4y;
             cmul(dx, dy, dx, dy, d2x, d2y);
             cmul(d2x, d2y, dx, dy, d3x, d3y);
@@ -601,6 +598,24 @@ __global__ void k_inner_moments(int64_t a0, int64_t cnt, const int32_t* __restri
     }
 #pragma unroll
     for (int q = 0; q < 12; q++) mom[12 * k + q] = out[q];
+}
+
+// All inner nodes bottom-up in one pass: each leaf's thread climbs, and at each node the
+// second child to arrive computes the node (children in the order ch1, ch1 + 1 either way).
+__global__ void k_inner_moments(int64_t nn, const int32_t* __restrict__ ch1, const int32_t* __restrict__ parent,
+                                const double* __restrict__ cm, double* mom, int32_t* arrive) {
+    const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k0 >= nn || ch1[k0] >= 0) return;
+    int32_t k = (int32_t)k0;
+    for (int it = 0; it <= MAX_DEPTH; it++) {
+        const int32_t p = parent[k];
+        if (p < 0) return;
+        __threadfence();  // this subtree's moments before the arrival
+        if (atomicAdd(&arrive[p], 1) == 0) return;  // the sibling computes p
+        __threadfence();
+        inner_moments(p, ch1[p], cm, mom);
+        k = p;
+    }
 }
 
 struct WalkView {
@@ -881,13 +896,11 @@ void ensure_moments(Ctx& c) {
     k_leaf_moments<<<grid_for(nn, 128), 128, 0, s>>>(nn, c.nd_ch1.p, c.nd_vf.p, c.nd_vl.p, c.nd_cm.p, c.x.p, c.y.p,
                                                      c.g.p, c.nd_mom.p);
     VV_LAUNCH_CHECK();
-    const int64_t nlev = (int64_t)c.level_begin.size() - 1;
-    for (int64_t lv = nlev - 1; lv >= 0; lv--) {
-        const int64_t a = c.level_begin[lv], b = std::min<int64_t>(c.level_begin[lv + 1], nn);
-        if (b <= a) continue;
-        k_inner_moments<<<grid_for(b - a, 128), 128, 0, s>>>(a, b - a, c.nd_ch1.p, c.nd_cm.p, c.nd_mom.p);
-        VV_LAUNCH_CHECK();
-    }
+    c.nd_arrive.reserve(nn + 1);
+    VV_CUDA(cudaMemsetAsync(c.nd_arrive.p, 0, nn * sizeof(int32_t), s));
+    k_inner_moments<<<grid_for(nn, 128), 128, 0, s>>>(nn, c.nd_ch1.p, c.nd_parent.p, c.nd_cm.p, c.nd_mom.p,
+                                                      c.nd_arrive.p);
+    VV_LAUNCH_CHECK();
     c.mom_valid = true;
 }
 

@@ -105,27 +105,42 @@ __global__ void k_finalize_root(double4* geom, const unsigned long long* bbox, i
     ch1[0] = -1; depth[0] = 0; path[0] = 0;
 }
 
-// snode::DivideNode leaf rules (TSortedTree.cpp:36-56).
-// DivideNode's test (TSortedTree.cpp:36-79): split unless small enough; the split is at the
-// box midpoint across the longer side.  Returns the flag.
+// snode::DivideNode's test (TSortedTree.cpp:36-79): split unless small enough; the split is
+// at the box midpoint across the longer side.  Returns 1 to split.
+__device__ __forceinline__ int decide_vals(double4 gm, int64_t nv, int64_t ns, int32_t depth, double min_node,
+                                           double max_node, int32_t* err, int32_t& axis, double& pivot) {
+    const double h = gm.z, w = gm.w;
+    const double mx = smax(h, w), mn = smin(h, w);
+    const int64_t maxlist = nv > ns ? nv : ns;
+    const bool leaf = (mx < max_node && mn <= min_node) || (mx < max_node && maxlist < TREE_MAX_LIST_SIZE);
+    int s = leaf ? 0 : 1;
+    if (s && depth >= MAX_DEPTH) { s = 0; atomicExch(err, 1); }
+    const bool byx = h < w;
+    axis = byx ? 1 : 0;
+    pivot = byx ? gm.x : gm.y;
+    return s;
+}
+
+// Largest node (vortices, no segments) whose whole subtree one block builds (k_subtree).
+constexpr int SUB_N = 1024;
+
+// split[k]: 0 leaf, 1 split by the level loop, 2 split by k_subtree (no segments and at most
+// SUB_N vortices: the node and its descendants are finished after the loop).  Returns 1 for
+// a split by the level loop (the flag that allocates its children in this pass).
 __device__ __forceinline__ int decide_node(int64_t k, const double4* __restrict__ geom, const int32_t* __restrict__ vf,
                                            const int32_t* __restrict__ vl, const int32_t* __restrict__ sf,
                                            const int32_t* __restrict__ sl, const int32_t* __restrict__ depth,
                                            double min_node, double max_node, int32_t* split, double* pivot,
                                            int32_t* axis, int32_t* err) {
-    double4 gm = geom[k];
-    double h = gm.z, w = gm.w;
-    double mx = smax(h, w), mn = smin(h, w);
-    int64_t nv = (int64_t)vl[k] - vf[k], ns = (int64_t)sl[k] - sf[k];
-    int64_t maxlist = nv > ns ? nv : ns;
-    bool leaf = (mx < max_node && mn <= min_node) || (mx < max_node && maxlist < TREE_MAX_LIST_SIZE);
-    int s = leaf ? 0 : 1;
-    if (s && depth[k] >= MAX_DEPTH) { s = 0; atomicExch(err, 1); }
+    const int64_t nv = (int64_t)vl[k] - vf[k], ns = (int64_t)sl[k] - sf[k];
+    int32_t ax;
+    double pv;
+    int s = decide_vals(geom[k], nv, ns, depth[k], min_node, max_node, err, ax, pv);
+    if (s && ns == 0 && nv <= SUB_N) s = 2;
     split[k] = s;
-    bool byx = h < w;
-    axis[k] = byx ? 1 : 0;
-    pivot[k] = byx ? gm.x : gm.y;
-    return s;
+    axis[k] = ax;
+    pivot[k] = pv;
+    return s == 1;
 }
 
 __global__ void k_decide(int64_t a, int64_t cnt, const double4* __restrict__ geom, const int32_t* __restrict__ vf,
@@ -158,7 +173,7 @@ __device__ __forceinline__ void make_children(int64_t k, int64_t c1, int32_t* ch
 }
 
 __device__ __forceinline__ bool in_level_split(int32_t k, int64_t a, int64_t b, const int32_t* split) {
-    return k >= a && k < b && split[k];
+    return k >= a && k < b && split[k] == 1;
 }
 
 __global__ void k_perm_gather(int64_t n, const int32_t* __restrict__ perm, const double* __restrict__ g,
@@ -213,12 +228,12 @@ __global__ void k_route(int64_t a, int64_t b, int64_t cnt, const int32_t* __rest
     const int32_t k = (int32_t)(a + t);
     if (t == 0) counts[2] = lscan[cnt];
     if (t < cnt) {
-        if (split[k]) make_children(k, b + 2 * (int64_t)lscan[t], ch1, depth, path, parent, bbox, nlow, nlow_s);
+        if (split[k] == 1) make_children(k, b + 2 * (int64_t)lscan[t], ch1, depth, path, parent, bbox, nlow, nlow_s);
         else ch1[k] = -1;
     }
     bool small = false;
     int nch = 0;
-    if (t < cnt && split[k]) {
+    if (t < cnt && split[k] == 1) {
         const int32_t nv = vl[k] - vf[k];
         if (nv <= SMALL_N) small = true;
         else nch = (nv + CH - 1) / CH;
@@ -640,7 +655,7 @@ __global__ void k_finalize(int64_t a, int64_t b, int64_t cnt, const int32_t* spl
     if (t >= cnt) return;
     if (t == 0) counts[0] = counts[1] = 0;  // the next level's route counters
     int64_t k = a + t;
-    if (!split[k]) return;
+    if (split[k] != 1) return;
     int32_t c1 = ch1[k], c2 = c1 + 1;
     vf[c1] = vf[k]; vl[c1] = vf[k] + nlow[k];
     vf[c2] = vf[k] + nlow[k]; vl[c2] = vl[k];
@@ -651,6 +666,295 @@ __global__ void k_finalize(int64_t a, int64_t b, int64_t cnt, const int32_t* spl
     for (int q = 0; q < 2; q++) {
         const int64_t c = c1 + q;
         flags[c - b] = decide_node(c, geom, vf, vl, sf, sl, depth, min_node, max_node, nsplit_flag, pivot, axis, err);
+    }
+}
+
+// ---- subtrees of small nodes, one block each ----
+//
+// A node without segments and with at most SUB_N vortices (split[k] == 2) is left alone by
+// the level loop; afterwards one block loads its vortices into shared memory and builds
+// its whole subtree there, level by level, with the same decisions (decide_vals) and the
+// same swap pairing as the loop.  The subtree's nodes are numbered breadth-first from 1
+// (the root is 0) and recorded in scratch slots 2 vf(root) + id (a subtree of n vortices
+// has at most 2 n - 1 nodes, and the roots' vortex ranges are disjoint); k_subtree_place
+// then moves them to ids after the loop's nodes.
+constexpr int SUB_T = 256;
+constexpr int SUB_E = SUB_N / SUB_T;
+constexpr int SUB_NW = SUB_T / 32;
+static_assert(SUB_N % SUB_T == 0 && SUB_NW <= 32, "subtree block shape");
+
+struct SubNode {  // a node made by k_subtree, before its final id is known
+    double4 geom;  // holds the box keys while the node's box is reduced
+    int64_t path;
+    int32_t vf, vl, ch1, parent, depth, pad;
+};
+static_assert(sizeof(SubNode) == 64, "SubNode is one 64-byte line");
+
+constexpr size_t SUB_SMEM = (size_t)SUB_N * (6 * 8 + 4 * 4 + 10 * 2 + 4) + 64 * 4;
+
+// Exclusive prefix of a[0 .. SUB_N) in place (thread-contiguous runs), a[SUB_N] = total.
+__device__ __forceinline__ int32_t sub_exscan(int32_t* a, int32_t* wt) {
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    int32_t v[SUB_E], sum = 0;
+#pragma unroll
+    for (int e = 0; e < SUB_E; e++) { v[e] = a[t * SUB_E + e]; sum += v[e]; }
+    int32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) wt[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int32_t x = lane < SUB_NW ? wt[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += u;
+        }
+        if (lane < SUB_NW) wt[lane] = x;
+    }
+    __syncthreads();
+    int32_t off = (w ? wt[w - 1] : 0) + incl - sum;
+#pragma unroll
+    for (int e = 0; e < SUB_E; e++) { a[t * SUB_E + e] = off; off += v[e]; }
+    if (t == SUB_T - 1) a[SUB_N] = off;
+    __syncthreads();
+    return a[SUB_N];
+}
+
+__global__ void k_defer_flags(int64_t nn, const int32_t* __restrict__ split, int32_t* flags) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nn) flags[k] = split[k] == 2;
+}
+__global__ void k_defer_list(int64_t nn, const int32_t* __restrict__ split, const int32_t* __restrict__ pos,
+                             int32_t* roots) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nn && split[k] == 2) roots[pos[k]] = (int32_t)k;
+}
+
+__global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ roots,
+                                                   const int32_t* __restrict__ vf, const int32_t* __restrict__ vl,
+                                                   const int32_t* __restrict__ depth, const int64_t* __restrict__ path,
+                                                   const double* __restrict__ pivot, const int32_t* __restrict__ axis,
+                                                   double min_node, double max_node, double* x, double* y,
+                                                   int32_t* perm, SubNode* scratch, int32_t* nnew, int32_t* err,
+                                                   int32_t* maxdepth) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    // per vortex: position, permutation, level-node slot (-1: in a finished leaf), prefix,
+    // pairing tables; per level node (two levels, ping-pong): pivot, path, id, first, size,
+    // axis, split; per current node: rank among the split nodes, lows, pairs
+    double* sx = (double*)smem;
+    double* sy = sx + SUB_N;
+    double* lpiv = sy + SUB_N;                                // [2][SUB_N], level ping-pong
+    int64_t* lpath = (int64_t*)(sy + 3 * SUB_N);              // [2][SUB_N]
+    int32_t* sp = (int32_t*)(sy + 5 * SUB_N);
+    int32_t* pre = sp + SUB_N;                                // SUB_N + 1
+    int32_t* llid = pre + SUB_N + 4;                          // [2][SUB_N]
+    int32_t* wt = llid + 2 * SUB_N;                           // SUB_NW (60 ints reserved)
+    int16_t* en = (int16_t*)(wt + 60);
+    int16_t* tl = en + SUB_N;
+    int16_t* tr = tl + SUB_N;
+    int16_t* lvf = tr + SUB_N;                                // [2][SUB_N]
+    int16_t* ln = tr + 3 * SUB_N;                             // [2][SUB_N]
+    int16_t* rank = tr + 5 * SUB_N;
+    int16_t* cL = tr + 6 * SUB_N;
+    int16_t* cH = tr + 7 * SUB_N;
+    int8_t* lax = (int8_t*)(tr + 8 * SUB_N);                  // [2][SUB_N]
+    int8_t* lsp = lax + 2 * SUB_N;                            // [2][SUB_N]
+
+    const int t = threadIdx.x, lane = t & 31;
+    const int32_t root = roots[blockIdx.x];
+    const int32_t f0 = vf[root], nr = vl[root] - f0;
+    if (nr > SUB_N || nr < 1) {  // not a deferred node (cannot happen): leave it alone
+        if (t == 0) { atomicExch(err, 3); nnew[blockIdx.x] = 0; }
+        return;
+    }
+    SubNode* rec = scratch + 2 * (size_t)f0;  // local id u at rec[u], u < 2 nr
+    for (int i = t; i < SUB_N; i += SUB_T) {
+        if (i < nr) {
+            sx[i] = x[f0 + i];
+            sy[i] = y[f0 + i];
+            sp[i] = perm[f0 + i];
+            en[i] = 0;
+        } else {
+            en[i] = -1;
+        }
+    }
+    if (t == 0) {
+        lvf[0] = 0; ln[0] = (int16_t)nr; lpiv[0] = pivot[root]; lax[0] = (int8_t)axis[root];
+        lsp[0] = 1; llid[0] = 0; lpath[0] = path[root];
+    }
+    int cur = 0, ncur = 1, next_lid = 1;
+    int32_t dep = depth[root];
+    __syncthreads();
+    for (int level = 0; level <= MAX_DEPTH; level++) {
+        const int co = cur * SUB_N;
+        // (a) rank of each split node among the level's split nodes
+        for (int j = t; j < SUB_N; j += SUB_T) pre[j] = (j < ncur && lsp[co + j]) ? 1 : 0;
+        __syncthreads();
+        const int nsplit = sub_exscan(pre, wt);
+        if (nsplit == 0) break;
+        if (next_lid + 2 * nsplit > 2 * nr) {
+            // only a chain of splits that leave one side empty (a box midpoint rounding onto
+            // its lower edge) outgrows 2 n - 1 nodes; the level loop reports it as too deep
+            if (t == 0) atomicExch(err, 1);
+            break;
+        }
+        for (int j = t; j < ncur; j += SUB_T) rank[j] = (int16_t)pre[j];
+        __syncthreads();
+        // (b) low flags (key < pivot) of the split nodes' vortices, prefix over positions
+#pragma unroll
+        for (int e = 0; e < SUB_E; e++) {
+            const int i = e * SUB_T + t;
+            const int nd = en[i];
+            bool low = false;
+            if (nd >= 0 && lsp[co + nd]) low = (lax[co + nd] ? sx[i] : sy[i]) < lpiv[co + nd];
+            pre[i] = low ? 1 : 0;
+        }
+        __syncthreads();
+        sub_exscan(pre, wt);
+        // (c) lows and pairs of each split node; its children take slots 2 rank, 2 rank + 1
+        const int nxt = cur ^ 1, no = nxt * SUB_N;
+        for (int j = t; j < ncur; j += SUB_T) {
+            if (!lsp[co + j]) continue;
+            const int f = lvf[co + j], n = ln[co + j];
+            const int L = pre[f + n] - pre[f];
+            cL[j] = (int16_t)L;
+            cH[j] = (int16_t)(L - (pre[f + L] - pre[f]));  // highs in the left part
+            const int r = rank[j];
+            const int32_t c1 = next_lid + 2 * r;
+            if (llid[co + j] > 0) rec[llid[co + j]].ch1 = c1;
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int cs = 2 * r + q;
+                lvf[no + cs] = (int16_t)(q ? f + L : f);
+                ln[no + cs] = (int16_t)(q ? n - L : L);
+                llid[no + cs] = c1 + q;
+                lpath[no + cs] = lpath[co + j] * 2 + q;
+                unsigned long long* bb = reinterpret_cast<unsigned long long*>(&rec[c1 + q].geom);
+                bb[0] = bb[1] = dkey(DBL_MAX);
+                bb[2] = bb[3] = dkey(-DBL_MAX);
+                rec[c1 + q].parent = llid[co + j];
+            }
+        }
+        __syncthreads();
+        // (d) pairing tables (the pairing of TSortedTree.cpp:81-99, as in the level loop)
+#pragma unroll
+        for (int e = 0; e < SUB_E; e++) {
+            const int i = e * SUB_T + t;
+            const int nd = en[i];
+            if (nd < 0 || !lsp[co + nd]) continue;
+            const int f = lvf[co + nd], L = cL[nd], q = i - f, lb = pre[i] - pre[f];
+            const bool low = pre[i + 1] != pre[i];
+            if (q >= L && low) tr[f + L - lb - 1] = (int16_t)q;
+            if (q < L && !low) tl[f + q - lb] = (int16_t)q;
+        }
+        __syncthreads();
+        // (e) swaps
+#pragma unroll
+        for (int e = 0; e < SUB_E; e++) {
+            const int i = e * SUB_T + t;
+            const int nd = en[i];
+            if (nd < 0 || !lsp[co + nd]) continue;
+            const int f = lvf[co + nd], pq = i - f;
+            if (pq >= cH[nd]) continue;
+            const int ia = f + tl[f + pq], ib = f + tr[f + pq];
+            const double tx = sx[ia], ty = sy[ia];
+            const int32_t tp = sp[ia];
+            sx[ia] = sx[ib]; sy[ia] = sy[ib]; sp[ia] = sp[ib];
+            sx[ib] = tx; sy[ib] = ty; sp[ib] = tp;
+        }
+        __syncthreads();
+        // (f) each vortex moves to its child's slot; the children's boxes (warp-combined
+        // atomics on the scratch records)
+#pragma unroll
+        for (int e = 0; e < SUB_E; e++) {
+            const int i = e * SUB_T + t;
+            const int nd = en[i];
+            int cs = -1;
+            if (nd >= 0 && lsp[co + nd]) cs = 2 * rank[nd] + ((i - lvf[co + nd]) >= cL[nd] ? 1 : 0);
+            en[i] = (int16_t)cs;
+            unsigned long long b4[4];
+            if (cs >= 0) {
+                b4[0] = b4[2] = dkey(sx[i]);
+                b4[1] = b4[3] = dkey(sy[i]);
+            } else {
+                bbox_init(b4);
+            }
+            const int c0 = __shfl_sync(0xffffffffu, cs, 0);
+            if (__all_sync(0xffffffffu, cs == c0)) {
+                if (c0 >= 0) {
+                    bbox_warp_reduce(b4);
+                    if (lane == 0) bbox_commit(reinterpret_cast<unsigned long long*>(&rec[next_lid + c0].geom), b4);
+                }
+            } else if (cs >= 0) {
+                bbox_commit(reinterpret_cast<unsigned long long*>(&rec[next_lid + cs].geom), b4);
+            }
+        }
+        __syncthreads();
+        // (g) the children: geometry, decision, record
+        for (int cs = t; cs < 2 * nsplit; cs += SUB_T) {
+            SubNode* o = rec + next_lid + cs;
+            const unsigned long long* bk = reinterpret_cast<const unsigned long long*>(&o->geom);
+            unsigned long long b4[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) b4[q] = __ldcg(bk + q);
+            const double4 gm = geom_from_bbox(b4);
+            const int n = ln[no + cs];
+            int32_t ax;
+            double pv;
+            lsp[no + cs] = (int8_t)decide_vals(gm, n, 0, dep + 1, min_node, max_node, err, ax, pv);
+            lax[no + cs] = (int8_t)ax;
+            lpiv[no + cs] = pv;
+            o->geom = gm;
+            o->path = lpath[no + cs];
+            o->vf = f0 + lvf[no + cs];
+            o->vl = f0 + lvf[no + cs] + n;
+            o->ch1 = -1;
+            o->depth = dep + 1;
+        }
+        next_lid += 2 * nsplit;
+        dep++;
+        ncur = 2 * nsplit;
+        cur = nxt;
+        __syncthreads();
+    }
+    for (int i = t; i < nr; i += SUB_T) {
+        x[f0 + i] = sx[i];
+        y[f0 + i] = sy[i];
+        perm[f0 + i] = sp[i];
+    }
+    if (t == 0) {
+        nnew[blockIdx.x] = next_lid - 1;
+        atomicMax(maxdepth, dep);
+    }
+}
+
+// Moves subtree r's new nodes (local ids 1 .. nnew) to ids base + pos[r] + id - 1.
+__global__ void k_subtree_place(const int32_t* __restrict__ roots, const int32_t* __restrict__ pos,
+                                const int32_t* __restrict__ nnew, int64_t base, const SubNode* __restrict__ scratch,
+                                double4* geom, int32_t* vf, int32_t* vl, int32_t* sf, int32_t* sl, int32_t* ch1,
+                                int32_t* depth, int64_t* path, int32_t* parent) {
+    const int32_t root = roots[blockIdx.x];
+    const int32_t cnt = nnew[blockIdx.x];
+    const int64_t b = base + pos[blockIdx.x] - 1;  // id of local node u >= 1 is b + u
+    const SubNode* rec = scratch + 2 * (size_t)vf[root];
+    const int32_t s0 = sf[root];
+    if (threadIdx.x == 0) ch1[root] = cnt > 0 ? (int32_t)(b + 1) : -1;
+    for (int32_t u = 1 + threadIdx.x; u <= cnt; u += blockDim.x) {
+        const SubNode o = rec[u];
+        const int64_t g = b + u;
+        geom[g] = o.geom;
+        vf[g] = o.vf;
+        vl[g] = o.vl;
+        sf[g] = s0;
+        sl[g] = s0;
+        ch1[g] = o.ch1 >= 0 ? (int32_t)(b + o.ch1) : -1;
+        depth[g] = o.depth;
+        path[g] = o.path;
+        parent[g] = o.parent > 0 ? (int32_t)(b + o.parent) : root;
     }
 }
 
@@ -904,6 +1208,41 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
         c.nnodes = b + 2 * (int64_t)nsplit;
     }
     c.depth = (int64_t)c.level_begin.size() - 1;
+    // the subtrees the loop deferred (split == 2), one block each, in node order
+    {
+        const int64_t nn0 = c.nnodes;
+        c.flags.reserve(nn0 + 2);
+        c.scan.reserve(nn0 + 2);
+        k_defer_flags<<<grid_for(nn0, TB), TB, 0, s>>>(nn0, c.nd_split.p, c.flags.p);
+        VV_LAUNCH_CHECK();
+        exclusive_scan(c, c.flags.p, c.scan.p, nn0);
+        const int32_t ndef = read_i32(c, c.scan.p + nn0);
+        if (ndef > 0) {
+            c.sub_i32.reserve(3 * (size_t)ndef + 4);
+            int32_t* roots = c.sub_i32.p;
+            int32_t* nnew = roots + ndef;
+            int32_t* pos = nnew + ndef + 1;
+            k_defer_list<<<grid_for(nn0, TB), TB, 0, s>>>(nn0, c.nd_split.p, c.scan.p, roots);
+            VV_LAUNCH_CHECK();
+            c.sub_scratch.reserve(4 * (size_t)n + 2);
+            SubNode* scratch = reinterpret_cast<SubNode*>(c.sub_scratch.p);
+            int32_t* maxdep = (int32_t*)(c.counters.p + 3);
+            VV_CUDA(cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SUB_SMEM));
+            k_subtree<<<ndef, SUB_T, SUB_SMEM, s>>>(roots, c.nd_vf.p, c.nd_vl.p, c.nd_depth.p, c.nd_path.p,
+                                                    c.nd_pivot.p, c.nd_axis.p, min_node, max_node, c.x.p, c.y.p,
+                                                    c.perm.p, scratch, nnew, err, maxdep);
+            VV_LAUNCH_CHECK();
+            exclusive_scan(c, nnew, pos, ndef);
+            const int32_t added = read_i32(c, pos + ndef);
+            ensure_nodes(nn0 + added + 1);
+            k_subtree_place<<<ndef, 128, 0, s>>>(roots, pos, nnew, nn0, scratch, c.nd_geom.p, c.nd_vf.p, c.nd_vl.p,
+                                                 c.nd_sf.p, c.nd_sl.p, c.nd_ch1.p, c.nd_depth.p, c.nd_path.p,
+                                                 c.nd_parent.p);
+            VV_LAUNCH_CHECK();
+            c.nnodes = nn0 + added;
+            c.depth = std::max<int64_t>(c.depth, (int64_t)read_i32(c, maxdep) + 1);
+        }
+    }
     if (n > 0) {
         c.ptmp.reserve(4 * (size_t)n);
         c.otmp.reserve(n);

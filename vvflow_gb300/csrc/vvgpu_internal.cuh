@@ -234,6 +234,8 @@ struct Ctx {
     int64_t neq_cached = 0;
     std::vector<double> slae_sig;   // inputs of the matrix in A (A is reused while they are equal)
     uint64_t seg_version = 0;       // bumped whenever the segment geometry changes
+    DArr<int32_t> sub_i32;          // subtree pass: roots, new-node counts, their prefix
+    DArr<double4> sub_scratch;      // subtree pass: node records (two double4 per record)
     DArr<int32_t> slae_maps;        // column / row maps of the system
     DArr<double> slae_bodies;       // per-body row data
     DArr<double> slae_r, slae_sq;   // refinement residual and its squared terms
