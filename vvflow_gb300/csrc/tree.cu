@@ -690,7 +690,7 @@ struct SubNode {  // a node made by k_subtree, before its final id is known
 };
 static_assert(sizeof(SubNode) == 64, "SubNode is one 64-byte line");
 
-constexpr size_t SUB_SMEM = (size_t)SUB_N * (6 * 8 + 4 * 4 + 10 * 2 + 4) + 64 * 4;
+constexpr size_t SUB_SMEM = (size_t)SUB_N * (5 * 8 + 2 * 4 + 12 * 2 + 2) + 64 * 4;
 
 // Exclusive prefix of a[0 .. SUB_N) in place (thread-contiguous runs), a[SUB_N] = total.
 __device__ __forceinline__ int32_t sub_exscan(int32_t* a, int32_t* wt) {
@@ -742,29 +742,31 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
                                                    int32_t* perm, SubNode* scratch, int32_t* nnew, int32_t* err,
                                                    int32_t* maxdepth) {
     extern __shared__ __align__(16) unsigned char smem[];
-    // per vortex: position, permutation, level-node slot (-1: in a finished leaf), prefix,
-    // pairing tables; per level node (two levels, ping-pong): pivot, path, id, first, size,
-    // axis, split; per current node: rank among the split nodes, lows, pairs
+    // per vortex: position, permutation, level-node slot (two levels: -1 = in a finished
+    // leaf), prefix, pairing tables.  Per level node: pivot, axis, split (the next level's
+    // overwrite them once the current level's partition is done), and, for two levels,
+    // path, first, size; per current node: rank among the split nodes, lows, pairs; per
+    // next node: its parent's slot.
     double* sx = (double*)smem;
     double* sy = sx + SUB_N;
-    double* lpiv = sy + SUB_N;                                // [2][SUB_N], level ping-pong
-    int64_t* lpath = (int64_t*)(sy + 3 * SUB_N);              // [2][SUB_N]
-    int32_t* sp = (int32_t*)(sy + 5 * SUB_N);
+    double* lpiv = sy + SUB_N;
+    int64_t* lpath = (int64_t*)(lpiv + SUB_N);                // [2][SUB_N]
+    int32_t* sp = (int32_t*)(lpath + 2 * SUB_N);
     int32_t* pre = sp + SUB_N;                                // SUB_N + 1
-    int32_t* llid = pre + SUB_N + 4;                          // [2][SUB_N]
-    int32_t* wt = llid + 2 * SUB_N;                           // SUB_NW (60 ints reserved)
-    int16_t* en = (int16_t*)(wt + 60);
-    int16_t* tl = en + SUB_N;
+    int32_t* wt = pre + SUB_N + 4;                            // SUB_NW (60 ints reserved)
+    int16_t* en = (int16_t*)(wt + 60);                        // [2][SUB_N]
+    int16_t* tl = en + 2 * SUB_N;
     int16_t* tr = tl + SUB_N;
     int16_t* lvf = tr + SUB_N;                                // [2][SUB_N]
-    int16_t* ln = tr + 3 * SUB_N;                             // [2][SUB_N]
-    int16_t* rank = tr + 5 * SUB_N;
-    int16_t* cL = tr + 6 * SUB_N;
-    int16_t* cH = tr + 7 * SUB_N;
-    int8_t* lax = (int8_t*)(tr + 8 * SUB_N);                  // [2][SUB_N]
-    int8_t* lsp = lax + 2 * SUB_N;                            // [2][SUB_N]
+    int16_t* ln = lvf + 2 * SUB_N;                            // [2][SUB_N]
+    int16_t* rank = ln + 2 * SUB_N;
+    int16_t* cL = rank + SUB_N;
+    int16_t* cH = cL + SUB_N;
+    int16_t* par = cH + SUB_N;
+    int8_t* lax = (int8_t*)(par + SUB_N);
+    int8_t* lsp = lax + SUB_N;
 
-    const int t = threadIdx.x, lane = t & 31;
+    const int t = threadIdx.x;
     const int32_t root = roots[blockIdx.x];
     const int32_t f0 = vf[root], nr = vl[root] - f0;
     if (nr > SUB_N || nr < 1) {  // not a deferred node (cannot happen): leave it alone
@@ -784,15 +786,15 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
     }
     if (t == 0) {
         lvf[0] = 0; ln[0] = (int16_t)nr; lpiv[0] = pivot[root]; lax[0] = (int8_t)axis[root];
-        lsp[0] = 1; llid[0] = 0; lpath[0] = path[root];
+        lsp[0] = 1; lpath[0] = path[root];
     }
-    int cur = 0, ncur = 1, next_lid = 1;
+    int cur = 0, ncur = 1, base = 0, next_lid = 1;  // base: local id of the level's slot 0
     int32_t dep = depth[root];
     __syncthreads();
     for (int level = 0; level <= MAX_DEPTH; level++) {
-        const int co = cur * SUB_N;
+        const int co = cur * SUB_N, no = (cur ^ 1) * SUB_N;
         // (a) rank of each split node among the level's split nodes
-        for (int j = t; j < SUB_N; j += SUB_T) pre[j] = (j < ncur && lsp[co + j]) ? 1 : 0;
+        for (int j = t; j < SUB_N; j += SUB_T) pre[j] = (j < ncur && lsp[j]) ? 1 : 0;
         __syncthreads();
         const int nsplit = sub_exscan(pre, wt);
         if (nsplit == 0) break;
@@ -808,56 +810,55 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
 #pragma unroll
         for (int e = 0; e < SUB_E; e++) {
             const int i = e * SUB_T + t;
-            const int nd = en[i];
+            const int nd = en[co + i];
             bool low = false;
-            if (nd >= 0 && lsp[co + nd]) low = (lax[co + nd] ? sx[i] : sy[i]) < lpiv[co + nd];
+            if (nd >= 0 && lsp[nd]) low = (lax[nd] ? sx[i] : sy[i]) < lpiv[nd];
             pre[i] = low ? 1 : 0;
         }
         __syncthreads();
         sub_exscan(pre, wt);
         // (c) lows and pairs of each split node; its children take slots 2 rank, 2 rank + 1
-        const int nxt = cur ^ 1, no = nxt * SUB_N;
         for (int j = t; j < ncur; j += SUB_T) {
-            if (!lsp[co + j]) continue;
+            if (!lsp[j]) continue;
             const int f = lvf[co + j], n = ln[co + j];
             const int L = pre[f + n] - pre[f];
             cL[j] = (int16_t)L;
             cH[j] = (int16_t)(L - (pre[f + L] - pre[f]));  // highs in the left part
             const int r = rank[j];
-            const int32_t c1 = next_lid + 2 * r;
-            if (llid[co + j] > 0) rec[llid[co + j]].ch1 = c1;
+            if (base + j > 0) rec[base + j].ch1 = next_lid + 2 * r;
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 const int cs = 2 * r + q;
                 lvf[no + cs] = (int16_t)(q ? f + L : f);
                 ln[no + cs] = (int16_t)(q ? n - L : L);
-                llid[no + cs] = c1 + q;
                 lpath[no + cs] = lpath[co + j] * 2 + q;
-                unsigned long long* bb = reinterpret_cast<unsigned long long*>(&rec[c1 + q].geom);
-                bb[0] = bb[1] = dkey(DBL_MAX);
-                bb[2] = bb[3] = dkey(-DBL_MAX);
-                rec[c1 + q].parent = llid[co + j];
+                par[cs] = (int16_t)j;
             }
         }
         __syncthreads();
-        // (d) pairing tables (the pairing of TSortedTree.cpp:81-99, as in the level loop)
+        // (d) pairing tables (the pairing of TSortedTree.cpp:81-99, as in the level loop) and
+        // each position's slot in the next level
 #pragma unroll
         for (int e = 0; e < SUB_E; e++) {
             const int i = e * SUB_T + t;
-            const int nd = en[i];
-            if (nd < 0 || !lsp[co + nd]) continue;
-            const int f = lvf[co + nd], L = cL[nd], q = i - f, lb = pre[i] - pre[f];
-            const bool low = pre[i + 1] != pre[i];
-            if (q >= L && low) tr[f + L - lb - 1] = (int16_t)q;
-            if (q < L && !low) tl[f + q - lb] = (int16_t)q;
+            const int nd = en[co + i];
+            int cs = -1;
+            if (nd >= 0 && lsp[nd]) {
+                const int f = lvf[co + nd], L = cL[nd], q = i - f, lb = pre[i] - pre[f];
+                const bool low = pre[i + 1] != pre[i];
+                if (q >= L && low) tr[f + L - lb - 1] = (int16_t)q;
+                if (q < L && !low) tl[f + q - lb] = (int16_t)q;
+                cs = 2 * rank[nd] + (q >= L ? 1 : 0);
+            }
+            en[no + i] = (int16_t)cs;
         }
         __syncthreads();
         // (e) swaps
 #pragma unroll
         for (int e = 0; e < SUB_E; e++) {
             const int i = e * SUB_T + t;
-            const int nd = en[i];
-            if (nd < 0 || !lsp[co + nd]) continue;
+            const int nd = en[co + i];
+            if (nd < 0 || !lsp[nd]) continue;
             const int f = lvf[co + nd], pq = i - f;
             if (pq >= cH[nd]) continue;
             const int ia = f + tl[f + pq], ib = f + tr[f + pq];
@@ -867,58 +868,52 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
             sx[ib] = tx; sy[ib] = ty; sp[ib] = tp;
         }
         __syncthreads();
-        // (f) each vortex moves to its child's slot; the children's boxes (warp-combined
-        // atomics on the scratch records)
-#pragma unroll
-        for (int e = 0; e < SUB_E; e++) {
-            const int i = e * SUB_T + t;
-            const int nd = en[i];
-            int cs = -1;
-            if (nd >= 0 && lsp[co + nd]) cs = 2 * rank[nd] + ((i - lvf[co + nd]) >= cL[nd] ? 1 : 0);
-            en[i] = (int16_t)cs;
+        // (f) the children: box (a group of G lanes per child), geometry, decision, record
+        const int nch = 2 * nsplit;
+        const int G = nch <= SUB_NW ? 32 : nch <= 2 * SUB_NW ? 16 : nch <= 4 * SUB_NW ? 8 : 4;
+        const int gl = t & (G - 1), ng = SUB_T / G;
+        for (int c0 = 0; c0 < nch; c0 += ng) {  // uniform trip count: every lane shuffles
+            const int cs = c0 + t / G;
             unsigned long long b4[4];
-            if (cs >= 0) {
-                b4[0] = b4[2] = dkey(sx[i]);
-                b4[1] = b4[3] = dkey(sy[i]);
-            } else {
-                bbox_init(b4);
+            bbox_init(b4);
+            int f = 0, n = 0;
+            if (cs < nch) {
+                f = lvf[no + cs];
+                n = ln[no + cs];
+                for (int i = f + gl; i < f + n; i += G) bbox_acc(b4, sx[i], sy[i]);
             }
-            const int c0 = __shfl_sync(0xffffffffu, cs, 0);
-            if (__all_sync(0xffffffffu, cs == c0)) {
-                if (c0 >= 0) {
-                    bbox_warp_reduce(b4);
-                    if (lane == 0) bbox_commit(reinterpret_cast<unsigned long long*>(&rec[next_lid + c0].geom), b4);
-                }
-            } else if (cs >= 0) {
-                bbox_commit(reinterpret_cast<unsigned long long*>(&rec[next_lid + cs].geom), b4);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                if (o >= G) continue;
+                unsigned long long u[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) u[e] = __shfl_xor_sync(0xffffffffu, b4[e], o);
+                bbox_merge(b4, u);
+            }
+            if (cs < nch && gl == 0) {
+                const double4 gm = geom_from_bbox(b4);
+                int32_t ax;
+                double pv;
+                lsp[cs] = (int8_t)decide_vals(gm, n, 0, dep + 1, min_node, max_node, err, ax, pv);
+                lax[cs] = (int8_t)ax;
+                lpiv[cs] = pv;
+                SubNode o;
+                o.geom = gm;
+                o.path = lpath[no + cs];
+                o.vf = f0 + f;
+                o.vl = f0 + f + n;
+                o.ch1 = -1;
+                o.parent = base + par[cs];
+                o.depth = dep + 1;
+                o.pad = 0;
+                rec[next_lid + cs] = o;
             }
         }
-        __syncthreads();
-        // (g) the children: geometry, decision, record
-        for (int cs = t; cs < 2 * nsplit; cs += SUB_T) {
-            SubNode* o = rec + next_lid + cs;
-            const unsigned long long* bk = reinterpret_cast<const unsigned long long*>(&o->geom);
-            unsigned long long b4[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) b4[q] = __ldcg(bk + q);
-            const double4 gm = geom_from_bbox(b4);
-            const int n = ln[no + cs];
-            int32_t ax;
-            double pv;
-            lsp[no + cs] = (int8_t)decide_vals(gm, n, 0, dep + 1, min_node, max_node, err, ax, pv);
-            lax[no + cs] = (int8_t)ax;
-            lpiv[no + cs] = pv;
-            o->geom = gm;
-            o->path = lpath[no + cs];
-            o->vf = f0 + lvf[no + cs];
-            o->vl = f0 + lvf[no + cs] + n;
-            o->ch1 = -1;
-            o->depth = dep + 1;
-        }
-        next_lid += 2 * nsplit;
+        base = next_lid;
+        next_lid += nch;
         dep++;
-        ncur = 2 * nsplit;
-        cur = nxt;
+        ncur = nch;
+        cur ^= 1;
         __syncthreads();
     }
     for (int i = t; i < nr; i += SUB_T) {
