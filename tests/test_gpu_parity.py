@@ -113,3 +113,27 @@ def test_slae_matrix_reused_until_its_inputs_change(precision):
     assert np.array_equal(A3, A4) and np.array_equal(b3, b4) and np.array_equal(x3, x4)
     S.close()
     F.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [700, 1024, 1025, 5000])
+def test_gpu_matches_oracle_subtree_sizes(n):
+    """Body-free clouds around the size limit of the one-block subtree build (1024
+    vortices): at 700 and 1024 the root's whole tree is built by one block, at 1025 and
+    5000 the level loop hands its children over.  Exact duplicates and a tight cluster
+    exercise empty and degenerate boxes."""
+    x, y, g = W.annulus_cloud(n, 0.1, 2.0, seed=20 + n)
+    x[n // 3: n // 3 + 5] = x[n // 3]
+    y[n // 3: n // 3 + 5] = y[n // 3]
+    x[-40:] = 1.5 + 1e-9 * np.arange(40)
+    y[-40:] = -0.25
+    wl = W.Workload("subtree", [], x, y, g, re=600.0, dt=0.005)
+    S = oracle.OracleSpace("port")
+    S.load(wl)
+    ref = run_step(S, wl, full_lists=True)
+    S.close()
+    for precision in (0, 1):
+        got, _ = run_gpu(wl, precision, full_lists=True)
+        tol = TOL64 if precision == 0 else TOL32
+        bad = check_step(ref, got, **tol)
+        assert not bad, (precision, bad)
