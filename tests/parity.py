@@ -47,7 +47,17 @@ def load_workload(path):
 
 def rel_err_vec(ax, ay, bx, by):
     """max_i |a_i - b_i| / (|b_i| + 1e-3 * rms|b|): per-vortex relative error with a floor
-    that keeps near-zero velocities from dominating."""
+    that keeps near-zero velocities from dominating.  Non-finite reference values (the
+    reference's own 0 * inf for coincident vortices whose epsilon is 0) must be matched
+    position for position (inf is returned otherwise) and are left out of the measure."""
+    if len(bx) == 0:
+        return 0.0
+    ax, ay, bx, by = (np.asarray(v, np.float64) for v in (ax, ay, bx, by))
+    fb = np.isfinite(bx) & np.isfinite(by)
+    fa = np.isfinite(ax) & np.isfinite(ay)
+    if not np.array_equal(fa, fb):
+        return float("inf")
+    ax, ay, bx, by = ax[fb], ay[fb], bx[fb], by[fb]
     if len(bx) == 0:
         return 0.0
     mag = np.hypot(bx, by)

@@ -132,8 +132,12 @@ def test_gpu_matches_oracle_subtree_sizes(n):
     S.load(wl)
     ref = run_step(S, wl, full_lists=True)
     S.close()
+    # FP32: inside the 1e-9 cluster single pair terms are ~1e4 times the velocities they
+    # sum to (alternating signs cancel), so the FP32 rounding of each pair reaches ~1e-5 of
+    # the result there; the decisions (tree, epsilon, merges) stay exact.
+    tol32 = dict(TOL32, vel_tol=5e-5, diff_tol=5e-5)
     for precision in (0, 1):
         got, _ = run_gpu(wl, precision, full_lists=True)
-        tol = TOL64 if precision == 0 else TOL32
+        tol = TOL64 if precision == 0 else tol32
         bad = check_step(ref, got, **tol)
         assert not bad, (precision, bad)

@@ -28,6 +28,10 @@ constexpr int CW = 4;  // warps per block
 __device__ __forceinline__ double rcp64(double x) {
     double r;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    // x = +-0 or +-inf: the approximation is already the exact 1/x, and a Newton step
+    // would turn it into NaN (0 * inf); the reference's 1/inf = 0 and g/0 = inf matter for
+    // vortices whose epsilon is 0 (coincident vortices)
+    if (r == 0.0 || isinf(r)) return r;
     double e = fma(-x, r, 1.0);
     r = fma(r, e, r);
     e = fma(-x, r, 1.0);
