@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(SW * 32) k_small_split(const int32_t* __restri
     const int32_t k = list[t];
     const int32_t f = vf[k], n = vl[k] - f;
     const bool byx = axis[k] != 0;
-    const double pv = pivot[k];
+    const unsigned long long kp = lt_key_of(pivot[k]);
     double ex[2], ey[2];
     int32_t ep[2];
     bool val[2], low[2];
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(SW * 32) k_small_split(const int32_t* __restri
         ex[h] = val[h] ? x[f + q] : 0.;
         ey[h] = val[h] ? y[f + q] : 0.;
         ep[h] = val[h] ? perm[f + q] : 0;
-        low[h] = val[h] && ((byx ? ex[h] : ey[h]) < pv);
+        low[h] = val[h] && lt_key(byx ? ex[h] : ey[h], kp);
     }
     const unsigned m0 = __ballot_sync(0xffffffffu, low[0]), m1 = __ballot_sync(0xffffffffu, low[1]);
     const int L = __popc(m0) + __popc(m1);
@@ -393,12 +393,12 @@ __global__ void __launch_bounds__(CT) k_chunk_count(const int32_t* __restrict__ 
     __shared__ int s_c[CNW];
     const ChunkPos p = chunk_pos(blockIdx.x, chunk_node, cbase, vf, vl);
     const double* key = axis[p.k] ? x : y;
-    const double pv = pivot[p.k];
+    const unsigned long long kp = lt_key_of(pivot[p.k]);
     int cl = 0;
 #pragma unroll
     for (int e = 0; e < CE; e++) {
         const int q = p.j * CH + e * CT + threadIdx.x;
-        cl += __popc(__ballot_sync(0xffffffffu, q < p.n && key[p.f + q] < pv));
+        cl += __popc(__ballot_sync(0xffffffffu, q < p.n && lt_key(key[p.f + q], kp)));
     }
     if ((threadIdx.x & 31) == 0) s_c[threadIdx.x >> 5] = cl;
     __syncthreads();
@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(CT) k_chunk_place(const int32_t* __restrict__ 
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const ChunkPos p = chunk_pos(blockIdx.x, chunk_node, cbase, vf, vl);
     const bool byx = axis[p.k] != 0;
-    const double pv = pivot[p.k];
+    const unsigned long long kp = lt_key_of(pivot[p.k]);
     const int L = pre[p.cb + p.nch] - pre[p.cb];
     const int before = pre[blockIdx.x] - pre[p.cb];  // lows in the node's earlier chunks
     double ex[CE], ey[CE];
@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(CT) k_chunk_place(const int32_t* __restrict__ 
         const bool v = q < p.n;
         ex[e] = v ? x[p.f + q] : 0.;
         ey[e] = v ? y[p.f + q] : 0.;
-        lowm[e] = __ballot_sync(0xffffffffu, v && ((byx ? ex[e] : ey[e]) < pv));
+        lowm[e] = __ballot_sync(0xffffffffu, v && lt_key(byx ? ex[e] : ey[e], kp));
         if (lane == 0) s_cnt[e * CNW + w] = __popc(lowm[e]);
     }
     __syncthreads();
@@ -749,8 +749,8 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
     // next node: its parent's slot.
     double* sx = (double*)smem;
     double* sy = sx + SUB_N;
-    double* lpiv = sy + SUB_N;
-    int64_t* lpath = (int64_t*)(lpiv + SUB_N);                // [2][SUB_N]
+    unsigned long long* lkp = (unsigned long long*)(sy + SUB_N);  // pivot keys (lt_key_of)
+    int64_t* lpath = (int64_t*)(lkp + SUB_N);                 // [2][SUB_N]
     int32_t* sp = (int32_t*)(lpath + 2 * SUB_N);
     int32_t* pre = sp + SUB_N;                                // SUB_N + 1
     int32_t* wt = pre + SUB_N + 4;                            // SUB_NW (60 ints reserved)
@@ -785,7 +785,7 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
         }
     }
     if (t == 0) {
-        lvf[0] = 0; ln[0] = (int16_t)nr; lpiv[0] = pivot[root]; lax[0] = (int8_t)axis[root];
+        lvf[0] = 0; ln[0] = (int16_t)nr; lkp[0] = lt_key_of(pivot[root]); lax[0] = (int8_t)axis[root];
         lsp[0] = 1; lpath[0] = path[root];
     }
     int cur = 0, ncur = 1, base = 0, next_lid = 1;  // base: local id of the level's slot 0
@@ -812,7 +812,7 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
             const int i = e * SUB_T + t;
             const int nd = en[co + i];
             bool low = false;
-            if (nd >= 0 && lsp[nd]) low = (lax[nd] ? sx[i] : sy[i]) < lpiv[nd];
+            if (nd >= 0 && lsp[nd]) low = lt_key(lax[nd] ? sx[i] : sy[i], lkp[nd]);
             pre[i] = low ? 1 : 0;
         }
         __syncthreads();
@@ -896,7 +896,7 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
                 double pv;
                 lsp[cs] = (int8_t)decide_vals(gm, n, 0, dep + 1, min_node, max_node, err, ax, pv);
                 lax[cs] = (int8_t)ax;
-                lpiv[cs] = pv;
+                lkp[cs] = lt_key_of(pv);
                 SubNode o;
                 o.geom = gm;
                 o.path = lpath[no + cs];

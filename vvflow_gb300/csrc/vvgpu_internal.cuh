@@ -284,6 +284,17 @@ __device__ __forceinline__ double dunkey(unsigned long long k) {
     unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
     return __longlong_as_double((long long)u);
 }
+// x < p on the integer pipe (sm_103's FP64 pipe is narrow): order-preserving keys with -0
+// folded onto +0, and NaN never below, as the IEEE comparison.  kp = lt_key_of(p), p not NaN.
+__device__ __forceinline__ unsigned long long lt_key_of(double v) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    if ((u << 1) == 0ull) u = 0ull;
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ bool lt_key(double x, unsigned long long kp) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    return lt_key_of(x) < kp && (u & 0x7fffffffffffffffull) <= 0x7ff0000000000000ull;
+}
 inline unsigned long long dkey_host(double v) {
     unsigned long long u;
     memcpy(&u, &v, 8);
