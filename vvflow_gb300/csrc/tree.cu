@@ -988,10 +988,13 @@ __device__ __forceinline__ void combine_cm(const double* a, const double* b, dou
 // All inner centroids in one pass: each leaf's thread climbs towards the root, and at each
 // node the second child to arrive combines both children (always in the order ch1, ch1 + 1,
 // so the result does not depend on which arrives last) and climbs on.
-__global__ void k_tree_cm(int64_t nn, const int32_t* __restrict__ ch1, const int32_t* __restrict__ parent,
-                          const double4* __restrict__ geom, double* cm, int32_t* lc, int32_t* arrive) {
+// Climbs start at the leaves of nodes [0, nn), and with `split` also at the subtree roots
+// (split == 2), whose subtrees k_subtree_cm has completed.
+__global__ void k_tree_cm(int64_t nn, const int32_t* __restrict__ ch1, const int32_t* __restrict__ split,
+                          const int32_t* __restrict__ parent, const double4* __restrict__ geom, double* cm,
+                          int32_t* lc, int32_t* arrive) {
     const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k0 >= nn || ch1[k0] >= 0) return;
+    if (k0 >= nn || (ch1[k0] >= 0 && !(split && split[k0] == 2))) return;
     int32_t k = (int32_t)k0;
     for (int it = 0; it <= MAX_DEPTH; it++) {
         const int32_t p = parent[k];
@@ -1013,6 +1016,71 @@ __global__ void k_tree_cm(int64_t nn, const int32_t* __restrict__ ch1, const int
         for (int q = 0; q < 6; q++) cm[6 * (size_t)p + q] = o[q];
         lc[p] = __ldcg(lc + c1) + __ldcg(lc + c1 + 1);
         k = p;
+    }
+}
+
+// Centroids and leaf counts of every subtree built by k_subtree, one block per subtree:
+// its vortices are staged in shared memory (one coalesced read), each leaf sums its own in
+// the order of k_leaf_cm, then the inner nodes combine their children deepest level first
+// as k_tree_cm does (a subtree's ids are breadth-first, so its deepest node is the last).
+// The subtree's root is completed here too; the level loop's nodes above it climb later.
+__global__ void __launch_bounds__(SUB_T) k_subtree_cm(const int32_t* __restrict__ roots,
+                                                      const int32_t* __restrict__ pos,
+                                                      const int32_t* __restrict__ nnew, int64_t base0,
+                                                      const int32_t* __restrict__ vf, const int32_t* __restrict__ vl,
+                                                      const int32_t* __restrict__ ch1,
+                                                      const int32_t* __restrict__ depth,
+                                                      const double4* __restrict__ geom, const double* __restrict__ x,
+                                                      const double* __restrict__ y, const double* __restrict__ g,
+                                                      double* cm, int32_t* lc) {
+    __shared__ double sx[SUB_N], sy[SUB_N], sg[SUB_N];
+    const int t = threadIdx.x;
+    const int32_t root = roots[blockIdx.x], cnt = nnew[blockIdx.x];
+    const int64_t b = base0 + pos[blockIdx.x] - 1;  // id of local node u >= 1
+    const int32_t f0 = vf[root], nr = vl[root] - f0;
+    if (cnt <= 0 || nr > SUB_N) return;
+    for (int i = t; i < nr; i += SUB_T) {
+        sx[i] = x[f0 + i];
+        sy[i] = y[f0 + i];
+        sg[i] = g[f0 + i];
+    }
+    __syncthreads();
+    for (int32_t u = 1 + t; u <= cnt; u += SUB_T) {
+        const int64_t k = b + u;
+        if (ch1[k] >= 0) continue;
+        double px = 0, py = 0, pg = 0, mx = 0, my = 0, mg = 0;
+        for (int32_t i = vf[k] - f0; i < vl[k] - f0; i++) {
+            const double gi = sg[i];
+            if (gi > 0) { px = dadd(px, dmul(sx[i], gi)); py = dadd(py, dmul(sy[i], gi)); pg = dadd(pg, gi); }
+            else        { mx = dadd(mx, dmul(sx[i], gi)); my = dadd(my, dmul(sy[i], gi)); mg = dadd(mg, gi); }
+        }
+        const double4 gm = geom[k];
+        if (pg != 0) { double inv = ddiv(1., pg); px = dmul(px, inv); py = dmul(py, inv); } else { px = gm.x; py = gm.y; }
+        if (mg != 0) { double inv = ddiv(1., mg); mx = dmul(mx, inv); my = dmul(my, inv); } else { mx = gm.x; my = gm.y; }
+        double* c = cm + 6 * k;
+        c[0] = px; c[1] = py; c[2] = pg; c[3] = mx; c[4] = my; c[5] = mg;
+        lc[k] = 1;
+    }
+    const int32_t dmax = depth[b + cnt], droot = depth[root];
+    for (int32_t d = dmax - 1; d >= droot; d--) {
+        __syncthreads();
+        for (int32_t u = t; u <= cnt; u += SUB_T) {
+            const int64_t k = u == 0 ? (int64_t)root : b + u;
+            const int32_t c1 = ch1[k];
+            if (c1 < 0 || depth[k] != d) continue;
+            const double4 gm = geom[k];
+            double A[6], B[6], o[6];
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                A[q] = __ldcg(cm + 6 * (size_t)c1 + q);
+                B[q] = __ldcg(cm + 6 * (size_t)(c1 + 1) + q);
+            }
+            combine_cm(A, B, o, gm.x, gm.y);
+            combine_cm(A + 3, B + 3, o + 3, gm.x, gm.y);
+#pragma unroll
+            for (int q = 0; q < 6; q++) cm[6 * k + q] = o[q];
+            lc[k] = __ldcg(lc + c1) + __ldcg(lc + c1 + 1);
+        }
     }
 }
 
@@ -1204,14 +1272,15 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
     }
     c.depth = (int64_t)c.level_begin.size() - 1;
     // the subtrees the loop deferred (split == 2), one block each, in node order
+    const int64_t nn0 = c.nnodes;
+    int32_t ndef = 0;
     {
-        const int64_t nn0 = c.nnodes;
         c.flags.reserve(nn0 + 2);
         c.scan.reserve(nn0 + 2);
         k_defer_flags<<<grid_for(nn0, TB), TB, 0, s>>>(nn0, c.nd_split.p, c.flags.p);
         VV_LAUNCH_CHECK();
         exclusive_scan(c, c.flags.p, c.scan.p, nn0);
-        const int32_t ndef = read_i32(c, c.scan.p + nn0);
+        ndef = read_i32(c, c.scan.p + nn0);
         if (ndef > 0) {
             c.sub_i32.reserve(3 * (size_t)ndef + 4);
             int32_t* roots = c.sub_i32.p;
@@ -1256,11 +1325,19 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
     c.nd_dfs.reserve(nn);
     c.nd_arrive.reserve(nn);
     VV_CUDA(cudaMemsetAsync(c.nd_arrive.p, 0, nn * sizeof(int32_t), s));
-    k_leaf_cm<<<grid_for(nn, TB), TB, 0, s>>>(nn, c.nd_ch1.p, c.nd_vf.p, c.nd_vl.p, c.nd_geom.p, c.x.p, c.y.p,
-                                              c.g.p, c.nd_cm.p, c.nd_lc.p);
+    // the loop's leaves; the subtrees whole (one block each); then the climbs above them
+    k_leaf_cm<<<grid_for(nn0, TB), TB, 0, s>>>(nn0, c.nd_ch1.p, c.nd_vf.p, c.nd_vl.p, c.nd_geom.p, c.x.p, c.y.p,
+                                               c.g.p, c.nd_cm.p, c.nd_lc.p);
     VV_LAUNCH_CHECK();
-    k_tree_cm<<<grid_for(nn, TB), TB, 0, s>>>(nn, c.nd_ch1.p, c.nd_parent.p, c.nd_geom.p, c.nd_cm.p, c.nd_lc.p,
-                                              c.nd_arrive.p);
+    if (ndef > 0) {
+        const int32_t* roots = c.sub_i32.p;
+        k_subtree_cm<<<ndef, SUB_T, 0, s>>>(roots, roots + 2 * ndef + 1, roots + ndef, nn0, c.nd_vf.p, c.nd_vl.p,
+                                            c.nd_ch1.p, c.nd_depth.p, c.nd_geom.p, c.x.p, c.y.p, c.g.p, c.nd_cm.p,
+                                            c.nd_lc.p);
+        VV_LAUNCH_CHECK();
+    }
+    k_tree_cm<<<grid_for(nn0, TB), TB, 0, s>>>(nn0, c.nd_ch1.p, ndef > 0 ? c.nd_split.p : nullptr, c.nd_parent.p,
+                                               c.nd_geom.p, c.nd_cm.p, c.nd_lc.p, c.nd_arrive.p);
     VV_LAUNCH_CHECK();
     int32_t nl = read_i32(c, c.nd_lc.p);
     c.nleaves = nl;
