@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--config", default="wake4m", choices=["wake4m", "batched", "learned"],
                     help="wake4m: the 4M-vortex ellipse wake (default); batched: the sweep of independent "
                          "cylinder simulations advanced together (vvgpu_batch_step); learned: the far-field MLP "
-                         "trained on cylinder-annulus runs and judged at theta = 0.8 on the 4M cylinder wake")
+                         "trained on cylinder-annulus runs and evaluated at theta = 0.8 on the 4M cylinder wake")
     ap.add_argument("--instances", type=int, default=256, help="--config batched: number of simulations")
     return ap.parse_args()
 
@@ -618,7 +618,7 @@ def batched_arm(args):
 
 
 # ---------------------------------------------------------------------------------------
-# learned far-field correction: train, then judge at theta = 0.8 on the 4M cylinder wake
+# learned far-field correction: train, then evaluate at theta = 0.8 on the 4M cylinder wake
 def learned_arm(args):
     import torch
 
@@ -708,7 +708,7 @@ def learned_arm(args):
     learned = err(lx, ly)
     plain08 = err(ux, uy)
     plain05 = err(wx, wy)
-    judge_gap = float(np.sqrt(np.mean((lx - wx) ** 2 + (ly - wy) ** 2)) / np.sqrt(np.mean(mag ** 2)))
+    check_gap = float(np.sqrt(np.mean((lx - wx) ** 2 + (ly - wy) ** 2)) / np.sqrt(np.mean(mag ** 2)))
     pairs_per_target = npairs / len(px)
     per_pair_s = corr_s / max(1, npairs)
     fwd_flop = 2 * (20 * 64 + 64 * 64 + 64 * 2)
@@ -716,7 +716,7 @@ def learned_arm(args):
         "metric": "learned far-field correction: (cell, target) pairs/s evaluated (features + tcgen05 MLP)",
         "value": npairs / corr_s, "unit": "pairs/s", "n_gpus": 1, "higher_is_better": True,
         "dtype": "bf16 (fp32 accumulate)", "data": "synthetic (seeded)",
-        "config": {"workload": f"train: cylinder-annulus runs (20k vortices, M=500), theta=0.8; judge: "
+        "config": {"workload": f"train: cylinder-annulus runs (20k vortices, M=500), theta=0.8; evaluated on: "
                                f"cylinder wake {N} vortices (M=2000), 4096 sampled targets",
                    "network": "20-64-64-2 tanh-GELU"},
         "training": {"pairs": int(nsamp), "runs": runs, "sample_seconds": round(gen_s, 2),
@@ -726,8 +726,8 @@ def learned_arm(args):
         "error_vs_fp64_direct": {"learned_theta_0.8": learned, "plain_theta_0.8": plain08,
                                  "plain_theta_0.5": plain05},
         "error_ratio_learned_over_plain_theta_0.8": learned["rms_rel"] / plain08["rms_rel"],
-        "judge": {"reference": "plain tree theta 0.5 on the sampled targets", "rms_rel_gap": judge_gap,
-                  "bound": 1e-5, "pass": bool(judge_gap <= 1e-5)},
+        "accuracy_check": {"reference": "plain tree theta 0.5 on the sampled targets", "rms_rel_gap": check_gap,
+                  "bound": 1e-5, "pass": bool(check_gap <= 1e-5)},
         "fp32_step_ms": step_ms,
         "cost": {"pairs_per_target": pairs_per_target, "correction_seconds_4096": round(corr_s, 4),
                  "moments_and_first_call_seconds": round(first_s, 4),

@@ -134,7 +134,7 @@ def test_gpu_mlp_training_lowers_tree_error():
     losses = M.train(epochs=40, batch=4096, lr=2e-3, seed=5)
     assert losses[-1] < 0.2 * losses[0], losses
     # held-out configuration: the loose tree with and without the correction, the FP64
-    # direct sum (each source's own epsilon) as the judge
+    # direct sum (each source's own epsilon) as the reference
     wl = W.cylinder_annulus(20000, 500, seed=21)
     G = _space(wl, FC08)
     G.eps(False)
