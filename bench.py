@@ -69,6 +69,22 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(v, dist=None, device="cpu"):
+    """Largest v over the ranks (every rank gets it); v itself without a process group."""
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(world, n_per_replica, ms_max):
+    """Whole-job throughput of `world` independent replicas of n_per_replica vortices each,
+    timed by the slowest rank (vortex-steps/s)."""
+    return world * n_per_replica / (ms_max / 1e3)
+
+
 def workload(n, m, rank):
     from vvflow_gb300 import workloads as W
     return W.ellipse_wake(n, m, seed=3 + rank, angle_deg=10.0)
@@ -262,11 +278,7 @@ def gpu_arm(args):
             dist.barrier()
 
     def maxall(v):
-        if dist is None:
-            return v
-        t = torch.tensor([v], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks(v, dist, dev)
 
     # ---- FP32-pairwise path (headline) -------------------------------------------------
     S = make(VVGPU_FP32)
@@ -293,7 +305,7 @@ def gpu_arm(args):
     st1 = S.stats()
     conv_ms = float(np.mean([a.elapsed_time(b) for a, b in cev]))
     launches = int(st1["launches"] - st0["launches"])
-    value = world * N / (ms_max / 1e3)
+    value = replicas_value(world, N, ms_max)
 
     # phase split of one step (host-timed with synchronisation, for the record)
     phases = {}
@@ -447,7 +459,7 @@ def gpu_arm(args):
                                          "diff_candidates")},
             "roofline": roof,
             "cpu_baseline": cpu,
-            "e2e": {"value": world * N / (e2e_ms / 1e3), "unit": "vortex-steps/s", "ms_per_step": e2e_ms,
+            "e2e": {"value": replicas_value(world, N, e2e_ms), "unit": "vortex-steps/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clocks,
         }
