@@ -479,17 +479,22 @@ __global__ void __launch_bounds__(CT) k_chunk_place(const int32_t* __restrict__ 
         for (int e = 0; e < 4; e++) { s_b[w][e] = b0[e]; s_b[w][4 + e] = b1[e]; }
     }
     __syncthreads();
-    if (tid == 0) {
+    if (tid < 8) {
+        // thread 4 child + c merges component c of that child's box over the warps and
+        // commits it (min for the lower corner, max for the upper)
+        const int comp = tid & 3, chd = tid >> 2;
+        unsigned long long v = s_b[0][4 * chd + comp];
         for (int q = 1; q < CNW; q++) {
-            bbox_merge(b0, &s_b[q][0]);
-            bbox_merge(b1, &s_b[q][4]);
+            const unsigned long long u = s_b[q][4 * chd + comp];
+            v = comp < 2 ? (u < v ? u : v) : (u > v ? u : v);
         }
-        int lows = 0;
-        for (int q = 0; q < CE * CNW; q++) lows += s_cnt[q];
+        const int lows = s_pre[CE * CNW - 1] + s_cnt[CE * CNW - 1];
         const int lo = p.j * CH, hi = min(p.n, lo + CH);
-        const int32_t c1 = ch1[k];
-        if (lows > 0) bbox_commit(bbox + 4 * (size_t)c1, b0);
-        if (lows < hi - lo) bbox_commit(bbox + 4 * (size_t)(c1 + 1), b1);
+        if (chd == 0 ? lows > 0 : lows < hi - lo) {
+            unsigned long long* dst = bbox + 4 * (size_t)(ch1[k] + chd) + comp;
+            if (comp < 2) atomicMin(dst, v);
+            else atomicMax(dst, v);
+        }
     }
 }
 
