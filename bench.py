@@ -204,8 +204,9 @@ class Clocks:
 
 # ---------------------------------------------------------------------------------------
 # GPU arm
-def hot_path(S, wl, mn, mx, times=None, ev=None):
-    """One simulate() iteration of the hot path (utils/vvflow/vvflow.cpp:214-255)."""
+def hot_path(S, wl, mn, mx, times=None, ev=None, evd=None):
+    """One simulate() iteration of the hot path (utils/vvflow/vvflow.cpp:214-255).  ev / evd:
+    CUDA event pairs recorded around the convective / diffusive calls."""
     S.tree_build(wl.far_criteria, mn, mx)
     S.slae()
     S.tree_destroy()
@@ -217,7 +218,11 @@ def hot_path(S, wl, mn, mx, times=None, ev=None):
     S.convective()
     if ev is not None:
         ev[1].record()
+    if evd is not None:
+        evd[0].record()
     S.diffusive()
+    if evd is not None:
+        evd[1].record()
     S.tree_destroy()
 
 
@@ -289,13 +294,14 @@ def gpu_arm(args):
     st0 = S.stats()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    dev_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     clk = Clocks(local)
     barrier()
     torch.cuda.synchronize()
     e0.record()
     for k in range(args.steps):
         restore(S)
-        hot_path(S, wl, mn, mx, ev=cev[k])
+        hot_path(S, wl, mn, mx, ev=cev[k], evd=dev_ev[k])
     e1.record()
     torch.cuda.synchronize()
     barrier()
@@ -304,6 +310,7 @@ def gpu_arm(args):
     ms_max = maxall(ms)
     st1 = S.stats()
     conv_ms = float(np.mean([a.elapsed_time(b) for a, b in cev]))
+    diff_ms = float(np.mean([a.elapsed_time(b) for a, b in dev_ev]))
     launches = int(st1["launches"] - st0["launches"])
     value = replicas_value(world, N, ms_max)
 
@@ -437,6 +444,23 @@ def gpu_arm(args):
             "launch_ms": conv_ms,
             "peak_source": "cuBLAS FP32 SGEMM (TF32 off) measured in this run"}
 
+    # The diffusive pass against HBM (its data stays in L2 at this size, so this says how far
+    # from a bandwidth bound it runs): bytes of the pruned candidate stream, per 8-target
+    # chunk, 16 B per source record; each target's record and velocity (16 + 16 B read and
+    # written); 8 B per near run read.
+    hbm = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm = float(json.load(f)["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        hbm = 6800.0
+    diff_bytes = 16 * st1["diff_sources"] + 48 * N + 8 * stp["near_runs"]
+    roof_diff = {"bound": "hbm", "kernel": "k_diff32<2> (diffusive)",
+                 "achieved": diff_bytes / (diff_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                 "frac": diff_bytes / (diff_ms / 1e3) / 1e9 / hbm, "traffic": None,
+                 "algorithmic_bytes_per_launch": diff_bytes, "candidate_sources": st1["diff_sources"],
+                 "launch_ms": diff_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, burst)"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(wl, args.cpu_stride)
@@ -458,6 +482,7 @@ def gpu_arm(args):
                                          "merged", "eps_evaluations", "near_pairs", "far_pairs",
                                          "diff_candidates")},
             "roofline": roof,
+            "roofline_diffusive": roof_diff,
             "cpu_baseline": cpu,
             "e2e": {"value": replicas_value(world, N, e2e_ms), "unit": "vortex-steps/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -119,7 +119,9 @@ typedef struct vvgpu_stats {
     int64_t merged;             /* merges in the last epsilon pass                       */
     int64_t diff_candidates;    /* vortex pairs inside the 8-eps cut-off boxes           */
     int64_t reserved[8];        /* reserved[0]: kernels launched by the context so far;
-                                   reserved[1]: target evaluations over all epsilon rounds */
+                                   reserved[1]: target evaluations over all epsilon rounds;
+                                   reserved[2]: sources in the candidate leaves of every
+                                   8-target chunk of the last FP32 diffusive pass */
 } vvgpu_stats;
 
 /* ---- context --------------------------------------------------------------------- */

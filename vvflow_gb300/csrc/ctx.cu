@@ -218,6 +218,7 @@ int vvgpu_get_stats(const vvgpu_ctx* h, vvgpu_stats* out) {
     *out = h->c.stats;
     out->reserved[0] = h->c.launches;
     out->reserved[1] = h->c.eps_evaluations;
+    out->reserved[2] = h->c.diff_sources;
     return VVGPU_OK;
 }
 

@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
     const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
     const float bandc = ldexpf(64.f, -19);
     double(&d64)[DT * 6][32] = s_d64[wq];
-    unsigned long long ncand = 0;
+    unsigned long long ncand = 0, nsrc = 0;
     for (int32_t c0 = v0; c0 < v1; c0 += 8) {
         const int32_t tb = c0 + grp * DT;  // first target of this lane's group
         float tx[DT], ty[DT], ief[DT], ie2[DT], b16[DT], iefl[DT];
@@ -445,7 +445,10 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
                 s_hitq[wq][nh_acc + r] = q;
             }
             __syncwarp();
-            if (lane == 0) ncand += (unsigned long long)nact * (unsigned long long)total;
+            if (lane == 0) {
+                ncand += (unsigned long long)nact * (unsigned long long)total;
+                nsrc += (unsigned long long)total;
+            }
             nh_acc += nh;
             tot_acc += total;
             seg_acc = seg_acc || any_seg;
@@ -512,7 +515,9 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
         }
     }
     ncand = warp_sum_u64(ncand);
+    nsrc = warp_sum_u64(nsrc);
     if (lane == 0 && ncand) atomicAdd(a.cand, ncand);
+    if (lane == 0 && nsrc) atomicAdd(a.cand + 1, nsrc);
 }
 
 // two targets per lane, four lane groups: measured faster than four targets per lane at 4M
@@ -541,16 +546,17 @@ void diffusive(Ctx& c) {
     a.rx = c.s_rx.p; a.ry = c.s_ry.p; a.dlx = c.s_dlx.p; a.dly = c.s_dly.p; a.fric = c.s_fric.p;
     a.anchor = c.lf_anchor.p; a.box = c.lf_dbox.p; a.src32 = c.src32.p; a.src_k = c.src_k.p; a.src_ie = c.src_ie.p;
     a.G = c.frame_G; a.Gf = (float)c.frame_G; a.re = c.re;
-    VV_CUDA(cudaMemsetAsync(c.counters.p + 2, 0, 8, s));
+    VV_CUDA(cudaMemsetAsync(c.counters.p + 2, 0, 16, s));  // candidate pairs, candidate sources
     a.cand = c.counters.p + 2;
     unsigned grid = grid_for(nl, DW);
     if (c.precision == VVGPU_FP32) k_diff32<DIFF32_DT><<<grid, DW * 32, 0, s>>>(a);
     else k_diff64<<<grid, DW * 32, 0, s>>>(a);
     VV_LAUNCH_CHECK();
-    unsigned long long cand = 0;
-    VV_CUDA(cudaMemcpyAsync(&cand, c.counters.p + 2, 8, cudaMemcpyDeviceToHost, s));
+    unsigned long long cand[2] = {0, 0};
+    VV_CUDA(cudaMemcpyAsync(cand, c.counters.p + 2, 16, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));
-    c.stats.diff_candidates = (int64_t)cand;
+    c.stats.diff_candidates = (int64_t)cand[0];
+    c.diff_sources = (int64_t)cand[1];
 }
 
 }  // namespace vvgpu

@@ -1295,7 +1295,7 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
             VV_LAUNCH_CHECK();
             c.sub_scratch.reserve(4 * (size_t)n + 2);
             SubNode* scratch = reinterpret_cast<SubNode*>(c.sub_scratch.p);
-            int32_t* maxdep = (int32_t*)(c.counters.p + 3);
+            int32_t* maxdep = (int32_t*)(c.counters.p + 5);
             VV_CUDA(cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SUB_SMEM));
             k_subtree<<<ndef, SUB_T, SUB_SMEM, s>>>(roots, c.nd_vf.p, c.nd_vl.p, c.nd_depth.p, c.nd_path.p,
                                                     c.nd_pivot.p, c.nd_axis.p, min_node, max_node, c.x.p, c.y.p,

@@ -242,6 +242,7 @@ struct Ctx {
     vvgpu_stats stats{};
     int64_t launches = 0;           // kernels launched by this context
     int64_t eps_evaluations = 0;    // target evaluations over the rounds of the last epsilon pass
+    int64_t diff_sources = 0;       // sources in the candidate leaves of every diffusive target chunk
     bool count_pairs = true;        // count algorithmic near pairs before each convective pass
 
     cudaStream_t st() const { return stream; }

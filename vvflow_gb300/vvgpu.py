@@ -219,6 +219,7 @@ class GpuSpace:
         d = {k: getattr(s, k) for k, _ in Stats._fields_ if k != "reserved"}
         d["launches"] = int(s.reserved[0])
         d["eps_evaluations"] = int(s.reserved[1])
+        d["diff_sources"] = int(s.reserved[2])
         return d
 
     # -- state -----------------------------------------------------------------------
