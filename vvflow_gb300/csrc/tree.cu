@@ -689,7 +689,7 @@ constexpr int SUB_NW = SUB_T / 32;
 static_assert(SUB_N % SUB_T == 0 && SUB_NW <= 32, "subtree block shape");
 
 struct SubNode {  // a node made by k_subtree, before its final id is known
-    double4 geom;  // holds the box keys while the node's box is reduced
+    double4 geom;  // centre x, y, h, w (Stretch)
     int64_t path;
     int32_t vf, vl, ch1, parent, depth, pad;
 };
