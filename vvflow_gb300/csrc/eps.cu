@@ -220,7 +220,7 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
                            float* rlist, float* rnear, const int32_t* __restrict__ leaf_changed, int32_t* dirty,
                            int32_t* chg, int32_t* nchg, const float4* __restrict__ box_prev,
                            const float* __restrict__ rreg, const int32_t* __restrict__ chg_pre, int first_round,
-                           const float* __restrict__ dmax_p) {
+                           const int32_t* __restrict__ leaf_disp) {
     __shared__ int2 s_runs[EB / 32][32];
     const int wq = threadIdx.x >> 5;
     const int64_t L = (int64_t)blockIdx.x * (blockDim.x / 32) + wq;
@@ -243,7 +243,6 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
     }
     const float4 bL = box[L];
     const float2 aL = anchor[L];
-    const float dmax = first_round ? 0.f : *dmax_p;
     // upper bound on every target's second-nearest distance (squared)
     float R2 = INFINITY;
     if (bL.x <= bL.z) {
@@ -266,9 +265,8 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
         }
     }
     const float absm = ldexpf(fabsf(bL.x) + fabsf(bL.z) + fabsf(bL.y) + fabsf(bL.w) + Gf, -12);
-    const float need_r = isfinite(R2) ? sqrtf(R2) * (1.f + 1e-4f) + dmax + absm : INFINITY;
     const int32_t nc_old = first_round ? -2 : ncand[L];
-    const bool reuse = !first_round && nc_old >= 0 && need_r <= rlist[L];
+    const bool try_reuse = !first_round && nc_old >= 0 && isfinite(R2);
     // Near leaves whose members' outcomes changed in the last round and whose box (this or
     // the last round's, which hold every position those members had) comes within the
     // largest search radius of L's targets; each target then checks them against its own
@@ -301,13 +299,27 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
         }
         nch += __popc(m);
     };
-    if (reuse) {
-        for_near_leaves(near_run, r0, r1, s_runs[wq], collect);
-        if (lane == 0) {
-            nchg[L] = (nch > CHG_CAP) ? -1 : nch;
-            dirty[L] = nch > 0 ? 1 : 0;
+    // The list stays valid while R_L (now) plus the largest merge displacement of the near
+    // leaves' members fits inside the radius it was built with: a leaf left out had its box
+    // farther than that radius, and a box only grows by its members' merged positions.
+    bool collected = false;
+    if (try_reuse) {
+        float dloc = 0.f;
+        for_near_leaves(near_run, r0, r1, s_runs[wq], [&](int32_t q, bool ok) {
+            collect(q, ok);
+            if (ok) dloc = fmaxf(dloc, __int_as_float(leaf_disp[q]));
+        });
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dloc = fmaxf(dloc, __shfl_xor_sync(0xffffffffu, dloc, o));
+        const float need_r = sqrtf(R2) * (1.f + 1e-4f) + dloc + absm;
+        if (need_r <= rlist[L]) {
+            if (lane == 0) {
+                nchg[L] = (nch > CHG_CAP) ? -1 : nch;
+                dirty[L] = nch > 0 ? 1 : 0;
+            }
+            return;
         }
-        return;
+        collected = true;
     }
     // (re)build: near leaves within 2 R_L of L's box (FP32 with margins)
     const float lim = isfinite(R2) ? 2.f * sqrtf(R2) * (1.f + 1e-4f) + absm : INFINITY;
@@ -336,7 +348,7 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
         }
         cnt += __popc(mask);
         ext = fmaxf(ext, e);
-        collect(q, ok);
+        if (!collected) collect(q, ok);
     });
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -674,7 +686,7 @@ __global__ void k_zb_scatter(int64_t n, const int32_t* __restrict__ partner, con
                              const float2* __restrict__ anchor, double G, const double* __restrict__ ox,
                              const double* __restrict__ oy, const double* __restrict__ og,
                              const double* __restrict__ x0, const double* __restrict__ y0, int32_t* zb, float4* recO,
-                             int32_t* dmax_bits) {
+                             int32_t* dmax_bits, int32_t* leaf_disp) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int32_t p = partner[i];
@@ -685,6 +697,7 @@ __global__ void k_zb_scatter(int64_t n, const int32_t* __restrict__ partner, con
         // displacement of the merged position (rounded up), for the candidate-list check
         float d = (float)(fabs(ox[i] - x0[i]) + fabs(oy[i] - y0[i])) * (1.f + 1e-5f);
         atomicMax(dmax_bits, __float_as_int(d));
+        atomicMax(&leaf_disp[leaf_of[i]], __float_as_int(d));  // per leaf, for the list check
     }
 }
 
@@ -801,6 +814,7 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
     int64_t rounds = 0;
     const int64_t max_rounds = 4096;
     c.e_rlist.reserve(nl + 1);
+    c.e_ldisp.reserve(nl + 1);
     c.e_rnear.reserve(nl + 1);
     int32_t* dmax_bits = (int32_t*)(c.counters.p + 13);
     VV_CUDA(cudaMemsetAsync(dmax_bits, 0, 4, s));
@@ -816,8 +830,7 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                        c.lf_box32.p, c.e_live.p, fr.Gf, c.e_cand.p, c.e_ncand.p,
                                                        c.lf_rn.p, c.e_rlist.p, c.e_rnear.p, c.e_lchanged.p,
                                                        c.e_dirty.p, c.e_chg.p, c.e_nchg.p, c.e_box_prev.p,
-                                                       c.e_rreg.p, c.e_lchg_pre.p, rounds == 1,
-                                                       (const float*)dmax_bits);
+                                                       c.e_rreg.p, c.e_lchg_pre.p, rounds == 1, c.e_ldisp.p);
         VV_LAUNCH_CHECK();
         VV_CUDA(cudaMemsetAsync(c.e_changed.p, 0, 4, s));
         EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.e_rnear.p,
@@ -852,9 +865,10 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
         k_zb_reset<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_zb.p, c.e_zb_prev.p, c.e_zb.p);
         VV_LAUNCH_CHECK();
         VV_CUDA(cudaMemsetAsync(dmax_bits, 0, 4, s));
+        VV_CUDA(cudaMemsetAsync(c.e_ldisp.p, 0, (nl + 1) * 4, s));
         k_zb_scatter<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_partner[nx].p, c.leaf_of.p, c.lf_anchor.p, fr.G,
                                                     c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_x0.p, c.e_y0.p,
-                                                    c.e_zb.p, c.e_recO[nx].p, dmax_bits);
+                                                    c.e_zb.p, c.e_recO[nx].p, dmax_bits, c.e_ldisp.p);
         VV_LAUNCH_CHECK();
         VV_CUDA(cudaMemsetAsync(c.e_lchanged.p, 0, (nl + 1) * 4, s));
         k_leaf_changed<<<grid_for(n, EB), EB, 0, s>>>(n, c.leaf_of.p, c.e_partner[cur].p, c.e_partner[nx].p,

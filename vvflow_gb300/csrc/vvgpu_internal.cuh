@@ -213,6 +213,7 @@ struct Ctx {
     DArr<double> lf_mcs, lf_epr;
     DArr<int32_t> e_zb_prev, e_live, e_cand, e_ncand, e_dirty, e_lchanged;
     DArr<float> e_rlist, e_rnear;
+    DArr<int32_t> e_ldisp;          // per leaf: largest merge displacement of its members (float bits)
 
     // local FP32 frames (frame.cuh)
     double frame_G = 1.0;
