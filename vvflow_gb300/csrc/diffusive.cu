@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
     __shared__ float2 s_hitb[DW][HIT_CAP];  // error bound D of the leaf
     __shared__ float4 s_src[DW][SRC_CAP];  // staged sources: x, y in L's frame, g, index (bits)
     __shared__ int32_t s_hitq[DW][HIT_CAP]; // leaf
+    __shared__ unsigned long long s_nsrc[DW];  // candidate sources of the warp's chunks
     // per lane FP64 accumulators (s2x, s2y, s1, s3x, s3y, s0 of its targets), touched only by
     // band pairs and wall segments; lane-major so that lanes never share a bank row
     __shared__ double s_d64[DW][DT * 6][32];
@@ -236,7 +237,8 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
     const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
     const float bandc = ldexpf(64.f, -19);
     double(&d64)[DT * 6][32] = s_d64[wq];
-    unsigned long long ncand = 0, nsrc = 0;
+    unsigned long long ncand = 0;
+    if (lane == 0) s_nsrc[wq] = 0ull;
     for (int32_t c0 = v0; c0 < v1; c0 += 8) {
         const int32_t tb = c0 + grp * DT;  // first target of this lane's group
         float tx[DT], ty[DT], ief[DT], ie2[DT], b16[DT], iefl[DT];
@@ -447,7 +449,7 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
             __syncwarp();
             if (lane == 0) {
                 ncand += (unsigned long long)nact * (unsigned long long)total;
-                nsrc += (unsigned long long)total;
+                s_nsrc[wq] += (unsigned long long)total;  // in shared memory: no register held
             }
             nh_acc += nh;
             tot_acc += total;
@@ -515,9 +517,8 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
         }
     }
     ncand = warp_sum_u64(ncand);
-    nsrc = warp_sum_u64(nsrc);
     if (lane == 0 && ncand) atomicAdd(a.cand, ncand);
-    if (lane == 0 && nsrc) atomicAdd(a.cand + 1, nsrc);
+    if (lane == 0 && s_nsrc[wq]) atomicAdd(a.cand + 1, s_nsrc[wq]);
 }
 
 // two targets per lane, four lane groups: measured faster than four targets per lane at 4M

@@ -673,7 +673,8 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
         ox_new[i] = px; oy_new[i] = py; og_new[i] = gi; oie_new[i] = ie;
         dv.sr1[i] = sr1;
         dv.sr2[i] = sr2;
-        if (ch) *changed = 1;
+        const unsigned am = __activemask();  // one store per warp to the shared flag
+        if (__any_sync(am, ch) && (threadIdx.x & 31) == __ffs(am) - 1) *changed = 1;
     }
 }
 
@@ -696,8 +697,11 @@ __global__ void k_zb_scatter(int64_t n, const int32_t* __restrict__ partner, con
         recO[i] = make_float4(rel(ox[i], a.x), rel(oy[i], a.y), (float)dsgn(og[i]), 0.f);
         // displacement of the merged position (rounded up), for the candidate-list check
         float d = (float)(fabs(ox[i] - x0[i]) + fabs(oy[i] - y0[i])) * (1.f + 1e-5f);
-        atomicMax(dmax_bits, __float_as_int(d));
         atomicMax(&leaf_disp[leaf_of[i]], __float_as_int(d));  // per leaf, for the list check
+        // the global maximum: one atomic per warp (all merged vortices hit one address)
+        const unsigned am = __activemask();
+        const int wmax = __reduce_max_sync(am, __float_as_int(d));
+        if ((threadIdx.x & 31) == __ffs(am) - 1) atomicMax(dmax_bits, wmax);
     }
 }
 
@@ -731,7 +735,8 @@ __global__ void k_eps_final(int64_t n, const int32_t* __restrict__ partner, cons
     if (p != SKIPPED) ie[i] = oie[i];
     if (p >= 0) {
         x[i] = ox[i]; y[i] = oy[i]; g[i] = og[i];
-        atomicAdd(merged, 1ull);
+        const unsigned am = __activemask();  // one atomic per warp
+        if ((threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(merged, (unsigned long long)__popc(am));
     }
     if (zb[i] != INT_MAX) g[i] = 0.;
 }
