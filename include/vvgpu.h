@@ -196,7 +196,11 @@ int vvgpu_velocity_points(vvgpu_ctx* ctx, int64_t n, const double* px, const dou
 int vvgpu_velocity_points_noalloc(vvgpu_ctx* ctx, int64_t n, const double* px, const double* py,
                                   double* vx, double* vy);
 /* calc_circulation with no collision; rigid bodies at rest or in prescribed translation
- * are in scope (VVGPU_ERR_UNSUPPORTED otherwise). */
+ * are in scope (VVGPU_ERR_UNSUPPORTED otherwise).  The matrix and its inverse are refilled
+ * only when an input of the cells changed (bodies added or cleared, body parameters, dt,
+ * precision); otherwise only the right-hand side is filled, as the reference does once
+ * its matrix and inverse are in place (MConvectiveFast.cpp:245-246).  The FP32 context
+ * evaluates the right-hand side's tree sums in FP32 (cells stay FP64). */
 int vvgpu_slae(vvgpu_ctx* ctx, vvgpu_body_out* out);
 int vvgpu_vortex_shed(vvgpu_ctx* ctx);
 /* MFlowmove::move_and_clean(remove, &collision, &cleaned) (libvvhd/src/MFlowmove.cpp:11-215)
