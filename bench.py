@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "vortex-steps/s @4M vortices: learned/FP32 vs plain FP64 GPU at ≤1e-5 rel err"
 CONV32_DRAM_BYTES_4M = 444.3e6 + 54.1e6
+DIFF32_DRAM_BYTES_4M = 347.3e6 + 56.1e6
 L2_BYTES = 129 * 2**20
 
 
@@ -457,7 +458,10 @@ def gpu_arm(args):
     diff_bytes = 16 * st1["diff_sources"] + 48 * N + 8 * stp["near_runs"]
     roof_diff = {"bound": "hbm", "kernel": "k_diff32<2> (diffusive)",
                  "achieved": diff_bytes / (diff_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
-                 "frac": diff_bytes / (diff_ms / 1e3) / 1e9 / hbm, "traffic": None,
+                 "frac": diff_bytes / (diff_ms / 1e3) / 1e9 / hbm,
+                 # DRAM bytes of one k_diff32 launch of this workload, from one ncu capture
+                 # (profiles/step_dram_ellipse_wake_4M.md)
+                 "traffic": DIFF32_DRAM_BYTES_4M if (args.n, args.m) == (4_000_000, 4000) else None,
                  "algorithmic_bytes_per_launch": diff_bytes, "candidate_sources": st1["diff_sources"],
                  "launch_ms": diff_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, burst)"}
 
