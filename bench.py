@@ -456,7 +456,7 @@ def gpu_arm(args):
     except (OSError, ValueError, KeyError):
         hbm = 6800.0
     diff_bytes = 16 * st1["diff_sources"] + 48 * N + 8 * stp["near_runs"]
-    roof_diff = {"bound": "hbm", "kernel": "k_diff32<2> (diffusive)",
+    roof_diff = {"bound": "hbm", "kernel": "k_diff32 (diffusive)",
                  "achieved": diff_bytes / (diff_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
                  "frac": diff_bytes / (diff_ms / 1e3) / 1e9 / hbm,
                  # DRAM bytes of one k_diff32 launch of this workload, from one ncu capture

@@ -10,8 +10,9 @@
 //
 // One warp per target leaf in both paths.  FP64 path (k_diff64): eight target slots times
 // four source lanes, every pair in double precision with the reference's formulas.  FP32
-// path (k_diff32): two targets per lane in four lane groups, the eight lanes of a group
-// stride over the sources of the candidate leaves (staged in shared memory per batch);
+// path (k_diff32): DIFF32_DT targets per lane in 8 / DIFF32_DT lane groups (one target per
+// lane, eight groups of four lanes), the lanes of a group striding over the sources of the
+// candidate leaves (staged in shared memory per batch);
 // vortex pairs in local frames (frame.cuh) with
 // FP32 exp/rsqrt; pairs whose cut-off or coincidence test falls within a rigorous bound of
 // the FP32 error of its threshold are re-evaluated in FP64, so the set of contributing
@@ -521,10 +522,10 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
     if (lane == 0 && s_nsrc[wq]) atomicAdd(a.cand + 1, s_nsrc[wq]);
 }
 
-// two targets per lane, four lane groups: measured faster than four targets per lane at 4M
-// (11.0 vs 11.9 ms), the smaller register footprint allowing six blocks per SM
+// one target per lane, eight lane groups of four: measured faster than two targets per lane
+// (9.25 vs 9.92 ms at 4M) and four (11.9 ms), with fewer registers and spills
 #ifndef DIFF32_DT
-#define DIFF32_DT 2
+#define DIFF32_DT 1
 #endif
 
 }  // namespace
