@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(DW * 32) k_diff64(DiffArgs a) {
 // and the wall-segment terms, are evaluated in FP64 into per-lane accumulators that are
 // reduced in a fixed order, so results are reproducible.
 template <int DT>
-__global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
+__global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
     constexpr int LG = 4 * DT;  // lanes per group (source stride)
     __shared__ int2 s_runs[DW][32];
     __shared__ int4 s_hit[DW][HIT_CAP];     // flattened start, first vortex, shift x, shift y (bits)
@@ -523,7 +523,8 @@ __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
 }
 
 // one target per lane, eight lane groups of four: measured faster than two targets per lane
-// (9.25 vs 9.92 ms at 4M) and four (11.9 ms), with fewer registers and spills
+// (9.25 vs 9.92 ms at 4M) and four (11.9 ms), with fewer registers and spills; k_diff32's
+// launch bound of 7 blocks per SM (9.14 ms) beats 6 (9.25) and 8 (10.07, more spills)
 #ifndef DIFF32_DT
 #define DIFF32_DT 1
 #endif
