@@ -133,6 +133,11 @@ int vvgpu_set_precision(vvgpu_ctx* ctx, int precision);
 int vvgpu_set_stream(vvgpu_ctx* ctx, void* stream);
 int vvgpu_synchronize(vvgpu_ctx* ctx);
 int vvgpu_get_stats(const vvgpu_ctx* ctx, vvgpu_stats* out);
+/* Largest number of fixed-point rounds vvgpu_eps may take (default 4096; the passes measured
+ * take 5 to 7).  A pass that has not converged within it returns VVGPU_ERR_TIMEOUT and
+ * leaves the vortex list as it was; the tree stays built.  The reference's sequential pass
+ * has no such bound (MEpsilonFast.cpp:11-63). */
+int vvgpu_set_eps_round_limit(vvgpu_ctx* ctx, int64_t max_rounds);
 
 /* ---- Space state (host pointers) -------------------------------------------------- */
 /* Space::re, dt, inf_speed(), inf_g, time, gravity (libvvhd/headers/TSpace.hpp:19-36). */
@@ -150,7 +155,11 @@ int vvgpu_clear_bodies(vvgpu_ctx* ctx);
 /* Updates the parameters of body b (time functions evaluated at the current time). */
 int vvgpu_set_body_params(vvgpu_ctx* ctx, int body, const vvgpu_body_params* params);
 int vvgpu_set_sinks(vvgpu_ctx* ctx, int64_t n, const double* x, const double* y, const double* g);
-/* Replaces the vortex list (v = 0).  inv_eps may be NULL (= 0, a freshly loaded list). */
+/* Replaces the vortex list (v = 0).  inv_eps may be NULL (= 0, a freshly loaded list).
+ * The values are checked on the device: the next call that reads the list (tree build,
+ * direct sum, move_and_clean) returns VVGPU_ERR_ARG if a position or circulation is not
+ * finite or an inverse epsilon is NaN or negative (+inf, epsilon 0, is valid).  The
+ * reference does not check and carries NaN through its sums. */
 int vvgpu_set_vortices(vvgpu_ctx* ctx, int64_t n, const double* x, const double* y,
                        const double* g, const double* inv_eps);
 /* Same with device pointers (data already resident in HBM on the context's device). */
@@ -260,6 +269,11 @@ typedef struct vvgpu_mlp vvgpu_mlp;
 int vvgpu_mlp_create(int device, uint64_t seed, vvgpu_mlp** out);
 int vvgpu_mlp_destroy(vvgpu_mlp* m);
 const char* vvgpu_mlp_last_error(const vvgpu_mlp* m);
+/* Polls per tensor-core completion wait (default and largest 2^22).  A wait that runs out
+ * makes the call return VVGPU_ERR_TIMEOUT; the kernel lets its MMA land and releases its
+ * tensor memory first, so the model and the device stay usable.  0 makes every wait run
+ * out at once (the time-out path, exercised without a fault). */
+int vvgpu_mlp_set_wait_limit(vvgpu_mlp* m, int64_t spins);
 int64_t vvgpu_mlp_num_params(void);
 int vvgpu_mlp_get_params(vvgpu_mlp* m, float* out);
 int vvgpu_mlp_set_params(vvgpu_mlp* m, const float* in);

@@ -18,7 +18,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libvvref.so")
-REF_SRC = os.environ.get("VVD_REFERENCE_DIR", "/root/reference")
+# the reference checkout: VVD_REFERENCE_DIR, else a sibling folder "reference" of this repository
+REF_SRC = os.environ.get("VVD_REFERENCE_DIR", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 
 class BodyParams(C.Structure):

@@ -8,7 +8,8 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_HEADERS = os.path.join(os.environ.get("VVD_REFERENCE_DIR", "/root/reference"), "libvvhd", "headers")
+REF_HEADERS = os.path.join(os.environ.get("VVD_REFERENCE_DIR", os.path.join(os.path.dirname(ROOT), "reference")),
+                           "libvvhd", "headers")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_HEADERS), reason="reference headers not present")

@@ -82,6 +82,34 @@ def test_gpu_matches_oracle_wake_200k(precision):
     assert st["merge_rounds"] >= 1
 
 
+@pytest.fixture(scope="module")
+def wake_1m_oracle():
+    """One full, unsampled step of the oracle on the 1M-vortex cylinder wake (2000
+    segments, farCriteria 8): about a minute on the host cores."""
+    wl = W.cylinder_wake(1_000_000, 2000, seed=2)
+    S = oracle.OracleSpace("port")
+    S.load(wl)
+    ref = run_step(S, wl, full_lists=False)
+    S.close()
+    return wl, ref
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_gpu_matches_oracle_wake_1m(wake_1m_oracle, precision):
+    """The plain method at scale: 1M vortices, a 2000-segment cylinder.  Bit-exact: both
+    trees (permutation, leaf boxes and ranges, node centroids), the digests of every leaf's
+    near and far lists, the merge count, the merged positions and circulations and epsilon;
+    velocities, friction and the SLAE within the tolerances above."""
+    wl, ref = wake_1m_oracle
+    got, st = run_gpu(wl, precision, d={"seg_g": ref["seg_g"]}, full_lists=False)
+    tol = TOL64 if precision == 0 else TOL32
+    bad = check_step(ref, got, **tol)
+    assert not bad, bad
+    assert int(ref["merged"]) > 1000 and st["merge_rounds"] >= 2
+    assert int(ref["t2_sizes"][1]) > 50_000  # leaves
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
 def test_slae_matrix_reused_until_its_inputs_change(precision):

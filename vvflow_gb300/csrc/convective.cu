@@ -30,8 +30,10 @@ __device__ __forceinline__ double rcp64(double x) {
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
     // x = +-0 or +-inf: the approximation is already the exact 1/x, and a Newton step
     // would turn it into NaN (0 * inf); the reference's 1/inf = 0 and g/0 = inf matter for
-    // vortices whose epsilon is 0 (coincident vortices)
-    if (r == 0.0 || isinf(r)) return r;
+    // vortices whose epsilon is 0 (coincident vortices).  The approximation flushes
+    // subnormal inputs and results to zero: a subnormal x (|x| < 2.2e-308, whose 1/x is
+    // finite) or an x whose 1/x is subnormal takes the IEEE quotient instead.
+    if (r == 0.0 || isinf(r)) return (x == 0.0 || isinf(x)) ? r : 1.0 / x;
     double e = fma(-x, r, 1.0);
     r = fma(r, e, r);
     e = fma(-x, r, 1.0);
@@ -586,6 +588,7 @@ void velocity_points(Ctx& c, int64_t np, const double* px, const double* py, dou
 }
 
 void direct_velocity(Ctx& c, int64_t np, const double* px, const double* py, double* vx, double* vy) {
+    check_input(c);
     check_bodies_at_rest(c);
     if (np == 0) return;
     upload_segments(c);

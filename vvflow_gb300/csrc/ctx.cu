@@ -100,6 +100,21 @@ __global__ void k_iota64(int64_t* out, int64_t n, int64_t base) {
     if (i < n) out[i] = base + i;
 }
 
+// orig = 0..n-1, and *bad = 1 if a position or circulation is not finite or an inverse
+// epsilon is NaN or negative (+inf is a valid _1_eps: coincident vortices have epsilon 0)
+__global__ void k_set_orig_check(int64_t n, int64_t* __restrict__ orig, const double* __restrict__ x,
+                                 const double* __restrict__ y, const double* __restrict__ g,
+                                 const double* __restrict__ ie, int32_t* bad) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool b = false;
+    if (i < n) {
+        orig[i] = i;
+        b = !isfinite(x[i]) || !isfinite(y[i]) || !isfinite(g[i]);
+        if (ie) b = b || !(ie[i] >= 0.0);
+    }
+    if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) *bad = 1;
+}
+
 }  // namespace
 
 namespace vvgpu {
@@ -118,6 +133,14 @@ void upload_segments(Ctx& c) {
     h2d(c.s_slip, c.h_slip.data(), m, s);
     VV_CUDA(cudaStreamSynchronize(s));
     c.segs_dirty = false;
+}
+
+void check_input(Ctx& c) {
+    if (!c.in_pending) return;
+    c.in_pending = false;
+    if (read_i32(c, c.in_bad.p))
+        throw ApiError{VVGPU_ERR_ARG, "vortex list holds a non-finite position or circulation, or a NaN or "
+                                      "negative inverse epsilon"};
 }
 
 void ensure_vortex_capacity(Ctx& c, int64_t n, bool keep) {
@@ -204,6 +227,13 @@ int vvgpu_set_stream(vvgpu_ctx* h, void* stream) {
     API_BEGIN(h)
     VV_CUDA(cudaStreamSynchronize(c.stream));
     c.stream = stream ? (cudaStream_t)stream : c.own_stream;
+    API_END
+}
+
+int vvgpu_set_eps_round_limit(vvgpu_ctx* h, int64_t max_rounds) {
+    API_BEGIN(h)
+    if (max_rounds < 1) throw ApiError{VVGPU_ERR_ARG, "the round limit must be at least 1"};
+    c.eps_max_rounds = max_rounds;
     API_END
 }
 
@@ -353,8 +383,15 @@ static int set_vortices_impl(vvgpu_ctx* h, int64_t n, const double* x, const dou
         else VV_CUDA(cudaMemsetAsync(c.ie.p, 0, bytes, s));
         VV_CUDA(cudaMemsetAsync(c.vx.p, 0, bytes, s));
         VV_CUDA(cudaMemsetAsync(c.vy.p, 0, bytes, s));
-        k_iota64<<<grid_for(n, 256), 256, 0, s>>>(c.orig.p, n, 0);
+        // the check is read by the next call that consumes the list (check_input)
+        c.in_bad.reserve(1);
+        VV_CUDA(cudaMemsetAsync(c.in_bad.p, 0, 4, s));
+        k_set_orig_check<<<grid_for(n, 256), 256, 0, s>>>(n, c.orig.p, c.x.p, c.y.p, c.g.p, ie ? c.ie.p : nullptr,
+                                                          c.in_bad.p);
         VV_LAUNCH_CHECK();
+        c.in_pending = true;
+    } else {
+        c.in_pending = false;
     }
     c.n = n;
     c.next_orig = n;

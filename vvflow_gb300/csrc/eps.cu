@@ -817,7 +817,7 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
     VV_CUDA(cudaMemcpyAsync(c.e_oie[0].p, c.ie.p, n * 8, cudaMemcpyDeviceToDevice, s));
     int cur = 0;
     int64_t rounds = 0;
-    const int64_t max_rounds = 4096;
+    const int64_t max_rounds = c.eps_max_rounds;
     c.e_rlist.reserve(nl + 1);
     c.e_ldisp.reserve(nl + 1);
     c.e_rnear.reserve(nl + 1);

@@ -100,10 +100,11 @@ __device__ __forceinline__ void mma_commit(uint64_t* mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar)));
 }
 
-// bounded wait for the mbarrier phase `parity`; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
+// bounded wait for the mbarrier phase `parity` (at most `spins` polls); false on timeout
+constexpr uint32_t MBAR_SPINS = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t spins) {
     uint32_t done = 0;
-    for (int it = 0; it < (1 << 22) && !done; it++)
+    for (uint32_t it = 0; it < spins && !done; it++)
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
             : "=r"(done)
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(TILE) k_mlp_forward(int64_t n, const float* __
                                                      const __nv_bfloat16* __restrict__ img,
                                                      const float* __restrict__ params,
                                                      const float* __restrict__ norm, float* __restrict__ y,
-                                                     int* err) {
+                                                     int* err, uint32_t spins) {
     extern __shared__ __align__(1024) unsigned char smraw[];
     FwdSmem& S = *reinterpret_cast<FwdSmem*>(smraw);
     const int tid = threadIdx.x, w = tid >> 5;
@@ -188,7 +189,7 @@ __global__ void __launch_bounds__(TILE) k_mlp_forward(int64_t n, const float* __
     __syncthreads();
     fence_after();
     const uint32_t tm = S.tmem;
-    uint32_t phase = 0;
+    uint32_t phase = 0, lost = 2;  // lost: the phase whose completion a timed-out wait missed
     bool ok = true;
     const int64_t ntiles = (n + TILE - 1) / TILE;
     for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
@@ -203,7 +204,8 @@ __global__ void __launch_bounds__(TILE) k_mlp_forward(int64_t n, const float* __
         __syncthreads();
         fence_after();
         if (tid == 0) { mma_issue(tm, S.x0, S.w + I_W1, KIN, HID, false); mma_commit(&S.mbar); }
-        ok = __syncthreads_and(mbar_wait(&S.mbar, phase));
+        ok = __syncthreads_and(mbar_wait(&S.mbar, phase, spins));
+        if (!ok) lost = phase;
         phase ^= 1;
         fence_after();
         if (!ok) break;
@@ -218,7 +220,8 @@ __global__ void __launch_bounds__(TILE) k_mlp_forward(int64_t n, const float* __
         __syncthreads();
         fence_after();
         if (tid == 0) { mma_issue(tm + 64, S.h1, S.w + I_W2, HID, HID, false); mma_commit(&S.mbar); }
-        ok = __syncthreads_and(mbar_wait(&S.mbar, phase));
+        ok = __syncthreads_and(mbar_wait(&S.mbar, phase, spins));
+        if (!ok) lost = phase;
         phase ^= 1;
         fence_after();
         if (!ok) break;
@@ -233,7 +236,8 @@ __global__ void __launch_bounds__(TILE) k_mlp_forward(int64_t n, const float* __
         __syncthreads();
         fence_after();
         if (tid == 0) { mma_issue(tm, S.h2, S.w + I_W3, HID, NOUTP, false); mma_commit(&S.mbar); }
-        ok = __syncthreads_and(mbar_wait(&S.mbar, phase));
+        ok = __syncthreads_and(mbar_wait(&S.mbar, phase, spins));
+        if (!ok) lost = phase;
         phase ^= 1;
         fence_after();
         if (!ok) break;
@@ -250,6 +254,9 @@ __global__ void __launch_bounds__(TILE) k_mlp_forward(int64_t n, const float* __
         fence_after();
     }
     if (!ok && tid == 0) atomicExch(err, 1);
+    // a wait that gave up leaves its MMA in flight: let it land (bounded) before the tensor
+    // memory it writes is released
+    if (lost != 2) mbar_wait(&S.mbar, lost, MBAR_SPINS);
     fence_before();
     __syncthreads();
     if (w == 0) tmem_free(tm, FWD_TMEM);
@@ -299,7 +306,7 @@ __global__ void __launch_bounds__(TILE) k_mlp_train_tile(const float* __restrict
                                                         const __nv_bfloat16* __restrict__ img,
                                                         const float* __restrict__ params,
                                                         const float* __restrict__ norm, float scale,
-                                                        float* __restrict__ part, int* err) {
+                                                        float* __restrict__ part, int* err, uint32_t spins) {
     extern __shared__ __align__(1024) unsigned char smraw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smraw);
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -323,7 +330,7 @@ __global__ void __launch_bounds__(TILE) k_mlp_train_tile(const float* __restrict
     __syncthreads();
     fence_after();
     const uint32_t tm = S.tmem;
-    uint32_t phase = 0;
+    uint32_t phase = 0, lost = 2;  // lost: the phase whose completion a timed-out wait missed
     bool ok = true;
     auto sync_mma = [&]() {
         fence_smem_to_mma();
@@ -333,8 +340,10 @@ __global__ void __launch_bounds__(TILE) k_mlp_train_tile(const float* __restrict
     };
     // every thread waits, then all agree (tcgen05.ld needs converged warps)
     auto wait = [&]() {
-        const bool mine = ok ? mbar_wait(&S.mbar, phase) : false;
-        ok = __syncthreads_and(mine) != 0;
+        const bool mine = ok ? mbar_wait(&S.mbar, phase, spins) : false;
+        const bool all = __syncthreads_and(mine) != 0;
+        if (ok && !all) lost = phase;
+        ok = all;
         phase ^= 1;
         fence_after();
     };
@@ -470,6 +479,7 @@ __global__ void __launch_bounds__(TILE) k_mlp_train_tile(const float* __restrict
         }
     }
     if (!ok && tid == 0) atomicExch(err, 1);
+    if (lost != 2) mbar_wait(&S.mbar, lost, MBAR_SPINS);  // the abandoned MMA lands first
     fence_before();
     __syncthreads();
     if (w == 0) tmem_free(tm, TR_TMEM);
@@ -784,6 +794,7 @@ struct vvgpu_mlp {
     DArr<int32_t> err;
     int64_t steps = 0;            // Adam steps taken
     int64_t launches = 0;
+    uint32_t wait_spins = MBAR_SPINS;  // polls of one tensor-core completion wait
 };
 
 namespace {
@@ -844,7 +855,8 @@ void train_batch(vvgpu_mlp& M, const int64_t* ids, int ntiles, float scale, floa
                  float* loss_slot) {
     M.part.reserve((size_t)ntiles * PSTRIDE);
     k_mlp_train_tile<<<ntiles, TILE, train_smem(), M.stream>>>(M.feat.p, M.lab.p, ids, M.img.p, M.params.p,
-                                                             M.norm.p, scale, M.part.p, M.err.p);
+                                                             M.norm.p, scale, M.part.p, M.err.p,
+                                                             M.wait_spins);
     MLP_LAUNCH_CHECK();
     float c1 = 1.f, c2 = 1.f;
     if (lr != 0.f) {
@@ -876,7 +888,8 @@ void forward_device(vvgpu_mlp& M, int64_t n, const float* dfeat, float* dy) {
     if (n <= 0) return;
     const int64_t ntiles = (n + TILE - 1) / TILE;
     const int grid = (int)std::min<int64_t>(ntiles, 152 * 4);
-    k_mlp_forward<<<grid, TILE, fwd_smem(), M.stream>>>(n, dfeat, M.img.p, M.params.p, M.norm.p, dy, M.err.p);
+    k_mlp_forward<<<grid, TILE, fwd_smem(), M.stream>>>(n, dfeat, M.img.p, M.params.p, M.norm.p, dy, M.err.p,
+                                                         M.wait_spins);
     MLP_LAUNCH_CHECK();
 }
 
@@ -1010,6 +1023,13 @@ int vvgpu_mlp_destroy(vvgpu_mlp* m) {
 }
 
 const char* vvgpu_mlp_last_error(const vvgpu_mlp* m) { return m ? m->last_error.c_str() : "null model"; }
+
+int vvgpu_mlp_set_wait_limit(vvgpu_mlp* m, int64_t spins) {
+    MLP_BEGIN(m)
+    if (spins < 0) throw ApiError{VVGPU_ERR_ARG, "negative wait limit"};
+    M.wait_spins = spins > (int64_t)MBAR_SPINS ? MBAR_SPINS : (uint32_t)spins;
+    MLP_END
+}
 
 int64_t vvgpu_mlp_num_params(void) { return NPARAM; }
 

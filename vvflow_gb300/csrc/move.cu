@@ -123,6 +123,7 @@ __global__ void k_move_bookkeep(const int32_t* __restrict__ list, const int32_t*
 }  // namespace
 
 void move_and_clean(Ctx& c, int remove, int64_t* cleaned) {
+    check_input(c);
     for (auto& b : c.bodies) {
         const vvgpu_body_params& p = b.p;
         auto rigid = [](double k) { return !(k >= 0 && std::isfinite(k)); };

@@ -311,11 +311,29 @@ __global__ void k_body_rows(int64_t n, double* A, double* B, const BodyDev* bd, 
 }
 
 // ---- Gauss-Jordan inversion in place (row pivoting; columns unscrambled at the end) ----
+// Step k eliminates column k from every other row with the pivot row as it stands
+// (M[i][j] -= (M[i][k] / d) M[k][j]) and normalises the pivot row afterwards (at the start
+// of step k + 1, or by k_gj_norm after the last step).  Rows that are equal stay equal
+// under the same operations and the second of them becomes exactly zero, so an exactly
+// singular system ends with a zero (or NaN) pivot, as in LAPACK's LU (dgetrf's info > 0,
+// where the reference exits, TMatrix.cpp:195-213).
+
+// Row r of M divided by its pivot d = dpiv[r] (the diagonal entry becomes 1 / d).
+template <class T>
+__device__ __forceinline__ void gj_normalise_row(int64_t n, int64_t r, T* M, const T* dpiv) {
+    const T d = dpiv[r];
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+        if (j == r) M[r * n + r] = (T)1 / d;
+        else M[r * n + j] = M[r * n + j] / d;
+    }
+}
 
 template <class T>
-__global__ void k_gj_pivot(int64_t n, int64_t k, T* M, int32_t* perm, T* col, int32_t* singular) {
+__global__ void k_gj_pivot(int64_t n, int64_t k, T* M, int32_t* perm, T* col, T* dpiv, int32_t* singular) {
     __shared__ double bv[1024];
     __shared__ int32_t bi[1024];
+    if (k > 0) gj_normalise_row(n, k - 1, M, dpiv);
+    __syncthreads();
     double best = -1;
     int32_t arg = -1;
     for (int64_t i = k + threadIdx.x; i < n; i += blockDim.x) {
@@ -337,8 +355,8 @@ __global__ void k_gj_pivot(int64_t n, int64_t k, T* M, int32_t* perm, T* col, in
         __syncthreads();
     }
     const int32_t p = bi[0];
-    if (bv[0] <= 0 || p < 0) {
-        if (threadIdx.x == 0) { *singular = 1; perm[k] = (int32_t)k; }
+    if (bv[0] <= 0 || p < 0) {  // zero or NaN column: singular (the rest of the inverse is void)
+        if (threadIdx.x == 0) { *singular = 1; perm[k] = (int32_t)k; dpiv[k] = (T)1; }
         for (int64_t i = threadIdx.x; i < n; i += blockDim.x) col[i] = 0;
         return;
     }
@@ -351,13 +369,8 @@ __global__ void k_gj_pivot(int64_t n, int64_t k, T* M, int32_t* perm, T* col, in
         }
     __syncthreads();
     const T d = M[k * n + k];
-    __syncthreads();
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) col[i] = M[i * n + k];
-    __syncthreads();
-    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-        if (j == k) M[k * n + k] = (T)1 / d;
-        else M[k * n + j] = M[k * n + j] / d;
-    }
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) col[i] = (i == k) ? (T)0 : M[i * n + k] / d;
+    if (threadIdx.x == 0) dpiv[k] = d;
 }
 
 template <class T>
@@ -366,8 +379,13 @@ __global__ void k_gj_elim(int64_t n, int64_t k, T* M, const T* __restrict__ col)
     int64_t i = blockIdx.y;
     if (j >= n || i == k) return;
     const T f = col[i];
-    if (j == k) M[i * n + k] = -f * M[k * n + k];
+    if (j == k) M[i * n + k] = -f;
     else M[i * n + j] -= f * M[k * n + j];
+}
+
+template <class T>
+__global__ void k_gj_norm(int64_t n, int64_t r, T* M, const T* dpiv) {
+    gj_normalise_row(n, r, M, dpiv);
 }
 
 template <class T>
@@ -384,14 +402,19 @@ __global__ void k_gj_colswap(int64_t n, T* M, const int32_t* perm, int64_t k) {
 template <class T>
 void invert(Ctx& c, T* M, int64_t n, int32_t* singular) {
     cudaStream_t s = c.st();
-    DArr<T> col;
+    DArr<T> col, dpiv;
     col.reserve(n);
+    dpiv.reserve(n);
     c.piv.reserve(n);
     for (int64_t k = 0; k < n; k++) {
-        k_gj_pivot<T><<<1, 1024, 0, s>>>(n, k, M, c.piv.p, col.p, singular);
+        k_gj_pivot<T><<<1, 1024, 0, s>>>(n, k, M, c.piv.p, col.p, dpiv.p, singular);
         VV_LAUNCH_CHECK();
         dim3 grid(grid_for(n, 256), (unsigned)n);
         k_gj_elim<T><<<grid, 256, 0, s>>>(n, k, M, col.p);
+        VV_LAUNCH_CHECK();
+    }
+    if (n > 0) {
+        k_gj_norm<T><<<1, 1024, 0, s>>>(n, n - 1, M, dpiv.p);
         VV_LAUNCH_CHECK();
     }
     for (int64_t k = n - 1; k >= 0; k--) {

@@ -1124,6 +1124,7 @@ __global__ void k_leaf_arrays(int64_t nl, const int32_t* __restrict__ leaf_node,
 void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
     if (c.built) throw ApiError{VVGPU_ERR_STATE, "tree is already built"};
     if (c.n > 0x3fffffff || c.m > 0x3fffffff) throw ApiError{VVGPU_ERR_LIMIT, "too many vortices or segments"};
+    check_input(c);
     upload_segments(c);
     c.far_criteria = far_criteria; c.min_node = min_node; c.max_node = max_node;
     const int64_t n = c.n, m = c.m;

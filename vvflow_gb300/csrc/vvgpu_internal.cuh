@@ -124,6 +124,11 @@ struct Ctx {
     DArr<double> x, y, g, ie, vx, vy;
     DArr<int64_t> orig;
     int64_t next_orig = 0;
+    // input check of the last vvgpu_set_vortices* (non-finite values), read on first use
+    DArr<int32_t> in_bad;
+    bool in_pending = false;
+    // fixed-point rounds the epsilon/merge pass may take (vvgpu_set_eps_round_limit)
+    int64_t eps_max_rounds = 4096;
 
     // segments (host copies of geometry are kept for body bookkeeping)
     int64_t m = 0;
@@ -367,6 +372,9 @@ int32_t read_i32(Ctx& c, const int32_t* p);
 
 // ---- per-module entry points (throw ApiError / CudaError) ----
 void ensure_vortex_capacity(Ctx& c, int64_t n, bool keep);
+// VVGPU_ERR_ARG if the last vortex list set holds a non-finite position or circulation or a
+// NaN / negative inverse epsilon (reads the device flag once per list; synchronises).
+void check_input(Ctx& c);
 // Leaf anchors (frame.cuh) and per-leaf FP32 boxes of the current vortex positions.
 void build_frames(Ctx& c);
 void tree_build(Ctx& c, double far_criteria, double min_node, double max_node);

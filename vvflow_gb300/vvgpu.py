@@ -84,6 +84,7 @@ SIGNATURES = {
     "vvgpu_set_stream": (C.c_int, [_H, C.c_void_p]),
     "vvgpu_synchronize": (C.c_int, [_H]),
     "vvgpu_get_stats": (C.c_int, [_H, C.POINTER(Stats)]),
+    "vvgpu_set_eps_round_limit": (C.c_int, [_H, C.c_int64]),
     "vvgpu_set_params": (C.c_int, [_H] + [C.c_double] * 8),
     "vvgpu_add_body": (C.c_int, [_H, C.c_int64, _D, _D, _U32, C.POINTER(BodyParams)]),
     "vvgpu_set_segment_g": (C.c_int, [_H, _D]),
@@ -122,6 +123,7 @@ SIGNATURES = {
     "vvgpu_mlp_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(_H)]),
     "vvgpu_mlp_destroy": (C.c_int, [_H]),
     "vvgpu_mlp_last_error": (C.c_char_p, [_H]),
+    "vvgpu_mlp_set_wait_limit": (C.c_int, [_H, C.c_int64]),
     "vvgpu_mlp_num_params": (C.c_int64, []),
     "vvgpu_mlp_get_params": (C.c_int, [_H, _F]),
     "vvgpu_mlp_set_params": (C.c_int, [_H, _F]),
@@ -223,6 +225,9 @@ class GpuSpace:
         return d
 
     # -- state -----------------------------------------------------------------------
+    def set_eps_round_limit(self, max_rounds: int):
+        self._ok(self.lib.vvgpu_set_eps_round_limit(self.h, int(max_rounds)), "set_eps_round_limit")
+
     def set_params(self, re, dt, inf_vx=1.0, inf_vy=0.0, inf_g=0.0, time=0.0, gx=0.0, gy=0.0):
         self._ok(self.lib.vvgpu_set_params(self.h, re, dt, inf_vx, inf_vy, inf_g, time, gx, gy), "set_params")
 
@@ -233,6 +238,9 @@ class GpuSpace:
         bp = params if params is not None else default_body_params()
         self._ok(self.lib.vvgpu_add_body(self.h, len(cx), _p(cx), _p(cy), _p(sl, C.c_uint32), C.byref(bp)), "add_body")
         self.nbodies += 1
+
+    def clear_bodies(self):
+        self._ok(self.lib.vvgpu_clear_bodies(self.h), "clear_bodies")
 
     def set_segment_g(self, g):
         g = np.ascontiguousarray(g, np.float64)
@@ -558,6 +566,9 @@ class Mlp:
         if rc != 0:
             msg = self.lib.vvgpu_mlp_last_error(self.h)
             raise VVGpuError(rc, what, msg.decode() if msg else "")
+
+    def set_wait_limit(self, spins: int):
+        self._ok(self.lib.vvgpu_mlp_set_wait_limit(self.h, int(spins)), "mlp_set_wait_limit")
 
     def params(self):
         out = np.empty(self.nparam, np.float32)
