@@ -121,8 +121,24 @@ typedef struct vvgpu_stats {
     int64_t reserved[8];        /* reserved[0]: kernels launched by the context so far;
                                    reserved[1]: target evaluations over all epsilon rounds;
                                    reserved[2]: sources in the candidate leaves of every
-                                   8-target chunk of the last FP32 diffusive pass */
+                                   8-target chunk of the last FP32 diffusive pass;
+                                   reserved[3]: candidate records read by the FP32 filter
+                                   of every epsilon evaluation of the last pass */
 } vvgpu_stats;
+
+/* Device time per kernel (vvgpu_get_kernel_timing slots): CUDA events recorded on the
+ * context's stream around these launches while timing is on. */
+enum {
+    VVGPU_T_TREE_BUILD = 0,   /* vvgpu_tree_build, whole call                             */
+    VVGPU_T_WALK = 1,         /* near/far walk with the far-field expansion (k_walk_warp)  */
+    VVGPU_T_EPS_ROUND = 2,    /* epsilon/merge two-nearest searches, every round           */
+    VVGPU_T_EPS_CAND = 3,     /* epsilon/merge candidate leaves, every round               */
+    VVGPU_T_EPS_PASS = 4,     /* vvgpu_eps after the walk, whole pass                      */
+    VVGPU_T_CONVECTIVE = 5,   /* convective near field and far-field application          */
+    VVGPU_T_DIFFUSIVE = 6,    /* diffusive sums                                           */
+    VVGPU_T_SLAE = 7,         /* vvgpu_slae, whole call                                   */
+    VVGPU_T_COUNT = 8
+};
 
 /* ---- context --------------------------------------------------------------------- */
 int vvgpu_ctx_create(const vvgpu_cfg* cfg, vvgpu_ctx** out);
@@ -138,6 +154,12 @@ int vvgpu_get_stats(const vvgpu_ctx* ctx, vvgpu_stats* out);
  * leaves the vortex list as it was; the tree stays built.  The reference's sequential pass
  * has no such bound (MEpsilonFast.cpp:11-63). */
 int vvgpu_set_eps_round_limit(vvgpu_ctx* ctx, int64_t max_rounds);
+/* Kernel timing on (1) or off (0); either clears the sums.  No counterpart in the
+ * reference (it has no GPU). */
+int vvgpu_set_kernel_timing(vvgpu_ctx* ctx, int on);
+/* Sums since timing was switched on: ms[k] device milliseconds and launches[k] timed
+ * launches of slot k (arrays of VVGPU_T_COUNT; either may be NULL).  Synchronises. */
+int vvgpu_get_kernel_timing(vvgpu_ctx* ctx, double* ms, int64_t* launches);
 
 /* ---- Space state (host pointers) -------------------------------------------------- */
 /* Space::re, dt, inf_speed(), inf_g, time, gravity (libvvhd/headers/TSpace.hpp:19-36). */

@@ -273,11 +273,13 @@ class OracleSpace:
         self._ok(self.f["tree_seg_order"](self.h, _p(so, C.c_int64)), "tree_seg_order")
         return so
 
-    def tree_lists(self):
+    def tree_lists(self, far=True):
         _, nl, nnear, nfar = self.tree_sizes()
         d = {"near_off": np.empty(nl + 1, np.int64), "far_off": np.empty(nl + 1, np.int64),
              "near_depth": np.empty(nnear, np.int32), "near_path": np.empty(nnear, np.int64),
-             "far_depth": np.empty(nfar, np.int32), "far_path": np.empty(nfar, np.int64)}
+             "far_depth": np.empty(nfar if far else 0, np.int32), "far_path": np.empty(nfar if far else 0, np.int64)}
+        if not far:
+            d["far_depth"] = d["far_path"] = None
         self._ok(self.f["tree_lists"](self.h, _p(d["near_off"], C.c_int64), _p(d["near_depth"], C.c_int32),
                                       _p(d["near_path"], C.c_int64), _p(d["far_off"], C.c_int64),
                                       _p(d["far_depth"], C.c_int32), _p(d["far_path"], C.c_int64)), "tree_lists")

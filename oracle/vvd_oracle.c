@@ -1054,6 +1054,9 @@ int vvo_slae(vvo_space* S, vvo_body_out* out) {
     const double _1_dt = 1 / S->dt;
     const double _1_2dt = 0.5 / S->dt;
     const double gsum = vvo_gsum(S);
+    /* node -> leaf position (the reference's findNode returns the leaf itself) */
+    int64_t* leaf_pos = (int64_t*)xrealloc(NULL, sizeof(int64_t) * (size_t)(S->nnodes ? S->nnodes : 1));
+    for (int64_t t = 0; t < S->nleaves; t++) leaf_pos[S->leaves[t]] = t;
     int once = 0;
     for (int bi = 0; bi < S->nb; bi++) {
         const obody* b = &S->bodies[bi];
@@ -1068,9 +1071,7 @@ int vvo_slae(vvo_space* S, vvo_body_out* out) {
                 sink_influence(S, S->rx[s], S->ry[s], &sx, &sy);
                 r += (-sy) * S->dlx[s] + sx * S->dly[s];
                 int32_t nk = find_node(S, S->rx[s], S->ry[s]);
-                int64_t L = -1;
-                for (int64_t t = 0; t < S->nleaves; t++) if (S->leaves[t] == nk) { L = t; break; }
-                r -= node_influence(S, L, s);
+                r -= node_influence(S, leaf_pos[nk], s);
                 B[eq] = r;
                 for (int bj = 0; bj < S->nb; bj++) {
                     const obody* jb = &S->bodies[bj];
@@ -1199,7 +1200,7 @@ int vvo_slae(vvo_space* S, vvo_body_out* out) {
     memcpy(S->sol, B, sizeof(double) * (size_t)n);
     int rc = lu_solve(n, LU, S->sol);
     free(LU);
-    if (rc) { free(col0); return rc; }
+    if (rc) { free(col0); free(leaf_pos); return rc; }
     for (int bi = 0; bi < S->nb; bi++) {
         const obody* b = &S->bodies[bi];
         for (int64_t q = 0; q < b->count; q++) S->sg[b->first + q] = S->sol[SEGCOL(bi, q)];
@@ -1215,6 +1216,7 @@ int vvo_slae(vvo_space* S, vvo_body_out* out) {
 #undef SEGCOL
 #undef BCOL
     free(col0);
+    free(leaf_pos);
     return 0;
 }
 
@@ -1236,6 +1238,10 @@ int vvo_slae_rhs_step(vvo_space* S, double* rhs_out) {
     double* y = (double*)calloc((size_t)n, sizeof(double));
     if (!inv || !b || !y) { free(inv); free(b); free(y); return -7; }
     for (int64_t i = 0; i < n; i++) inv[i * n + i] = 1.0;
+    /* node -> leaf position (the reference's findNode returns the leaf itself) */
+    int64_t* pos = (int64_t*)malloc(sizeof(int64_t) * (size_t)(S->nnodes ? S->nnodes : 1));
+    if (!pos) { free(inv); free(b); free(y); return -7; }
+    for (int64_t t = 0; t < S->nleaves; t++) pos[S->leaves[t]] = t;
     int64_t row = 0;
     for (int bi = 0; bi < S->nb; bi++) {
         const obody* bd = &S->bodies[bi];
@@ -1244,9 +1250,7 @@ int vvo_slae_rhs_step(vvo_space* S, double* rhs_out) {
             int64_t s = bd->first + k;
             double r = (-S->inf_vy) * S->dlx[s] + S->inf_vx * S->dly[s];
             int32_t nk = find_node(S, S->rx[s], S->ry[s]);
-            int64_t L = -1;
-            for (int64_t t = 0; t < S->nleaves; t++) if (S->leaves[t] == nk) { L = t; break; }
-            r -= node_influence(S, L, s);
+            r -= node_influence(S, pos[nk], s);
             b[row] = r;
         }
         row += 9;
@@ -1258,7 +1262,7 @@ int vvo_slae_rhs_step(vvo_space* S, double* rhs_out) {
         y[i] = acc;
     }
     if (rhs_out) memcpy(rhs_out, y, sizeof(double) * (size_t)n);
-    free(inv); free(b); free(y);
+    free(pos); free(inv); free(b); free(y);
     return 0;
 }
 

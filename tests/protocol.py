@@ -25,7 +25,9 @@ def digest(*arrays) -> str:
     return h.hexdigest()
 
 
-def tree_record(S, prefix: str, out: dict, full_lists: bool):
+def tree_record(S, prefix: str, out: dict, full_lists: bool, far_lists: bool = True):
+    """far_lists=False: the digest covers the near lists and the far-list offsets only (the
+    far nodes of every leaf at 4M vortices are ~7e8 entries)."""
     nn, nl, nnear, nfar = S.tree_sizes()
     out[prefix + "sizes"] = np.array([nn, nl, nnear, nfar], np.int64)
     v = S.vortices()
@@ -34,14 +36,18 @@ def tree_record(S, prefix: str, out: dict, full_lists: bool):
     for k in ("x", "y", "h", "w", "vfirst", "vlast", "depth", "path", "sfirst", "slast"):
         out[prefix + "leaf_" + k] = lv[k]
     out[prefix + "seg_order"] = S.tree_seg_order()
-    li = S.tree_lists()
+    li = S.tree_lists(far=far_lists or full_lists)
     out[prefix + "near_off"] = li["near_off"]
     out[prefix + "far_off"] = li["far_off"]
     if full_lists:
         for k in ("near_depth", "near_path", "far_depth", "far_path"):
             out[prefix + k] = li[k]
-    out[prefix + "lists_sha"] = np.array(digest(li["near_depth"], li["near_path"],
-                                                li["far_depth"], li["far_path"]))
+    if far_lists or full_lists:
+        out[prefix + "lists_sha"] = np.array(digest(li["near_depth"], li["near_path"],
+                                                    li["far_depth"], li["far_path"]))
+    else:
+        out[prefix + "near_sha"] = np.array(digest(li["near_depth"], li["near_path"]))
+    del li
     nd = S.tree_nodes()
     order = np.lexsort((nd["path"], nd["depth"]))
     for k in nd:

@@ -562,11 +562,14 @@ void convective(Ctx& c) {
     if (c.precision == VVGPU_FP32) {
         build_frames(c);
         a.src32 = c.src32.p; a.src_k = c.src_k.p; a.anchor = c.lf_anchor.p; a.G = c.frame_G; a.Gf = (float)c.frame_G;
+        KernelTimer kt(c, VVGPU_T_CONVECTIVE);
         k_conv32<<<grid, CW * 32, 0, s>>>(a);
+        VV_LAUNCH_CHECK();
     } else {
+        KernelTimer kt(c, VVGPU_T_CONVECTIVE);
         k_conv64<8><<<grid, CW * 32, 0, s>>>(a);
+        VV_LAUNCH_CHECK();
     }
-    VV_LAUNCH_CHECK();
     VV_CUDA(cudaStreamSynchronize(s));
 }
 

@@ -135,6 +135,20 @@ void upload_segments(Ctx& c) {
     c.segs_dirty = false;
 }
 
+void collect_kernel_timing(Ctx& c) {
+    if (c.ev_rec.empty()) return;
+    VV_CUDA(cudaEventSynchronize(c.ev_rec.back().b));
+    for (auto& r : c.ev_rec) {
+        float ms = 0;
+        VV_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+        c.t_ms[r.slot] += ms;
+        c.t_count[r.slot]++;
+        c.ev_free.push_back(r.a);
+        c.ev_free.push_back(r.b);
+    }
+    c.ev_rec.clear();
+}
+
 void check_input(Ctx& c) {
     if (!c.in_pending) return;
     c.in_pending = false;
@@ -206,6 +220,11 @@ int vvgpu_ctx_destroy(vvgpu_ctx* h) {
     if (c.side) cudaStreamSynchronize(c.side);
     cudaStream_t own = c.own_stream, side = c.side;
     cudaEvent_t e1 = c.ev_fork, e2 = c.ev_join;
+    for (auto& r : c.ev_rec) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (cudaEvent_t e : c.ev_free) cudaEventDestroy(e);
     delete h;  // device arrays are released by their destructors
     if (own) cudaStreamDestroy(own);
     if (side) cudaStreamDestroy(side);
@@ -237,6 +256,24 @@ int vvgpu_set_eps_round_limit(vvgpu_ctx* h, int64_t max_rounds) {
     API_END
 }
 
+int vvgpu_set_kernel_timing(vvgpu_ctx* h, int on) {
+    API_BEGIN(h)
+    collect_kernel_timing(c);
+    c.timing = on != 0;
+    for (int k = 0; k < VVGPU_T_COUNT; k++) { c.t_ms[k] = 0; c.t_count[k] = 0; }
+    API_END
+}
+
+int vvgpu_get_kernel_timing(vvgpu_ctx* h, double* ms, int64_t* launches) {
+    API_BEGIN(h)
+    collect_kernel_timing(c);
+    for (int k = 0; k < VVGPU_T_COUNT; k++) {
+        if (ms) ms[k] = c.t_ms[k];
+        if (launches) launches[k] = c.t_count[k];
+    }
+    API_END
+}
+
 int vvgpu_synchronize(vvgpu_ctx* h) {
     API_BEGIN(h)
     VV_CUDA(cudaStreamSynchronize(c.stream));
@@ -249,6 +286,7 @@ int vvgpu_get_stats(const vvgpu_ctx* h, vvgpu_stats* out) {
     out->reserved[0] = h->c.launches;
     out->reserved[1] = h->c.eps_evaluations;
     out->reserved[2] = h->c.diff_sources;
+    out->reserved[3] = h->c.eps_records;
     return VVGPU_OK;
 }
 
@@ -472,6 +510,7 @@ int vvgpu_tree_build(vvgpu_ctx* h, double far_criteria, double min_node, double 
     API_BEGIN(h)
     if (!(far_criteria > 0) || std::isnan(min_node) || std::isnan(max_node))
         throw ApiError{VVGPU_ERR_ARG, "bad tree parameters"};
+    KernelTimer kt(c, VVGPU_T_TREE_BUILD);
     tree_build(c, far_criteria, min_node, max_node);
     API_END
 }
@@ -487,7 +526,10 @@ int vvgpu_eps(vvgpu_ctx* h, int merge, int64_t* merged) {
     API_BEGIN(h)
     if (!c.built) throw ApiError{VVGPU_ERR_NOT_BUILT, "tree is not built"};
     ensure_full_lists(c);
-    eps_pass(c, merge, merged);
+    {
+        KernelTimer kt(c, VVGPU_T_EPS_PASS);
+        eps_pass(c, merge, merged);
+    }
     c.mom_valid = false;  // merges move circulation
     API_END
 }
@@ -520,6 +562,7 @@ int vvgpu_velocity_points(vvgpu_ctx* h, int64_t n, const double* px, const doubl
 int vvgpu_slae(vvgpu_ctx* h, vvgpu_body_out* out) {
     API_BEGIN(h)
     if (!c.built) throw ApiError{VVGPU_ERR_NOT_BUILT, "tree is not built"};
+    KernelTimer kt(c, VVGPU_T_SLAE);
     slae(c, out);
     API_END
 }
@@ -618,11 +661,11 @@ int vvgpu_tree_sizes(vvgpu_ctx* h, int64_t* nnodes, int64_t* nleaves, int64_t* n
     int64_t tot = 0;
     for (auto& r : runs) tot += r.y - r.x;
     std::vector<int32_t> foff, fnode;
-    if (nfar) tree_lists_exact(c, foff, fnode);
+    if (nfar) tree_lists_exact(c, foff, fnode, false);
     if (nnodes) *nnodes = c.nnodes;
     if (nleaves) *nleaves = c.nleaves;
     if (nnear) *nnear = tot;
-    if (nfar) *nfar = (int64_t)fnode.size();
+    if (nfar) *nfar = foff.empty() ? 0 : (int64_t)foff.back();
     API_END
 }
 
@@ -716,7 +759,7 @@ int vvgpu_tree_lists(vvgpu_ctx* h, int64_t* near_off, int32_t* near_depth, int64
     std::vector<int32_t> noff(nl + 1), foff, fnode, ln(nl), dep(nn);
     std::vector<int2> runs(c.n_near_runs);
     std::vector<int64_t> pth(nn);
-    tree_lists_exact(c, foff, fnode);
+    tree_lists_exact(c, foff, fnode, far_depth || far_path);
     d2h(noff.data(), c.near_off.p, nl + 1, s);
     d2h(runs.data(), c.near_run.p, c.n_near_runs, s);
     d2h(ln.data(), c.leaf_node.p, nl, s);

@@ -552,9 +552,12 @@ void diffusive(Ctx& c) {
     VV_CUDA(cudaMemsetAsync(c.counters.p + 2, 0, 16, s));  // candidate pairs, candidate sources
     a.cand = c.counters.p + 2;
     unsigned grid = grid_for(nl, DW);
-    if (c.precision == VVGPU_FP32) k_diff32<DIFF32_DT><<<grid, DW * 32, 0, s>>>(a);
-    else k_diff64<<<grid, DW * 32, 0, s>>>(a);
-    VV_LAUNCH_CHECK();
+    {
+        KernelTimer kt(c, VVGPU_T_DIFFUSIVE);
+        if (c.precision == VVGPU_FP32) k_diff32<DIFF32_DT><<<grid, DW * 32, 0, s>>>(a);
+        else k_diff64<<<grid, DW * 32, 0, s>>>(a);
+        VV_LAUNCH_CHECK();
+    }
     unsigned long long cand[2] = {0, 0};
     VV_CUDA(cudaMemcpyAsync(cand, c.counters.p + 2, 16, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));

@@ -371,6 +371,7 @@ struct Top2 {
     double r1, r2;
     int32_t l1, l2;
     float thr;  // FP32 squared radius in the leaf frame holding every candidate that can decide
+    uint32_t nrec;  // candidate records read by the FP32 pass
 };
 
 __device__ __forceinline__ void top2_push(Top2& t, double d, int32_t j) {
@@ -444,6 +445,7 @@ struct NearBuf {
     int32_t j[NBUF];
     int n = 0;
     bool ovf = false;
+    uint32_t nrec = 0;  // records read by the FP32 pass (leaves its box test did not prune)
     __device__ __forceinline__ void push(float dd, int32_t jj, float thr) {
         if (n == NBUF) {  // drop what the threshold has excluded since
             int m = 0;
@@ -463,6 +465,7 @@ __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, float2 aL
                                           float& thr, Top2& best, NearBuf& buf) {
     float2 sh = frame_shift(v.anchor[q], aL, v.Gf);
     if (box_lb(v.box[q], sh, tx, ty) > thr) return;
+    if (PASS == 0) buf.nrec += (uint32_t)(v.lvl[q] - v.lvf[q]);
     for (int32_t j = v.lvf[q]; j < v.lvl[q]; j++) {
         Cand c = cand_state<FIRST>(v, j, i, excl);
         if (!c.live) continue;
@@ -490,7 +493,7 @@ __device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl
     const float ext = (use_list ? v.rn[L] : v.rnear[L]) + *v.dmax;
     const float D = ldexpf(ext + fabsf(tx) + fabsf(ty) + v.Gf, -17);
     float t1 = INFINITY, t2 = INFINITY, thr = INFINITY;
-    Top2 best{DBL_MAX, DBL_MAX, INT_MAX, INT_MAX, INFINITY};
+    Top2 best{DBL_MAX, DBL_MAX, INT_MAX, INT_MAX, INFINITY, 0};
     const int32_t nc = use_list ? v.ncand[L] : -1;
     NearBuf buf;
     // pass 0: FP32 second-smallest distance, buffering the candidates within the running
@@ -532,6 +535,7 @@ __device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl
         }
     }
     best.thr = thr;
+    best.nrec = buf.nrec;
     return best;
 }
 
@@ -614,7 +618,7 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
                             const double* __restrict__ mcs_l, const double* __restrict__ epr_l,
                             const double* __restrict__ ie_in, const double* __restrict__ oie_old,
                             int32_t* partner_new, double* ox_new, double* oy_new, double* og_new, double* oie_new,
-                            int32_t* changed, unsigned long long* evals) {
+                            int32_t* changed, unsigned long long* evals, unsigned long long* nrec_total) {
     const int64_t cnt = FIRST ? n : (int64_t)*count;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(evals, (unsigned long long)cnt);
     const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -626,10 +630,12 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
         int32_t partner = SKIPPED;
         double px = v.x0[i], py = v.y0[i], gi = gi0, ie = ie_in[i];
         float sr1 = -1.f, sr2 = -1.f;
+        uint32_t nrec = 0;
         if (gi0 != 0 && !(v.zb[i] < i)) {
             const double mcs = mcs_l[L];
             Top2 t = two_nearest<FIRST>(v, L, i, -1, px, py, true);
             sr1 = t.thr;
+            nrec += t.nrec;
             double e;
             partner = -1;
             if (t.l1 == INT_MAX) e = DBL_MIN;
@@ -655,6 +661,7 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
                     partner = t.l1;
                     Top2 u = two_nearest<FIRST>(v, L, i, t.l1, px, py, false);
                     sr2 = u.thr;
+                    nrec += u.nrec;
                     if (u.l1 == INT_MAX) e = DBL_MIN;
                     else if (u.l2 == INT_MAX) e = __dsqrt_rn(u.r1);
                     else e = __dsqrt_rn(u.r2);
@@ -675,6 +682,8 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
         dv.sr2[i] = sr2;
         const unsigned am = __activemask();  // one store per warp to the shared flag
         if (__any_sync(am, ch) && (threadIdx.x & 31) == __ffs(am) - 1) *changed = 1;
+        const unsigned wrec = __reduce_add_sync(am, nrec);
+        if ((threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(nrec_total, (unsigned long long)wrec);
     }
 }
 
@@ -824,6 +833,7 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
     int32_t* dmax_bits = (int32_t*)(c.counters.p + 13);
     VV_CUDA(cudaMemsetAsync(dmax_bits, 0, 4, s));
     VV_CUDA(cudaMemsetAsync(c.counters.p + 14, 0, 8, s));
+    VV_CUDA(cudaMemsetAsync(c.counters.p + 16, 0, 8, s));
     for (;;) {
         rounds++;
         // boxes and candidate leaves from the current guesses
@@ -831,12 +841,15 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                   c.e_partner[cur].p, c.e_zb.p, c.lf_box32.p, c.e_box_prev.p,
                                                   c.e_live.p, c.e_sr1.p, c.e_sr2.p, c.e_rreg.p, rounds == 1);
         VV_LAUNCH_CHECK();
-        k_eps_cand<<<grid_for(nl, EB / 32), EB, 0, s>>>(nl, c.near_off.p, c.near_run.p, c.lf_anchor.p,
-                                                       c.lf_box32.p, c.e_live.p, fr.Gf, c.e_cand.p, c.e_ncand.p,
-                                                       c.lf_rn.p, c.e_rlist.p, c.e_rnear.p, c.e_lchanged.p,
-                                                       c.e_dirty.p, c.e_chg.p, c.e_nchg.p, c.e_box_prev.p,
-                                                       c.e_rreg.p, c.e_lchg_pre.p, rounds == 1, c.e_ldisp.p);
-        VV_LAUNCH_CHECK();
+        {
+            KernelTimer kt(c, VVGPU_T_EPS_CAND);
+            k_eps_cand<<<grid_for(nl, EB / 32), EB, 0, s>>>(nl, c.near_off.p, c.near_run.p, c.lf_anchor.p,
+                                                           c.lf_box32.p, c.e_live.p, fr.Gf, c.e_cand.p, c.e_ncand.p,
+                                                           c.lf_rn.p, c.e_rlist.p, c.e_rnear.p, c.e_lchanged.p,
+                                                           c.e_dirty.p, c.e_chg.p, c.e_nchg.p, c.e_box_prev.p,
+                                                           c.e_rreg.p, c.e_lchg_pre.p, rounds == 1, c.e_ldisp.p);
+            VV_LAUNCH_CHECK();
+        }
         VV_CUDA(cudaMemsetAsync(c.e_changed.p, 0, 4, s));
         EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.e_rnear.p,
                   (const float*)dmax_bits, c.near_off.p, c.near_run.p,
@@ -855,17 +868,20 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
             VV_LAUNCH_CHECK();
             list = c.e_list.p;
         }
-        if (rounds == 1)
-            k_eps_round<true><<<grid_for(n, EB), EB, 0, s>>>(
-                n, v, dv, nullptr, nullptr, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
-                c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
-                c.counters.p + 14);
-        else
-            k_eps_round<false><<<std::min<unsigned>(grid_for(n, EB), 152u * 32u), EB, 0, s>>>(
-                n, v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
-                c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
-                c.counters.p + 14);
-        VV_LAUNCH_CHECK();
+        {
+            KernelTimer kt(c, VVGPU_T_EPS_ROUND);
+            if (rounds == 1)
+                k_eps_round<true><<<grid_for(n, EB), EB, 0, s>>>(
+                    n, v, dv, nullptr, nullptr, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
+                    c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
+                    c.counters.p + 14, c.counters.p + 16);
+            else
+                k_eps_round<false><<<std::min<unsigned>(grid_for(n, EB), 152u * 32u), EB, 0, s>>>(
+                    n, v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
+                    c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
+                    c.counters.p + 14, c.counters.p + 16);
+            VV_LAUNCH_CHECK();
+        }
         // new absorber table and merged records; leaves whose members changed
         k_zb_reset<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_zb.p, c.e_zb_prev.p, c.e_zb.p);
         VV_LAUNCH_CHECK();
@@ -892,11 +908,13 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                c.e_og[cur].p, c.e_oie[cur].p, c.x.p, c.y.p, c.g.p, c.ie.p,
                                                c.counters.p);
     VV_LAUNCH_CHECK();
-    unsigned long long mcount = 0, nev = 0;
+    unsigned long long mcount = 0, nev = 0, nrec = 0;
     VV_CUDA(cudaMemcpyAsync(&mcount, c.counters.p, 8, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaMemcpyAsync(&nev, c.counters.p + 14, 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaMemcpyAsync(&nrec, c.counters.p + 16, 8, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));
     c.eps_evaluations = (int64_t)nev;
+    c.eps_records = (int64_t)nrec;
     if (merged) *merged = (int64_t)mcount;
     c.stats.merged = (int64_t)mcount;
     c.stats.merge_rounds = rounds;

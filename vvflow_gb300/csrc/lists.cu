@@ -600,11 +600,14 @@ void ensure_full_lists(Ctx& c) {
     VV_CUDA(cudaMemsetAsync(far_total, 0, 8, s));
     const bool fp32 = c.precision == VVGPU_FP32;
     const unsigned gw = grid_for((nl + 31) / 32, WW);
-    if (fp32) k_walk_warp<true><<<gw, WW * 32, 0, s>>>(nl, v, c.leaf_node.p, c.near_cnt.p, c.run_buf.p,
-                                                        c.lf_taylor.p, far_total, nn, err);
-    else k_walk_warp<false><<<gw, WW * 32, 0, s>>>(nl, v, c.leaf_node.p, c.near_cnt.p, c.run_buf.p,
-                                                     c.lf_taylor.p, far_total, nn, err);
-    VV_LAUNCH_CHECK();
+    {
+        KernelTimer kt(c, VVGPU_T_WALK);
+        if (fp32) k_walk_warp<true><<<gw, WW * 32, 0, s>>>(nl, v, c.leaf_node.p, c.near_cnt.p, c.run_buf.p,
+                                                            c.lf_taylor.p, far_total, nn, err);
+        else k_walk_warp<false><<<gw, WW * 32, 0, s>>>(nl, v, c.leaf_node.p, c.near_cnt.p, c.run_buf.p,
+                                                         c.lf_taylor.p, far_total, nn, err);
+        VV_LAUNCH_CHECK();
+    }
     exclusive_scan(c, c.near_cnt.p, c.near_off.p, nl);
     c.n_near_runs = read_i32(c, c.near_off.p + nl);
     c.near_run.reserve(c.n_near_runs + 1);
@@ -629,7 +632,7 @@ void ensure_full_lists(Ctx& c) {
     c.stats.far_pairs = 2 * (int64_t)ft;  // two monopoles per far node
 }
 
-void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t>& far_node) {
+void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t>& far_node, bool fill) {
     cudaStream_t s = c.st();
     const int64_t nl = c.nleaves, nn = c.nnodes;
     int32_t* err = (int32_t*)c.counters.p + 1;
@@ -642,11 +645,18 @@ void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t
     VV_LAUNCH_CHECK();
     exclusive_scan(c, cnt.p, off.p, nl);
     int32_t tot = read_i32(c, off.p + nl);
+    far_off.resize(nl + 1);
+    if (!fill) {
+        VV_CUDA(cudaMemcpyAsync(far_off.data(), off.p, (nl + 1) * 4, cudaMemcpyDeviceToHost, s));
+        VV_CUDA(cudaStreamSynchronize(s));
+        if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
+        far_node.clear();
+        return;
+    }
     fnode.reserve(tot + 1);
     k_walk_exact<true><<<grid_for(nl, LB), LB, 0, s>>>(nl, c.leaf_node.p, c.nd_geom.p, c.nd_ch1.p, c.far_criteria,
                                                        nullptr, off.p, fnode.p, nn, err);
     VV_LAUNCH_CHECK();
-    far_off.resize(nl + 1);
     far_node.resize(tot);
     VV_CUDA(cudaMemcpyAsync(far_off.data(), off.p, (nl + 1) * 4, cudaMemcpyDeviceToHost, s));
     if (tot) VV_CUDA(cudaMemcpyAsync(far_node.data(), fnode.p, (size_t)tot * 4, cudaMemcpyDeviceToHost, s));

@@ -499,7 +499,7 @@ __global__ void k_scatter_solution(int64_t nb, const int32_t* col_seg0, const in
 
 double gsum(Ctx& c) {
     cudaStream_t s = c.st();
-    c.counters.reserve(16);
+    c.counters.reserve(24);
     double* out = (double*)(c.counters.p + 4);
     VV_CUDA(cudaMemsetAsync(out, 0, 8, s));
     if (c.n) {

@@ -1154,7 +1154,7 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
     c.tab_lh.reserve(n + 1);
     c.seg_order.reserve(m + 1); c.seg_order2.reserve(m + 1);
     c.seg_node_of.reserve(m + 1); c.seg_node_of2.reserve(m + 1);
-    c.counters.reserve(16);
+    c.counters.reserve(24);
     VV_CUDA(cudaMemsetAsync(c.counters.p, 0, 16 * sizeof(unsigned long long), s));
     int32_t* err = (int32_t*)c.counters.p;
 

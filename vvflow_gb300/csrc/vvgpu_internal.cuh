@@ -246,13 +246,55 @@ struct Ctx {
     DArr<double> slae_bodies;       // per-body row data
     DArr<double> slae_r, slae_sq;   // refinement residual and its squared terms
     vvgpu_stats stats{};
+    // per-kernel device time (vvgpu_set_kernel_timing): event pairs recorded on the stream,
+    // summed per slot when the host asks
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_free;
+    struct TimedLaunch { int slot; cudaEvent_t a, b; };
+    std::vector<TimedLaunch> ev_rec;
+    double t_ms[VVGPU_T_COUNT] = {};
+    int64_t t_count[VVGPU_T_COUNT] = {};
     int64_t launches = 0;           // kernels launched by this context
     int64_t eps_evaluations = 0;    // target evaluations over the rounds of the last epsilon pass
+    int64_t eps_records = 0;        // candidate records read by those evaluations' FP32 passes
     int64_t diff_sources = 0;       // sources in the candidate leaves of every diffusive target chunk
     bool count_pairs = true;        // count algorithmic near pairs before each convective pass
 
     cudaStream_t st() const { return stream; }
 };
+
+// Device time of the work queued on the context's stream while an instance lives, added to
+// slot `slot` of the kernel timing (nothing is recorded while timing is off).
+struct KernelTimer {
+    Ctx& c;
+    int slot;
+    cudaEvent_t a = nullptr;
+    KernelTimer(Ctx& cc, int sl) : c(cc), slot(sl) {
+        if (!c.timing) return;
+        a = take();
+        if (a && cudaEventRecord(a, c.st()) != cudaSuccess) { c.ev_free.push_back(a); a = nullptr; }
+    }
+    ~KernelTimer() {
+        if (!a) return;
+        cudaEvent_t b = take();
+        if (b && cudaEventRecord(b, c.st()) == cudaSuccess) c.ev_rec.push_back({slot, a, b});
+        else {
+            c.ev_free.push_back(a);
+            if (b) c.ev_free.push_back(b);
+        }
+    }
+    cudaEvent_t take() {
+        if (!c.ev_free.empty()) {
+            cudaEvent_t e = c.ev_free.back();
+            c.ev_free.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        return cudaEventCreate(&e) == cudaSuccess ? e : nullptr;
+    }
+};
+// Folds the recorded event pairs into t_ms / t_count (synchronises on the last one).
+void collect_kernel_timing(Ctx& c);
 
 // The context's side stream (and its fork / join events), created on first use.
 inline cudaStream_t side_stream(Ctx& c) {
@@ -383,8 +425,8 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node);
 void tree_lists(Ctx& c);
 // Near runs and far-field coefficients of every leaf, built once per tree on first use.
 void ensure_full_lists(Ctx& c);
-// Full far lists by an exact FP64 walk (inspection).
-void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t>& far_node);
+// Far lists by an exact FP64 walk (inspection): offsets, and the nodes when fill is set.
+void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t>& far_node, bool fill);
 void eps_pass(Ctx& c, int merge, int64_t* merged);
 void convective(Ctx& c);
 void velocity_points(Ctx& c, int64_t n, const double* px, const double* py, double* vx, double* vy);

@@ -85,6 +85,8 @@ SIGNATURES = {
     "vvgpu_synchronize": (C.c_int, [_H]),
     "vvgpu_get_stats": (C.c_int, [_H, C.POINTER(Stats)]),
     "vvgpu_set_eps_round_limit": (C.c_int, [_H, C.c_int64]),
+    "vvgpu_set_kernel_timing": (C.c_int, [_H, C.c_int]),
+    "vvgpu_get_kernel_timing": (C.c_int, [_H, _D, _I64]),
     "vvgpu_set_params": (C.c_int, [_H] + [C.c_double] * 8),
     "vvgpu_add_body": (C.c_int, [_H, C.c_int64, _D, _D, _U32, C.POINTER(BodyParams)]),
     "vvgpu_set_segment_g": (C.c_int, [_H, _D]),
@@ -222,9 +224,22 @@ class GpuSpace:
         d["launches"] = int(s.reserved[0])
         d["eps_evaluations"] = int(s.reserved[1])
         d["diff_sources"] = int(s.reserved[2])
+        d["eps_records"] = int(s.reserved[3])
         return d
 
     # -- state -----------------------------------------------------------------------
+    TIMING_SLOTS = ("tree_build", "walk", "eps_round", "eps_cand", "eps_pass", "convective", "diffusive", "slae")
+
+    def set_kernel_timing(self, on: bool = True):
+        self._ok(self.lib.vvgpu_set_kernel_timing(self.h, int(bool(on))), "set_kernel_timing")
+
+    def kernel_timing(self):
+        """{slot: (device ms, timed launches)} since timing was switched on."""
+        ms = np.zeros(len(self.TIMING_SLOTS))
+        cnt = np.zeros(len(self.TIMING_SLOTS), np.int64)
+        self._ok(self.lib.vvgpu_get_kernel_timing(self.h, _p(ms), _p(cnt, C.c_int64)), "get_kernel_timing")
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.TIMING_SLOTS)}
+
     def set_eps_round_limit(self, max_rounds: int):
         self._ok(self.lib.vvgpu_set_eps_round_limit(self.h, int(max_rounds)), "set_eps_round_limit")
 
@@ -480,11 +495,15 @@ class GpuSpace:
         self._ok(self.lib.vvgpu_tree_seg_order(self.h, _p(so, C.c_int64)), "tree_seg_order")
         return so
 
-    def tree_lists(self):
+    def tree_lists(self, far=True):
+        """Near and far lists of every leaf as (depth, path) of the nodes; far=False leaves
+        out the far nodes (only their offsets)."""
         _, nl, nnear, nfar = self.tree_sizes()
         d = {"near_off": np.empty(nl + 1, np.int64), "far_off": np.empty(nl + 1, np.int64),
              "near_depth": np.empty(nnear, np.int32), "near_path": np.empty(nnear, np.int64),
-             "far_depth": np.empty(nfar, np.int32), "far_path": np.empty(nfar, np.int64)}
+             "far_depth": np.empty(nfar if far else 0, np.int32), "far_path": np.empty(nfar if far else 0, np.int64)}
+        if not far:
+            d["far_depth"] = d["far_path"] = None
         self._ok(self.lib.vvgpu_tree_lists(self.h, _p(d["near_off"], C.c_int64), _p(d["near_depth"], C.c_int32),
                                            _p(d["near_path"], C.c_int64), _p(d["far_off"], C.c_int64),
                                            _p(d["far_depth"], C.c_int32), _p(d["far_path"], C.c_int64)), "tree_lists")
