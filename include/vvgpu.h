@@ -123,7 +123,9 @@ typedef struct vvgpu_stats {
                                    reserved[2]: sources in the candidate leaves of every
                                    8-target chunk of the last FP32 diffusive pass;
                                    reserved[3]: candidate records read by the FP32 filter
-                                   of every epsilon evaluation of the last pass */
+                                   of every epsilon evaluation of the last pass;
+                                   reserved[4]: node records loaded by the warps of the
+                                   last near/far walk (each shared by its 32 leaves) */
 } vvgpu_stats;
 
 /* Device time per kernel (vvgpu_get_kernel_timing slots): CUDA events recorded on the
@@ -137,7 +139,9 @@ enum {
     VVGPU_T_CONVECTIVE = 5,   /* convective near field and far-field application          */
     VVGPU_T_DIFFUSIVE = 6,    /* diffusive sums                                           */
     VVGPU_T_SLAE = 7,         /* vvgpu_slae, whole call                                   */
-    VVGPU_T_COUNT = 8
+    VVGPU_T_LEARNED = 8,      /* learned far-field corrections (network and leaf sums)     */
+    VVGPU_T_JUDGE = 9,        /* the judge's plain-tree velocities                         */
+    VVGPU_T_COUNT = 10
 };
 
 /* ---- context --------------------------------------------------------------------- */
@@ -322,6 +326,36 @@ int vvgpu_mlp_forward(vvgpu_mlp* m, int64_t n, const float* feat, float* y);
  * cell of p's leaf; *npairs = cells evaluated (may be NULL) */
 int vvgpu_velocity_points_learned(vvgpu_ctx* ctx, vvgpu_mlp* m, int64_t np, const double* px, const double* py,
                                   double* vx, double* vy, int64_t* npairs);
+
+/* The judge of the learned convective pass: velocity(p) of the plain tree (far criterion
+ * far_criteria, e.g. 8 for theta 0.5) at `targets` vortices drawn per call from `seed` and
+ * a call counter, against the learned pass's increments there.  gap = rms |learned -
+ * plain| / rms |plain - free stream| over the drawn vortices with g != 0. */
+typedef struct vvgpu_judge_cfg {
+    int64_t targets;            /* vortices judged per call (0: no judge)                */
+    double far_criteria;        /* the plain tree's far criterion                        */
+    double bound;               /* largest gap accepted                                   */
+    uint64_t seed;
+} vvgpu_judge_cfg;
+typedef struct vvgpu_judge_out {
+    double gap_rms, gap_max;    /* gap (above) and the largest single gap, same scale     */
+    int64_t pairs;              /* (leaf, far node) pairs the network corrected           */
+    int64_t judged;             /* vortices judged (g != 0)                               */
+    int32_t reverted;           /* 1: gap above the bound, the plain tree's pass was used */
+    int32_t reserved;
+} vvgpu_judge_out;
+/* MConvectiveFast::process_all_lists (MConvectiveFast.cpp:36-114) with the learned far
+ * field: for every (leaf, far node) pair of the built tree, the network's correction of the
+ * node's monopole field at the leaf's centre is added to the leaf's constant far-field
+ * terms, then the pass runs as vvgpu_convective.  judge (may be NULL: no judge) checks the
+ * increments against the plain tree; above the bound they are undone and the pass is redone
+ * with the plain tree at the judge's far criterion (the near lists then follow that
+ * criterion until the tree is destroyed).  The tree's walk keeps every leaf's far nodes for
+ * this; a tree built after vvgpu_keep_far_lists(ctx, 1) keeps them from its first walk,
+ * otherwise the first call walks once more.  No counterpart in the reference. */
+int vvgpu_convective_learned(vvgpu_ctx* ctx, vvgpu_mlp* m, const vvgpu_judge_cfg* judge, vvgpu_judge_out* out);
+/* Makes the near/far walk of later trees keep every leaf's far nodes (on = 1). */
+int vvgpu_keep_far_lists(vvgpu_ctx* ctx, int on);
 
 /* ---- grid fields (libvvhd/src/XVelocity.cpp, XStreamfunction.cpp, XVorticity.cpp) ---- */
 /* An xres x yres grid p = (xmin, ymin) + dxdy * (xi, yj), with xmin, ymin and dxdy rounded

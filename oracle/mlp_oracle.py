@@ -146,8 +146,9 @@ def far_cells(nodes, px, py, far_criteria):
     return out
 
 
-def cell_sample(nodes, vort, u, px, py):
-    """(features [20], label [2], factor back to velocity) of far cell u for target (px, py)."""
+def cell_sample(nodes, vort, u, px, py, with_label=True):
+    """(features [20], label [2], factor back to velocity) of far cell u for target (px, py);
+    with_label=False leaves the label (an exact sum over the cell) at 0."""
     gx, gy = nodes["x"][u], nodes["y"][u]
     sz = nodes["h"][u] + nodes["w"][u]
     cp = (nodes["cmp_x"][u], nodes["cmp_y"][u], nodes["cmp_g"][u])
@@ -173,6 +174,8 @@ def cell_sample(nodes, vort, u, px, py):
             f[6 + 6 * sgn + 2 * e + 1] = mk.imag
     f[18], f[19] = dx / sz, dy / sz
     norm = 2 * math.pi * d2 * d / (G * sz * sz)
+    if not with_label:
+        return f, np.zeros(2), 1.0 / norm
     nz = gs != 0
     rx, ry = px - xs[nz], py - ys[nz]
     q = gs[nz] / (rx * rx + ry * ry)
@@ -202,3 +205,24 @@ def samples(nodes, vort, px, py, far_criteria):
     if not F:
         return np.zeros((0, NF)), np.zeros((0, 2)), np.zeros(0)
     return np.array(F), np.array(L), np.array(B)
+
+
+def leaf_correction(p, norm, nodes, vort, cx, cy, far_criteria):
+    """The learned correction of one leaf's constant far-field terms (the convective pass
+    with the learned far field, vvflow_gb300/csrc/learned_step.cu): the network at the
+    leaf's centre (cx, cy) for every far cell of the leaf, inputs standardised by norm,
+    outputs scaled back to velocity and summed.  Returns (dvx, dvy, sum of |pair
+    corrections|)."""
+    norm = np.asarray(norm, np.float64)
+    cells = far_cells(nodes, cx, cy, far_criteria)
+    if not cells:
+        return 0.0, 0.0, 0.0
+    F, B = [], []
+    for u in cells:
+        f, _, back = cell_sample(nodes, vort, u, cx, cy, with_label=False)
+        F.append(f)
+        B.append(back)
+    F = (np.array(F) - norm[:NF]) * norm[NF:2 * NF]
+    Y, _ = forward(p, F, quant=True)
+    C = Y * norm[2 * NF:2 * NF + 2] * np.array(B)[:, None]
+    return float(C[:, 0].sum()), float(C[:, 1].sum()), float(np.abs(C).sum())

@@ -484,6 +484,71 @@ __global__ void k_near_pairs(int64_t nl, const int32_t* __restrict__ nz, const i
     if ((threadIdx.x & 31) == 0 && v) atomicAdd(out, v);
 }
 
+// The judge of the learned far field: MConvectiveFast::velocity(p) (:20-34) at the positions
+// of vortices idx[k], with the tree's near/far split redone at far criterion fc (the plain
+// tree's) by the reference's depth-first walk with its exact FP64 test.  out[3 k ..] =
+// (vx, vy, 1) for a vortex with g != 0, (0, 0, 0) otherwise (it takes no convective term).
+__global__ void k_judge(int64_t nt, const int32_t* __restrict__ idx, const double4* __restrict__ geom,
+                        const int32_t* __restrict__ ch1, const int32_t* __restrict__ nvf,
+                        const int32_t* __restrict__ nvl, ConvArgs a, double fc, double* out) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nt) return;
+    const int32_t i = idx[q];
+    if (a.g[i] == 0.) {
+        out[3 * q] = 0.; out[3 * q + 1] = 0.; out[3 * q + 2] = 0.;
+        return;
+    }
+    const double px = a.x[i], py = a.y[i];
+    int32_t k = 0;
+    for (int it = 0; it <= MAX_DEPTH && ch1[k] >= 0; it++) {
+        const double4 gm = geom[k];
+        if (gm.z < gm.w) k = (px < gm.x) ? ch1[k] : ch1[k] + 1;
+        else k = (py < gm.y) ? ch1[k] : ch1[k] + 1;
+    }
+    const double4 me = geom[k];
+    double rx = 0, ry = 0, fx = 0, fy = 0;
+    int32_t stack[MAX_DEPTH + 2];
+    int sp = 0;
+    stack[sp++] = 0;
+    int64_t guard = 0;
+    while (sp && ++guard <= a.nnodes) {
+        const int32_t t = stack[--sp];
+        const double4 tg = geom[t];
+        const double ddx = dsub(tg.x, me.x), ddy = dsub(tg.y, me.y);
+        const double hp = dadd(dadd(dadd(tg.z, tg.w), me.z), me.w);
+        if (dabs2(ddx, ddy) > dmul(dmul(fc, hp), hp)) {
+            const double* c = a.cm + 6 * (size_t)t;
+            double dx = px - c[0], dy = py - c[1];
+            double s = c[2] / (dx * dx + dy * dy);
+            fx -= dy * s; fy += dx * s;
+            dx = px - c[3]; dy = py - c[4];
+            s = c[5] / (dx * dx + dy * dy);
+            fx -= dy * s; fy += dx * s;
+            continue;
+        }
+        const int32_t c1 = ch1[t];
+        if (c1 >= 0) {
+            if (sp + 2 <= MAX_DEPTH + 2) {
+                stack[sp++] = c1 + 1;
+                stack[sp++] = c1;
+            }
+            continue;
+        }
+        for (int32_t j = nvf[t]; j < nvl[t]; j++) {  // a near leaf
+            if (a.g[j] == 0.) continue;
+            const double dx = px - a.x[j], dy = py - a.y[j];
+            const double e = 1. / a.ie[j];
+            const double s = a.g[j] / (dx * dx + dy * dy + e * e);
+            rx -= dy * s; ry += dx * s;
+        }
+    }
+    double ex, ey;
+    extra_terms(a, px, py, ex, ey);
+    out[3 * q] = rx * C_1_2PI + fx * C_1_2PI + ex + a.inf_vx;
+    out[3 * q + 1] = ry * C_1_2PI + fy * C_1_2PI + ey + a.inf_vy;
+    out[3 * q + 2] = 1.;
+}
+
 ConvArgs make_args(Ctx& c) {
     ConvArgs a{};
     a.nl = c.nleaves;
@@ -610,6 +675,14 @@ void direct_velocity(Ctx& c, int64_t np, const double* px, const double* py, dou
     VV_CUDA(cudaMemcpyAsync(vx, q.p + 2 * np, np * 8, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaMemcpyAsync(vy, q.p + 3 * np, np * 8, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));
+}
+
+void judge_velocity(Ctx& c, int64_t nt, const int32_t* d_idx, double fc, double* d_out) {
+    if (nt <= 0) return;
+    ConvArgs a = make_args(c);
+    k_judge<<<grid_for(nt, 64), 64, 0, c.st()>>>(nt, d_idx, c.nd_geom.p, c.nd_ch1.p, c.nd_vf.p, c.nd_vl.p, a, fc,
+                                                 d_out);
+    VV_LAUNCH_CHECK();
 }
 
 // Point velocities for points already in device memory: the same kernel as

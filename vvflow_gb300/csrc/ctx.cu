@@ -287,6 +287,7 @@ int vvgpu_get_stats(const vvgpu_ctx* h, vvgpu_stats* out) {
     out->reserved[1] = h->c.eps_evaluations;
     out->reserved[2] = h->c.diff_sources;
     out->reserved[3] = h->c.eps_records;
+    out->reserved[4] = h->c.walk_loads;
     return VVGPU_OK;
 }
 
@@ -519,6 +520,7 @@ int vvgpu_tree_destroy(vvgpu_ctx* h) {
     API_BEGIN(h)
     c.built = false;
     c.lists_full = false;
+    c.far_kept = false;
     API_END
 }
 

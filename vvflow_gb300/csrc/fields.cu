@@ -307,6 +307,7 @@ void restore_state(Ctx& c, Saved& sv) {
     const int64_t n = sv.n, m = c.m;
     c.built = false;
     c.lists_full = false;
+    c.far_kept = false;
     double* dst[6] = {c.x.p, c.y.p, c.g.p, c.ie.p, c.vx.p, c.vy.p};
     if (n > 0) {
         for (int k = 0; k < 6; k++)

@@ -359,17 +359,21 @@ struct Taylor {
 };
 
 constexpr int RUN_CAP = 64;   // near runs kept per leaf by the warp walk
+constexpr int FAR_CAP = 2048; // far nodes kept per leaf by the warp walk (when asked to keep them)
 constexpr int WW = 4;         // warps per block in the warp walk
 
 // One warp walks the tree for 32 consecutive leaves at once (they are neighbours in space,
 // so their walks share most nodes).  The stack holds (node, mask of lanes still walking
 // below it); node data are broadcast loads.  Each lane keeps its own near runs (in depth-
 // first order) and far-field coefficients.  Runs beyond RUN_CAP are counted, not stored.
+// With far_buf set, each leaf's far nodes are also kept (walk order, at most far_cap of
+// them; the count in far_cnt may exceed far_cap, and the caller then rebuilds that list).
 template <bool FP32>
 __global__ void __launch_bounds__(WW * 32) k_walk_warp(int64_t nl, ListView v, const int32_t* __restrict__ leaf_node,
                                                        int32_t* near_cnt, int2* run_buf, double4* taylor,
                                                        unsigned long long* far_total, int64_t nodes_bound,
-                                                       int32_t* err) {
+                                                       int32_t* err, int32_t* far_buf, int32_t far_cap,
+                                                       int32_t* far_cnt) {
     __shared__ int32_t s_node[WW][MAX_DEPTH + 2];
     __shared__ uint32_t s_mask[WW][MAX_DEPTH + 2];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -401,6 +405,7 @@ __global__ void __launch_bounds__(WW * 32) k_walk_warp(int64_t nl, ListView v, c
         const bool far = act && far_test_at(v, cur.r0, make_float2(cur.r1.x, cur.r1.y), t, meN, mg, mk);
         if (far) {
             if (FP32) tay.add_rec(cur, mg, mk); else tay.add(v, t, mg, mk, me);
+            if (far_buf && nfar < far_cap) far_buf[(size_t)L * far_cap + nfar] = t;
             nfar++;
         }
         const uint32_t rest = mask & ~__ballot_sync(0xffffffffu, far);
@@ -431,9 +436,19 @@ __global__ void __launch_bounds__(WW * 32) k_walk_warp(int64_t nl, ListView v, c
         if (rfirst >= 0 && nr <= RUN_CAP) myruns[nr - 1] = make_int2(rfirst, last + 1);
         near_cnt[L] = nr;
         taylor[L] = tay.result();
+        if (far_cnt) far_cnt[L] = nfar;
     }
     unsigned long long f = warp_sum_u64(valid ? (unsigned long long)nfar : 0ull);
-    if (lane == 0) atomicAdd(far_total, f);
+    if (lane == 0) {
+        atomicAdd(far_total, f);
+        atomicAdd(far_total + 8, (unsigned long long)guard);  // node records this warp loaded
+    }
+}
+
+__global__ void k_count_over(int64_t nl, const int32_t* __restrict__ cnt, int32_t cap, int32_t* n_over) {
+    const int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool o = L < nl && cnt[L] > cap;
+    if (__any_sync(0xffffffffu, o) && (threadIdx.x & 31) == 0) atomicAdd(n_over, 1);
 }
 
 __global__ void k_runs_compact(int64_t nl, const int32_t* __restrict__ near_cnt, const int32_t* __restrict__ near_off,
@@ -537,6 +552,28 @@ void walk_selected(Ctx& c, const ListView& v, const int32_t* sel, int what, bool
     }
 }
 
+// Far nodes of every leaf, contiguous in leaf order: node ids and their leaf.  One warp per
+// leaf copies its walk buffer.
+__global__ void k_far_compact(int64_t nl, const int32_t* __restrict__ far_cnt, const int32_t* __restrict__ far_off,
+                              const int32_t* __restrict__ far_buf, int32_t far_cap, int32_t* node, int32_t* leaf) {
+    const int64_t L = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (L >= nl) return;
+    const int32_t n = far_cnt[L], o = far_off[L];
+    const int32_t* src = far_buf + (size_t)L * far_cap;
+    for (int32_t k = lane; k < n; k += 32) {
+        node[o + k] = src[k];
+        leaf[o + k] = (int32_t)L;
+    }
+}
+
+__global__ void k_far_leaf_of(int64_t nl, const int32_t* __restrict__ far_off, int32_t* leaf) {
+    const int64_t L = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (L >= nl) return;
+    for (int32_t k = far_off[L] + lane; k < far_off[L + 1]; k += 32) leaf[k] = (int32_t)L;
+}
+
 ListView list_view(Ctx& c) {
     return ListView{c.nd_geom.p, c.nd_ch1.p, c.nd_dfs.p, c.nf_geo.p, c.nf_k.p, c.nf_cm.p, c.nf_g.p, c.nd_cm.p,
                     c.nf_rec.p, c.far_criteria, (float)c.far_criteria, (float)c.frame_G};
@@ -582,8 +619,45 @@ void tree_lists(Ctx& c) {
     walk_selected(c, v, c.lf_flag.p, 3, /*count=*/false);
     if (read_i32(c, err)) throw ApiError{VVGPU_ERR_LIMIT, "tree traversal exceeded its bound"};
     c.lists_full = false;
+    c.far_kept = false;
     c.stats.near_runs = c.n_near_runs;
     c.stats.far_pairs = 0;
+}
+
+// The far nodes the warp walk kept, compacted (lf_far_off / lf_far_node / lf_far_leaf).  A
+// leaf with more than FAR_CAP far nodes makes every list come from the exact walk instead
+// (the same nodes in the same depth-first order).
+void keep_far_lists(Ctx& c) {
+    cudaStream_t s = c.st();
+    const int64_t nl = c.nleaves;
+    c.lf_far_off.reserve(nl + 2);
+    int32_t* n_over = (int32_t*)(c.counters.p + 17);
+    VV_CUDA(cudaMemsetAsync(n_over, 0, 4, s));
+    k_count_over<<<grid_for(nl, 256), 256, 0, s>>>(nl, c.lf_far_cnt.p, FAR_CAP, n_over);
+    VV_LAUNCH_CHECK();
+    if (read_i32(c, n_over) > 0) {
+        std::vector<int32_t> off, node;
+        tree_lists_exact(c, off, node, true);
+        if ((int64_t)node.size() > 0x7fffffffLL) throw ApiError{VVGPU_ERR_LIMIT, "more than 2^31 far pairs"};
+        c.n_far_pairs = (int64_t)node.size();
+        c.lf_far_node.reserve(c.n_far_pairs + 1);
+        c.lf_far_leaf.reserve(c.n_far_pairs + 1);
+        VV_CUDA(cudaMemcpyAsync(c.lf_far_off.p, off.data(), (nl + 1) * 4, cudaMemcpyHostToDevice, s));
+        if (c.n_far_pairs)
+            VV_CUDA(cudaMemcpyAsync(c.lf_far_node.p, node.data(), c.n_far_pairs * 4, cudaMemcpyHostToDevice, s));
+        k_far_leaf_of<<<grid_for(nl, 8), 256, 0, s>>>(nl, c.lf_far_off.p, c.lf_far_leaf.p);
+        VV_LAUNCH_CHECK();
+        VV_CUDA(cudaStreamSynchronize(s));
+    } else {
+        exclusive_scan(c, c.lf_far_cnt.p, c.lf_far_off.p, nl);
+        c.n_far_pairs = (uint32_t)read_i32(c, c.lf_far_off.p + nl);
+        c.lf_far_node.reserve(c.n_far_pairs + 1);
+        c.lf_far_leaf.reserve(c.n_far_pairs + 1);
+        k_far_compact<<<grid_for(nl, 8), 256, 0, s>>>(nl, c.lf_far_cnt.p, c.lf_far_off.p, c.far_buf.p, FAR_CAP,
+                                                      c.lf_far_node.p, c.lf_far_leaf.p);
+        VV_LAUNCH_CHECK();
+    }
+    c.far_kept = true;
 }
 
 void ensure_full_lists(Ctx& c) {
@@ -596,16 +670,25 @@ void ensure_full_lists(Ctx& c) {
     c.lf_taylor.reserve(nl + 1);
     c.run_buf.reserve((size_t)nl * RUN_CAP + 1);
     c.lf_overflow.reserve(nl + 1);
-    unsigned long long* far_total = c.counters.p + 10;
+    unsigned long long* far_total = c.counters.p + 10;  // and, at + 8, the walk's record loads
     VV_CUDA(cudaMemsetAsync(far_total, 0, 8, s));
+    VV_CUDA(cudaMemsetAsync(far_total + 8, 0, 8, s));
     const bool fp32 = c.precision == VVGPU_FP32;
     const unsigned gw = grid_for((nl + 31) / 32, WW);
     {
         KernelTimer kt(c, VVGPU_T_WALK);
+        int32_t* fb = nullptr;
+        int32_t* fcnt = nullptr;
+        if (c.keep_far) {
+            c.far_buf.reserve((size_t)nl * FAR_CAP + 1);
+            c.lf_far_cnt.reserve(nl + 1);
+            fb = c.far_buf.p;
+            fcnt = c.lf_far_cnt.p;
+        }
         if (fp32) k_walk_warp<true><<<gw, WW * 32, 0, s>>>(nl, v, c.leaf_node.p, c.near_cnt.p, c.run_buf.p,
-                                                            c.lf_taylor.p, far_total, nn, err);
+                                                            c.lf_taylor.p, far_total, nn, err, fb, FAR_CAP, fcnt);
         else k_walk_warp<false><<<gw, WW * 32, 0, s>>>(nl, v, c.leaf_node.p, c.near_cnt.p, c.run_buf.p,
-                                                         c.lf_taylor.p, far_total, nn, err);
+                                                         c.lf_taylor.p, far_total, nn, err, fb, FAR_CAP, fcnt);
         VV_LAUNCH_CHECK();
     }
     exclusive_scan(c, c.near_cnt.p, c.near_off.p, nl);
@@ -626,10 +709,16 @@ void ensure_full_lists(Ctx& c) {
     c.lists_full = true;
     c.stats.near_runs = c.n_near_runs;
     c.taylor_precision = c.precision;
-    unsigned long long ft = 0;
+    unsigned long long ft = 0, nv = 0;
     VV_CUDA(cudaMemcpyAsync(&ft, far_total, 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaMemcpyAsync(&nv, far_total + 8, 8, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));
+    c.walk_loads = (int64_t)nv;
     c.stats.far_pairs = 2 * (int64_t)ft;  // two monopoles per far node
+    if (c.keep_far) {
+        if (ft > 0x7fffffffull) throw ApiError{VVGPU_ERR_LIMIT, "more than 2^31 far pairs to keep"};
+        keep_far_lists(c);
+    }
 }
 
 void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t>& far_node, bool fill) {

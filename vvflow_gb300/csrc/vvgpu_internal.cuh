@@ -181,6 +181,18 @@ struct Ctx {
     DArr<int2> run_buf;             // warp walk: fixed-capacity near runs per leaf
     DArr<int32_t> lf_overflow;      // leaf had more runs than the buffer holds
     DArr<double4> lf_taylor;        // far-field expansion coefficients T1..T4 per leaf
+    // far nodes of every leaf, kept by the warp walk when keep_far is set (learned far field)
+    bool keep_far = false, far_kept = false;
+    DArr<int32_t> far_buf, lf_far_cnt, lf_far_off, lf_far_node, lf_far_leaf;
+    int64_t n_far_pairs = 0;
+    // learned far field (learned_step.cu): per-node inputs (BF16 bits) and geometry, per-pair
+    // corrections, corrected coefficients, the judge's samples and results
+    DArr<uint16_t> ln_row;
+    DArr<double4> ln_geo, lf_taylor_l;
+    DArr<float2> ln_pv;
+    DArr<double> ln_v0, ln_judge;
+    DArr<int32_t> ln_idx;
+    uint64_t judge_calls = 0;
     int taylor_precision = 0;
     DArr<float4> nf_geo, nf_cm;     // per node, anchor frame: centre + (h+w); centroids
     DArr<float2> nf_k;              // per node anchor (FP32, exact)
@@ -257,6 +269,7 @@ struct Ctx {
     int64_t launches = 0;           // kernels launched by this context
     int64_t eps_evaluations = 0;    // target evaluations over the rounds of the last epsilon pass
     int64_t eps_records = 0;        // candidate records read by those evaluations' FP32 passes
+    int64_t walk_loads = 0;         // node records loaded by the warps of the last full walk
     int64_t diff_sources = 0;       // sources in the candidate leaves of every diffusive target chunk
     bool count_pairs = true;        // count algorithmic near pairs before each convective pass
 
@@ -425,13 +438,20 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node);
 void tree_lists(Ctx& c);
 // Near runs and far-field coefficients of every leaf, built once per tree on first use.
 void ensure_full_lists(Ctx& c);
+// Compacts the far nodes the walk kept (keep_far) into lf_far_off / lf_far_node / lf_far_leaf.
+void keep_far_lists(Ctx& c);
 // Far lists by an exact FP64 walk (inspection): offsets, and the nodes when fill is set.
 void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t>& far_node, bool fill);
 void eps_pass(Ctx& c, int merge, int64_t* merged);
+// the learned far field in the convective pass with its judge (learned_step.cu)
+void convective_learned(Ctx& c, vvgpu_mlp& M, const vvgpu_judge_cfg* jc, vvgpu_judge_out* jo);
 void convective(Ctx& c);
 void velocity_points(Ctx& c, int64_t n, const double* px, const double* py, double* vx, double* vy);
 void velocity_points_on_device(Ctx& c, int64_t n, const double* dpx, const double* dpy, double* dvx, double* dvy);
 void direct_velocity(Ctx& c, int64_t n, const double* px, const double* py, double* vx, double* vy);
+// velocity(p) at the vortices d_idx[0 .. nt) with the near/far split of far criterion fc on
+// the built tree (the learned far field's judge); d_out: (vx, vy, valid) per target.
+void judge_velocity(Ctx& c, int64_t nt, const int32_t* d_idx, double fc, double* d_out);
 // TVec3D::iszero of every body's speed_slae (TVec3D.hpp:17), else VVGPU_ERR_UNSUPPORTED.
 void check_bodies_at_rest(Ctx& c);
 // grid fields (fields.cu)

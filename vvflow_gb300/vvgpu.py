@@ -55,6 +55,15 @@ class StepCfg(C.Structure):
                 ("merge", C.c_int32), ("move", C.c_int32)]
 
 
+class JudgeCfg(C.Structure):
+    _fields_ = [("targets", C.c_int64), ("far_criteria", C.c_double), ("bound", C.c_double), ("seed", C.c_uint64)]
+
+
+class JudgeOut(C.Structure):
+    _fields_ = [("gap_rms", C.c_double), ("gap_max", C.c_double), ("pairs", C.c_int64), ("judged", C.c_int64),
+                ("reverted", C.c_int32), ("reserved", C.c_int32)]
+
+
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "n_vortices", "n_segments", "n_nodes", "n_leaves", "tree_depth", "near_pairs", "far_pairs",
@@ -140,6 +149,8 @@ SIGNATURES = {
     "vvgpu_mlp_train": (C.c_int, [_H, C.c_int64, C.c_int64, C.c_float, C.c_uint64, _F]),
     "vvgpu_mlp_forward": (C.c_int, [_H, C.c_int64, _F, _F]),
     "vvgpu_velocity_points_learned": (C.c_int, [_H, _H, C.c_int64, _D, _D, _D, _D, _I64]),
+    "vvgpu_convective_learned": (C.c_int, [_H, _H, C.POINTER(JudgeCfg), C.POINTER(JudgeOut)]),
+    "vvgpu_keep_far_lists": (C.c_int, [_H, C.c_int]),
     "vvgpu_field_velocity": (C.c_int, [_H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
                                        C.c_char, C.c_char, _F]),
     "vvgpu_field_streamfunction": (C.c_int, [_H, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
@@ -225,10 +236,12 @@ class GpuSpace:
         d["eps_evaluations"] = int(s.reserved[1])
         d["diff_sources"] = int(s.reserved[2])
         d["eps_records"] = int(s.reserved[3])
+        d["walk_loads"] = int(s.reserved[4])
         return d
 
     # -- state -----------------------------------------------------------------------
-    TIMING_SLOTS = ("tree_build", "walk", "eps_round", "eps_cand", "eps_pass", "convective", "diffusive", "slae")
+    TIMING_SLOTS = ("tree_build", "walk", "eps_round", "eps_cand", "eps_pass", "convective", "diffusive", "slae",
+                    "learned", "judge")
 
     def set_kernel_timing(self, on: bool = True):
         self._ok(self.lib.vvgpu_set_kernel_timing(self.h, int(bool(on))), "set_kernel_timing")
@@ -239,6 +252,18 @@ class GpuSpace:
         cnt = np.zeros(len(self.TIMING_SLOTS), np.int64)
         self._ok(self.lib.vvgpu_get_kernel_timing(self.h, _p(ms), _p(cnt, C.c_int64)), "get_kernel_timing")
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.TIMING_SLOTS)}
+
+    def keep_far_lists(self, on: bool = True):
+        self._ok(self.lib.vvgpu_keep_far_lists(self.h, int(bool(on))), "keep_far_lists")
+
+    def convective_learned(self, mlp, targets=4096, far_criteria=8.0, bound=5e-3, seed=1):
+        """process_all_lists with the learned far field, judged by the plain tree at
+        far_criteria on `targets` sampled vortices (0: no judge).  Returns the verdict."""
+        cfg = JudgeCfg(int(targets), float(far_criteria), float(bound), int(seed))
+        out = JudgeOut()
+        self._ok(self.lib.vvgpu_convective_learned(self.h, mlp.h, C.byref(cfg) if targets else None,
+                                                   C.byref(out)), "convective_learned")
+        return {k: getattr(out, k) for k, _ in JudgeOut._fields_ if k != "reserved"}
 
     def set_eps_round_limit(self, max_rounds: int):
         self._ok(self.lib.vvgpu_set_eps_round_limit(self.h, int(max_rounds)), "set_eps_round_limit")
