@@ -486,67 +486,130 @@ __global__ void k_near_pairs(int64_t nl, const int32_t* __restrict__ nz, const i
 
 // The judge of the learned far field: MConvectiveFast::velocity(p) (:20-34) at the positions
 // of vortices idx[k], with the tree's near/far split redone at far criterion fc (the plain
-// tree's) by the reference's depth-first walk with its exact FP64 test.  out[3 k ..] =
-// (vx, vy, 1) for a vortex with g != 0, (0, 0, 0) otherwise (it takes no convective term).
-__global__ void k_judge(int64_t nt, const int32_t* __restrict__ idx, const double4* __restrict__ geom,
-                        const int32_t* __restrict__ ch1, const int32_t* __restrict__ nvf,
-                        const int32_t* __restrict__ nvl, ConvArgs a, double fc, double* out) {
+// tree's) by the reference's depth-first walk with its exact FP64 test.
+// Pass 1 (k_judge_walk<false>, one thread per target): counts each target's far nodes and
+// near leaves; pass 2 (<true>): writes them at the scanned offsets.  Then k_judge_sum, one
+// warp per target: the lanes split the far nodes' monopoles and the near leaves' vortices
+// (FP64, reciprocal by Newton steps), partials reduced by a fixed shuffle tree.
+// out[3 k ..] = (vx, vy, 1) for a vortex with g != 0, (0, 0, 0) otherwise (it takes no
+// convective term).
+template <bool FILL>
+__global__ void k_judge_walk(int64_t nt, const int32_t* __restrict__ idx, const double* __restrict__ x,
+                             const double* __restrict__ y, const double* __restrict__ g,
+                             const double4* __restrict__ geom, const int32_t* __restrict__ ch1, double fc,
+                             int64_t nnodes, int32_t* cnt, const int64_t* __restrict__ off, int32_t* list,
+                             int32_t* err) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nt) return;
     const int32_t i = idx[q];
+    int32_t nf = 0, nn = 0;
+    if (g[i] != 0.) {
+        const double px = x[i], py = y[i];
+        int32_t k = 0;
+        for (int it = 0; it <= MAX_DEPTH && ch1[k] >= 0; it++) {
+            const double4 gm = geom[k];
+            if (gm.z < gm.w) k = (px < gm.x) ? ch1[k] : ch1[k] + 1;
+            else k = (py < gm.y) ? ch1[k] : ch1[k] + 1;
+        }
+        const double4 me = geom[k];
+        // far nodes from the front of the target's range, near leaves from its back
+        int32_t* fl = FILL ? list + off[q] : nullptr;
+        int32_t* nl = FILL ? list + off[q + 1] : nullptr;
+        int32_t stack[MAX_DEPTH + 2];
+        int sp = 0;
+        stack[sp++] = 0;
+        int64_t guard = 0;
+        while (sp) {
+            if (++guard > nnodes) { atomicExch(err, 1); break; }
+            const int32_t t = stack[--sp];
+            const double4 tg = geom[t];
+            const double ddx = dsub(tg.x, me.x), ddy = dsub(tg.y, me.y);
+            const double hp = dadd(dadd(dadd(tg.z, tg.w), me.z), me.w);
+            if (dabs2(ddx, ddy) > dmul(dmul(fc, hp), hp)) {
+                if (FILL) fl[nf] = t;
+                nf++;
+                continue;
+            }
+            const int32_t c1 = ch1[t];
+            if (c1 < 0) {
+                nn++;
+                if (FILL) nl[-nn] = t;
+                continue;
+            }
+            if (sp + 2 > MAX_DEPTH + 2) { atomicExch(err, 1); break; }
+            stack[sp++] = c1 + 1;
+            stack[sp++] = c1;
+        }
+    }
+    if (!FILL) {
+        cnt[2 * q] = nf;
+        cnt[2 * q + 1] = nn;
+    }
+}
+
+__global__ void k_judge_sum(int64_t nt, const int32_t* __restrict__ idx, const int32_t* __restrict__ cnt,
+                            const int64_t* __restrict__ off, const int32_t* __restrict__ list,
+                            const int32_t* __restrict__ nvf, const int32_t* __restrict__ nvl, ConvArgs a,
+                            double* out) {
+    const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (q >= nt) return;
+    const int32_t i = idx[q];
     if (a.g[i] == 0.) {
-        out[3 * q] = 0.; out[3 * q + 1] = 0.; out[3 * q + 2] = 0.;
+        if (lane == 0) { out[3 * q] = 0.; out[3 * q + 1] = 0.; out[3 * q + 2] = 0.; }
         return;
     }
     const double px = a.x[i], py = a.y[i];
-    int32_t k = 0;
-    for (int it = 0; it <= MAX_DEPTH && ch1[k] >= 0; it++) {
-        const double4 gm = geom[k];
-        if (gm.z < gm.w) k = (px < gm.x) ? ch1[k] : ch1[k] + 1;
-        else k = (py < gm.y) ? ch1[k] : ch1[k] + 1;
-    }
-    const double4 me = geom[k];
-    double rx = 0, ry = 0, fx = 0, fy = 0;
-    int32_t stack[MAX_DEPTH + 2];
-    int sp = 0;
-    stack[sp++] = 0;
-    int64_t guard = 0;
-    while (sp && ++guard <= a.nnodes) {
-        const int32_t t = stack[--sp];
-        const double4 tg = geom[t];
-        const double ddx = dsub(tg.x, me.x), ddy = dsub(tg.y, me.y);
-        const double hp = dadd(dadd(dadd(tg.z, tg.w), me.z), me.w);
-        if (dabs2(ddx, ddy) > dmul(dmul(fc, hp), hp)) {
-            const double* c = a.cm + 6 * (size_t)t;
-            double dx = px - c[0], dy = py - c[1];
-            double s = c[2] / (dx * dx + dy * dy);
-            fx -= dy * s; fy += dx * s;
-            dx = px - c[3]; dy = py - c[4];
-            s = c[5] / (dx * dx + dy * dy);
-            fx -= dy * s; fy += dx * s;
-            continue;
-        }
-        const int32_t c1 = ch1[t];
-        if (c1 >= 0) {
-            if (sp + 2 <= MAX_DEPTH + 2) {
-                stack[sp++] = c1 + 1;
-                stack[sp++] = c1;
-            }
-            continue;
-        }
-        for (int32_t j = nvf[t]; j < nvl[t]; j++) {  // a near leaf
-            if (a.g[j] == 0.) continue;
-            const double dx = px - a.x[j], dy = py - a.y[j];
-            const double e = 1. / a.ie[j];
-            const double s = a.g[j] / (dx * dx + dy * dy + e * e);
+    const int32_t nf = cnt[2 * q], nn = cnt[2 * q + 1];
+    const int32_t* fl = list + off[q];
+    const int32_t* nl = list + off[q + 1] - nn;
+    double rx = 0, ry = 0;
+    for (int32_t k = lane; k < nf; k += 32) {  // far_nodes_influence (:139-151)
+        const double* c = a.cm + 6 * (size_t)fl[k];
+#pragma unroll
+        for (int sgn = 0; sgn < 2; sgn++) {
+            const double gs = c[3 * sgn + 2];
+            const double dx = px - c[3 * sgn], dy = py - c[3 * sgn + 1];
+            const double s = gs * rcp64(dx * dx + dy * dy);
             rx -= dy * s; ry += dx * s;
         }
     }
-    double ex, ey;
-    extra_terms(a, px, py, ex, ey);
-    out[3 * q] = rx * C_1_2PI + fx * C_1_2PI + ex + a.inf_vx;
-    out[3 * q + 1] = ry * C_1_2PI + fy * C_1_2PI + ey + a.inf_vy;
-    out[3 * q + 2] = 1.;
+    for (int32_t k = lane; k < nn; k += 32) {  // near_nodes_influence (:122-137)
+        const int32_t t = nl[k];
+        for (int32_t j = nvf[t]; j < nvl[t]; j++) {
+            const double gj = a.g[j];
+            if (gj == 0.) continue;
+            const double dx = px - a.x[j], dy = py - a.y[j];
+            const double e = rcp64(a.ie[j]);
+            const double s = gj * rcp64(dx * dx + dy * dy + e * e);
+            rx -= dy * s; ry += dx * s;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        rx += __shfl_xor_sync(0xffffffffu, rx, o);
+        ry += __shfl_xor_sync(0xffffffffu, ry, o);
+    }
+    if (lane == 0) {
+        double ex, ey;
+        extra_terms(a, px, py, ex, ey);
+        out[3 * q] = rx * C_1_2PI + ex + a.inf_vx;
+        out[3 * q + 1] = ry * C_1_2PI + ey + a.inf_vy;
+        out[3 * q + 2] = 1.;
+    }
+}
+
+__global__ void k_pair_counts(int64_t nt, const int32_t* __restrict__ cnt, int32_t* tot) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nt) tot[q] = cnt[2 * q] + cnt[2 * q + 1];
+}
+
+__global__ void k_i32_prefix64(int64_t n, const int32_t* __restrict__ in, int64_t* out) {
+    // one thread: n is the number of judged targets (thousands)
+    if (blockIdx.x || threadIdx.x) return;
+    int64_t s = 0;
+    for (int64_t k = 0; k < n; k++) { out[k] = s; s += in[k]; }
+    out[n] = s;
 }
 
 ConvArgs make_args(Ctx& c) {
@@ -679,10 +742,33 @@ void direct_velocity(Ctx& c, int64_t np, const double* px, const double* py, dou
 
 void judge_velocity(Ctx& c, int64_t nt, const int32_t* d_idx, double fc, double* d_out) {
     if (nt <= 0) return;
+    cudaStream_t s = c.st();
     ConvArgs a = make_args(c);
-    k_judge<<<grid_for(nt, 64), 64, 0, c.st()>>>(nt, d_idx, c.nd_geom.p, c.nd_ch1.p, c.nd_vf.p, c.nd_vl.p, a, fc,
-                                                 d_out);
+    DArr<int32_t> cnt, tot, err;
+    DArr<int64_t> off;
+    cnt.reserve(2 * nt);
+    tot.reserve(nt);
+    off.reserve(nt + 1);
+    err.reserve(1);
+    VV_CUDA(cudaMemsetAsync(err.p, 0, 4, s));
+    k_judge_walk<false><<<grid_for(nt, 64), 64, 0, s>>>(nt, d_idx, c.x.p, c.y.p, c.g.p, c.nd_geom.p, c.nd_ch1.p, fc,
+                                                        c.nnodes, cnt.p, nullptr, nullptr, err.p);
     VV_LAUNCH_CHECK();
+    k_pair_counts<<<grid_for(nt, 256), 256, 0, s>>>(nt, cnt.p, tot.p);
+    VV_LAUNCH_CHECK();
+    k_i32_prefix64<<<1, 32, 0, s>>>(nt, tot.p, off.p);
+    VV_LAUNCH_CHECK();
+    int64_t total = 0;
+    VV_CUDA(cudaMemcpyAsync(&total, off.p + nt, 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    DArr<int32_t> list;
+    list.reserve(total + 1);
+    k_judge_walk<true><<<grid_for(nt, 64), 64, 0, s>>>(nt, d_idx, c.x.p, c.y.p, c.g.p, c.nd_geom.p, c.nd_ch1.p, fc,
+                                                       c.nnodes, cnt.p, off.p, list.p, err.p);
+    VV_LAUNCH_CHECK();
+    k_judge_sum<<<grid_for(nt, 4), 128, 0, s>>>(nt, d_idx, cnt.p, off.p, list.p, c.nd_vf.p, c.nd_vl.p, a, d_out);
+    VV_LAUNCH_CHECK();
+    if (read_i32(c, err.p)) throw ApiError{VVGPU_ERR_LIMIT, "judge walk exceeded its bound"};
 }
 
 // Point velocities for points already in device memory: the same kernel as

@@ -97,7 +97,8 @@ __device__ __forceinline__ uint4* chunk_at(__nv_bfloat16* base, int r, int q, in
     return reinterpret_cast<uint4*>(base + tile_off(r, 8 * q, kc));
 }
 
-constexpr int PT_TMEM = 128;  // Z1 at columns 0..63, Z2 at 64..127
+constexpr int PT_TMEM = 64;   // Z1, then Z2 over it (Z1 is read out before the second MMA)
+constexpr int PT_CTAS = 6;    // resident per SM (shared memory ~38 KB, 64 TMEM columns each)
 struct PairSmem {
     __nv_bfloat16 w[I_W3];         // W1 and W2 images (learned.cu's layout)
     __nv_bfloat16 x0[TILE * KIN];
@@ -110,7 +111,7 @@ struct PairSmem {
 
 // Velocity correction of every (leaf, far node) pair, pv[p] = network output times the
 // output scale times the pair's back factor.  Persistent over tiles of 128 pairs.
-__global__ void __launch_bounds__(TILE) k_mlp_far_pairs(int64_t np, const int32_t* __restrict__ pnode,
+__global__ void __launch_bounds__(TILE, PT_CTAS) k_mlp_far_pairs(int64_t np, const int32_t* __restrict__ pnode,
                                                        const int32_t* __restrict__ pleaf,
                                                        const double4* __restrict__ lgeom,
                                                        const __nv_bfloat16* __restrict__ nrow,
@@ -156,12 +157,16 @@ __global__ void __launch_bounds__(TILE) k_mlp_far_pairs(int64_t np, const int32_
             c2 = fr[2];
             const double4 ng = ngeo[N];
             const double4 lg = lgeom[pleaf[p]];
-            const double dx = lg.x - ng.x, dy = lg.y - ng.y;
-            const float o0 = ((float)(dx * ng.z) - S.inorm[0]) * S.inorm[2];
-            const float o1 = ((float)(dy * ng.z) - S.inorm[1]) * S.inorm[3];
+            // the offset exactly in FP64, the rest in FP32 (sm_103's FP64 pipe is narrow; the
+            // inputs are rounded to BF16 anyway)
+            const float dx = (float)(lg.x - ng.x), dy = (float)(lg.y - ng.y);
+            const float is = (float)ng.z;
+            const float o0 = (dx * is - S.inorm[0]) * S.inorm[2];
+            const float o1 = (dy * is - S.inorm[1]) * S.inorm[3];
             c2.y = pack_bf16(o0, o1);  // inputs 18, 19 follow the 18 cell inputs
-            const double d2 = dx * dx + dy * dy;
-            back = (ng.w > 0. && d2 > 0.) ? (float)(ng.w / (d2 * sqrt(d2))) : 0.f;
+            const float d2 = dx * dx + dy * dy;
+            const float r = rsqrtf(d2);
+            back = (ng.w > 0. && d2 > 0.f) ? (float)ng.w * (r * r * r) : 0.f;
         }
         *chunk_at(S.x0, tid, 0, KIN / 8) = c0;
         *chunk_at(S.x0, tid, 1, KIN / 8) = c1;
@@ -191,7 +196,7 @@ __global__ void __launch_bounds__(TILE) k_mlp_far_pairs(int64_t np, const int32_
         fence_before();
         __syncthreads();
         fence_after();
-        if (tid == 0) { mma_issue(tm + 64, S.h1, S.w + I_W2, HID, HID, false); mma_commit(&S.mbar); }
+        if (tid == 0) { mma_issue(tm, S.h1, S.w + I_W2, HID, HID, false); mma_commit(&S.mbar); }
         ok = __syncthreads_and(mbar_wait(&S.mbar, phase, spins));
         if (!ok) lost = phase;
         phase ^= 1;
@@ -200,7 +205,7 @@ __global__ void __launch_bounds__(TILE) k_mlp_far_pairs(int64_t np, const int32_
         float y0 = 0.f, y1 = 0.f;
         for (int c = 0; c < HID; c += 16) {
             float v[16];
-            tmem_ld16(tmem_lane_addr(tm, w, 64 + c), v);
+            tmem_ld16(tmem_lane_addr(tm, w, c), v);
 #pragma unroll
             for (int j = 0; j < 16; j++) {
                 const float h = __bfloat162float(__float2bfloat16(gelu_fast(v[j] + S.b2[c + j])));
@@ -306,7 +311,9 @@ void convective_learned(Ctx& c, vvgpu_mlp& M, const vvgpu_judge_cfg* jc, vvgpu_j
             VV_CUDA(cudaFuncSetAttribute(k_mlp_far_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)pair_smem()));
             const int64_t ntiles = (np + TILE - 1) / TILE;
-            const int grid = (int)std::min<int64_t>(ntiles, 152 * 4);
+            int dev_sms = 0;
+            VV_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c.device));
+            const int grid = (int)std::min<int64_t>(ntiles, (int64_t)dev_sms * PT_CTAS);
             k_mlp_far_pairs<<<grid, TILE, pair_smem(), s>>>(np, c.lf_far_node.p, c.lf_far_leaf.p, c.lf_geom.p,
                                                             nrow, c.ln_geo.p, M.img.p, M.params.p, M.norm.p,
                                                             c.ln_pv.p, M.err.p, M.wait_spins);
