@@ -975,19 +975,19 @@ def learned_arm(args):
         e1.record()
         torch.cuda.synchronize()
         kt = {k: round(v[0] / steps, 4) for k, v in S.kernel_timing().items() if v[1]}
-        launches = S.stats()["launches"]
+        st = S.stats()
         S.close()
-        return e0.elapsed_time(e1) / steps, kt, launches
+        return e0.elapsed_time(e1) / steps, kt, st
 
     clk = Clocks(0)
-    ms_l, kt_l, _ = timed(VVGPU_FP32, FC08, True, args.steps)
+    ms_l, kt_l, st_l = timed(VVGPU_FP32, FC08, True, args.steps)
     clocks = clk.stop()
     judge = {"steps": len(verdicts), "reverted": int(sum(v["reverted"] for v in verdicts)),
              "gap_rms_max": max(v["gap_rms"] for v in verdicts), "pairs_per_step": verdicts[-1]["pairs"],
              "judged_per_step": verdicts[-1]["judged"], "bound": args.judge_bound}
-    ms_05, kt_05, _ = timed(VVGPU_FP32, FC05, False, args.steps)
+    ms_05, kt_05, st_05 = timed(VVGPU_FP32, FC05, False, args.steps)
     ms_08, _, _ = timed(VVGPU_FP32, FC08, False, args.steps)
-    ms_64, _, _ = timed(VVGPU_FP64, FC05, False, args.fp64_steps)
+    ms_64 = timed(VVGPU_FP64, FC05, False, args.fp64_steps)[0] if args.fp64_steps > 0 else float("nan")
 
     # convective error against the FP64 direct sum, every variant on one shared state (the
     # list after the shed and the epsilon/merge pass of a plain theta 0.5 step)
@@ -1047,6 +1047,9 @@ def learned_arm(args):
         "step_ms": {"learned_fp32_theta_0.8": ms_l, "plain_fp32_theta_0.5": ms_05, "plain_fp32_theta_0.8": ms_08,
                     "plain_fp64_theta_0.5": ms_64},
         "kernel_ms_per_step": {"learned_fp32_theta_0.8": kt_l, "plain_fp32_theta_0.5": kt_05},
+        "tree": {name: {k: st[k] for k in ("n_leaves", "near_pairs", "far_pairs", "merge_rounds", "merged",
+                                             "eps_evaluations", "eps_records", "walk_loads")}
+                 for name, st in (("learned_fp32_theta_0.8", st_l), ("plain_fp32_theta_0.5", st_05))},
         "judge": judge,
         "convective_error_vs_fp64_direct": acc,
         "far_criteria_sweep_plain_fp32": sweep,

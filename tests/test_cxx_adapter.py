@@ -19,3 +19,13 @@ def test_dropin_compiles_against_reference_headers():
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-I", REF_HEADERS,
                         "-I", os.path.join(ROOT, "include"), src], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no C++ compiler")
+def test_dropin_step_driver_compiles():
+    """tests/cxx/dropin_step.cpp (run on the GPU by test_gpu_dropin.py) against the project's
+    minimal host Space."""
+    src = os.path.join(ROOT, "tests", "cxx", "dropin_step.cpp")
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-I", os.path.join(ROOT, "include"),
+                        "-I", os.path.join(ROOT, "tests", "cxx"), src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]

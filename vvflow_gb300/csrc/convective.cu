@@ -599,6 +599,17 @@ __global__ void k_judge_sum(int64_t nt, const int32_t* __restrict__ idx, const i
     }
 }
 
+// Free-stream, sink and slip-segment terms added to the judge's vortex part (lists.cu).
+__global__ void k_judge_finish(int64_t nt, const int32_t* __restrict__ idx, ConvArgs a, double* out) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nt || out[3 * q + 2] != 1.) return;
+    const int32_t i = idx[q];
+    double ex, ey;
+    extra_terms(a, a.x[i], a.y[i], ex, ey);
+    out[3 * q] += ex + a.inf_vx;
+    out[3 * q + 1] += ey + a.inf_vy;
+}
+
 __global__ void k_pair_counts(int64_t nt, const int32_t* __restrict__ cnt, int32_t* tot) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q < nt) tot[q] = cnt[2 * q] + cnt[2 * q + 1];
@@ -740,7 +751,41 @@ void direct_velocity(Ctx& c, int64_t np, const double* px, const double* py, dou
     VV_CUDA(cudaStreamSynchronize(s));
 }
 
+// The judged velocities: the warp walk, then the per-thread FP64 walk for the few targets
+// whose level walk did not fit its buffers.
 void judge_velocity(Ctx& c, int64_t nt, const int32_t* d_idx, double fc, double* d_out) {
+    if (nt <= 0) return;
+    cudaStream_t s = c.st();
+    judge_walk(c, nt, d_idx, fc, d_out);
+    ConvArgs a = make_args(c);
+    k_judge_finish<<<grid_for(nt, 128), 128, 0, s>>>(nt, d_idx, a, d_out);
+    VV_LAUNCH_CHECK();
+    std::vector<double> h(3 * (size_t)nt);
+    VV_CUDA(cudaMemcpyAsync(h.data(), d_out, 3 * nt * 8, cudaMemcpyDeviceToHost, s));
+    std::vector<int32_t> hidx(nt);
+    VV_CUDA(cudaMemcpyAsync(hidx.data(), d_idx, nt * 4, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    std::vector<int32_t> rest;
+    std::vector<int64_t> where;
+    for (int64_t q = 0; q < nt; q++)
+        if (h[3 * q + 2] < 0.) { rest.push_back(hidx[q]); where.push_back(q); }
+    if (rest.empty()) return;
+    DArr<int32_t> ridx;
+    DArr<double> rout;
+    ridx.reserve(rest.size());
+    rout.reserve(3 * rest.size());
+    VV_CUDA(cudaMemcpyAsync(ridx.p, rest.data(), rest.size() * 4, cudaMemcpyHostToDevice, s));
+    judge_velocity_exact(c, (int64_t)rest.size(), ridx.p, fc, rout.p);
+    std::vector<double> hr(3 * rest.size());
+    VV_CUDA(cudaMemcpyAsync(hr.data(), rout.p, hr.size() * 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+    for (size_t k = 0; k < rest.size(); k++)
+        VV_CUDA(cudaMemcpyAsync(d_out + 3 * where[k], &hr[3 * k], 24, cudaMemcpyHostToDevice, s));
+    VV_CUDA(cudaStreamSynchronize(s));
+}
+
+// Per-thread FP64 walks (k_judge_walk) and warp sums (k_judge_sum) at the vortices d_idx.
+void judge_velocity_exact(Ctx& c, int64_t nt, const int32_t* d_idx, double fc, double* d_out) {
     if (nt <= 0) return;
     cudaStream_t s = c.st();
     ConvArgs a = make_args(c);

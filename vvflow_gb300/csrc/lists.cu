@@ -292,6 +292,114 @@ __global__ void __launch_bounds__(BW * 32) k_walk_bfs(int64_t nsel, const int32_
     }
 }
 
+// The judge of the learned far field (learned_step.cu): the vortex part of velocity(p) at
+// vortex idx[q] with the near/far split of the judge's far criterion (v.fc).  One warp per
+// target walks the tree level by level as k_walk_bfs does (same far decisions), adding the
+// far nodes' monopoles as it goes, then the lanes split the near leaves' vortices.  Pair
+// terms in FP32 from FP64 offsets, compensated sums, partials by a fixed shuffle tree.
+// out[3 q ..] = (vx, vy, 1) without the free-stream, sink and slip terms; (0, 0, 0) for a
+// vortex with g = 0; out[3 q + 2] = -1 when the walk did not fit the shared buffers.
+__global__ void __launch_bounds__(BW * 32) k_judge_bfs(int64_t nt, const int32_t* __restrict__ idx, ListView v,
+                                                       const double* __restrict__ x, const double* __restrict__ y,
+                                                       const double* __restrict__ g, const double* __restrict__ ie,
+                                                       const int32_t* __restrict__ nvf, const int32_t* __restrict__ nvl,
+                                                       double* out) {
+    __shared__ int32_t s_f[BW][2][FCAP];
+    __shared__ int32_t s_near[BW][FCAP];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t q = (int64_t)blockIdx.x * BW + w;
+    if (q >= nt) return;
+    const int32_t i = idx[q];
+    if (g[i] == 0.) {
+        if (lane == 0) { out[3 * q] = 0.; out[3 * q + 1] = 0.; out[3 * q + 2] = 0.; }
+        return;
+    }
+    const double px = x[i], py = y[i];
+    int32_t meN = 0;
+    for (int it = 0; it <= MAX_DEPTH && v.ch1[meN] >= 0; it++) {
+        const double4 gm = v.geom[meN];
+        if (gm.z < gm.w) meN = (px < gm.x) ? v.ch1[meN] : v.ch1[meN] + 1;
+        else meN = (py < gm.y) ? v.ch1[meN] : v.ch1[meN] + 1;
+    }
+    const float4 mg = v.nf_geo[meN];
+    const float2 mk = v.nf_k[meN];
+    const unsigned lt = (1u << lane) - 1;
+    float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
+    auto pair = [&](double sx, double sy, float gs, float e2) {
+        const float dx = (float)(px - sx), dy = (float)(py - sy);
+        const float s = gs * rcp_approx(fmaf(dx, dx, fmaf(dy, dy, e2)));
+        two_sum_acc(hx, lx, -dy * s);
+        two_sum_acc(hy, ly, dx * s);
+    };
+    int cur = 0, ncur = 1, nnear = 0;
+    bool ovf = false;
+    if (lane == 0) s_f[w][0][0] = 0;
+    __syncwarp();
+    for (int depth = 0; ncur > 0; depth++) {
+        if (depth > MAX_DEPTH + 1) { ovf = true; break; }
+        int nnext = 0;
+        for (int base = 0; base < ncur; base += 32) {
+            const int k = base + lane;
+            int32_t t = -1, c1 = -1;
+            bool far = false, inner = false, leaf = false;
+            if (k < ncur) {
+                t = s_f[w][cur][k];
+                far = far_test(v, t, meN, mg, mk);
+                if (far) {  // far_nodes_influence (MConvectiveFast.cpp:139-151)
+                    const double* c = v.cm + 6 * (size_t)t;
+                    if (c[2] != 0.) pair(c[0], c[1], (float)c[2], 0.f);
+                    if (c[5] != 0.) pair(c[3], c[4], (float)c[5], 0.f);
+                } else {
+                    c1 = v.ch1[t];
+                    inner = c1 >= 0;
+                    leaf = !inner;
+                }
+            }
+            unsigned m = __ballot_sync(0xffffffffu, inner);
+            if (inner) {
+                const int pos = nnext + 2 * __popc(m & lt);
+                if (pos + 1 < FCAP) { s_f[w][cur ^ 1][pos] = c1; s_f[w][cur ^ 1][pos + 1] = c1 + 1; }
+            }
+            nnext += 2 * __popc(m);
+            m = __ballot_sync(0xffffffffu, leaf);
+            if (leaf) {
+                const int pos = nnear + __popc(m & lt);
+                if (pos < FCAP) s_near[w][pos] = t;
+            }
+            nnear += __popc(m);
+        }
+        if (nnext > FCAP || nnear > FCAP) { ovf = true; break; }
+        __syncwarp();
+        cur ^= 1;
+        ncur = nnext;
+    }
+    if (ovf) {
+        if (lane == 0) out[3 * q + 2] = -1.;
+        return;
+    }
+    __syncwarp();
+    for (int e = lane; e < nnear; e += 32) {  // near_nodes_influence (MConvectiveFast.cpp:122-137)
+        const int32_t t = s_near[w][e];
+        for (int32_t j = nvf[t]; j < nvl[t]; j++) {
+            const double gj = g[j];
+            if (gj == 0.) continue;
+            const float ep = rcp_approx((float)ie[j]);  // 1/_1_eps; _1_eps = 0 gives inf, s = 0
+            pair(x[j], y[j], (float)gj, ep * ep);
+        }
+    }
+    double sx = (double)hx + (double)lx, sy = (double)hy + (double)ly;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    }
+    if (lane == 0) {
+        out[3 * q] = sx * C_1_2PI;
+        out[3 * q + 1] = sy * C_1_2PI;
+        out[3 * q + 2] = 1.;
+    }
+}
+
 // Indices of the flagged leaves, in order.
 __global__ void k_list_flags(int64_t nl, const int32_t* __restrict__ flag, const int32_t* __restrict__ pos,
                              int32_t* list) {
@@ -719,6 +827,16 @@ void ensure_full_lists(Ctx& c) {
         if (ft > 0x7fffffffull) throw ApiError{VVGPU_ERR_LIMIT, "more than 2^31 far pairs to keep"};
         keep_far_lists(c);
     }
+}
+
+void judge_walk(Ctx& c, int64_t nt, const int32_t* d_idx, double fc, double* d_out) {
+    if (nt <= 0) return;
+    ListView v = list_view(c);
+    v.fc = fc;
+    v.fcf = (float)fc;
+    k_judge_bfs<<<grid_for(nt, BW), BW * 32, 0, c.st()>>>(nt, d_idx, v, c.x.p, c.y.p, c.g.p, c.ie.p, c.nd_vf.p,
+                                                            c.nd_vl.p, d_out);
+    VV_LAUNCH_CHECK();
 }
 
 void tree_lists_exact(Ctx& c, std::vector<int32_t>& far_off, std::vector<int32_t>& far_node, bool fill) {

@@ -452,6 +452,11 @@ void direct_velocity(Ctx& c, int64_t n, const double* px, const double* py, doub
 // velocity(p) at the vortices d_idx[0 .. nt) with the near/far split of far criterion fc on
 // the built tree (the learned far field's judge); d_out: (vx, vy, valid) per target.
 void judge_velocity(Ctx& c, int64_t nt, const int32_t* d_idx, double fc, double* d_out);
+// Its vortex part by a warp-per-target level walk (lists.cu); out[3 q + 2] = -1 where the walk
+// did not fit its buffers.
+void judge_walk(Ctx& c, int64_t nt, const int32_t* d_idx, double fc, double* d_out);
+// The same by one FP64 walk per target (any size).
+void judge_velocity_exact(Ctx& c, int64_t nt, const int32_t* d_idx, double fc, double* d_out);
 // TVec3D::iszero of every body's speed_slae (TVec3D.hpp:17), else VVGPU_ERR_UNSUPPORTED.
 void check_bodies_at_rest(Ctx& c);
 // grid fields (fields.cu)
