@@ -39,7 +39,6 @@ constexpr int EB = 128;
 constexpr int32_t SKIPPED = -2;  // partner code: vortex not evaluated (g = 0 at its turn)
 constexpr int CAND_CAP = 96;     // candidate leaves kept per target leaf
 constexpr int CHG_CAP = 48;      // changed near leaves kept per target leaf
-constexpr int EPS_NS = 4;        // lanes per target in the two-nearest searches
 
 // MEpsilonFast::nearestBodySegment (MEpsilonFast.cpp:214-253) and the per-leaf merge
 // criterion / epsilon floor (MEpsilonFast.cpp:25-47).
@@ -460,12 +459,10 @@ struct NearBuf {
 };
 
 // Visits leaf q's live candidates for target i (shared by both passes).
-// tsh: an upper bound on the final second distance known from elsewhere (the other lanes of
-// the target's group; INFINITY for a lone lane); the threshold follows min(t2, tsh).
 template <int PASS, bool FIRST>
 __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, float2 aL, int32_t i, int32_t excl, float tx,
                                           float ty, double px, double py, float D, float& t1, float& t2,
-                                          float& thr, Top2& best, NearBuf& buf, float tsh = INFINITY) {
+                                          float& thr, Top2& best, NearBuf& buf) {
     float2 sh = frame_shift(v.anchor[q], aL, v.Gf);
     if (box_lb(v.box[q], sh, tx, ty) > thr) return;
     if (PASS == 0) buf.nrec += (uint32_t)(v.lvl[q] - v.lvf[q]);
@@ -475,8 +472,8 @@ __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, float2 aL
         float dx = tx - (c.rec.x + sh.x), dy = ty - (c.rec.y + sh.y);
         float d = dx * dx + dy * dy;
         if (PASS == 0) {
-            if (d < t1) { t2 = t1; t1 = d; thr = thr_of(fminf(t2, tsh), D); }
-            else if (d < t2) { t2 = d; thr = thr_of(fminf(t2, tsh), D); }
+            if (d < t1) { t2 = t1; t1 = d; thr = thr_of(t2, D); }
+            else if (d < t2) { t2 = d; thr = thr_of(t2, D); }
             if (d <= thr) buf.push(d, j, thr);
         } else if (d <= thr) {
             double xj, yj, gj;
@@ -536,102 +533,6 @@ __device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl
                 }
             }
         }
-    }
-    best.thr = thr;
-    best.nrec = buf.nrec;
-    return best;
-}
-
-// (d, slot) order of the reference's top-2 (top2_push): distance, then list position
-__device__ __forceinline__ bool lex_lt(double a, int32_t ia, double b, int32_t ib) {
-    return a < b || (a == b && ia < ib);
-}
-
-// two_nearest by a group of NS consecutive lanes of a warp (all of them with the same
-// target): lane `sub` of the group scans every NS-th leaf of the search (the target's own
-// leaf first, then the candidate or near leaves in list order), the lanes share the
-// smallest second distance after every NS leaves to prune with, then merge their FP32
-// second distances for the final margin, evaluate their own buffered candidates inside it
-// exactly, and merge their exact top-2 in the reference's (distance, position) order.
-// Every leaf is scanned by exactly one lane, so the merged top-2 is the one lane's top-2
-// over all candidates: the result equals two_nearest's.  Group-uniform control flow.
-template <bool FIRST, int NS>
-__device__ Top2 two_nearest_g(const EpsView& v, int32_t L, int32_t i, int32_t excl, double px, double py,
-                              bool use_list, unsigned gmask, int sub) {
-    const float2 aL = v.anchor[L];
-    const float tx = (float)(px - (double)aL.x), ty = (float)(py - (double)aL.y);
-    const float ext = (use_list ? v.rn[L] : v.rnear[L]) + *v.dmax;
-    const float D = ldexpf(ext + fabsf(tx) + fabsf(ty) + v.Gf, -17);
-    float t1 = INFINITY, t2 = INFINITY, thr = INFINITY, tsh = INFINITY;
-    Top2 best{DBL_MAX, DBL_MAX, INT_MAX, INT_MAX, INFINITY, 0};
-    const int32_t nc = use_list ? v.ncand[L] : -1;
-    NearBuf buf;
-    // visits every leaf of the search in order (the same sequence in every lane of the group)
-    auto each_leaf = [&](auto&& f) {
-        f(L);
-        if (nc >= 0) {
-            const int32_t* cl = v.cand + (size_t)L * CAND_CAP;
-            for (int32_t k = 0; k < nc; k++) {
-                const int32_t q = cl[k];
-                if (q != L) f(q);
-            }
-        } else {
-            for (int32_t r = v.near_off[L]; r < v.near_off[L + 1]; r++) {
-                const int2 run = v.near_run[r];
-                for (int32_t q = run.x; q < run.y; q++)
-                    if (q != L) f(q);
-            }
-        }
-    };
-    int k = 0;
-    each_leaf([&](int32_t q) {
-        if (k % NS == sub) scan_leaf<0, FIRST>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf, tsh);
-        if (++k % NS == 0) {
-            float m = t2;
-#pragma unroll
-            for (int o = 1; o < NS; o <<= 1) m = fminf(m, __shfl_xor_sync(gmask, m, o, NS));
-            tsh = m;
-            thr = thr_of(fminf(t2, tsh), D);
-        }
-    });
-    // the group's two smallest FP32 distances
-#pragma unroll
-    for (int o = 1; o < NS; o <<= 1) {
-        const float b1 = __shfl_xor_sync(gmask, t1, o, NS), b2 = __shfl_xor_sync(gmask, t2, o, NS);
-        const float m2 = fminf(fmaxf(t1, b1), fminf(t2, b2));
-        t1 = fminf(t1, b1);
-        t2 = m2;
-    }
-    thr = thr_of(t2, D);
-    if (!buf.ovf) {
-        for (int b = 0; b < buf.n; b++) {
-            if (!(buf.d[b] <= thr)) continue;
-            double xj, yj, gj;
-            cand_exact<FIRST>(v, buf.j[b], i, xj, yj, gj);
-            top2_push(best, dabs2(dsub(px, xj), dsub(py, yj)), buf.j[b]);
-        }
-    } else {
-        k = 0;
-        each_leaf([&](int32_t q) {
-            if (k % NS == sub) scan_leaf<1, FIRST>(v, q, aL, i, excl, tx, ty, px, py, D, t1, t2, thr, best, buf);
-            k++;
-        });
-    }
-    // the group's exact top-2
-#pragma unroll
-    for (int o = 1; o < NS; o <<= 1) {
-        const double o1 = __shfl_xor_sync(gmask, best.r1, o, NS), o2 = __shfl_xor_sync(gmask, best.r2, o, NS);
-        const int32_t p1 = __shfl_xor_sync(gmask, best.l1, o, NS), p2 = __shfl_xor_sync(gmask, best.l2, o, NS);
-        double n1, n2, c1, c2;
-        int32_t m1, m2, q1, q2;
-        if (lex_lt(best.r1, best.l1, o1, p1)) { n1 = best.r1; m1 = best.l1; c1 = o1; q1 = p1; }
-        else { n1 = o1; m1 = p1; c1 = best.r1; q1 = best.l1; }
-        // second: the smaller of the other first and the smaller of the two seconds
-        if (lex_lt(best.r2, best.l2, o2, p2)) { c2 = best.r2; q2 = best.l2; }
-        else { c2 = o2; q2 = p2; }
-        if (lex_lt(c2, q2, c1, q1)) { n2 = c2; m2 = q2; }
-        else { n2 = c1; m2 = q1; }
-        best.r1 = n1; best.l1 = m1; best.r2 = n2; best.l2 = m2;
     }
     best.thr = thr;
     best.nrec = buf.nrec;
@@ -710,9 +611,8 @@ __global__ void k_eps_compact(int64_t n, const int32_t* __restrict__ flag, const
     if (i < n && flag[i]) list[pos[i]] = (int32_t)i;
 }
 
-// Evaluates every target (FIRST: the first round) or the targets list[0 .. *count), one
-// target per group of NS consecutive lanes (two_nearest_g); the group's lane 0 writes.
-template <bool FIRST, int NS>
+// Evaluates every target (FIRST: the first round) or the targets list[0 .. *count).
+template <bool FIRST>
 __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* __restrict__ list,
                             const int32_t* __restrict__ count, const int32_t* __restrict__ leaf_of,
                             const double* __restrict__ mcs_l, const double* __restrict__ epr_l,
@@ -721,10 +621,8 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
                             int32_t* changed, unsigned long long* evals, unsigned long long* nrec_total) {
     const int64_t cnt = FIRST ? n : (int64_t)*count;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(evals, (unsigned long long)cnt);
-    const int lane = threadIdx.x & 31, sub = lane % NS;
-    const unsigned gmask = (NS == 32) ? 0xffffffffu : (((1u << NS) - 1u) << (lane - sub));
-    const int64_t k0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / NS;
-    const int64_t kstep = FIRST ? cnt : (int64_t)gridDim.x * blockDim.x / NS;  // FIRST: one target per group
+    const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t kstep = FIRST ? cnt : (int64_t)gridDim.x * blockDim.x;  // FIRST: one target per thread
     for (int64_t kk = k0; kk < cnt; kk += kstep) {
         const int32_t i = FIRST ? (int32_t)kk : list[kk];
         const int32_t L = leaf_of[i];
@@ -735,7 +633,7 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
         uint32_t nrec = 0;
         if (gi0 != 0 && !(v.zb[i] < i)) {
             const double mcs = mcs_l[L];
-            Top2 t = two_nearest_g<FIRST, NS>(v, L, i, -1, px, py, true, gmask, sub);
+            Top2 t = two_nearest<FIRST>(v, L, i, -1, px, py, true);
             sr1 = t.thr;
             nrec += t.nrec;
             double e;
@@ -761,7 +659,7 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
                     }
                     gi = dadd(gi, g1);
                     partner = t.l1;
-                    Top2 u = two_nearest_g<FIRST, NS>(v, L, i, t.l1, px, py, false, gmask, sub);
+                    Top2 u = two_nearest<FIRST>(v, L, i, t.l1, px, py, false);
                     sr2 = u.thr;
                     nrec += u.nrec;
                     if (u.l1 == INT_MAX) e = DBL_MIN;
@@ -778,12 +676,10 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
                   (__double_as_longlong(py) != __double_as_longlong(v.oy[i])) ||
                   (__double_as_longlong(gi) != __double_as_longlong(v.og[i])) ||
                   (__double_as_longlong(ie) != __double_as_longlong(oie_old[i]));
-        if (sub == 0) {
-            partner_new[i] = partner;
-            ox_new[i] = px; oy_new[i] = py; og_new[i] = gi; oie_new[i] = ie;
-            dv.sr1[i] = sr1;
-            dv.sr2[i] = sr2;
-        }
+        partner_new[i] = partner;
+        ox_new[i] = px; oy_new[i] = py; og_new[i] = gi; oie_new[i] = ie;
+        dv.sr1[i] = sr1;
+        dv.sr2[i] = sr2;
         const unsigned am = __activemask();  // one store per warp to the shared flag
         if (__any_sync(am, ch) && (threadIdx.x & 31) == __ffs(am) - 1) *changed = 1;
         const unsigned wrec = __reduce_add_sync(am, nrec);
@@ -975,12 +871,12 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
         {
             KernelTimer kt(c, VVGPU_T_EPS_ROUND);
             if (rounds == 1)
-                k_eps_round<true, EPS_NS><<<grid_for(n * EPS_NS, EB), EB, 0, s>>>(
+                k_eps_round<true><<<grid_for(n, EB), EB, 0, s>>>(
                     n, v, dv, nullptr, nullptr, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
                     c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
                     c.counters.p + 14, c.counters.p + 16);
             else
-                k_eps_round<false, EPS_NS><<<std::min<unsigned>(grid_for(n * EPS_NS, EB), 152u * 32u), EB, 0, s>>>(
+                k_eps_round<false><<<std::min<unsigned>(grid_for(n, EB), 152u * 32u), EB, 0, s>>>(
                     n, v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
                     c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
                     c.counters.p + 14, c.counters.p + 16);
