@@ -22,6 +22,7 @@
 // (convective.cu, k_judge), against the learned pass's convective increments there.  If the
 // relative rms gap exceeds the bound, the increments are undone and the pass is redone with
 // the plain tree at the judge's criterion (near/far walk again, plain expansion).
+#include "frame.cuh"
 #include "mlp.cuh"
 
 namespace vvgpu {
@@ -32,12 +33,13 @@ constexpr int NCF = 18;   // cell inputs; inputs 18, 19 are the target's offset
 constexpr int NROW = 24;  // BF16 per node row: 18 inputs, 6 zeros (48 bytes, 16-byte aligned)
 
 // Per node: the standardised cell inputs (the features of k_pair_samples, learned.cu) as
-// BF16, and (centre x, y, 1 / s, G s^2 / 2pi) for the per-pair offset inputs and the factor
-// back to velocity, back = G s^2 / (2 pi d^3).  A node with no circulation or no extent gets
-// back factor 0 (no correction), as its samples have.
+// BF16, and (1 / s, G s^2 / 2pi) for the per-pair offset inputs and the factor back to
+// velocity, back = G s^2 / (2 pi d^3) (the offset itself comes from the node frames of
+// frame.cuh).  A node with no circulation or no extent gets back factor 0 (no
+// correction), as its samples have.
 __global__ void k_node_inputs(int64_t nn, const double4* __restrict__ geom, const double* __restrict__ cm,
                               const double* __restrict__ mom, const float* __restrict__ norm, __nv_bfloat16* nrow,
-                              double4* ngeo) {
+                              float2* ngeo) {
     const int64_t S = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (S >= nn) return;
     const double4 gm = geom[S];
@@ -71,7 +73,7 @@ __global__ void k_node_inputs(int64_t nn, const double4* __restrict__ geom, cons
     __nv_bfloat16* r = nrow + NROW * S;
 #pragma unroll
     for (int k = 0; k < NROW; k++) r[k] = __float2bfloat16(k < NCF ? (f[k] - norm[k]) * norm[NF + k] : 0.f);
-    ngeo[S] = make_double4(gm.x, gm.y, is, back0);
+    ngeo[S] = make_float2((float)is, (float)back0);
 }
 
 __device__ __forceinline__ float tanh_fast(float x) {
@@ -98,10 +100,11 @@ __device__ __forceinline__ uint4* chunk_at(__nv_bfloat16* base, int r, int q, in
 }
 
 constexpr int PT_TMEM = 64;   // Z1, then Z2 over it (Z1 is read out before the second MMA)
-constexpr int PT_CTAS = 6;    // resident per SM (shared memory ~38 KB, 64 TMEM columns each)
+constexpr int PT_CTAS = 7;    // resident per SM (shared memory ~30 KB, 64 TMEM columns each)
 struct PairSmem {
     __nv_bfloat16 w[I_W3];         // W1 and W2 images (learned.cu's layout)
-    __nv_bfloat16 x0[TILE * KIN];
+    // the tile's inputs, then its first hidden layer: the inputs are read by the first MMA,
+    // which has completed before the hidden layer is written
     __nv_bfloat16 h1[TILE * HID];
     float b1[HID], b2[HID], w3[NOUT][HID];
     float b3[NOUT], onorm[NOUT], inorm[4];
@@ -113,15 +116,18 @@ struct PairSmem {
 // output scale times the pair's back factor.  Persistent over tiles of 128 pairs.
 __global__ void __launch_bounds__(TILE, PT_CTAS) k_mlp_far_pairs(int64_t np, const int32_t* __restrict__ pnode,
                                                        const int32_t* __restrict__ pleaf,
-                                                       const double4* __restrict__ lgeom,
+                                                       const int32_t* __restrict__ leaf_node,
+                                                       const float4* __restrict__ nf_geo,
+                                                       const float2* __restrict__ nf_k,
                                                        const __nv_bfloat16* __restrict__ nrow,
-                                                       const double4* __restrict__ ngeo,
+                                                       const float2* __restrict__ ngeo,
                                                        const __nv_bfloat16* __restrict__ img,
                                                        const float* __restrict__ params,
                                                        const float* __restrict__ norm, float2* __restrict__ pv,
                                                        int* err, uint32_t spins) {
-    extern __shared__ __align__(1024) unsigned char smraw[];
+    extern __shared__ __align__(128) unsigned char smraw[];
     PairSmem& S = *reinterpret_cast<PairSmem*>(smraw);
+    __nv_bfloat16* const x0 = S.h1;  // [TILE][KIN] at the start of h1's space
     const int tid = threadIdx.x, w = tid >> 5;
     for (int i = tid; i < I_W3; i += TILE) S.w[i] = img[i];
     for (int i = tid; i < HID; i += TILE) {
@@ -155,28 +161,29 @@ __global__ void __launch_bounds__(TILE, PT_CTAS) k_mlp_far_pairs(int64_t np, con
             c0 = fr[0];
             c1 = fr[1];
             c2 = fr[2];
-            const double4 ng = ngeo[N];
-            const double4 lg = lgeom[pleaf[p]];
-            // the offset exactly in FP64, the rest in FP32 (sm_103's FP64 pipe is narrow; the
-            // inputs are rounded to BF16 anyway)
-            const float dx = (float)(lg.x - ng.x), dy = (float)(lg.y - ng.y);
-            const float is = (float)ng.z;
-            const float o0 = (dx * is - S.inorm[0]) * S.inorm[2];
-            const float o1 = (dy * is - S.inorm[1]) * S.inorm[3];
+            const float2 ng = ngeo[N];
+            // the leaf centre's offset from the node centre in FP32 from the node frames (the
+            // shift between two anchors is exact); the inputs are rounded to BF16 anyway
+            const int32_t meL = leaf_node[pleaf[p]];
+            const float2 sh = frame_shift(nf_k[meL], nf_k[N], 0.f);
+            const float4 gL = nf_geo[meL], gN = nf_geo[N];
+            const float dx = sh.x + (gL.x - gN.x), dy = sh.y + (gL.y - gN.y);
+            const float o0 = (dx * ng.x - S.inorm[0]) * S.inorm[2];
+            const float o1 = (dy * ng.x - S.inorm[1]) * S.inorm[3];
             c2.y = pack_bf16(o0, o1);  // inputs 18, 19 follow the 18 cell inputs
             const float d2 = dx * dx + dy * dy;
             const float r = rsqrtf(d2);
-            back = (ng.w > 0. && d2 > 0.f) ? (float)ng.w * (r * r * r) : 0.f;
+            back = (ng.y > 0.f && d2 > 0.f) ? ng.y * (r * r * r) : 0.f;
         }
-        *chunk_at(S.x0, tid, 0, KIN / 8) = c0;
-        *chunk_at(S.x0, tid, 1, KIN / 8) = c1;
-        *chunk_at(S.x0, tid, 2, KIN / 8) = c2;
-        *chunk_at(S.x0, tid, 3, KIN / 8) = make_uint4(0, 0, 0, 0);
+        *chunk_at(x0, tid, 0, KIN / 8) = c0;
+        *chunk_at(x0, tid, 1, KIN / 8) = c1;
+        *chunk_at(x0, tid, 2, KIN / 8) = c2;
+        *chunk_at(x0, tid, 3, KIN / 8) = make_uint4(0, 0, 0, 0);
         fence_smem_to_mma();
         fence_before();
         __syncthreads();
         fence_after();
-        if (tid == 0) { mma_issue(tm, S.x0, S.w + I_W1, KIN, HID, false); mma_commit(&S.mbar); }
+        if (tid == 0) { mma_issue(tm, x0, S.w + I_W1, KIN, HID, false); mma_commit(&S.mbar); }
         ok = __syncthreads_and(mbar_wait(&S.mbar, phase, spins));
         if (!ok) lost = phase;
         phase ^= 1;
@@ -268,7 +275,7 @@ uint64_t mix64(uint64_t z) {
     return z ^ (z >> 31);
 }
 
-size_t pair_smem() { return sizeof(PairSmem) + 1024; }
+size_t pair_smem() { return sizeof(PairSmem); }
 
 }  // namespace mlp
 
@@ -298,6 +305,7 @@ void convective_learned(Ctx& c, vvgpu_mlp& M, const vvgpu_judge_cfg* jc, vvgpu_j
     VV_CUDA(cudaStreamSynchronize(M.stream));
     c.ln_row.reserve((size_t)NROW * nn + 8);
     c.ln_geo.reserve(nn + 1);
+    if (!c.nf_geo.p || !c.nf_k.p) throw ApiError{VVGPU_ERR_STATE, "node frames missing"};
     __nv_bfloat16* nrow = reinterpret_cast<__nv_bfloat16*>(c.ln_row.p);
     k_node_inputs<<<grid_for(nn, 128), 128, 0, s>>>(nn, c.nd_geom.p, c.nd_cm.p, c.nd_mom.p, M.norm.p, nrow,
                                                     c.ln_geo.p);
@@ -311,11 +319,15 @@ void convective_learned(Ctx& c, vvgpu_mlp& M, const vvgpu_judge_cfg* jc, vvgpu_j
             VV_CUDA(cudaFuncSetAttribute(k_mlp_far_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)pair_smem()));
             const int64_t ntiles = (np + TILE - 1) / TILE;
-            int dev_sms = 0;
+            // persistent: exactly the CTAs that fit at once
+            int dev_sms = 0, per_sm = 0;
             VV_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c.device));
-            const int grid = (int)std::min<int64_t>(ntiles, (int64_t)dev_sms * PT_CTAS);
-            k_mlp_far_pairs<<<grid, TILE, pair_smem(), s>>>(np, c.lf_far_node.p, c.lf_far_leaf.p, c.lf_geom.p,
-                                                            nrow, c.ln_geo.p, M.img.p, M.params.p, M.norm.p,
+            VV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_far_pairs, TILE, pair_smem()));
+            per_sm = std::max(1, std::min(per_sm, 512 / PT_TMEM));  // tensor-memory columns per SM
+            const int grid = (int)std::min<int64_t>(ntiles, (int64_t)dev_sms * per_sm);
+            k_mlp_far_pairs<<<grid, TILE, pair_smem(), s>>>(np, c.lf_far_node.p, c.lf_far_leaf.p, c.leaf_node.p,
+                                                            c.nf_geo.p, c.nf_k.p, nrow, c.ln_geo.p, M.img.p,
+                                                            M.params.p, M.norm.p,
                                                             c.ln_pv.p, M.err.p, M.wait_spins);
             VV_LAUNCH_CHECK();
         }

@@ -468,7 +468,13 @@ struct Taylor {
 
 constexpr int RUN_CAP = 64;   // near runs kept per leaf by the warp walk
 constexpr int FAR_CAP = 2048; // far nodes kept per leaf by the warp walk (when asked to keep them)
-constexpr int WW = 4;         // warps per block in the warp walk
+#ifndef VV_WALK_WARPS
+#define VV_WALK_WARPS 4
+#endif
+#ifndef VV_WALK_MIN_BLOCKS
+#define VV_WALK_MIN_BLOCKS 1
+#endif
+constexpr int WW = VV_WALK_WARPS;  // warps per block in the warp walk
 
 // One warp walks the tree for 32 consecutive leaves at once (they are neighbours in space,
 // so their walks share most nodes).  The stack holds (node, mask of lanes still walking
@@ -477,7 +483,7 @@ constexpr int WW = 4;         // warps per block in the warp walk
 // With far_buf set, each leaf's far nodes are also kept (walk order, at most far_cap of
 // them; the count in far_cnt may exceed far_cap, and the caller then rebuilds that list).
 template <bool FP32>
-__global__ void __launch_bounds__(WW * 32) k_walk_warp(int64_t nl, ListView v, const int32_t* __restrict__ leaf_node,
+__global__ void __launch_bounds__(WW * 32, VV_WALK_MIN_BLOCKS) k_walk_warp(int64_t nl, ListView v, const int32_t* __restrict__ leaf_node,
                                                        int32_t* near_cnt, int2* run_buf, double4* taylor,
                                                        unsigned long long* far_total, int64_t nodes_bound,
                                                        int32_t* err, int32_t* far_buf, int32_t far_cap,

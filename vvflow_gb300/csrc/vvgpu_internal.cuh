@@ -188,7 +188,8 @@ struct Ctx {
     // learned far field (learned_step.cu): per-node inputs (BF16 bits) and geometry, per-pair
     // corrections, corrected coefficients, the judge's samples and results
     DArr<uint16_t> ln_row;
-    DArr<double4> ln_geo, lf_taylor_l;
+    DArr<float2> ln_geo;
+    DArr<double4> lf_taylor_l;
     DArr<float2> ln_pv;
     DArr<double> ln_v0, ln_judge;
     DArr<int32_t> ln_idx;
