@@ -30,16 +30,21 @@ namespace vvgpu {
 namespace mlp {
 
 constexpr int NCF = 18;   // cell inputs; inputs 18, 19 are the target's offset
-constexpr int NROW = 24;  // BF16 per node row: 18 inputs, 6 zeros (48 bytes, 16-byte aligned)
 
-// Per node: the standardised cell inputs (the features of k_pair_samples, learned.cu) as
-// BF16, and (1 / s, G s^2 / 2pi) for the per-pair offset inputs and the factor back to
-// velocity, back = G s^2 / (2 pi d^3) (the offset itself comes from the node frames of
-// frame.cuh).  A node with no circulation or no extent gets back factor 0 (no
-// correction), as its samples have.
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// Per node, one 64-byte record (4 x uint4) with everything a pair reads about the node:
+//   q0, q1: standardised cell inputs 0..15 (the features of k_pair_samples, learned.cu), BF16
+//   q2: inputs 16, 17 (BF16 pair), 1 / s, G s^2 / 2pi (FP32 bits), 0
+//   q3: node centre x, y in its anchor frame and the anchor (FP32, frame.cuh)
+// The factor back to velocity is back = G s^2 / (2 pi d^3).  A node with no circulation or
+// no extent gets 0 there (no correction), as its samples have.
 __global__ void k_node_inputs(int64_t nn, const double4* __restrict__ geom, const double* __restrict__ cm,
-                              const double* __restrict__ mom, const float* __restrict__ norm, __nv_bfloat16* nrow,
-                              float2* ngeo) {
+                              const double* __restrict__ mom, const float* __restrict__ norm,
+                              const float4* __restrict__ nf_geo, const float2* __restrict__ nf_k, uint4* nrec) {
     const int64_t S = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (S >= nn) return;
     const double4 gm = geom[S];
@@ -47,9 +52,9 @@ __global__ void k_node_inputs(int64_t nn, const double4* __restrict__ geom, cons
     const double* mo = mom + 12 * S;
     const double sz = gm.z + gm.w;
     const double G = c[2] - c[5];
-    float f[NROW];
+    float f[NCF];
 #pragma unroll
-    for (int k = 0; k < NROW; k++) f[k] = 0.f;
+    for (int k = 0; k < NCF; k++) f[k] = 0.f;
     double is = 0., back0 = 0.;
     if (G > 0. && sz > 0.) {
         const double iG = 1. / G;
@@ -70,10 +75,17 @@ __global__ void k_node_inputs(int64_t nn, const double4* __restrict__ geom, cons
             }
         back0 = G * sz * sz * (0.5 / C_PI);
     }
-    __nv_bfloat16* r = nrow + NROW * S;
+    uint32_t b[9];
 #pragma unroll
-    for (int k = 0; k < NROW; k++) r[k] = __float2bfloat16(k < NCF ? (f[k] - norm[k]) * norm[NF + k] : 0.f);
-    ngeo[S] = make_float2((float)is, (float)back0);
+    for (int k = 0; k < 9; k++)
+        b[k] = pack_bf16((f[2 * k] - norm[2 * k]) * norm[NF + 2 * k], (f[2 * k + 1] - norm[2 * k + 1]) * norm[NF + 2 * k + 1]);
+    const float4 gq = nf_geo[S];
+    const float2 kq = nf_k[S];
+    uint4* r = nrec + 4 * S;
+    r[0] = make_uint4(b[0], b[1], b[2], b[3]);
+    r[1] = make_uint4(b[4], b[5], b[6], b[7]);
+    r[2] = make_uint4(b[8], __float_as_uint((float)is), __float_as_uint((float)back0), 0u);
+    r[3] = make_uint4(__float_as_uint(gq.x), __float_as_uint(gq.y), __float_as_uint(kq.x), __float_as_uint(kq.y));
 }
 
 __device__ __forceinline__ float tanh_fast(float x) {
@@ -87,11 +99,6 @@ __device__ __forceinline__ float gelu_fast(float z) {
     const float u = GC * fmaf(GA * z * z, z, z);
     const float hz = 0.5f * z;
     return fmaf(hz, tanh_fast(u), hz);
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-    return *reinterpret_cast<const uint32_t*>(&h);
 }
 
 // 16-byte chunk q (8 consecutive K elements) of row r of a K-major core-matrix operand
@@ -115,12 +122,8 @@ struct PairSmem {
 // Velocity correction of every (leaf, far node) pair, pv[p] = network output times the
 // output scale times the pair's back factor.  Persistent over tiles of 128 pairs.
 __global__ void __launch_bounds__(TILE, PT_CTAS) k_mlp_far_pairs(int64_t np, const int32_t* __restrict__ pnode,
-                                                       const int32_t* __restrict__ pleaf,
-                                                       const int32_t* __restrict__ leaf_node,
-                                                       const float4* __restrict__ nf_geo,
-                                                       const float2* __restrict__ nf_k,
-                                                       const __nv_bfloat16* __restrict__ nrow,
-                                                       const float2* __restrict__ ngeo,
+                                                       const int32_t* __restrict__ plnode,
+                                                       const uint4* __restrict__ nrec,
                                                        const __nv_bfloat16* __restrict__ img,
                                                        const float* __restrict__ params,
                                                        const float* __restrict__ norm, float2* __restrict__ pv,
@@ -156,24 +159,24 @@ __global__ void __launch_bounds__(TILE, PT_CTAS) k_mlp_far_pairs(int64_t np, con
         uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0, c2 = c0;
         float back = 0.f;
         if (p < np) {
-            const int32_t N = pnode[p];
-            const uint4* fr = reinterpret_cast<const uint4*>(nrow + (size_t)NROW * N);
-            c0 = fr[0];
-            c1 = fr[1];
-            c2 = fr[2];
-            const float2 ng = ngeo[N];
+            const uint4* rn = nrec + 4 * (size_t)pnode[p];
+            c0 = rn[0];
+            c1 = rn[1];
+            const uint4 a = rn[2], gN = rn[3];
+            const uint4 gL = nrec[4 * (size_t)plnode[p] + 3];  // the leaf's centre and anchor
             // the leaf centre's offset from the node centre in FP32 from the node frames (the
             // shift between two anchors is exact); the inputs are rounded to BF16 anyway
-            const int32_t meL = leaf_node[pleaf[p]];
-            const float2 sh = frame_shift(nf_k[meL], nf_k[N], 0.f);
-            const float4 gL = nf_geo[meL], gN = nf_geo[N];
-            const float dx = sh.x + (gL.x - gN.x), dy = sh.y + (gL.y - gN.y);
-            const float o0 = (dx * ng.x - S.inorm[0]) * S.inorm[2];
-            const float o1 = (dy * ng.x - S.inorm[1]) * S.inorm[3];
-            c2.y = pack_bf16(o0, o1);  // inputs 18, 19 follow the 18 cell inputs
+            const float dx = (__uint_as_float(gL.z) - __uint_as_float(gN.z)) +
+                             (__uint_as_float(gL.x) - __uint_as_float(gN.x));
+            const float dy = (__uint_as_float(gL.w) - __uint_as_float(gN.w)) +
+                             (__uint_as_float(gL.y) - __uint_as_float(gN.y));
+            const float is = __uint_as_float(a.y), back0 = __uint_as_float(a.z);
+            const float o0 = (dx * is - S.inorm[0]) * S.inorm[2];
+            const float o1 = (dy * is - S.inorm[1]) * S.inorm[3];
+            c2 = make_uint4(a.x, pack_bf16(o0, o1), 0u, 0u);  // inputs 16..19, then zeros
             const float d2 = dx * dx + dy * dy;
             const float r = rsqrtf(d2);
-            back = (ng.y > 0.f && d2 > 0.f) ? ng.y * (r * r * r) : 0.f;
+            back = (back0 > 0.f && d2 > 0.f) ? back0 * (r * r * r) : 0.f;
         }
         *chunk_at(x0, tid, 0, KIN / 8) = c0;
         *chunk_at(x0, tid, 1, KIN / 8) = c1;
@@ -303,12 +306,10 @@ void convective_learned(Ctx& c, vvgpu_mlp& M, const vvgpu_judge_cfg* jc, vvgpu_j
     ensure_moments(c);
     // the model's weights, as its last call left them
     VV_CUDA(cudaStreamSynchronize(M.stream));
-    c.ln_row.reserve((size_t)NROW * nn + 8);
-    c.ln_geo.reserve(nn + 1);
+    c.ln_rec.reserve(4 * (size_t)nn + 4);
     if (!c.nf_geo.p || !c.nf_k.p) throw ApiError{VVGPU_ERR_STATE, "node frames missing"};
-    __nv_bfloat16* nrow = reinterpret_cast<__nv_bfloat16*>(c.ln_row.p);
-    k_node_inputs<<<grid_for(nn, 128), 128, 0, s>>>(nn, c.nd_geom.p, c.nd_cm.p, c.nd_mom.p, M.norm.p, nrow,
-                                                    c.ln_geo.p);
+    k_node_inputs<<<grid_for(nn, 128), 128, 0, s>>>(nn, c.nd_geom.p, c.nd_cm.p, c.nd_mom.p, M.norm.p, c.nf_geo.p,
+                                                    c.nf_k.p, c.ln_rec.p);
     VV_LAUNCH_CHECK();
     const int64_t np = c.n_far_pairs;
     c.ln_pv.reserve(np + 1);
@@ -325,9 +326,8 @@ void convective_learned(Ctx& c, vvgpu_mlp& M, const vvgpu_judge_cfg* jc, vvgpu_j
             VV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_far_pairs, TILE, pair_smem()));
             per_sm = std::max(1, std::min(per_sm, 512 / PT_TMEM));  // tensor-memory columns per SM
             const int grid = (int)std::min<int64_t>(ntiles, (int64_t)dev_sms * per_sm);
-            k_mlp_far_pairs<<<grid, TILE, pair_smem(), s>>>(np, c.lf_far_node.p, c.lf_far_leaf.p, c.leaf_node.p,
-                                                            c.nf_geo.p, c.nf_k.p, nrow, c.ln_geo.p, M.img.p,
-                                                            M.params.p, M.norm.p,
+            k_mlp_far_pairs<<<grid, TILE, pair_smem(), s>>>(np, c.lf_far_node.p, c.lf_far_leaf.p, c.ln_rec.p,
+                                                            M.img.p, M.params.p, M.norm.p,
                                                             c.ln_pv.p, M.err.p, M.wait_spins);
             VV_LAUNCH_CHECK();
         }

@@ -183,12 +183,11 @@ struct Ctx {
     DArr<double4> lf_taylor;        // far-field expansion coefficients T1..T4 per leaf
     // far nodes of every leaf, kept by the warp walk when keep_far is set (learned far field)
     bool keep_far = false, far_kept = false;
-    DArr<int32_t> far_buf, lf_far_cnt, lf_far_off, lf_far_node, lf_far_leaf;
+    DArr<int32_t> far_buf, lf_far_cnt, lf_far_off, lf_far_node, lf_far_leaf;  // lf_far_leaf: the leaf's node id
     int64_t n_far_pairs = 0;
-    // learned far field (learned_step.cu): per-node inputs (BF16 bits) and geometry, per-pair
+    // learned far field (learned_step.cu): per-node 64-byte input records, per-pair
     // corrections, corrected coefficients, the judge's samples and results
-    DArr<uint16_t> ln_row;
-    DArr<float2> ln_geo;
+    DArr<uint4> ln_rec;
     DArr<double4> lf_taylor_l;
     DArr<float2> ln_pv;
     DArr<double> ln_v0, ln_judge;
