@@ -108,6 +108,7 @@ __device__ __forceinline__ uint4* chunk_at(__nv_bfloat16* base, int r, int q, in
 
 constexpr int PT_TMEM = 64;   // Z1, then Z2 over it (Z1 is read out before the second MMA)
 constexpr int PT_CTAS = 7;    // resident per SM (shared memory ~30 KB, 64 TMEM columns each)
+static_assert(PT_CTAS * PT_TMEM <= 512, "tensor-memory columns of the resident CTAs");
 struct PairSmem {
     __nv_bfloat16 w[I_W3];         // W1 and W2 images (learned.cu's layout)
     // the tile's inputs, then its first hidden layer: the inputs are read by the first MMA,
@@ -320,12 +321,12 @@ void convective_learned(Ctx& c, vvgpu_mlp& M, const vvgpu_judge_cfg* jc, vvgpu_j
             VV_CUDA(cudaFuncSetAttribute(k_mlp_far_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)pair_smem()));
             const int64_t ntiles = (np + TILE - 1) / TILE;
-            // persistent: exactly the CTAs that fit at once
-            int dev_sms = 0, per_sm = 0;
+            // persistent: exactly the CTAs that fit at once (PT_CTAS per SM by registers, shared
+            // and tensor memory; the runtime's occupancy query answered 1 for this kernel, which
+            // left six of every seven slots empty)
+            int dev_sms = 0;
             VV_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c.device));
-            VV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_far_pairs, TILE, pair_smem()));
-            per_sm = std::max(1, std::min(per_sm, 512 / PT_TMEM));  // tensor-memory columns per SM
-            const int grid = (int)std::min<int64_t>(ntiles, (int64_t)dev_sms * per_sm);
+            const int grid = (int)std::min<int64_t>(ntiles, (int64_t)dev_sms * PT_CTAS);
             k_mlp_far_pairs<<<grid, TILE, pair_smem(), s>>>(np, c.lf_far_node.p, c.lf_far_leaf.p, c.ln_rec.p,
                                                             M.img.p, M.params.p, M.norm.p,
                                                             c.ln_pv.p, M.err.p, M.wait_spins);
