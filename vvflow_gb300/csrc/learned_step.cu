@@ -93,12 +93,44 @@ __device__ __forceinline__ float tanh_fast(float x) {
     asm("tanh.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
-// the network's tanh-form GELU with the hardware tanh (the hidden values are rounded to
-// BF16 right after, far coarser than the approximation)
-__device__ __forceinline__ float gelu_fast(float z) {
-    const float u = GC * fmaf(GA * z * z, z, z);
-    const float hz = 0.5f * z;
-    return fmaf(hz, tanh_fast(u), hz);
+
+// Packed FP32 pairs (sm_100-family f32x2 arithmetic: one instruction for two lanes' worth)
+__device__ __forceinline__ uint64_t f2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void uf2(uint64_t v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t fadd2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t fmul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+// The network's tanh-form GELU of (z0 + b0, z1 + b1) with the hardware tanh, rounded to a
+// BF16 pair (the rounding is far coarser than the approximation)
+__device__ __forceinline__ uint32_t gelu2_bf16(float z0, float z1, float2 b) {
+    const uint64_t z = fadd2(f2(z0, z1), f2(b.x, b.y));
+    const uint64_t a = fmul2(fmul2(z, z), f2(GA, GA));
+    const uint64_t u = fmul2(ffma2(a, z, z), f2(GC, GC));
+    float u0, u1;
+    uf2(u, u0, u1);
+    const uint64_t hz = fmul2(z, f2(0.5f, 0.5f));
+    const uint64_t h = ffma2(hz, f2(tanh_fast(u0), tanh_fast(u1)), hz);
+    float h0, h1;
+    uf2(h, h0, h1);
+    return pack_bf16(h0, h1);
 }
 
 // 16-byte chunk q (8 consecutive K elements) of row r of a K-major core-matrix operand
@@ -110,11 +142,11 @@ constexpr int PT_TMEM = 64;   // Z1, then Z2 over it (Z1 is read out before the 
 constexpr int PT_CTAS = 7;    // resident per SM (shared memory ~30 KB, 64 TMEM columns each)
 static_assert(PT_CTAS * PT_TMEM <= 512, "tensor-memory columns of the resident CTAs");
 struct PairSmem {
-    __nv_bfloat16 w[I_W3];         // W1 and W2 images (learned.cu's layout)
-    // the tile's inputs, then its first hidden layer: the inputs are read by the first MMA,
-    // which has completed before the hidden layer is written
+    __nv_bfloat16 w[NIMG_FWD];     // W1, W2 and W3 images (learned.cu's layout)
+    // the tile's inputs, then its first hidden layer, then its second: each is read by its
+    // MMA, which has completed before the next is written
     __nv_bfloat16 h1[TILE * HID];
-    float b1[HID], b2[HID], w3[NOUT][HID];
+    float b1[HID], b2[HID];
     float b3[NOUT], onorm[NOUT], inorm[4];
     uint64_t mbar;
     uint32_t tmem;
@@ -133,12 +165,10 @@ __global__ void __launch_bounds__(TILE, PT_CTAS) k_mlp_far_pairs(int64_t np, con
     PairSmem& S = *reinterpret_cast<PairSmem*>(smraw);
     __nv_bfloat16* const x0 = S.h1;  // [TILE][KIN] at the start of h1's space
     const int tid = threadIdx.x, w = tid >> 5;
-    for (int i = tid; i < I_W3; i += TILE) S.w[i] = img[i];
+    for (int i = tid; i < NIMG_FWD; i += TILE) S.w[i] = img[i];
     for (int i = tid; i < HID; i += TILE) {
         S.b1[i] = params[P_B1 + i];
         S.b2[i] = params[P_B2 + i];
-        S.w3[0][i] = __bfloat162float(__float2bfloat16(params[P_W3 + i]));
-        S.w3[1][i] = __bfloat162float(__float2bfloat16(params[P_W3 + HID + i]));
     }
     if (tid < NOUT) {
         S.b3[tid] = params[P_B3 + tid];
@@ -199,7 +229,7 @@ __global__ void __launch_bounds__(TILE, PT_CTAS) k_mlp_far_pairs(int64_t np, con
             uint32_t q[8];
 #pragma unroll
             for (int j = 0; j < 8; j++)
-                q[j] = pack_bf16(gelu_fast(v[2 * j] + S.b1[c + 2 * j]), gelu_fast(v[2 * j + 1] + S.b1[c + 2 * j + 1]));
+                q[j] = gelu2_bf16(v[2 * j], v[2 * j + 1], *reinterpret_cast<const float2*>(&S.b1[c + 2 * j]));
             *chunk_at(S.h1, tid, c / 8, HID / 8) = make_uint4(q[0], q[1], q[2], q[3]);
             *chunk_at(S.h1, tid, c / 8 + 1, HID / 8) = make_uint4(q[4], q[5], q[6], q[7]);
         }
@@ -213,18 +243,33 @@ __global__ void __launch_bounds__(TILE, PT_CTAS) k_mlp_far_pairs(int64_t np, con
         phase ^= 1;
         fence_after();
         if (!ok) break;
-        float y0 = 0.f, y1 = 0.f;
         for (int c = 0; c < HID; c += 16) {
             float v[16];
             tmem_ld16(tmem_lane_addr(tm, w, c), v);
+            uint32_t q[8];
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const float h = __bfloat162float(__float2bfloat16(gelu_fast(v[j] + S.b2[c + j])));
-                y0 = fmaf(h, S.w3[0][c + j], y0);
-                y1 = fmaf(h, S.w3[1][c + j], y1);
-            }
+            for (int j = 0; j < 8; j++)
+                q[j] = gelu2_bf16(v[2 * j], v[2 * j + 1], *reinterpret_cast<const float2*>(&S.b2[c + 2 * j]));
+            *chunk_at(S.h1, tid, c / 8, HID / 8) = make_uint4(q[0], q[1], q[2], q[3]);
+            *chunk_at(S.h1, tid, c / 8 + 1, HID / 8) = make_uint4(q[4], q[5], q[6], q[7]);
         }
-        if (p < np) pv[p] = make_float2((y0 + S.b3[0]) * S.onorm[0] * back, (y1 + S.b3[1]) * S.onorm[1] * back);
+        // output layer on the tensor cores too (N padded to 16), as the training forward
+        fence_smem_to_mma();
+        fence_before();
+        __syncthreads();
+        fence_after();
+        if (tid == 0) { mma_issue(tm, S.h1, S.w + I_W3, HID, NOUTP, false); mma_commit(&S.mbar); }
+        ok = __syncthreads_and(mbar_wait(&S.mbar, phase, spins));
+        if (!ok) lost = phase;
+        phase ^= 1;
+        fence_after();
+        if (!ok) break;
+        {
+            float v[16];
+            tmem_ld16(tmem_lane_addr(tm, w, 0), v);
+            if (p < np)
+                pv[p] = make_float2((v[0] + S.b3[0]) * S.onorm[0] * back, (v[1] + S.b3[1]) * S.onorm[1] * back);
+        }
         fence_before();
         __syncthreads();
         fence_after();
