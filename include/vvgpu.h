@@ -214,6 +214,12 @@ int vvgpu_get_body_geom(vvgpu_ctx* ctx, int body, double* area, double* cofm_x, 
 int vvgpu_tree_build(vvgpu_ctx* ctx, double far_criteria, double min_node, double max_node);
 int vvgpu_tree_destroy(vvgpu_ctx* ctx);
 int vvgpu_eps(vvgpu_ctx* ctx, int merge, int64_t* merged);
+/* Bodies whose speed_slae is not zero (vvgpu_slae's solution for a body in prescribed
+ * translation, or vvgpu_set_body_params) carry the attached vortex and source sheets of
+ * body_list_influence (MConvectiveFast.cpp:185-210, SegmentInfluence_linear_source
+ * :440-457), rotation about holder + dpos included: in vvgpu_convective,
+ * vvgpu_velocity_points and vvgpu_direct_velocity.  Like the reference, every target then
+ * visits every segment of the moving bodies (FP64). */
 int vvgpu_convective(vvgpu_ctx* ctx);
 int vvgpu_diffusive(vvgpu_ctx* ctx);
 int vvgpu_velocity_points(vvgpu_ctx* ctx, int64_t n, const double* px, const double* py,

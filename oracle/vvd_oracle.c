@@ -8,6 +8,7 @@
  */
 #include "vvd_oracle.h"
 
+#include <complex.h>
 #include <float.h>
 #include <math.h>
 #include <stdlib.h>
@@ -742,8 +743,28 @@ static void sink_influence(const vvo_space* S, double px, double py, double* ox,
     *oy = ry * C_1_2PI;
 }
 
-/* body_list_influence (MConvectiveFast.cpp:172-215) for bodies at rest: slip segments act
- * as smoothed point vortices; the attached-sheet terms vanish when speed_slae is zero. */
+/* SegmentInfluence_linear_source (MConvectiveFast.cpp:440-457): the velocity of a source
+ * sheet of linearly varying strength q1 -> q2 along segment s, in the complex arithmetic of
+ * std::complex<double> (libgcc's complex multiply and divide, the C library's clog). */
+static void seg_linear_source(const vvo_space* S, int64_t s, double px, double py, double q1, double q2,
+                              double* ox, double* oy) {
+    const double complex z = CMPLX(px, py);
+    const double complex zc = CMPLX(S->rx[s], S->ry[s]);
+    const double complex dz = CMPLX(S->dlx[s], S->dly[s]);
+    const double complex zs1 = zc - dz * 0.5;
+    const double complex zs2 = zc + dz * 0.5;
+    const double complex z1 = z - zs1;
+    const double complex z2 = z - zs2;
+    const double complex zV = ((q2 - q1) - conj(q2 * z1 - q1 * z2) / conj(dz) * clog(conj(z2) / conj(z1))) / conj(dz);
+    *ox = creal(zV);
+    *oy = cimag(zV);
+}
+
+/* body_list_influence (MConvectiveFast.cpp:172-215): slip segments act as smoothed point
+ * vortices; a body whose speed_slae is not zero (TVec3D::iszero) carries attached vortex and
+ * source sheets of strengths -Vs.dl and -rotl(Vs).dl, Vs the body's velocity at the point of
+ * the segment (rotation about get_axis() = holder + dpos, TBody.hpp:124): linear sheets
+ * within |dl| of the segment centre, point singularities beyond. */
 static void body_influence(const vvo_space* S, double px, double py, double* ox, double* oy) {
     double rx = 0, ry = 0;
     for (int bi = 0; bi < S->nb; bi++) {
@@ -758,6 +779,40 @@ static void body_influence(const vvo_space* S, double px, double py, double* ox,
                 double e = 1. / S->sie[s];
                 double sc = S->sg[s] / (abs2(dx, dy) + e * e);
                 rx += (-dy) * sc; ry += dx * sc;
+            }
+        }
+        const vvo_body_params* p = &b->p;
+        if (fabs(p->speed_slae_x) + fabs(p->speed_slae_y) + fabs(p->speed_slae_o) < 1E-10) continue;
+        const double ax = p->holder_x + p->dpos_x, ay = p->holder_y + p->dpos_y;
+        const double vx = p->speed_slae_x, vy = p->speed_slae_y, vo = p->speed_slae_o;
+        for (int64_t k = 0; k < b->count; k++) {
+            const int64_t s = b->first + k;
+            const double dlx = S->dlx[s], dly = S->dly[s];
+            const double drabs2 = abs2(px - S->rx[s], py - S->ry[s]);
+            if (drabs2 < abs2(dlx, dly)) {
+                /* Vs1 = V.r + V.o rotl(corner - axis), Vs2 at corner + dl */
+                const double c1x = S->cx[s] - ax, c1y = S->cy[s] - ay;
+                const double w1x = vx + (-c1y) * vo, w1y = vy + c1x * vo;
+                const double g1 = (-w1x) * dlx + (-w1y) * dly;
+                const double q1 = w1y * dlx + (-w1x) * dly;
+                const double c2x = (S->cx[s] + dlx) - ax, c2y = (S->cy[s] + dly) - ay;
+                const double w2x = vx + (-c2y) * vo, w2y = vy + c2x * vo;
+                const double g2 = (-w2x) * dlx + (-w2y) * dly;
+                const double q2 = w2y * dlx + (-w2x) * dly;
+                double ux, uy;
+                seg_linear_source(S, s, px, py, g1, g2, &ux, &uy);
+                rx += -uy; ry += ux;  /* rotl */
+                seg_linear_source(S, s, px, py, q1, q2, &ux, &uy);
+                rx += ux; ry += uy;
+            } else {
+                const double cx = S->rx[s] - ax, cy = S->ry[s] - ay;
+                const double wx = vx + (-cy) * vo, wy = vy + cx * vo;
+                const double g = (-wx) * dlx + (-wy) * dly;
+                const double q = wy * dlx + (-wx) * dly;
+                const double dx = px - S->rx[s], dy = py - S->ry[s];
+                const double inv = 1. / drabs2;  /* TVec / c is TVec * (1 / c) */
+                rx += (dx * q + (-dy) * g) * inv;
+                ry += (dy * q + dx * g) * inv;
             }
         }
     }
@@ -777,7 +832,6 @@ static int bodies_at_rest(const vvo_space* S) {
 /* MConvectiveFast::process_all_lists (MConvectiveFast.cpp:36-114), vortex list. */
 int vvo_convective(vvo_space* S) {
     if (!S->built) return -3;
-    if (!bodies_at_rest(S)) return -4;
     for (int64_t L = 0; L < S->nleaves; L++) {
         if (L % S->stride) continue;
         const onode* nd = &S->nodes[S->leaves[L]];
@@ -819,7 +873,6 @@ int vvo_convective(vvo_space* S) {
 int vvo_velocity_points(vvo_space* S, int64_t n, const double* px, const double* py,
                         double* vx, double* vy) {
     if (!S->built) return -3;
-    if (!bodies_at_rest(S)) return -4;
     int32_t* pos = (int32_t*)xrealloc(NULL, sizeof(int32_t) * (size_t)(S->nnodes ? S->nnodes : 1));
     for (int64_t k = 0; k < S->nnodes; k++) pos[k] = -1;
     for (int64_t t = 0; t < S->nleaves; t++) pos[S->leaves[t]] = (int32_t)t;
@@ -851,7 +904,6 @@ int vvo_velocity_points(vvo_space* S, int64_t n, const double* px, const double*
 
 int vvo_direct_velocity(const vvo_space* S, int64_t n, const double* px, const double* py,
                         double* vx, double* vy) {
-    if (!bodies_at_rest(S)) return -4;
 #pragma omp parallel for schedule(dynamic, 16)
     for (int64_t q = 0; q < n; q++) {
         double rx = 0, ry = 0;

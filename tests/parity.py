@@ -20,7 +20,7 @@ def golden_cases(folder, prefix=None):
     import os
     names = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(folder, "*.npz")))
     if prefix is None:
-        return [n for n in names if not n.startswith(("move_", "forces_", "field_"))]
+        return [n for n in names if not n.startswith(("move_", "forces_", "field_", "attached_"))]
     return [n for n in names if n.startswith(prefix)]
 
 

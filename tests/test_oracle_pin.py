@@ -158,3 +158,32 @@ def test_port_fields_reject_bad_arguments():
     with pytest.raises(oracle.OracleError):
         S.field_vorticity(-1.0, -1.0, 0.1, 8, 8)
     S.close()
+
+
+# ---- moving bodies: attached sheets (MConvectiveFast.cpp:172-215, 440-457) ---------------
+def test_port_attached_sheets_match_golden():
+    import attached_cases as AC
+    d = np.load(os.path.join(GOLDEN, "attached_bodies.npz"))
+    S = oracle.OracleSpace("port")
+    got = AC.run(S, AC.case(), oracle.default_body_params)
+    S.close()
+    for k in d.files:
+        assert np.array_equal(got[k], d[k], equal_nan=True), k
+    # the sheets matter: the same state with the body at rest differs well beyond rounding
+    R = oracle.OracleSpace("port")
+    rest = AC.run(R, AC.case(), oracle.default_body_params, moving=False)
+    R.close()
+    assert np.abs(rest["probe_vx"] - d["probe_vx"]).max() > 1e-2
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference sources not present")
+def test_port_attached_sheets_match_reference_live():
+    import attached_cases as AC
+    c = AC.case()
+    out = {}
+    for kind in ("ref", "port"):
+        S = oracle.OracleSpace(kind)
+        out[kind] = AC.run(S, c, oracle.default_body_params, direct=False)
+        S.close()
+    for k in out["ref"]:
+        assert np.array_equal(out["port"][k], out["ref"][k], equal_nan=True), k

@@ -86,13 +86,78 @@ struct ConvArgs {
     int64_t ns; const double* kx; const double* ky; const double* kg; double sink_e2;
     int64_t m; const double* srx; const double* sry; const double* sg; const double* sie; const uint32_t* slip;
     int any_slip;
+    // attached sheets of moving bodies: per segment corner, dl, and (speed x, y, o, axis x,
+    // y) of its body, flagged where the body's speed_slae is not zero
+    int any_moving;
+    const double* scx; const double* scy; const double* sdlx; const double* sdly;
+    const double* att; const int32_t* att_on;
     double inf_vx, inf_vy;
     double fc; int64_t nnodes;
     // FP32 records
     const float4* src32; const float2* src_k; const float2* anchor; double G; float Gf;
 };
 
-// sink_list_influence + slip-segment part of body_list_influence, FP64 (per target).
+// (a + ib) / (c + id)
+__device__ __forceinline__ void cdiv(double a, double b, double c, double d, double& re, double& im) {
+    const double den = c * c + d * d;
+    re = (a * c + b * d) / den;
+    im = (b * c - a * d) / den;
+}
+
+// SegmentInfluence_linear_source (MConvectiveFast.cpp:440-457): a source sheet of strength
+// q1 -> q2 along the segment centred at (rx, ry) with vector (dlx, dly), at (px, py):
+// ((q2 - q1) - conj(q2 z1 - q1 z2) / conj(dz) log(conj(z2) / conj(z1))) / conj(dz) with
+// z1, z2 the point's offsets from the segment's ends; FP64 with CUDA's log and atan2.
+__device__ __forceinline__ void linear_source(double px, double py, double rx, double ry, double dlx, double dly,
+                                              double q1, double q2, double& ox, double& oy) {
+    const double z1x = px - (rx - dlx * 0.5), z1y = py - (ry - dly * 0.5);
+    const double z2x = px - (rx + dlx * 0.5), z2y = py - (ry + dly * 0.5);
+    double bx, by, wx, wy, nx, ny;
+    cdiv(q2 * z1x - q1 * z2x, -(q2 * z1y - q1 * z2y), dlx, -dly, bx, by);
+    cdiv(z2x, -z2y, z1x, -z1y, wx, wy);
+    const double lx = log(hypot(wx, wy)), ly = atan2(wy, wx);
+    nx = (q2 - q1) - (bx * lx - by * ly);
+    ny = -(bx * ly + by * lx);
+    cdiv(nx, ny, dlx, -dly, ox, oy);
+}
+
+// The attached vortex and source sheets of the moving bodies (body_list_influence,
+// MConvectiveFast.cpp:185-210) at (px, py), before the 1/2pi: sheets of strength
+// -Vs.dl and -rotl(Vs).dl with Vs the body's velocity at the segment (rotation about
+// holder + dpos); linear sheets within |dl| of the segment centre, point singularities
+// beyond.
+__device__ __forceinline__ void attached_terms(const ConvArgs& a, double px, double py, double& rx, double& ry) {
+    for (int64_t k = 0; k < a.m; k++) {
+        if (!a.att_on[k]) continue;
+        const double* w = a.att + 5 * k;
+        const double vx = w[0], vy = w[1], vo = w[2], ax = w[3], ay = w[4];
+        const double dlx = a.sdlx[k], dly = a.sdly[k];
+        const double dx = px - a.srx[k], dy = py - a.sry[k];
+        const double drabs2 = dx * dx + dy * dy;
+        if (drabs2 < dlx * dlx + dly * dly) {
+            const double c1x = a.scx[k] - ax, c1y = a.scy[k] - ay;
+            const double w1x = vx - c1y * vo, w1y = vy + c1x * vo;
+            const double c2x = (a.scx[k] + dlx) - ax, c2y = (a.scy[k] + dly) - ay;
+            const double w2x = vx - c2y * vo, w2y = vy + c2x * vo;
+            double ux, uy;
+            linear_source(px, py, a.srx[k], a.sry[k], dlx, dly, -(w1x * dlx + w1y * dly), -(w2x * dlx + w2y * dly),
+                          ux, uy);
+            rx -= uy; ry += ux;  // rotl
+            linear_source(px, py, a.srx[k], a.sry[k], dlx, dly, w1y * dlx - w1x * dly, w2y * dlx - w2x * dly, ux, uy);
+            rx += ux; ry += uy;
+        } else {
+            const double cx = a.srx[k] - ax, cy = a.sry[k] - ay;
+            const double wx = vx - cy * vo, wy = vy + cx * vo;
+            const double g = -(wx * dlx + wy * dly), q = wy * dlx - wx * dly;
+            const double inv = 1. / drabs2;
+            rx += (dx * q - dy * g) * inv;
+            ry += (dy * q + dx * g) * inv;
+        }
+    }
+}
+
+// sink_list_influence + body_list_influence (slip segments, attached sheets of moving
+// bodies), FP64 (per target).
 __device__ __forceinline__ void extra_terms(const ConvArgs& a, double px, double py, double& ox, double& oy) {
     double rx = 0, ry = 0;
     for (int64_t k = 0; k < a.ns; k++) {
@@ -110,6 +175,7 @@ __device__ __forceinline__ void extra_terms(const ConvArgs& a, double px, double
             bx -= dy * s; by += dx * s;
         }
     }
+    if (a.any_moving) attached_terms(a, px, py, bx, by);
     ox = (rx + bx) * C_1_2PI;
     oy = (ry + by) * C_1_2PI;
 }
@@ -634,6 +700,33 @@ ConvArgs make_args(Ctx& c) {
     a.m = c.m; a.srx = c.s_rx.p; a.sry = c.s_ry.p; a.sg = c.s_g.p; a.sie = c.s_ie.p; a.slip = c.s_slip.p;
     a.any_slip = 0;
     for (auto s : c.h_slip) a.any_slip |= (s != 0);
+    // moving bodies: per-segment speed and axis of the body (TBody::get_axis = holder + dpos)
+    a.any_moving = 0;
+    for (auto& b : c.bodies) {
+        const vvgpu_body_params& p = b.p;
+        if (!(std::fabs(p.speed_slae_x) + std::fabs(p.speed_slae_y) + std::fabs(p.speed_slae_o) < 1E-10))
+            a.any_moving = 1;
+    }
+    if (a.any_moving) {
+        c.h_att.assign(5 * (size_t)c.m, 0.);
+        c.h_att_on.assign((size_t)c.m, 0);
+        for (auto& b : c.bodies) {
+            const vvgpu_body_params& p = b.p;
+            if (std::fabs(p.speed_slae_x) + std::fabs(p.speed_slae_y) + std::fabs(p.speed_slae_o) < 1E-10) continue;
+            for (int64_t k = b.first; k < b.first + b.count; k++) {
+                double* w = c.h_att.data() + 5 * k;
+                w[0] = p.speed_slae_x; w[1] = p.speed_slae_y; w[2] = p.speed_slae_o;
+                w[3] = p.holder_x + p.dpos_x; w[4] = p.holder_y + p.dpos_y;
+                c.h_att_on[k] = 1;
+            }
+        }
+        c.s_att.reserve(5 * (size_t)c.m);
+        c.s_att_on.reserve((size_t)c.m);
+        VV_CUDA(cudaMemcpyAsync(c.s_att.p, c.h_att.data(), 5 * c.m * 8, cudaMemcpyHostToDevice, c.st()));
+        VV_CUDA(cudaMemcpyAsync(c.s_att_on.p, c.h_att_on.data(), c.m * 4, cudaMemcpyHostToDevice, c.st()));
+        a.scx = c.s_cx.p; a.scy = c.s_cy.p; a.sdlx = c.s_dlx.p; a.sdly = c.s_dly.p;
+        a.att = c.s_att.p; a.att_on = c.s_att_on.p;
+    }
     a.inf_vx = c.inf_vx; a.inf_vy = c.inf_vy;
     a.fc = c.far_criteria; a.nnodes = c.nnodes;
     return a;
@@ -692,7 +785,6 @@ void count_near_pairs(Ctx& c) {
 }
 
 void convective(Ctx& c) {
-    check_bodies_at_rest(c);
     if (c.n == 0 || c.nleaves == 0) return;
     cudaStream_t s = c.st();
     if (c.count_pairs) count_near_pairs(c);
@@ -713,7 +805,6 @@ void convective(Ctx& c) {
 }
 
 void velocity_points(Ctx& c, int64_t np, const double* px, const double* py, double* vx, double* vy) {
-    check_bodies_at_rest(c);
     if (np == 0) return;
     cudaStream_t s = c.st();
     DArr<double> q;
@@ -731,7 +822,6 @@ void velocity_points(Ctx& c, int64_t np, const double* px, const double* py, dou
 
 void direct_velocity(Ctx& c, int64_t np, const double* px, const double* py, double* vx, double* vy) {
     check_input(c);
-    check_bodies_at_rest(c);
     if (np == 0) return;
     upload_segments(c);
     cudaStream_t s = c.st();
@@ -820,7 +910,6 @@ void judge_velocity_exact(Ctx& c, int64_t nt, const int32_t* d_idx, double fc, d
 // velocity_points, launched on caller-provided device buffers, allocating nothing.
 void velocity_points_on_device(Ctx& c, int64_t np, const double* dpx, const double* dpy, double* dvx,
                                double* dvy) {
-    check_bodies_at_rest(c);
     if (np == 0) return;
     ConvArgs a = make_args(c);
     k_points<<<grid_for(np, 128), 128, 0, c.st()>>>(np, dpx, dpy, c.nd_geom.p, c.nd_ch1.p, c.nd_dfs.p, a, dvx, dvy);

@@ -332,7 +332,6 @@ size_t pair_smem() { return sizeof(PairSmem); }
 void convective_learned(Ctx& c, vvgpu_mlp& M, const vvgpu_judge_cfg* jc, vvgpu_judge_out* jo) {
     using namespace mlp;
     cudaStream_t s = c.st();
-    check_bodies_at_rest(c);
     if (jc && (jc->targets < 0 || !(jc->far_criteria > 0) || !(jc->bound >= 0)))
         throw ApiError{VVGPU_ERR_ARG, "bad judge parameters"};
     const int64_t n = c.n, nl = c.nleaves, nn = c.nnodes;

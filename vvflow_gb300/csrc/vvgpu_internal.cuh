@@ -140,6 +140,10 @@ struct Ctx {
     DArr<int64_t> f_fc;
     DArr<double> f_out;
     DArr<uint32_t> s_slip;
+    std::vector<double> h_att;       // attached sheets: per segment speed x, y, o and axis x, y
+    std::vector<int32_t> h_att_on;   // ... of a body whose speed_slae is not zero
+    DArr<double> s_att;
+    DArr<int32_t> s_att_on;
     bool segs_dirty = true;
     // sinks
     int64_t ns = 0;
