@@ -519,15 +519,6 @@ __global__ void __launch_bounds__(WW * 32, VV_WALK_MIN_BLOCKS) k_walk_warp(int64
         __syncwarp();
         const bool act = (mask >> lane) & 1u;
         const NodeRec cur = load_rec(v.rec, t);
-#ifndef VV_WALK_NO_PREFETCH
-        {
-            // the children's records, which the next step pops when the node is opened for
-            // any lane: requested now, while this node's far test runs
-            const int32_t cp = __float_as_int(cur.r0.w);
-            if (cp >= 0 && lane < 2)
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(v.rec + 4 * (size_t)(cp + lane)));
-        }
-#endif
         const bool far = act && far_test_at(v, cur.r0, make_float2(cur.r1.x, cur.r1.y), t, meN, mg, mk);
         if (far) {
             if (FP32) tay.add_rec(cur, mg, mk); else tay.add(v, t, mg, mk, me);
