@@ -158,6 +158,11 @@ int vvgpu_get_stats(const vvgpu_ctx* ctx, vvgpu_stats* out);
  * leaves the vortex list as it was; the tree stays built.  The reference's sequential pass
  * has no such bound (MEpsilonFast.cpp:11-63). */
 int vvgpu_set_eps_round_limit(vvgpu_ctx* ctx, int64_t max_rounds);
+/* Polls of one shared-memory staging wait in the FP32 near field (bulk copies completing
+ * on an mbarrier; default 4194304).  A wait that runs out makes the call return
+ * VVGPU_ERR_TIMEOUT after its copies in flight have landed; the context stays usable
+ * (0 polls: every wait runs out).  No counterpart in the reference (it has no GPU). */
+int vvgpu_set_wait_limit(vvgpu_ctx* ctx, uint32_t spins);
 /* Kernel timing on (1) or off (0); either clears the sums.  No counterpart in the
  * reference (it has no GPU). */
 int vvgpu_set_kernel_timing(vvgpu_ctx* ctx, int on);

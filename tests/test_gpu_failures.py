@@ -10,6 +10,9 @@ none of them faults the GPU.
 * Tensor-core waits given a limit of zero polls run out at once: the call returns
   VVGPU_ERR_TIMEOUT, and with the default limit back the model gives the same results as
   before (the kernels let their MMAs land and release their tensor memory).
+* The FP32 near field's shared-memory staging waits (bulk copies on an mbarrier), given
+  zero polls, run out at once: vvgpu_convective returns VVGPU_ERR_TIMEOUT after its copies
+  have landed, and with the default limit back it gives the same velocities as before.
 After each failure the context (or model) keeps working."""
 import numpy as np
 import pytest
@@ -144,3 +147,29 @@ def test_tensor_core_wait_limit_times_out_and_recovers():
     g1, _ = M.gradient()
     assert np.array_equal(g0, g1)
     M.close()
+
+
+@pytest.mark.gpu
+def test_staging_wait_limit_times_out_and_recovers():
+    wl = W.cylinder_annulus(20000, 500, seed=3)
+    mn, mx = wl.node_sizes()
+    S = _space(1)
+    S.load(wl)
+    S.tree_build(wl.far_criteria, mn, mx)
+    S.eps(False)
+    zero = np.zeros(wl.n)
+    S.set_velocities(zero, zero)
+    S.convective()
+    ref = S.vortices()
+    S.set_wait_limit(0)
+    S.set_velocities(zero, zero)
+    assert _err(S.convective) == ERR_TIMEOUT
+    S.set_wait_limit()
+    S.set_velocities(zero, zero)
+    S.convective()
+    got = S.vortices()
+    S.tree_destroy()
+    S.close()
+    assert np.abs(ref["vx"]).max() > 0
+    for k in ("vx", "vy", "orig"):
+        assert np.array_equal(ref[k], got[k]), k

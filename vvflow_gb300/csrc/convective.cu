@@ -9,13 +9,14 @@
 //
 // FP64 path: Biot-Savart kernel rotl(dr) g / (|dr|^2 + eps^2) / 2pi in double precision,
 // the reciprocal by Newton-Raphson iteration from the hardware approximation.
-// FP32 path: sources in local frames (frame.cuh), FP32 pair arithmetic, lane partials
-// accumulated per near run and folded into a two-sum (Knuth's TwoSum) compensated pair,
-// lane partials reduced as double-float pairs; FP64 (a narrow pipe on sm_103) only in the
-// final per-target update.
+// FP32 path: sources in local frames (frame.cuh), staged through shared memory by bulk
+// copies (stage.cuh), FP32 pair arithmetic, lane partials folded into a two-sum (Knuth's
+// TwoSum) compensated pair every at most 32 sources, lane partials reduced as double-float
+// pairs; FP64 (a narrow pipe on sm_103) only in the final per-target update.
 #include <cfloat>
 
 #include "frame.cuh"
+#include "stage.cuh"
 #include "vvgpu_internal.cuh"
 
 namespace vvgpu {
@@ -95,6 +96,11 @@ struct ConvArgs {
     double fc; int64_t nnodes;
     // FP32 records
     const float4* src32; const float2* src_k; const float2* anchor; double G; float Gf;
+    // FP32 near field: anchors of the sources' leaves as 16-byte records, and per near run
+    // (first source slot, offset in the leaf's flattened near sequence), per leaf the
+    // sequence's length; staging waits and their error flag
+    const float4* src_a4; const int2* run_js; const int32_t* leaf_tot; int64_t nsrc;
+    uint32_t spins; unsigned long long* err;
 };
 
 // (a + ib) / (c + id)
@@ -244,22 +250,82 @@ __global__ void __launch_bounds__(CW * 32) k_conv64(ConvArgs a) {
 
 // FP32 near field.  Eight targets per lane.  A leaf with at most 8 targets uses all 32
 // lanes over its sources; with 9..16 targets each half-warp takes 8 targets and strides
-// over the sources by 16 (larger leaves loop in groups of 16).  Each lane keeps plain FP32
-// partial sums for up to 32 sources and then folds them into a TwoSum-compensated pair.
+// over the sources by 16 (larger leaves loop in groups of 16).  The leaf's near sources are
+// one flattened sequence (its near runs in list order; run_js holds each run's first slot
+// and offset).  The warp streams it through shared memory in tiles of CT sources, two
+// buffers: for the next tile every lane whose run overlaps it issues one bulk copy of the
+// piece's records and one of their anchors, completing on the buffer's mbarrier, while the
+// lanes apply the current tile.  Each lane keeps plain FP32 partial sums over at most 32
+// of its sources and then folds them into a TwoSum-compensated pair.
 constexpr int TC32 = 8;
+constexpr int CT = 192;  // sources per staged tile
+constexpr size_t CONV32_SMEM = (size_t)CW * 2 * CT * 2 * sizeof(float4) + (size_t)CW * 2 * sizeof(uint64_t);
 
 __global__ void __launch_bounds__(CW * 32, 4) k_conv32(ConvArgs a) {
-    __shared__ int2 s_runs[CW][32];
+    extern __shared__ __align__(128) unsigned char conv_smem[];
     const int wq = threadIdx.x >> 5;
     const int64_t L = (int64_t)blockIdx.x * CW + wq;
     const int lane = threadIdx.x & 31;
     if (L >= a.nl) return;
+    float4* const t_rec = reinterpret_cast<float4*>(conv_smem) + (size_t)wq * 2 * CT;           // [2][CT]
+    float4* const t_anc = reinterpret_cast<float4*>(conv_smem) + (size_t)(CW + wq) * 2 * CT;    // [2][CT]
+    uint64_t* const bar = reinterpret_cast<uint64_t*>(reinterpret_cast<float4*>(conv_smem) + (size_t)CW * 4 * CT) +
+                          2 * wq;
+    if (lane == 0) {
+        stage_bar_init(&bar[0]);
+        stage_bar_init(&bar[1]);
+    }
+    __syncwarp();
     const double4 me = a.lgeom[L];
     const double4 tc = a.taylor[L];
     const float2 kL = a.anchor[L];
     const int32_t v0 = a.lvf[L], v1 = a.lvl[L];
     const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
-    for (int32_t c0 = v0; c0 < v1; c0 += 2 * TC32) {
+    const int32_t tot = a.leaf_tot[L];
+    const int ntile = (tot + CT - 1) / CT;
+    uint32_t parity = 0;  // bit b: parity of buffer b's next phase
+    int ib = 0, cb = 0;   // buffer of the next tile issued / consumed
+    int pending = 0;      // tiles issued and not yet consumed
+    bool fail = false;
+    // Issues tile t (sources [t CT, min((t+1) CT, tot))) into buffer ib.  rcur: the first
+    // run that ends beyond the tile's start; on return, the first run ending beyond its end.
+    auto issue = [&](int t, int32_t& rcur) {
+        const int32_t kb = t * CT, ke = min(kb + CT, tot);
+        const int b = ib;
+        ib ^= 1;
+        pending++;
+        if (lane == 0) stage_expect(&bar[b], (uint32_t)(ke - kb) * 32u);
+        __syncwarp();
+        for (int32_t rb = rcur; rb < r1; rb += 32) {
+            const int32_t r = rb + lane;
+            int32_t j0 = 0, off = tot;
+            if (r < r1) {
+                const int2 js = a.run_js[r];
+                j0 = js.x;
+                off = js.y;
+            }
+            int32_t end = __shfl_down_sync(0xffffffffu, off, 1);
+            if (lane == 31) end = (rb + 32 < r1) ? a.run_js[rb + 32].y : tot;
+            if (r >= r1) end = tot;
+            const int32_t lo = max(off, kb), hi = min(end, ke);
+            if (r < r1 && hi > lo) {
+                const int32_t j = j0 + (lo - off);
+                // every piece lies inside the vortex arrays and the tile (else the wait runs out)
+                if (j >= 0 && (int64_t)j + (hi - lo) <= a.nsrc && lo >= kb && hi <= kb + CT) {
+                    stage_fence();
+                    stage_copy(t_rec + b * CT + (lo - kb), a.src32 + j, (uint32_t)(hi - lo) * 16u, &bar[b]);
+                    stage_copy(t_anc + b * CT + (lo - kb), a.src_a4 + j, (uint32_t)(hi - lo) * 16u, &bar[b]);
+                }
+            }
+            const unsigned beyond = __ballot_sync(0xffffffffu, r < r1 && end > ke);
+            if (beyond) {
+                rcur = rb + __ffs(beyond) - 1;
+                return;
+            }
+            rcur = rb + 32;
+        }
+    };
+    for (int32_t c0 = v0; c0 < v1 && !fail; c0 += 2 * TC32) {
         const int32_t nt = min(v1 - c0, 2 * TC32);
         const bool split = nt > TC32;                 // two groups of 8 targets
         const int half = split ? (lane >> 4) : 0;
@@ -276,77 +342,51 @@ __global__ void __launch_bounds__(CW * 32, 4) k_conv32(ConvArgs a) {
             ty[t] = r4.y;
             hx[t] = hy[t] = lx[t] = ly[t] = px[t] = py[t] = 0.f;
         }
-        int since = 0;
-        // near runs in groups of 32: one lane resolves each run's vortex range, then the
-        // group's sources are walked as one flattened sequence (no per-run bubbles)
-        for (int32_t rb = r0; rb < r1; rb += 32) {
-            const int32_t rr = rb + lane;
-            int32_t j0 = 0, len = 0;
-            if (rr < r1) {
-                const int2 run = a.near_run[rr];
-                j0 = a.lvf[run.x];
-                len = a.lvl[run.y - 1] - j0;
+        int since = 0;  // sources in the plain partial sums (at most, over the lanes)
+        int32_t rcur = r0;
+        if (ntile > 0) issue(0, rcur);
+        for (int t = 0; t < ntile; t++) {
+            if (t + 1 < ntile) issue(t + 1, rcur);
+            const int b = cb;
+            const bool ok = stage_wait(&bar[b], (parity >> b) & 1u, a.spins);
+            if (!__all_sync(0xffffffffu, ok)) {
+                fail = true;  // this tile stays pending: the drain below waits for it
+                break;
             }
-            int32_t incl = len;
+            cb ^= 1;
+            parity ^= 1u << b;
+            pending--;
+            const int32_t ns = min(CT, tot - t * CT);
+            const int per = (ns + stride - 1) / stride;  // sources of lane 0 in this tile
+            if (since + per > 32) {
+                since = 0;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
-            }
-            const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
-            const int32_t nrun = min(32, r1 - rb);
-            s_runs[wq][lane] = make_int2(incl - len, j0);
-            __syncwarp();
-            int cur = 0;
-            int32_t nextb = (nrun > 1) ? s_runs[wq][1].x : total;
-            // the next source's record is requested before the current one is applied
-            float4 s4n = make_float4(0.f, 0.f, 0.f, 1.f);
-            float2 kkn = make_float2(0.f, 0.f);
-            if (sub < total) {
-                while (sub >= nextb) {
-                    cur++;
-                    nextb = (cur + 1 < nrun) ? s_runs[wq][cur + 1].x : total;
+                for (int tt = 0; tt < TC32; tt++) {
+                    float sv, e;
+                    two_sum(hx[tt], px[tt], sv, e); hx[tt] = sv; lx[tt] += e; px[tt] = 0.f;
+                    two_sum(hy[tt], py[tt], sv, e); hy[tt] = sv; ly[tt] += e; py[tt] = 0.f;
                 }
-                const int2 rc = s_runs[wq][cur];
-                const int32_t j = rc.y + (sub - rc.x);
-                s4n = a.src32[j];
-                kkn = a.src_k[j];
             }
-            for (int32_t k = sub; k < total; k += stride) {
-                const float4 s4 = s4n;
-                const float2 kk = kkn;
-                const int32_t kn = k + stride;
-                if (kn < total) {
-                    while (kn >= nextb) {
-                        cur++;
-                        nextb = (cur + 1 < nrun) ? s_runs[wq][cur + 1].x : total;
-                    }
-                    const int2 rc = s_runs[wq][cur];
-                    const int32_t j = rc.y + (kn - rc.x);
-                    s4n = a.src32[j];
-                    kkn = a.src_k[j];
-                }
-                const float sx = s4.x + (kk.x - kL.x);
-                const float sy = s4.y + (kk.y - kL.y);
+            since += per;
+            const float4* rt = t_rec + b * CT;
+            const float4* at = t_anc + b * CT;
+#pragma unroll 2
+            for (int k = sub; k < ns; k += stride) {
+                const float4 s4 = rt[k];
+                const float4 k4 = at[k];
+                const float sx = s4.x + (k4.x - kL.x);
+                const float sy = s4.y + (k4.y - kL.y);
 #pragma unroll
-                for (int t = 0; t < TC32; t++) {
-                    const float dx = tx[t] - sx, dy = ty[t] - sy;
+                for (int tt = 0; tt < TC32; tt++) {
+                    const float dx = tx[tt] - sx, dy = ty[tt] - sy;
                     const float q = s4.z * rcp32(fmaf(dx, dx, fmaf(dy, dy, s4.w)));
-                    px[t] = fmaf(-dy, q, px[t]);
-                    py[t] = fmaf(dx, q, py[t]);
-                }
-                if (++since == 32) {
-                    since = 0;
-#pragma unroll
-                    for (int t = 0; t < TC32; t++) {
-                        float sv, e;
-                        two_sum(hx[t], px[t], sv, e); hx[t] = sv; lx[t] += e; px[t] = 0.f;
-                        two_sum(hy[t], py[t], sv, e); hy[t] = sv; ly[t] += e; py[t] = 0.f;
-                    }
+                    px[tt] = fmaf(-dy, q, px[tt]);
+                    py[tt] = fmaf(dx, q, py[tt]);
                 }
             }
-            __syncwarp();
+            __syncwarp();  // the buffer is free for the tile after next
         }
+        if (fail) break;
         // Reduce-scatter of the 16 float-float partials (x and y of 8 targets) over the 16
         // lanes of each source stride: after the xor-8/4/2/1 steps lane k (= lane & 15)
         // holds value k, i.e. coordinate k >> 3 of target k & 7, summed over its 16 lanes.
@@ -398,13 +438,53 @@ __global__ void __launch_bounds__(CW * 32, 4) k_conv32(ConvArgs a) {
             }
         }
     }
+    if (fail) {
+        // a staging wait ran out: drain the copies in flight (bounded), flag the error
+        for (; pending > 0; pending--) {
+            stage_wait(&bar[cb], (parity >> cb) & 1u, STAGE_SPINS);
+            parity ^= 1u << cb;
+            cb ^= 1;
+        }
+        if (lane == 0) atomicExch(a.err, 1ull);
+    }
+}
+
+// Per near run of every leaf: its first source slot and its offset in the leaf's flattened
+// near sequence (the runs in list order); per leaf the sequence's length.  One warp per leaf.
+__global__ void k_run_table(int64_t nl, const int32_t* __restrict__ near_off, const int2* __restrict__ near_run,
+                            const int32_t* __restrict__ lvf, const int32_t* __restrict__ lvl, int2* run_js,
+                            int32_t* leaf_tot) {
+    const int64_t L = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (L >= nl) return;
+    const int32_t r0 = near_off[L], r1 = near_off[L + 1];
+    int32_t base = 0;
+    for (int32_t rb = r0; rb < r1; rb += 32) {
+        const int32_t r = rb + lane;
+        int32_t j0 = 0, len = 0;
+        if (r < r1) {
+            const int2 run = near_run[r];
+            j0 = lvf[run.x];
+            len = lvl[run.y - 1] - j0;
+        }
+        int32_t incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (r < r1) run_js[r] = make_int2(j0, base + incl - len);
+        base += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) leaf_tot[L] = base;
 }
 
 // FP32 source records: position in own leaf frame, g, eps^2 (eps = 1/_1_eps; a zero
 // _1_eps or zero g gives a record that contributes exactly zero).
 __global__ void k_src32(int64_t n, const int32_t* __restrict__ leaf_of, const float2* __restrict__ anchor, double G,
                         const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ g,
-                        const double* __restrict__ ie, float4* src, float2* src_k, float* src_ie) {
+                        const double* __restrict__ ie, float4* src, float2* src_k, float* src_ie,
+                        float4* src_a4) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float2 k = anchor[leaf_of[i]];
@@ -414,6 +494,7 @@ __global__ void k_src32(int64_t n, const int32_t* __restrict__ leaf_of, const fl
     if (ie[i] == 0.) { gf = 0.f; e2 = 1.f; }
     src[i] = make_float4((float)(x[i] - (double)k.x), (float)(y[i] - (double)k.y), gf, e2);
     src_k[i] = k;
+    src_a4[i] = make_float4(k.x, k.y, 0.f, 0.f);
     src_ie[i] = (float)ie[i];
 }
 
@@ -754,13 +835,14 @@ void build_frames(Ctx& c) {
     c.src32.reserve(n + 1);
     c.src_k.reserve(n + 1);
     c.src_ie.reserve(n + 1);
+    c.src_a4.reserve(n + 1);
     if (nl) {
         k_anchor2<<<grid_for(nl, 128), 128, 0, s>>>(nl, c.lf_geom.p, fr.G, c.lf_anchor.p);
         VV_LAUNCH_CHECK();
     }
     if (n) {
         k_src32<<<grid_for(n, 256), 256, 0, s>>>(n, c.leaf_of.p, c.lf_anchor.p, fr.G, c.x.p, c.y.p, c.g.p, c.ie.p,
-                                                 c.src32.p, c.src_k.p, c.src_ie.p);
+                                                 c.src32.p, c.src_k.p, c.src_ie.p, c.src_a4.p);
         VV_LAUNCH_CHECK();
     }
 }
@@ -793,9 +875,26 @@ void convective(Ctx& c) {
     if (c.precision == VVGPU_FP32) {
         build_frames(c);
         a.src32 = c.src32.p; a.src_k = c.src_k.p; a.anchor = c.lf_anchor.p; a.G = c.frame_G; a.Gf = (float)c.frame_G;
-        KernelTimer kt(c, VVGPU_T_CONVECTIVE);
-        k_conv32<<<grid, CW * 32, 0, s>>>(a);
+        const int64_t nr = c.n_near_runs;
+        c.run_js.reserve(nr + 1);
+        c.leaf_tot.reserve(c.nleaves + 1);
+        k_run_table<<<grid_for(c.nleaves, 8), 256, 0, s>>>(c.nleaves, c.near_off.p, c.near_run.p, c.lf_vf.p,
+                                                         c.lf_vl.p, c.run_js.p, c.leaf_tot.p);
         VV_LAUNCH_CHECK();
+        a.src_a4 = c.src_a4.p; a.run_js = c.run_js.p; a.leaf_tot = c.leaf_tot.p; a.nsrc = c.n;
+        a.spins = c.wait_spins;
+        a.err = c.counters.p + 20;
+        VV_CUDA(cudaMemsetAsync(a.err, 0, 8, s));
+        VV_CUDA(cudaFuncSetAttribute(k_conv32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV32_SMEM));
+        {
+            KernelTimer kt(c, VVGPU_T_CONVECTIVE);
+            k_conv32<<<grid, CW * 32, CONV32_SMEM, s>>>(a);
+            VV_LAUNCH_CHECK();
+        }
+        unsigned long long e = 0;
+        VV_CUDA(cudaMemcpyAsync(&e, a.err, 8, cudaMemcpyDeviceToHost, s));
+        VV_CUDA(cudaStreamSynchronize(s));
+        if (e) throw ApiError{VVGPU_ERR_TIMEOUT, "near-field staging wait timed out"};
     } else {
         KernelTimer kt(c, VVGPU_T_CONVECTIVE);
         k_conv64<8><<<grid, CW * 32, 0, s>>>(a);

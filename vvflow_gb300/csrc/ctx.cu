@@ -256,6 +256,12 @@ int vvgpu_set_eps_round_limit(vvgpu_ctx* h, int64_t max_rounds) {
     API_END
 }
 
+int vvgpu_set_wait_limit(vvgpu_ctx* h, uint32_t spins) {
+    API_BEGIN(h)
+    c.wait_spins = spins;
+    API_END
+}
+
 int vvgpu_set_kernel_timing(vvgpu_ctx* h, int on) {
     API_BEGIN(h)
     collect_kernel_timing(c);

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/vvgpu.h"
+#include "stage.cuh"
 
 namespace vvgpu {
 
@@ -129,6 +130,7 @@ struct Ctx {
     bool in_pending = false;
     // fixed-point rounds the epsilon/merge pass may take (vvgpu_set_eps_round_limit)
     int64_t eps_max_rounds = 4096;
+    uint32_t wait_spins = STAGE_SPINS;  // polls of one shared-memory staging wait
 
     // segments (host copies of geometry are kept for body bookkeeping)
     int64_t m = 0;
@@ -244,6 +246,9 @@ struct Ctx {
     DArr<float4> src32;             // per vortex: x, y in own leaf frame, g, eps^2
     DArr<float2> src_k;             // per vortex: anchor of its leaf
     DArr<float> src_ie;             // per vortex: (float)_1_eps
+    DArr<float4> src_a4;            // per vortex: anchor of its leaf (x, y, 0, 0), 16-byte records
+    DArr<int2> run_js;              // per near run: first source slot, offset in its leaf's near sequence
+    DArr<int32_t> leaf_tot;         // per leaf: length of its near sequence
     DArr<float4> lf_dbox;           // per leaf (diffusive): box of non-zero vortices and segment centres
 
     // SLAE

@@ -94,6 +94,7 @@ SIGNATURES = {
     "vvgpu_synchronize": (C.c_int, [_H]),
     "vvgpu_get_stats": (C.c_int, [_H, C.POINTER(Stats)]),
     "vvgpu_set_eps_round_limit": (C.c_int, [_H, C.c_int64]),
+    "vvgpu_set_wait_limit": (C.c_int, [_H, C.c_uint32]),
     "vvgpu_set_kernel_timing": (C.c_int, [_H, C.c_int]),
     "vvgpu_get_kernel_timing": (C.c_int, [_H, _D, _I64]),
     "vvgpu_set_params": (C.c_int, [_H] + [C.c_double] * 8),
@@ -267,6 +268,13 @@ class GpuSpace:
 
     def set_eps_round_limit(self, max_rounds: int):
         self._ok(self.lib.vvgpu_set_eps_round_limit(self.h, int(max_rounds)), "set_eps_round_limit")
+
+    STAGE_SPINS = 1 << 22  # default polls of one staging wait
+
+    def set_wait_limit(self, spins: int = STAGE_SPINS):
+        """polls of one shared-memory staging wait of the FP32 near field (0: every wait
+        runs out and the call raises VVGPU_ERR_TIMEOUT)"""
+        self._ok(self.lib.vvgpu_set_wait_limit(self.h, int(spins)), "set_wait_limit")
 
     def set_params(self, re, dt, inf_vx=1.0, inf_vy=0.0, inf_g=0.0, time=0.0, gx=0.0, gy=0.0):
         self._ok(self.lib.vvgpu_set_params(self.h, re, dt, inf_vx, inf_vy, inf_g, time, gx, gy), "set_params")
