@@ -235,7 +235,7 @@ int vvgpu_velocity_points(vvgpu_ctx* ctx, int64_t n, const double* px, const dou
  * in one fixed device array of VVGPU_NOALLOC_MAX_POINTS points that every call shares: at
  * most that many points per call (VVGPU_ERR_LIMIT otherwise), and calls whose GPU work
  * overlaps race on the array.  The first call on each device looks the array's device
- * address up (cudaGetSymbolAddress); make it before any stream capture.  It reads the near
+ * address up (cudaGetSymbolAddress).  It reads the near
  * lists of every leaf, which the tree builds on its first vvgpu_eps, vvgpu_convective,
  * vvgpu_diffusive or vvgpu_velocity_points call; before that it returns VVGPU_ERR_STATE. */
 #define VVGPU_NOALLOC_MAX_POINTS 16384

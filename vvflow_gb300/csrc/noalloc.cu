@@ -9,8 +9,8 @@
 // The array is a file-scope __device__ object of VVGPU_NOALLOC_MAX_POINTS x 4 doubles
 // (512 KiB).  Every GPU that loads the library holds it until the process exits.  Host code
 // cannot use the array's name as a device address, so the first call on each device, with
-// that device current, looks the address up with cudaGetSymbolAddress and keeps it; make
-// that first call before any stream capture.  All calls share the one array and it keeps
+// that device current, looks the address up with cudaGetSymbolAddress and keeps it.  All
+// calls share the one array and it keeps
 // the last call's contents (every call overwrites the points and results it uses, so
 // nothing needs clearing); calls whose GPU work overlaps, from different contexts or
 // streams, race on it.
