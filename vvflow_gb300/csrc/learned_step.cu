@@ -24,6 +24,7 @@
 // the plain tree at the judge's criterion (near/far walk again, plain expansion).
 #include "frame.cuh"
 #include "mlp.cuh"
+#include "pair.cuh"
 
 namespace vvgpu {
 
@@ -94,30 +95,6 @@ __device__ __forceinline__ float tanh_fast(float x) {
     return r;
 }
 
-// Packed FP32 pairs (sm_100-family f32x2 arithmetic: one instruction for two lanes' worth)
-__device__ __forceinline__ uint64_t f2(float a, float b) {
-    uint64_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void uf2(uint64_t v, float& a, float& b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ uint64_t fadd2(uint64_t a, uint64_t b) {
-    uint64_t d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ uint64_t fmul2(uint64_t a, uint64_t b) {
-    uint64_t d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
-    uint64_t d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
 // The network's tanh-form GELU of (z0 + b0, z1 + b1) with the hardware tanh, rounded to a
 // BF16 pair (the rounding is far coarser than the approximation)
 __device__ __forceinline__ uint32_t gelu2_bf16(float z0, float z1, float2 b) {
