@@ -73,6 +73,11 @@ def parse():
                          "cylinder simulations advanced together (vvgpu_batch_step); learned: the far-field MLP "
                          "trained on cylinder-annulus runs and evaluated at theta = 0.8 on the 4M cylinder wake")
     ap.add_argument("--instances", type=int, default=256, help="--config batched: number of simulations")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="wake4m: skip the learned-form measurement on the same workload")
+    ap.add_argument("--step-learn-runs", type=int, default=4,
+                    help="wake4m: cylinder-annulus runs whose (cell, target) pairs train the network")
+    ap.add_argument("--step-learn-epochs", type=int, default=4, help="wake4m: training epochs of the network")
     return ap.parse_args()
 
 
@@ -226,6 +231,116 @@ def hot_path(S, wl, mn, mx):
     S.convective()
     S.diffusive()
     S.tree_destroy()
+
+
+def learned_in_step(args, make, restore, wl, mn, mx, state, idx, ux, uy, rel, ms64):
+    """The learned form on the headline workload: the far-field network (trained here on the
+    GPU, on cylinder-annulus runs the workload does not contain) in every step at theta 0.8
+    (farCriteria 3.125), judged on 4096 sampled vortices per step by the plain theta 0.5
+    tree and reverted above the bound; its step time against the plain FP64 step, and the
+    convective error against the FP64 direct sum on one shared state (the list after a plain
+    step's epsilon/merge pass), beside the plain FP32 trees at theta 0.8 and 0.5."""
+    import torch
+
+    from vvflow_gb300 import workloads as W
+    from vvflow_gb300.vvgpu import VVGPU_FP32, VVGPU_FP64, GpuSpace, Mlp
+
+    FC08, FC05 = 3.125, wl.far_criteria
+    M = Mlp(seed=1)
+    t0 = time.time()
+    nsamp = 0
+    for r in range(args.step_learn_runs):
+        tw = W.cylinder_annulus(20000, 500, seed=1000 + r)
+        T = GpuSpace(VVGPU_FP64)
+        T.load(tw)
+        tmn, tmx = tw.node_sizes()
+        T.tree_build(FC08, tmn, tmx)
+        nsamp += M.add_samples(T, tw.x, tw.y)
+        T.tree_destroy()
+        T.close()
+    gen_s = time.time() - t0
+    M.fit_norm()
+    torch.cuda.synchronize()
+    t0 = time.time()
+    losses = M.train(epochs=args.step_learn_epochs, batch=8192, lr=3e-3, seed=5)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+
+    verdicts = []
+
+    def step(S):
+        S.tree_build(FC08, mn, mx)
+        S.slae()
+        S.tree_destroy()
+        S.vortex_shed()
+        S.tree_build(FC08, mn, mx)
+        S.eps(True)
+        verdicts.append(S.convective_learned(M, targets=4096, far_criteria=FC05, bound=args.judge_bound,
+                                             seed=len(verdicts) + 1))
+        S.diffusive()
+        S.tree_destroy()
+
+    S = make(VVGPU_FP32)
+    S.keep_far_lists(True)
+    for _ in range(args.warmup):
+        restore(S)
+        step(S)
+    verdicts.clear()
+    S.set_kernel_timing(True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        restore(S)
+        step(S)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    kt = {k: round(v[0] / args.steps, 4) for k, v in S.kernel_timing().items() if v[1]}
+    st = S.stats()
+    S.close()
+
+    def conv_err(fc, learned):
+        C = make(VVGPU_FP32)
+        C.keep_far_lists(learned)
+        C.set_vortices(state["x"], state["y"], state["g"], state["ie"])
+        C.tree_build(fc, mn, mx)
+        if learned:
+            C.convective_learned(M, targets=0)
+        else:
+            C.convective()
+        v = C.vortices()
+        C.tree_destroy()
+        C.close()
+        pos = np.empty(len(v["orig"]), np.int64)
+        pos[v["orig"]] = np.arange(len(v["orig"]))
+        k = pos[idx]
+        emax, erms = rel(v["vx"][k], v["vy"][k], ux, uy)
+        return {"max_rel": emax, "rms_rel": erms}
+
+    acc = {"learned_fp32_theta_0.8": conv_err(FC08, True), "plain_fp32_theta_0.8": conv_err(FC08, False),
+           "plain_fp32_theta_0.5": conv_err(FC05, False)}
+    M.close()
+    n = wl.n
+    return {
+        "value": n / (ms / 1e3), "unit": "vortex-steps/s", "ms_per_step": ms, "steps": args.steps,
+        "warmup": args.warmup,
+        "form": "FP32 pairwise, theta 0.8 (farCriteria 3.125) with the learned far-field correction "
+                "(20-64-64-2 tanh-GELU, BF16 tensor cores, FP32 accumulate); judge: plain theta 0.5 "
+                "tree on 4096 sampled vortices per step, revert above the bound",
+        "over_plain_fp64_theta_0.5": (ms64 / ms) if ms64 else None,
+        "judge": {"steps": len(verdicts), "reverted": int(sum(v["reverted"] for v in verdicts)),
+                  "gap_rms_max": max(v["gap_rms"] for v in verdicts), "pairs_per_step": verdicts[-1]["pairs"],
+                  "judged_per_step": verdicts[-1]["judged"], "bound": args.judge_bound},
+        "convective_error_vs_fp64_direct": acc,
+        "kernel_ms_per_step": kt,
+        "tree": {k: st[k] for k in ("n_leaves", "near_pairs", "far_pairs", "merged", "walk_loads")},
+        "training": {"pairs": int(nsamp), "runs": args.step_learn_runs, "sample_seconds": round(gen_s, 2),
+                     "epochs": args.step_learn_epochs, "train_seconds": round(train_s, 2),
+                     "loss_first_last": [float(losses[0]), float(losses[-1])],
+                     "data": "FP64 direct-sum labels of seeded cylinder-annulus runs (20k vortices, "
+                             "500 segments), not of this workload"},
+    }
 
 
 def config_dict(wl, world):
@@ -563,6 +678,7 @@ def gpu_arm(args):
 
     # ---- plain FP64 path and accuracy ---------------------------------------------------
     fp64 = None
+    learned = None
     acc = {}
     if args.fp64_steps > 0:
         S64 = make(VVGPU_FP64)
@@ -628,6 +744,9 @@ def gpu_arm(args):
             acc["oracle_bit_exact"] = bool(acc["oracle"]["fp64"]["bit_exact"] and acc["oracle"]["fp32"]["bit_exact"])
         fp64 = {"value": world * N / (ms64 / 1e3), "ms_per_step": ms64, "steps": args.fp64_steps,
                 "fp32_speedup": ms64 / ms_max}
+        if not args.no_learned:
+            state = {"x": r64["eps_x"], "y": r64["eps_y"], "g": r64["eps_g"], "ie": r64["eps_inv_eps"]}
+            learned = learned_in_step(args, make, restore, wl, mn, mx, state, idx, ux, uy, rel, ms64)
 
     # ---- rooflines: every timed kernel, the longest one as the headline -----------------
     hbm, hbm_src = hbm_peak()
@@ -662,7 +781,7 @@ def gpu_arm(args):
             "config": config_dict(wl, world),
             "path": "FP32 pairwise sums in local frames with compensated accumulation; FP64 decisions "
                     "(tree, lists, epsilon, merges) bit-exact with the reference",
-            "fp64": fp64, "accuracy": acc, "phases_ms": phases,
+            "fp64": fp64, "learned": learned, "accuracy": acc, "phases_ms": phases,
             "kernel_ms_per_step": {k: round(v[0], 4) for k, v in kt.items()},
             "kernel_launches_per_step": {k: v[1] for k, v in kt.items()},
             "tree": dict({k: stp[k] for k in ("n_leaves", "n_nodes", "tree_depth", "near_runs", "merge_rounds",
