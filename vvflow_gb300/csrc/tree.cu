@@ -121,12 +121,14 @@ __device__ __forceinline__ int decide_vals(double4 gm, int64_t nv, int64_t ns, i
     return s;
 }
 
-// Largest node (vortices, no segments) whose whole subtree one block builds (k_subtree).
+// Largest node whose whole subtree one block builds (k_subtree): at most SUB_N vortices,
+// or, with segments, at most SUB_N vortices and segments together.
 constexpr int SUB_N = 1024;
 
 // split[k]: 0 leaf, 1 split by the level loop, 2 split by k_subtree (no segments and at most
-// SUB_N vortices: the node and its descendants are finished after the loop).  Returns 1 for
-// a split by the level loop (the flag that allocates its children in this pass).
+// SUB_N vortices), 3 split by k_subtree with segments (vortices + segments at most SUB_N):
+// the node and its descendants are finished after the loop.  Returns 1 for a split by the
+// level loop (the flag that allocates its children in this pass).
 __device__ __forceinline__ int decide_node(int64_t k, const double4* __restrict__ geom, const int32_t* __restrict__ vf,
                                            const int32_t* __restrict__ vl, const int32_t* __restrict__ sf,
                                            const int32_t* __restrict__ sl, const int32_t* __restrict__ depth,
@@ -137,6 +139,7 @@ __device__ __forceinline__ int decide_node(int64_t k, const double4* __restrict_
     double pv;
     int s = decide_vals(geom[k], nv, ns, depth[k], min_node, max_node, err, ax, pv);
     if (s && ns == 0 && nv <= SUB_N) s = 2;
+    else if (s && nv + ns <= SUB_N) s = 3;
     split[k] = s;
     axis[k] = ax;
     pivot[k] = pv;
@@ -691,11 +694,14 @@ static_assert(SUB_N % SUB_T == 0 && SUB_NW <= 32, "subtree block shape");
 struct SubNode {  // a node made by k_subtree, before its final id is known
     double4 geom;  // centre x, y, h, w (Stretch)
     int64_t path;
-    int32_t vf, vl, ch1, parent, depth, pad;
+    int32_t vf, vl, sf, sl, ch1, parent, depth, pad;
 };
-static_assert(sizeof(SubNode) == 64, "SubNode is one 64-byte line");
+static_assert(sizeof(SubNode) == 80, "SubNode is 80 bytes (2.5 double4)");
 
 constexpr size_t SUB_SMEM = (size_t)SUB_N * (5 * 8 + 2 * 4 + 12 * 2 + 2) + 64 * 4;
+// with segments: per segment slot its centre (x, y), global id, and for two levels its
+// local index and node slot; per level node (two levels) its segment start and count
+constexpr size_t SUB_SMEM_SEG = SUB_SMEM + (size_t)SUB_N * (2 * 8 + 4 + 2 * 2 + 2 * 2 + 2 * 2 + 2 * 2);
 
 // Exclusive prefix of a[0 .. SUB_N) in place (thread-contiguous runs), a[SUB_N] = total.
 __device__ __forceinline__ int32_t sub_exscan(int32_t* a, int32_t* wt) {
@@ -731,21 +737,24 @@ __device__ __forceinline__ int32_t sub_exscan(int32_t* a, int32_t* wt) {
 
 __global__ void k_defer_flags(int64_t nn, const int32_t* __restrict__ split, int32_t* flags) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nn) flags[k] = split[k] == 2;
+    if (k < nn) flags[k] = split[k] >= 2;
 }
 __global__ void k_defer_list(int64_t nn, const int32_t* __restrict__ split, const int32_t* __restrict__ pos,
                              int32_t* roots) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nn && split[k] == 2) roots[pos[k]] = (int32_t)k;
+    if (k < nn && split[k] >= 2) roots[pos[k]] = (int32_t)k;
 }
 
+template <bool SEG>
 __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ roots,
                                                    const int32_t* __restrict__ vf, const int32_t* __restrict__ vl,
+                                                   const int32_t* __restrict__ sf, const int32_t* __restrict__ sl,
                                                    const int32_t* __restrict__ depth, const int64_t* __restrict__ path,
                                                    const double* __restrict__ pivot, const int32_t* __restrict__ axis,
                                                    double min_node, double max_node, double* x, double* y,
-                                                   int32_t* perm, SubNode* scratch, int32_t* nnew, int32_t* err,
-                                                   int32_t* maxdepth) {
+                                                   int32_t* perm, int32_t* seg_order, const double* __restrict__ rx,
+                                                   const double* __restrict__ ry, SubNode* scratch, int32_t* nnew,
+                                                   int32_t* err, int32_t* maxdepth) {
     extern __shared__ __align__(16) unsigned char smem[];
     // per vortex: position, permutation, level-node slot (two levels: -1 = in a finished
     // leaf), prefix, pairing tables.  Per level node: pivot, axis, split (the next level's
@@ -770,15 +779,26 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
     int16_t* par = cH + SUB_N;
     int8_t* lax = (int8_t*)(par + SUB_N);
     int8_t* lsp = lax + SUB_N;
+    // segments (SEG): centres by local index, global ids; for two levels the local index at
+    // each position, the node slot at each position, and each level node's segment range
+    double* gx = (double*)(smem + SUB_SMEM);
+    double* gy = gx + SUB_N;
+    int32_t* gid = (int32_t*)(gy + SUB_N);
+    int16_t* gix = (int16_t*)(gid + SUB_N);  // [2][SUB_N]
+    int16_t* gen = gix + 2 * SUB_N;          // [2][SUB_N]
+    int16_t* lsf = gen + 2 * SUB_N;          // [2][SUB_N]
+    int16_t* lsn = lsf + 2 * SUB_N;          // [2][SUB_N]
 
     const int t = threadIdx.x;
     const int32_t root = roots[blockIdx.x];
     const int32_t f0 = vf[root], nr = vl[root] - f0;
-    if (nr > SUB_N || nr < 1) {  // not a deferred node (cannot happen): leave it alone
+    const int32_t s0 = sf[root], ns = sl[root] - s0;
+    if ((ns > 0) != SEG) return;  // the other kernel's subtree
+    if (SEG ? (nr + ns > SUB_N) : (nr > SUB_N || nr < 1)) {  // not a deferred node (cannot happen)
         if (t == 0) { atomicExch(err, 3); nnew[blockIdx.x] = 0; }
         return;
     }
-    SubNode* rec = scratch + 2 * (size_t)f0;  // local id u at rec[u], u < 2 nr
+    SubNode* rec = scratch + 2 * ((size_t)f0 + (size_t)s0);  // local id u at rec[u], u < 2 (nr + ns)
     for (int i = t; i < SUB_N; i += SUB_T) {
         if (i < nr) {
             sx[i] = x[f0 + i];
@@ -788,10 +808,23 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
         } else {
             en[i] = -1;
         }
+        if (SEG) {
+            if (i < ns) {
+                const int32_t sg = seg_order[s0 + i];
+                gid[i] = sg;
+                gx[i] = rx[sg];
+                gy[i] = ry[sg];
+                gix[i] = (int16_t)i;
+                gen[i] = 0;
+            } else {
+                gen[i] = -1;
+            }
+        }
     }
     if (t == 0) {
         lvf[0] = 0; ln[0] = (int16_t)nr; lkp[0] = lt_key_of(pivot[root]); lax[0] = (int8_t)axis[root];
         lsp[0] = 1; lpath[0] = path[root];
+        if (SEG) { lsf[0] = 0; lsn[0] = (int16_t)ns; }
     }
     int cur = 0, ncur = 1, base = 0, next_lid = 1;  // base: local id of the level's slot 0
     int32_t dep = depth[root];
@@ -803,7 +836,7 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
         __syncthreads();
         const int nsplit = sub_exscan(pre, wt);
         if (nsplit == 0) break;
-        if (next_lid + 2 * nsplit > 2 * nr) {
+        if (next_lid + 2 * nsplit > 2 * (nr + ns)) {
             // only a chain of splits that leave one side empty (a box midpoint rounding onto
             // its lower edge) outgrows 2 n - 1 nodes; the level loop reports it as too deep
             if (t == 0) atomicExch(err, 1);
@@ -873,6 +906,52 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
             sx[ib] = tx; sy[ib] = ty; sp[ib] = tp;
         }
         __syncthreads();
+        if (SEG) {
+            // (g) the segment lists of the split nodes, split stably (TSortedTree.cpp:139-148):
+            // low flags (centre key < pivot) and their prefix, then each segment's position
+            // and child slot in the next level
+#pragma unroll
+            for (int e = 0; e < SUB_E; e++) {
+                const int i = e * SUB_T + t;
+                const int nd = gen[co + i];
+                bool low = false;
+                if (nd >= 0 && lsp[nd]) {
+                    const int li = gix[co + i];
+                    low = lt_key(lax[nd] ? gx[li] : gy[li], lkp[nd]);
+                }
+                pre[i] = low ? 1 : 0;
+            }
+            __syncthreads();
+            sub_exscan(pre, wt);
+            for (int j = t; j < ncur; j += SUB_T) {
+                if (!lsp[j]) continue;
+                const int f = lsf[co + j], n = lsn[co + j];
+                const int L = pre[f + n] - pre[f];
+                cH[j] = (int16_t)L;  // the vortex swaps are done: cH now holds the segment lows
+                const int r = rank[j];
+                lsf[no + 2 * r] = (int16_t)f;
+                lsn[no + 2 * r] = (int16_t)L;
+                lsf[no + 2 * r + 1] = (int16_t)(f + L);
+                lsn[no + 2 * r + 1] = (int16_t)(n - L);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int e = 0; e < SUB_E; e++) {
+                const int i = e * SUB_T + t;
+                const int nd = gen[co + i];
+                if (nd >= 0 && lsp[nd]) {
+                    const int f = lsf[co + nd], L = cH[nd], before = pre[i] - pre[f];
+                    const bool low = pre[i + 1] != pre[i];
+                    const int nq = low ? f + before : f + L + ((i - f) - before);
+                    gix[no + nq] = gix[co + i];
+                    gen[no + nq] = (int16_t)(2 * rank[nd] + (low ? 0 : 1));
+                } else {
+                    gix[no + i] = gix[co + i];
+                    gen[no + i] = -1;
+                }
+            }
+            __syncthreads();
+        }
         // (f) the children: box (a group of G lanes per child), geometry, decision, record
         const int nch = 2 * nsplit;
         const int G = nch <= SUB_NW ? 32 : nch <= 2 * SUB_NW ? 16 : nch <= 4 * SUB_NW ? 8 : 4;
@@ -881,11 +960,19 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
             const int cs = c0 + t / G;
             unsigned long long b4[4];
             bbox_init(b4);
-            int f = 0, n = 0;
+            int f = 0, n = 0, gf = 0, gn = 0;
             if (cs < nch) {
                 f = lvf[no + cs];
                 n = ln[no + cs];
                 for (int i = f + gl; i < f + n; i += G) bbox_acc(b4, sx[i], sy[i]);
+                if (SEG) {
+                    gf = lsf[no + cs];
+                    gn = lsn[no + cs];
+                    for (int i = gf + gl; i < gf + gn; i += G) {
+                        const int li = gix[no + i];
+                        bbox_acc(b4, gx[li], gy[li]);
+                    }
+                }
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -899,7 +986,7 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
                 const double4 gm = geom_from_bbox(b4);
                 int32_t ax;
                 double pv;
-                lsp[cs] = (int8_t)decide_vals(gm, n, 0, dep + 1, min_node, max_node, err, ax, pv);
+                lsp[cs] = (int8_t)decide_vals(gm, n, gn, dep + 1, min_node, max_node, err, ax, pv);
                 lax[cs] = (int8_t)ax;
                 lkp[cs] = lt_key_of(pv);
                 SubNode o;
@@ -907,6 +994,8 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
                 o.path = lpath[no + cs];
                 o.vf = f0 + f;
                 o.vl = f0 + f + n;
+                o.sf = s0 + gf;
+                o.sl = s0 + gf + gn;
                 o.ch1 = -1;
                 o.parent = base + par[cs];
                 o.depth = dep + 1;
@@ -926,6 +1015,8 @@ __global__ void __launch_bounds__(SUB_T) k_subtree(const int32_t* __restrict__ r
         y[f0 + i] = sy[i];
         perm[f0 + i] = sp[i];
     }
+    if (SEG)
+        for (int i = t; i < ns; i += SUB_T) seg_order[s0 + i] = gid[gix[cur * SUB_N + i]];
     if (t == 0) {
         nnew[blockIdx.x] = next_lid - 1;
         atomicMax(maxdepth, dep);
@@ -940,8 +1031,7 @@ __global__ void k_subtree_place(const int32_t* __restrict__ roots, const int32_t
     const int32_t root = roots[blockIdx.x];
     const int32_t cnt = nnew[blockIdx.x];
     const int64_t b = base + pos[blockIdx.x] - 1;  // id of local node u >= 1 is b + u
-    const SubNode* rec = scratch + 2 * (size_t)vf[root];
-    const int32_t s0 = sf[root];
+    const SubNode* rec = scratch + 2 * ((size_t)vf[root] + (size_t)sf[root]);
     if (threadIdx.x == 0) ch1[root] = cnt > 0 ? (int32_t)(b + 1) : -1;
     for (int32_t u = 1 + threadIdx.x; u <= cnt; u += blockDim.x) {
         const SubNode o = rec[u];
@@ -949,8 +1039,8 @@ __global__ void k_subtree_place(const int32_t* __restrict__ roots, const int32_t
         geom[g] = o.geom;
         vf[g] = o.vf;
         vl[g] = o.vl;
-        sf[g] = s0;
-        sl[g] = s0;
+        sf[g] = o.sf;
+        sl[g] = o.sl;
         ch1[g] = o.ch1 >= 0 ? (int32_t)(b + o.ch1) : -1;
         depth[g] = o.depth;
         path[g] = o.path;
@@ -994,12 +1084,12 @@ __device__ __forceinline__ void combine_cm(const double* a, const double* b, dou
 // node the second child to arrive combines both children (always in the order ch1, ch1 + 1,
 // so the result does not depend on which arrives last) and climbs on.
 // Climbs start at the leaves of nodes [0, nn), and with `split` also at the subtree roots
-// (split == 2), whose subtrees k_subtree_cm has completed.
+// (split >= 2), whose subtrees k_subtree_cm has completed.
 __global__ void k_tree_cm(int64_t nn, const int32_t* __restrict__ ch1, const int32_t* __restrict__ split,
                           const int32_t* __restrict__ parent, const double4* __restrict__ geom, double* cm,
                           int32_t* lc, int32_t* arrive) {
     const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k0 >= nn || (ch1[k0] >= 0 && !(split && split[k0] == 2))) return;
+    if (k0 >= nn || (ch1[k0] >= 0 && !(split && split[k0] >= 2))) return;
     int32_t k = (int32_t)k0;
     for (int it = 0; it <= MAX_DEPTH; it++) {
         const int32_t p = parent[k];
@@ -1294,14 +1384,28 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
             int32_t* pos = nnew + ndef + 1;
             k_defer_list<<<grid_for(nn0, TB), TB, 0, s>>>(nn0, c.nd_split.p, c.scan.p, roots);
             VV_LAUNCH_CHECK();
-            c.sub_scratch.reserve(4 * (size_t)n + 2);
+            // two 80-byte records per vortex and per segment (2.5 double4 each)
+            c.sub_scratch.reserve(5 * (size_t)(n + m) + 4);
             SubNode* scratch = reinterpret_cast<SubNode*>(c.sub_scratch.p);
             int32_t* maxdep = (int32_t*)(c.counters.p + 5);
-            VV_CUDA(cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SUB_SMEM));
-            k_subtree<<<ndef, SUB_T, SUB_SMEM, s>>>(roots, c.nd_vf.p, c.nd_vl.p, c.nd_depth.p, c.nd_path.p,
-                                                    c.nd_pivot.p, c.nd_axis.p, min_node, max_node, c.x.p, c.y.p,
-                                                    c.perm.p, scratch, nnew, err, maxdep);
+            // every root goes to both kernels; each builds the subtrees of its kind (without
+            // or with segments) and leaves the others
+            VV_CUDA(cudaFuncSetAttribute(k_subtree<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SUB_SMEM));
+            k_subtree<false><<<ndef, SUB_T, SUB_SMEM, s>>>(
+                roots, c.nd_vf.p, c.nd_vl.p, c.nd_sf.p, c.nd_sl.p, c.nd_depth.p, c.nd_path.p, c.nd_pivot.p,
+                c.nd_axis.p, min_node, max_node, c.x.p, c.y.p, c.perm.p, c.seg_order.p, c.s_rx.p, c.s_ry.p,
+                scratch, nnew, err, maxdep);
             VV_LAUNCH_CHECK();
+            if (m > 0) {
+                VV_CUDA(cudaFuncSetAttribute(k_subtree<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)SUB_SMEM_SEG));
+                k_subtree<true><<<ndef, SUB_T, SUB_SMEM_SEG, s>>>(
+                    roots, c.nd_vf.p, c.nd_vl.p, c.nd_sf.p, c.nd_sl.p, c.nd_depth.p, c.nd_path.p, c.nd_pivot.p,
+                    c.nd_axis.p, min_node, max_node, c.x.p, c.y.p, c.perm.p, c.seg_order.p, c.s_rx.p, c.s_ry.p,
+                    scratch, nnew, err, maxdep);
+                VV_LAUNCH_CHECK();
+            }
             exclusive_scan(c, nnew, pos, ndef);
             const int32_t added = read_i32(c, pos + ndef);
             ensure_nodes(nn0 + added + 1);
