@@ -162,16 +162,41 @@ __global__ void __launch_bounds__(TILE, PT_CTAS) k_mlp_far_pairs(int64_t np, con
     uint32_t phase = 0, lost = 2;  // lost: the phase whose completion a timed-out wait missed
     bool ok = true;
     const int64_t ntiles = (np + TILE - 1) / TILE;
+    // The gather is pipelined over the tiles: the pair indices of the next tile are read at
+    // the start of a tile and its node records right after the tile's first MMA is issued,
+    // so they arrive while the tile's layers run; the inputs are formed at the next tile.
+    auto fetch_idx = [&](int64_t tile, int32_t& node, int32_t& lnode) {
+        const int64_t p = tile * TILE + tid;
+        node = lnode = -1;
+        if (tile < ntiles && p < np) {
+            node = pnode[p];
+            lnode = plnode[p];
+        }
+    };
+    uint4 r0 = make_uint4(0, 0, 0, 0), r1 = r0, r2 = r0, r3 = r0, rl = r0;  // records of the tile
+    auto fetch_rec = [&](int32_t node, int32_t lnode) {
+        if (node >= 0) {
+            const uint4* rn = nrec + 4 * (size_t)node;
+            r0 = rn[0];
+            r1 = rn[1];
+            r2 = rn[2];
+            r3 = rn[3];
+            rl = nrec[4 * (size_t)lnode + 3];  // the leaf's centre and anchor
+        }
+    };
+    int32_t nx, nxl;
+    fetch_idx(blockIdx.x, nx, nxl);
+    fetch_rec(nx, nxl);
     for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const int64_t p = tile * TILE + tid;
+        const bool live = nx >= 0;
+        fetch_idx(tile + gridDim.x, nx, nxl);
         uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0, c2 = c0;
         float back = 0.f;
-        if (p < np) {
-            const uint4* rn = nrec + 4 * (size_t)pnode[p];
-            c0 = rn[0];
-            c1 = rn[1];
-            const uint4 a = rn[2], gN = rn[3];
-            const uint4 gL = nrec[4 * (size_t)plnode[p] + 3];  // the leaf's centre and anchor
+        if (live) {
+            c0 = r0;
+            c1 = r1;
+            const uint4 a = r2, gN = r3, gL = rl;
             // the leaf centre's offset from the node centre in FP32 from the node frames (the
             // shift between two anchors is exact); the inputs are rounded to BF16 anyway
             const float dx = (__uint_as_float(gL.z) - __uint_as_float(gN.z)) +
@@ -195,6 +220,7 @@ __global__ void __launch_bounds__(TILE, PT_CTAS) k_mlp_far_pairs(int64_t np, con
         __syncthreads();
         fence_after();
         if (tid == 0) { mma_issue(tm, x0, S.w + I_W1, KIN, HID, false); mma_commit(&S.mbar); }
+        fetch_rec(nx, nxl);
         ok = __syncthreads_and(mbar_wait(&S.mbar, phase, spins));
         if (!ok) lost = phase;
         phase ^= 1;
