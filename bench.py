@@ -414,12 +414,20 @@ def rooflines(stp, sizes, kt, N, peaks):
       8-target chunk, 48 B per target (record read, velocity read and written), 8 B per near
       run; HBM and L2.
     * k_eps_round: 16 B per candidate record read by the FP32 filters plus 64 B per target
-      evaluation (record, previous outcome and new outcome); HBM and L2."""
+      evaluation (record, previous outcome and new outcome); HBM and L2.
+    Beside them, frac_mufu: the special-function unit operations the pair arithmetic needs
+    (one reciprocal per convective near pair, two per far node of the walk, a reciprocal
+    square root and an exp2 per diffusive candidate pair) against the nominal 16 per clock
+    per SM at the SM clock measured in the run.  It is reported, not used as the binding."""
     fp32, hbm, l2 = peaks["fp32_tflops"], peaks["hbm_gbs"], peaks["l2_gbs"]
+    mufu = peaks.get("mufu_gops")
     out = {}
 
     def entry(kernel, ms, l2_only=False, **w):
         e = {"kernel": kernel, "launch_ms": ms}
+        if "mufu" in w and mufu:
+            a = w["mufu"] / (ms / 1e3) / 1e9
+            e.update({"mufu_ops_per_launch": w["mufu"], "achieved_mufu_gops": a, "frac_mufu": a / mufu})
         fr = {}
         if "flops" in w:
             a = w["flops"] / (ms / 1e3) / 1e12
@@ -437,16 +445,18 @@ def rooflines(stp, sizes, kt, N, peaks):
 
     if kt["convective"][1]:
         out["k_conv32"] = entry("k_conv32 (convective near field)", kt["convective"][0],
-                                flops=12 * stp["near_pairs"])
+                                flops=12 * stp["near_pairs"], mufu=stp["near_pairs"])
     if kt["walk"][1]:
         visits = 2 * (stp["far_pairs"] // 2 + sizes["near_leaves"]) - stp["n_leaves"]
         out["k_walk_warp"] = entry("k_walk_warp (near/far walk and far-field coefficients)", kt["walk"][0],
-                                   l2_only=True, flops=24 * stp["far_pairs"], bytes=64 * stp["walk_loads"])
+                                   l2_only=True, flops=24 * stp["far_pairs"], bytes=64 * stp["walk_loads"],
+                                   mufu=stp["far_pairs"])
         out["k_walk_warp"]["per_leaf_walk_visits"] = visits
         out["k_walk_warp"]["warp_record_loads"] = stp["walk_loads"]
     if kt["diffusive"][1]:
         out["k_diff32"] = entry("k_diff32 (diffusive)", kt["diffusive"][0],
-                                bytes=16 * stp["diff_sources"] + 48 * N + 8 * stp["near_runs"])
+                                bytes=16 * stp["diff_sources"] + 48 * N + 8 * stp["near_runs"],
+                                mufu=2 * stp["diff_candidates"])
     if kt["eps_round"][1]:
         out["k_eps_round"] = entry(f"k_eps_round (two-nearest searches, {kt['eps_round'][1]} rounds)",
                                    kt["eps_round"][0], bytes=16 * stp["eps_records"] + 64 * stp["eps_evaluations"])
@@ -751,6 +761,9 @@ def gpu_arm(args):
     # ---- rooflines: every timed kernel, the longest one as the headline -----------------
     hbm, hbm_src = hbm_peak()
     peaks = {"fp32_tflops": measure_fp32_peak(torch, dev), "hbm_gbs": hbm, "l2_gbs": measure_l2_copy(torch, dev)}
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    if clocks and clocks.get("sm_mhz"):
+        peaks["mufu_gops"] = 16 * sms * clocks["sm_mhz"] / 1e3  # nominal 16 per clock per SM
     roofs = rooflines(stp, sizes, kt, N, peaks)
     dom = max(roofs, key=lambda k: roofs[k]["launch_ms"]) if roofs else None
     roof = None
