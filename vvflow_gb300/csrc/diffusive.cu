@@ -314,14 +314,19 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
                                                __int_as_float(j));
                 }
                 __syncwarp();
-                for (int32_t k = sub; k < nst; k += LG) {
+                for (int32_t k0 = sub; k0 < nst;) {
+                  // at most 32 - since sources of this lane before the next fold
+                  const int32_t cnt = min(32 - since, (nst - k0 + LG - 1) / LG);
+                  const int32_t kend = k0 + cnt * LG;
+                  for (int32_t k = k0; k < kend; k += LG) {
                     const float4 sv = s_src[wq][k];
-                    if (sv.z == 0.f) continue;
                     const int32_t j = __float_as_int(sv.w);
-                    // a target's pair with itself is excluded by the reference's coincidence rule
+                    // a target's pair with itself is excluded by the reference's coincidence rule;
+                    // a source with g = 0 has no same-sign target
                     const int32_t jr = j - tb;
                     const unsigned self = (jr >= 0 && jr < DT) ? (1u << jr) : 0u;
-                    const unsigned same = (sv.z > 0.f ? pos : ~pos) & act & ~self;
+                    const unsigned sgn = sv.z > 0.f ? pos : (sv.z < 0.f ? ~pos : 0u);
+                    const unsigned same = sgn & act & ~self;
                     unsigned pend = 0;  // targets whose pair with this source goes to FP64
 #pragma unroll
                     for (int t = 0; t < DT; t++) {
@@ -355,15 +360,18 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
                                           d64[6 * t + 1][lane], d64[6 * t + 2][lane]);
                         }
                     }
-                    if (++since == 32) {
-                        since = 0;
+                  }
+                  k0 = kend;
+                  since += cnt;
+                  if (since == 32) {
+                      since = 0;
 #pragma unroll
-                        for (int t = 0; t < DT; t++) {
-                            acc_add(h2x[t], l2x[t], p2x[t]); p2x[t] = 0.f;
-                            acc_add(h2y[t], l2y[t], p2y[t]); p2y[t] = 0.f;
-                            acc_add(h1[t], l1[t], p1[t]); p1[t] = 0.f;
-                        }
-                    }
+                      for (int t = 0; t < DT; t++) {
+                          acc_add(h2x[t], l2x[t], p2x[t]); p2x[t] = 0.f;
+                          acc_add(h2y[t], l2y[t], p2y[t]); p2y[t] = 0.f;
+                          acc_add(h1[t], l1[t], p1[t]); p1[t] = 0.f;
+                      }
+                  }
                 }
                 __syncwarp();
             }
