@@ -163,6 +163,20 @@ int vvgpu_set_eps_round_limit(vvgpu_ctx* ctx, int64_t max_rounds);
  * VVGPU_ERR_TIMEOUT after its copies in flight have landed; the context stays usable
  * (0 polls: every wait runs out).  No counterpart in the reference (it has no GPU). */
 int vvgpu_set_wait_limit(vvgpu_ctx* ctx, uint32_t spins);
+/* Kernel shapes of the FP32 pair passes: sources per shared-memory tile of the convective
+ * near field (128, 192 or 256; default 192) and targets per lane of the diffusive pass (1
+ * or 2; default 1).  The variants compute the same sums in a different order of their FP32
+ * partial sums.  vvgpu_autotune_tiles times every shape on the context's current tree
+ * (built; after vvgpu_eps, where the pass would run) and keeps the fastest of each; the
+ * velocities and wall friction are left as they were.  ms (may be NULL) receives five
+ * device times in ms (convective at 128, 192, 256; diffusive at 1, 2 targets; the best of
+ * two runs each; -1 in an FP64 context, which has one shape).  vvgpu_set_autotune(ctx, 1)
+ * tunes at the next vvgpu_convective instead (vvgpu_batch_autotune uses it for every
+ * instance).  No counterpart in the reference (its OpenMP loops have no tile shapes). */
+int vvgpu_autotune_tiles(vvgpu_ctx* ctx, int32_t* conv_tile, int32_t* diff_targets, double* ms);
+int vvgpu_set_tiles(vvgpu_ctx* ctx, int32_t conv_tile, int32_t diff_targets);
+int vvgpu_get_tiles(vvgpu_ctx* ctx, int32_t* conv_tile, int32_t* diff_targets);
+int vvgpu_set_autotune(vvgpu_ctx* ctx, int on);
 /* Kernel timing on (1) or off (0); either clears the sums.  No counterpart in the
  * reference (it has no GPU). */
 int vvgpu_set_kernel_timing(vvgpu_ctx* ctx, int on);
@@ -290,8 +304,9 @@ typedef struct vvgpu_step_cfg {
  * (may be NULL) = its return code.  Returns the first non-zero status, else 0. */
 int vvgpu_batch_step(vvgpu_ctx* const* ctxs, int64_t count, const vvgpu_step_cfg* cfgs, int32_t nthreads,
                      double* step_ms, int32_t* status);
-/* Runs one batched step per candidate pool size (these steps advance the instances) and
- * returns the fastest in *best (its wall time in *best_ms, may be NULL). */
+/* Tunes every instance's kernel shapes in its next step (vvgpu_set_autotune), then runs
+ * one batched step per candidate pool size (these steps advance the instances) and returns
+ * the fastest in *best (its wall time in *best_ms, may be NULL). */
 int vvgpu_batch_autotune(vvgpu_ctx* const* ctxs, int64_t count, const vvgpu_step_cfg* cfgs,
                          const int32_t* candidates, int32_t ncand, int32_t* best, double* best_ms);
 

@@ -63,6 +63,9 @@ def test_gpu_batch_autotune_and_errors():
     batch = Batch(spaces, 8.0, [wl.node_sizes() for wl in wls])
     nt, ms = batch.autotune((1, 2, 3))
     assert nt in (1, 2, 3) and ms > 0
+    for S in spaces:  # every instance timed its own kernel shapes in the first step
+        t, d = S.tiles()
+        assert t in (128, 192, 256) and d in (1, 2)
     # a context with a tree left built fails its own step; the others still advance
     mn, mx = wls[1].node_sizes()
     spaces[1].tree_build(8.0, mn, mx)

@@ -7,7 +7,10 @@
 // processing time first keeps the tail short with sizes spread over 40x), and issues that
 // instance's launches on its stream, so the GPU runs many instances at once while the
 // per-level host reads of one instance's tree build overlap the kernels of the others.
-// vvgpu_batch_autotune times the pool sizes it is given on real steps and keeps the fastest.
+// vvgpu_batch_autotune first has every instance time its own kernel shapes in its next step
+// (sources per staged tile of the convective near field, targets per lane of the diffusive
+// pass; vvgpu_autotune_tiles), then times the pool sizes it is given on real steps and keeps
+// the fastest.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -94,6 +97,13 @@ extern "C" int vvgpu_batch_step(vvgpu_ctx* const* ctxs, int64_t count, const vvg
 extern "C" int vvgpu_batch_autotune(vvgpu_ctx* const* ctxs, int64_t count, const vvgpu_step_cfg* cfgs,
                                     const int32_t* candidates, int32_t ncand, int32_t* best, double* best_ms) {
     if (!candidates || ncand <= 0 || !best) return VVGPU_ERR_ARG;
+    if (count < 0 || (count > 0 && !ctxs)) return VVGPU_ERR_ARG;
+    // each instance's kernel shapes, timed on its own tree in the first step below
+    for (int64_t i = 0; i < count; i++) {
+        if (!ctxs[i]) return VVGPU_ERR_ARG;
+        const int rc = vvgpu_set_autotune(ctxs[i], 1);
+        if (rc) return rc;
+    }
     double bt = 0;
     int32_t bc = -1;
     for (int32_t k = 0; k < ncand; k++) {

@@ -258,9 +258,12 @@ __global__ void __launch_bounds__(CW * 32) k_conv64(ConvArgs a) {
 // lanes apply the current tile.  Each lane keeps plain FP32 partial sums over at most 32
 // of its sources and then folds them into a TwoSum-compensated pair.
 constexpr int TC32 = 8;
-constexpr int CT = 192;  // sources per staged tile
-constexpr size_t CONV32_SMEM = (size_t)CW * 2 * CT * 2 * sizeof(float4) + (size_t)CW * 2 * sizeof(uint64_t);
+// CT: sources per staged tile (128, 192 or 256; the context's choice, vvgpu_autotune_tiles)
+constexpr size_t conv32_smem(int ct) {
+    return (size_t)CW * 2 * ct * 2 * sizeof(float4) + (size_t)CW * 2 * sizeof(uint64_t);
+}
 
+template <int CT>
 __global__ void __launch_bounds__(CW * 32, 4) k_conv32(ConvArgs a) {
     extern __shared__ __align__(128) unsigned char conv_smem[];
     const int wq = threadIdx.x >> 5;
@@ -868,6 +871,7 @@ void count_near_pairs(Ctx& c) {
 
 void convective(Ctx& c) {
     if (c.n == 0 || c.nleaves == 0) return;
+    if (c.tune_pending) autotune_tiles(c, nullptr);  // the shapes of this and the later passes
     cudaStream_t s = c.st();
     if (c.count_pairs) count_near_pairs(c);
     ConvArgs a = make_args(c);
@@ -885,12 +889,15 @@ void convective(Ctx& c) {
         a.spins = c.wait_spins;
         a.err = c.counters.p + 20;
         VV_CUDA(cudaMemsetAsync(a.err, 0, 8, s));
-        VV_CUDA(cudaFuncSetAttribute(k_conv32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV32_SMEM));
-        {
+        auto launch = [&](auto kern, int ct) {
+            VV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)conv32_smem(ct)));
             KernelTimer kt(c, VVGPU_T_CONVECTIVE);
-            k_conv32<<<grid, CW * 32, CONV32_SMEM, s>>>(a);
+            kern<<<grid, CW * 32, conv32_smem(ct), s>>>(a);
             VV_LAUNCH_CHECK();
-        }
+        };
+        if (c.conv_tile == 128) launch(k_conv32<128>, 128);
+        else if (c.conv_tile == 256) launch(k_conv32<256>, 256);
+        else launch(k_conv32<192>, 192);
         unsigned long long e = 0;
         VV_CUDA(cudaMemcpyAsync(&e, a.err, 8, cudaMemcpyDeviceToHost, s));
         VV_CUDA(cudaStreamSynchronize(s));

@@ -256,6 +256,36 @@ int vvgpu_set_eps_round_limit(vvgpu_ctx* h, int64_t max_rounds) {
     API_END
 }
 
+int vvgpu_autotune_tiles(vvgpu_ctx* h, int32_t* conv_tile, int32_t* diff_targets, double* ms) {
+    API_BEGIN(h)
+    autotune_tiles(c, ms);
+    if (conv_tile) *conv_tile = c.conv_tile;
+    if (diff_targets) *diff_targets = c.diff_targets;
+    API_END
+}
+
+int vvgpu_set_tiles(vvgpu_ctx* h, int32_t conv_tile, int32_t diff_targets) {
+    API_BEGIN(h)
+    if (!(conv_tile == 128 || conv_tile == 192 || conv_tile == 256) || !(diff_targets == 1 || diff_targets == 2))
+        throw ApiError{VVGPU_ERR_ARG, "tile shapes: conv_tile 128, 192 or 256; diff_targets 1 or 2"};
+    c.conv_tile = conv_tile;
+    c.diff_targets = diff_targets;
+    API_END
+}
+
+int vvgpu_get_tiles(vvgpu_ctx* h, int32_t* conv_tile, int32_t* diff_targets) {
+    API_BEGIN(h)
+    if (conv_tile) *conv_tile = c.conv_tile;
+    if (diff_targets) *diff_targets = c.diff_targets;
+    API_END
+}
+
+int vvgpu_set_autotune(vvgpu_ctx* h, int on) {
+    API_BEGIN(h)
+    c.tune_pending = on != 0;
+    API_END
+}
+
 int vvgpu_set_wait_limit(vvgpu_ctx* h, uint32_t spins) {
     API_BEGIN(h)
     c.wait_spins = spins;

@@ -530,12 +530,10 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
     if (lane == 0 && s_nsrc[wq]) atomicAdd(a.cand + 1, s_nsrc[wq]);
 }
 
-// one target per lane, eight lane groups of four: measured faster than two targets per lane
-// (9.25 vs 9.92 ms at 4M) and four (11.9 ms), with fewer registers and spills; k_diff32's
-// launch bound of 7 blocks per SM (9.14 ms) beats 6 (9.25) and 8 (10.07, more spills)
-#ifndef DIFF32_DT
-#define DIFF32_DT 1
-#endif
+// Targets per lane: the context's choice (vvgpu_autotune_tiles), 1 by default: one target
+// per lane, eight lane groups of four, measured faster than two targets per lane (9.25 vs
+// 9.92 ms at 4M) and four (11.9 ms), with fewer registers and spills; k_diff32's launch
+// bound of 7 blocks per SM (9.14 ms) beats 6 (9.25) and 8 (10.07, more spills)
 
 }  // namespace
 
@@ -562,8 +560,9 @@ void diffusive(Ctx& c) {
     unsigned grid = grid_for(nl, DW);
     {
         KernelTimer kt(c, VVGPU_T_DIFFUSIVE);
-        if (c.precision == VVGPU_FP32) k_diff32<DIFF32_DT><<<grid, DW * 32, 0, s>>>(a);
-        else k_diff64<<<grid, DW * 32, 0, s>>>(a);
+        if (c.precision == VVGPU_FP64) k_diff64<<<grid, DW * 32, 0, s>>>(a);
+        else if (c.diff_targets == 2) k_diff32<2><<<grid, DW * 32, 0, s>>>(a);
+        else k_diff32<1><<<grid, DW * 32, 0, s>>>(a);
         VV_LAUNCH_CHECK();
     }
     unsigned long long cand[2] = {0, 0};

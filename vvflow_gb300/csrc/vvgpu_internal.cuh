@@ -131,6 +131,10 @@ struct Ctx {
     // fixed-point rounds the epsilon/merge pass may take (vvgpu_set_eps_round_limit)
     int64_t eps_max_rounds = 4096;
     uint32_t wait_spins = STAGE_SPINS;  // polls of one shared-memory staging wait
+    // kernel shapes of the FP32 pair passes (vvgpu_autotune_tiles): sources per staged tile
+    // of the convective near field, targets per lane of the diffusive pass
+    int conv_tile = 192, diff_targets = 1;
+    bool tune_pending = false;  // tune both at the next convective pass
 
     // segments (host copies of geometry are kept for body bookkeeping)
     int64_t m = 0;
@@ -455,6 +459,7 @@ void eps_pass(Ctx& c, int merge, int64_t* merged);
 // the learned far field in the convective pass with its judge (learned_step.cu)
 void convective_learned(Ctx& c, vvgpu_mlp& M, const vvgpu_judge_cfg* jc, vvgpu_judge_out* jo);
 void convective(Ctx& c);
+void autotune_tiles(Ctx& c, double* ms);
 void velocity_points(Ctx& c, int64_t n, const double* px, const double* py, double* vx, double* vy);
 void velocity_points_on_device(Ctx& c, int64_t n, const double* dpx, const double* dpy, double* dvx, double* dvy);
 void direct_velocity(Ctx& c, int64_t n, const double* px, const double* py, double* vx, double* vy);

@@ -95,6 +95,10 @@ SIGNATURES = {
     "vvgpu_get_stats": (C.c_int, [_H, C.POINTER(Stats)]),
     "vvgpu_set_eps_round_limit": (C.c_int, [_H, C.c_int64]),
     "vvgpu_set_wait_limit": (C.c_int, [_H, C.c_uint32]),
+    "vvgpu_autotune_tiles": (C.c_int, [_H, _I32, _I32, _D]),
+    "vvgpu_set_tiles": (C.c_int, [_H, C.c_int32, C.c_int32]),
+    "vvgpu_get_tiles": (C.c_int, [_H, _I32, _I32]),
+    "vvgpu_set_autotune": (C.c_int, [_H, C.c_int]),
     "vvgpu_set_kernel_timing": (C.c_int, [_H, C.c_int]),
     "vvgpu_get_kernel_timing": (C.c_int, [_H, _D, _I64]),
     "vvgpu_set_params": (C.c_int, [_H] + [C.c_double] * 8),
@@ -268,6 +272,26 @@ class GpuSpace:
 
     def set_eps_round_limit(self, max_rounds: int):
         self._ok(self.lib.vvgpu_set_eps_round_limit(self.h, int(max_rounds)), "set_eps_round_limit")
+
+    def autotune_tiles(self):
+        """Times the FP32 pair passes' kernel shapes on the current tree and keeps the fastest;
+        returns (conv_tile, diff_targets, ms[5])."""
+        t, d = np.zeros(1, np.int32), np.zeros(1, np.int32)
+        ms = np.zeros(5)
+        self._ok(self.lib.vvgpu_autotune_tiles(self.h, _p(t, C.c_int32), _p(d, C.c_int32), _p(ms, C.c_double)),
+                 "autotune_tiles")
+        return int(t[0]), int(d[0]), ms
+
+    def set_tiles(self, conv_tile: int = 192, diff_targets: int = 1):
+        self._ok(self.lib.vvgpu_set_tiles(self.h, int(conv_tile), int(diff_targets)), "set_tiles")
+
+    def tiles(self):
+        t, d = np.zeros(1, np.int32), np.zeros(1, np.int32)
+        self._ok(self.lib.vvgpu_get_tiles(self.h, _p(t, C.c_int32), _p(d, C.c_int32)), "get_tiles")
+        return int(t[0]), int(d[0])
+
+    def set_autotune(self, on: bool = True):
+        self._ok(self.lib.vvgpu_set_autotune(self.h, int(bool(on))), "set_autotune")
 
     STAGE_SPINS = 1 << 22  # default polls of one staging wait
 
