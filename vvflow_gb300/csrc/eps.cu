@@ -175,8 +175,9 @@ __global__ void k_eps_box(int64_t nl, const int32_t* __restrict__ lvf, const int
                           const float4* __restrict__ rec0, const float4* __restrict__ recO,
                           const int32_t* __restrict__ partner, const int32_t* __restrict__ zb, float4* box,
                           float4* box_prev, int32_t* live, const float* __restrict__ sr1,
-                          const float* __restrict__ sr2, float* rreg, int first_round) {
+                          const float* __restrict__ sr2, float* rreg, int first_round, int32_t* changed) {
     int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L == 0) *changed = 0;  // the round's changed flag (read by the host after the last round)
     if (L >= nl) return;
     float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
     int32_t nlive = 0;
@@ -687,9 +688,14 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
     }
 }
 
-__global__ void k_zb_reset(int64_t n, const int32_t* __restrict__ zb, int32_t* zb_prev, int32_t* zb_new) {
+// Also clears the round's per-leaf displacement bounds and changed flags [0, nl] and the
+// largest displacement, which k_zb_scatter and k_leaf_changed then fill.
+__global__ void k_zb_reset(int64_t n, int64_t nl, const int32_t* __restrict__ zb, int32_t* zb_prev, int32_t* zb_new,
+                           int32_t* dmax_bits, int32_t* leaf_disp, int32_t* leaf_changed) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) { zb_prev[i] = zb[i]; zb_new[i] = INT_MAX; }
+    if (i <= nl) { leaf_disp[i] = 0; leaf_changed[i] = 0; }
+    if (i == 0) *dmax_bits = 0;
 }
 
 __global__ void k_zb_scatter(int64_t n, const int32_t* __restrict__ partner, const int32_t* __restrict__ leaf_of,
@@ -839,7 +845,8 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
         // boxes and candidate leaves from the current guesses
         k_eps_box<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.lf_vf.p, c.lf_vl.p, c.e_rec0.p, c.e_recO[cur].p,
                                                   c.e_partner[cur].p, c.e_zb.p, c.lf_box32.p, c.e_box_prev.p,
-                                                  c.e_live.p, c.e_sr1.p, c.e_sr2.p, c.e_rreg.p, rounds == 1);
+                                                  c.e_live.p, c.e_sr1.p, c.e_sr2.p, c.e_rreg.p, rounds == 1,
+                                                  c.e_changed.p);
         VV_LAUNCH_CHECK();
         {
             KernelTimer kt(c, VVGPU_T_EPS_CAND);
@@ -850,7 +857,6 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                            c.e_rreg.p, c.e_lchg_pre.p, rounds == 1, c.e_ldisp.p);
             VV_LAUNCH_CHECK();
         }
-        VV_CUDA(cudaMemsetAsync(c.e_changed.p, 0, 4, s));
         EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.e_rnear.p,
                   (const float*)dmax_bits, c.near_off.p, c.near_run.p,
                   c.e_cand.p, c.e_ncand.p, c.e_rec0.p, c.e_recO[cur].p, c.e_x0.p, c.e_y0.p, c.e_g0.p,
@@ -883,15 +889,13 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
             VV_LAUNCH_CHECK();
         }
         // new absorber table and merged records; leaves whose members changed
-        k_zb_reset<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_zb.p, c.e_zb_prev.p, c.e_zb.p);
+        k_zb_reset<<<grid_for(std::max<int64_t>(n, nl + 1), EB), EB, 0, s>>>(
+            n, nl, c.e_zb.p, c.e_zb_prev.p, c.e_zb.p, dmax_bits, c.e_ldisp.p, c.e_lchanged.p);
         VV_LAUNCH_CHECK();
-        VV_CUDA(cudaMemsetAsync(dmax_bits, 0, 4, s));
-        VV_CUDA(cudaMemsetAsync(c.e_ldisp.p, 0, (nl + 1) * 4, s));
         k_zb_scatter<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_partner[nx].p, c.leaf_of.p, c.lf_anchor.p, fr.G,
                                                     c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_x0.p, c.e_y0.p,
                                                     c.e_zb.p, c.e_recO[nx].p, dmax_bits, c.e_ldisp.p);
         VV_LAUNCH_CHECK();
-        VV_CUDA(cudaMemsetAsync(c.e_lchanged.p, 0, (nl + 1) * 4, s));
         k_leaf_changed<<<grid_for(n, EB), EB, 0, s>>>(n, c.leaf_of.p, c.e_partner[cur].p, c.e_partner[nx].p,
                                                       c.e_ox[cur].p, c.e_ox[nx].p, c.e_oy[cur].p, c.e_oy[nx].p,
                                                       c.e_og[cur].p, c.e_og[nx].p, c.e_zb_prev.p, c.e_zb.p,
