@@ -221,7 +221,8 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
                            float* rlist, float* rnear, const int32_t* __restrict__ leaf_changed, int32_t* dirty,
                            int32_t* chg, int32_t* nchg, const float4* __restrict__ box_prev,
                            const float* __restrict__ rreg, const int32_t* __restrict__ chg_pre, int first_round,
-                           const int32_t* __restrict__ leaf_disp) {
+                           const int32_t* __restrict__ leaf_disp, const int32_t* __restrict__ chg_list,
+                           float* dloc_store) {
     __shared__ int2 s_runs[EB / 32][32];
     const int wq = threadIdx.x >> 5;
     const int64_t L = (int64_t)blockIdx.x * (blockDim.x / 32) + wq;
@@ -303,20 +304,25 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
     // The list stays valid while R_L (now) plus the largest merge displacement of the near
     // leaves' members fits inside the radius it was built with: a leaf left out had its box
     // farther than that radius, and a box only grows by its members' merged positions.
+    // That displacement is bounded by the one last computed for L (dloc_store) and the
+    // current one of the near leaves that changed since (an unchanged leaf's members have
+    // the same merges, so the same displacement); only the changed leaves are visited.
     bool collected = false;
     if (try_reuse) {
         float dloc = 0.f;
-        for_near_leaves(near_run, r0, r1, s_runs[wq], [&](int32_t q, bool ok) {
+        for_listed_near_leaves(near_run, r0, r1, chg_pre, chg_list, s_runs[wq], [&](int32_t q, bool ok) {
             collect(q, ok);
             if (ok) dloc = fmaxf(dloc, __int_as_float(leaf_disp[q]));
         });
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) dloc = fmaxf(dloc, __shfl_xor_sync(0xffffffffu, dloc, o));
+        dloc = fmaxf(dloc, dloc_store[L]);
         const float need_r = sqrtf(R2) * (1.f + 1e-4f) + dloc + absm;
         if (need_r <= rlist[L]) {
             if (lane == 0) {
                 nchg[L] = (nch > CHG_CAP) ? -1 : nch;
                 dirty[L] = nch > 0 ? 1 : 0;
+                dloc_store[L] = dloc;
             }
             return;
         }
@@ -324,11 +330,12 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
     }
     // (re)build: near leaves within 2 R_L of L's box (FP32 with margins)
     const float lim = isfinite(R2) ? 2.f * sqrtf(R2) * (1.f + 1e-4f) + absm : INFINITY;
-    float ext = 0.f, next = 0.f;
+    float ext = 0.f, next = 0.f, dall = 0.f;
     int32_t cnt = 0;
     for_near_leaves(near_run, r0, r1, s_runs[wq], [&](int32_t q, bool ok) {
         bool hit = false;
         float e = 0.f;
+        if (ok && !first_round) dall = fmaxf(dall, __int_as_float(leaf_disp[q]));  // none merged before round 1
         if (ok) {
             const float4 b = box[q];
             if (b.x <= b.z) {
@@ -355,8 +362,10 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
     for (int o = 16; o > 0; o >>= 1) {
         ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
         next = fmaxf(next, __shfl_xor_sync(0xffffffffu, next, o));
+        dall = fmaxf(dall, __shfl_xor_sync(0xffffffffu, dall, o));
     }
     if (lane == 0) {
+        dloc_store[L] = dall;
         ncand[L] = (cnt > CAND_CAP) ? -1 : cnt;  // -1: use the whole near list
         rlist[L] = (cnt > CAND_CAP) ? -1.f : lim;
         // extents of the coordinates the searches form in L's frame
@@ -688,6 +697,13 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
     }
 }
 
+// The changed leaves in order: list[rank] = q for every q with changed[q] (rank = pre[q]).
+__global__ void k_chg_list(int64_t nl, const int32_t* __restrict__ changed, const int32_t* __restrict__ pre,
+                           int32_t* list) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nl && changed[q]) list[pre[q]] = (int32_t)q;
+}
+
 // Also clears the round's per-leaf displacement bounds and changed flags [0, nl] and the
 // largest displacement, which k_zb_scatter and k_leaf_changed then fill.
 __global__ void k_zb_reset(int64_t n, int64_t nl, const int32_t* __restrict__ zb, int32_t* zb_prev, int32_t* zb_new,
@@ -835,6 +851,8 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
     const int64_t max_rounds = c.eps_max_rounds;
     c.e_rlist.reserve(nl + 1);
     c.e_ldisp.reserve(nl + 1);
+    c.e_dloc.reserve(nl + 1);
+    c.e_chglist.reserve(nl + 1);
     c.e_rnear.reserve(nl + 1);
     int32_t* dmax_bits = (int32_t*)(c.counters.p + 13);
     VV_CUDA(cudaMemsetAsync(dmax_bits, 0, 4, s));
@@ -854,7 +872,8 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                            c.lf_box32.p, c.e_live.p, fr.Gf, c.e_cand.p, c.e_ncand.p,
                                                            c.lf_rn.p, c.e_rlist.p, c.e_rnear.p, c.e_lchanged.p,
                                                            c.e_dirty.p, c.e_chg.p, c.e_nchg.p, c.e_box_prev.p,
-                                                           c.e_rreg.p, c.e_lchg_pre.p, rounds == 1, c.e_ldisp.p);
+                                                           c.e_rreg.p, c.e_lchg_pre.p, rounds == 1, c.e_ldisp.p,
+                                                           c.e_chglist.p, c.e_dloc.p);
             VV_LAUNCH_CHECK();
         }
         EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.e_rnear.p,
@@ -902,6 +921,8 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                       c.e_lchanged.p, c.e_vch.p);
         VV_LAUNCH_CHECK();
         exclusive_scan(c, c.e_lchanged.p, c.e_lchg_pre.p, nl);
+        k_chg_list<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.e_lchanged.p, c.e_lchg_pre.p, c.e_chglist.p);
+        VV_LAUNCH_CHECK();
         cur = nx;
         int32_t changed = read_i32(c, c.e_changed.p);
         if (!changed) break;

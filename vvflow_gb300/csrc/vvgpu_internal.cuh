@@ -241,6 +241,8 @@ struct Ctx {
     DArr<int32_t> e_zb_prev, e_live, e_cand, e_ncand, e_dirty, e_lchanged;
     DArr<float> e_rlist, e_rnear;
     DArr<int32_t> e_ldisp;          // per leaf: largest merge displacement of its members (float bits)
+    DArr<float> e_dloc;             // per leaf: bound on e_ldisp over its near leaves (as last computed)
+    DArr<int32_t> e_chglist;        // the changed leaves in order (rank = e_lchg_pre)
 
     // local FP32 frames (frame.cuh)
     double frame_G = 1.0;
@@ -420,6 +422,49 @@ __device__ __forceinline__ void for_near_leaves(const int2* __restrict__ near_ru
             }
             const int2 e = s[lo];
             f(e.y + (k - e.x), k < total);
+        }
+    }
+    __syncwarp();
+}
+
+// Calls f(q, ok) for the near leaves of [r0, r1) that are in the ranked list `list` (for
+// each leaf q of a run [x, y), the ones with pre[x] <= rank < pre[y], list[rank] = q), in
+// the order of for_near_leaves; ok is false (and q = 0) for the padding lanes.
+template <class F>
+__device__ __forceinline__ void for_listed_near_leaves(const int2* __restrict__ near_run, int32_t r0, int32_t r1,
+                                                       const int32_t* __restrict__ pre,
+                                                       const int32_t* __restrict__ list, int2* s, F&& f) {
+    const int lane = threadIdx.x & 31;
+    for (int32_t rb = r0; rb < r1; rb += 32) {
+        const int32_t rr = rb + lane;
+        int32_t first = 0, len = 0;
+        if (rr < r1) {
+            const int2 run = near_run[rr];
+            first = pre[run.x];
+            len = pre[run.y] - first;
+        }
+        int32_t incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const int nrun = min(32, r1 - rb);
+        __syncwarp();
+        s[lane] = make_int2(incl - len, first);
+        __syncwarp();
+        for (int32_t kb = 0; kb < total; kb += 32) {
+            const int32_t k = kb + lane;
+            int lo = 0, hi = nrun - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s[mid].x <= k) lo = mid;
+                else hi = mid - 1;
+            }
+            const int2 e = s[lo];
+            const bool ok = k < total;
+            f(ok ? list[e.y + (k - e.x)] : 0, ok);
         }
     }
     __syncwarp();
