@@ -201,9 +201,15 @@ int vvgpu_ctx_create(const vvgpu_cfg* cfg, vvgpu_ctx** out) {
         return VVGPU_ERR_CUDA;
     }
     c.stream = c.own_stream;
+    // pinned host words for the small device reads of the step (counts, flags)
+    if (cudaMallocHost(&c.h_pin, 16 * sizeof(int32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        c.h_pin = nullptr;  // the reads then go through pageable memory
+    }
     try {
         if (cfg && cfg->reserve_vortices > 0) ensure_vortex_capacity(c, cfg->reserve_vortices, false);
     } catch (...) {
+        if (c.h_pin) cudaFreeHost(c.h_pin);
         cudaStreamDestroy(c.own_stream);
         delete h;
         return VVGPU_ERR_NOMEM;
@@ -225,6 +231,7 @@ int vvgpu_ctx_destroy(vvgpu_ctx* h) {
         cudaEventDestroy(r.b);
     }
     for (cudaEvent_t e : c.ev_free) cudaEventDestroy(e);
+    if (c.h_pin) cudaFreeHost(c.h_pin);
     delete h;  // device arrays are released by their destructors
     if (own) cudaStreamDestroy(own);
     if (side) cudaStreamDestroy(side);

@@ -133,9 +133,10 @@ void exclusive_scan(Ctx& c, const int32_t* in, int32_t* out, int64_t n) {
 
 int32_t read_i32(Ctx& c, const int32_t* p) {
     int32_t v = 0;
-    VV_CUDA(cudaMemcpyAsync(&v, p, sizeof v, cudaMemcpyDeviceToHost, c.st()));
+    int32_t* dst = c.h_pin ? c.h_pin : &v;
+    VV_CUDA(cudaMemcpyAsync(dst, p, sizeof v, cudaMemcpyDeviceToHost, c.st()));
     VV_CUDA(cudaStreamSynchronize(c.st()));
-    return v;
+    return *dst;
 }
 
 }  // namespace vvgpu

@@ -1304,7 +1304,8 @@ void tree_build(Ctx& c, double far_criteria, double min_node, double max_node) {
             std::swap(c.seg_order, c.seg_order2);
             std::swap(c.seg_node_of, c.seg_node_of2);
         }
-        int32_t hc[3];
+        int32_t hl[3];
+        int32_t* hc = c.h_pin ? c.h_pin + 4 : hl;  // pinned when the context has its words
         VV_CUDA(cudaMemcpyAsync(hc, c.lvl_cnt.p, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         VV_CUDA(cudaStreamSynchronize(s));
         const int32_t nsmall = hc[0], nchunk = hc[1], nsplit = hc[2];
