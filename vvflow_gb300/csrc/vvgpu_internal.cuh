@@ -131,6 +131,7 @@ struct Ctx {
     // fixed-point rounds the epsilon/merge pass may take (vvgpu_set_eps_round_limit)
     int64_t eps_max_rounds = 4096;
     uint32_t wait_spins = STAGE_SPINS;  // polls of one shared-memory staging wait
+    int32_t* h_pin = nullptr;           // 16 pinned host words for small device reads
     // kernel shapes of the FP32 pair passes (vvgpu_autotune_tiles): sources per staged tile
     // of the convective near field, targets per lane of the diffusive pass
     int conv_tile = 192, diff_targets = 1;
@@ -272,6 +273,7 @@ struct Ctx {
     DArr<int32_t> slae_maps;        // column / row maps of the system
     DArr<double> slae_bodies;       // per-body row data
     DArr<double> slae_r, slae_sq;   // refinement residual and its squared terms
+    DArr<float2> slae_vs;           // a vector split into FP32 pairs for the FP32 inverse
     vvgpu_stats stats{};
     // per-kernel device time (vvgpu_set_kernel_timing): event pairs recorded on the stream,
     // summed per slot when the host asks
