@@ -449,6 +449,46 @@ __global__ void k_gemv(int64_t n, const T* __restrict__ M, const double* __restr
     if (lane == 0) y[row] = add ? y[row] + acc : acc;
 }
 
+// FP32 inverse times an FP64 vector on the FP32 pipe: the vector split once into FP32
+// pairs (hi, lo), each product m hi with its exact rounding error (an FMA) and m lo,
+// accumulated as a TwoSum pair per lane and reduced as double-float pairs: the accuracy of
+// FP64 accumulation (about 2^-48) without its narrow pipe.  One warp per row.
+__global__ void k_split_vec(int64_t n, const double* __restrict__ v, float2* vs) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = v[i];
+    const float hi = (float)x;
+    vs[i] = make_float2(hi, (float)(x - (double)hi));
+}
+__global__ void k_gemv32(int64_t n, const float* __restrict__ M, const float2* __restrict__ vs, double* y,
+                         bool add) {
+    const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const float* r = M + row * n;
+    float h = 0.f, l = 0.f;
+    for (int64_t j = lane; j < n; j += 32) {
+        const float m = r[j];
+        const float2 v = vs[j];
+        const float p = m * v.x;
+        const float pe = fmaf(m, v.x, -p);  // m v.x - p exactly
+        const float sm = h + p, bp = sm - h;
+        l += ((h - (sm - bp)) + (p - bp)) + fmaf(m, v.y, pe);
+        h = sm;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+        const float sm = h + oh, bp = sm - h;
+        l = l + ol + ((h - (sm - bp)) + (oh - bp));
+        h = sm;
+    }
+    if (lane == 0) {
+        const double acc = (double)h + (double)l;
+        y[row] = add ? y[row] + acc : acc;
+    }
+}
+
 // r = b - A x; sq[row] = r^2, sq[n + row] = b^2 (summed deterministically afterwards)
 __global__ void k_residual(int64_t n, const double* __restrict__ A, const double* __restrict__ x,
                            const double* __restrict__ b, double* r, double* sq) {
@@ -662,9 +702,15 @@ void slae(Ctx& c, vvgpu_body_out* out) {
     c.sum_part.reserve(2 * SUM_BLOCKS);
     double* acc = (double*)(c.counters.p + 8);
     const unsigned gg = grid_for(n, 8);
+    c.slae_vs.reserve(n + 1);
     auto apply_inv = [&](const double* v, double* y, bool add) {
-        if (c.lu_precision == VVGPU_FP32) k_gemv<float><<<gg, 256, 0, s>>>(n, c.inv32.p, v, y, add);
-        else k_gemv<double><<<gg, 256, 0, s>>>(n, c.inv.p, v, y, add);
+        if (c.lu_precision == VVGPU_FP32) {
+            k_split_vec<<<grid_for(n, 256), 256, 0, s>>>(n, v, c.slae_vs.p);
+            VV_LAUNCH_CHECK();
+            k_gemv32<<<gg, 256, 0, s>>>(n, c.inv32.p, c.slae_vs.p, y, add);
+        } else {
+            k_gemv<double><<<gg, 256, 0, s>>>(n, c.inv.p, v, y, add);
+        }
         VV_LAUNCH_CHECK();
     };
     apply_inv(c.B.p, c.X.p, false);
