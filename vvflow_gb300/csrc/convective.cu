@@ -491,10 +491,13 @@ __global__ void k_src32(int64_t n, const int32_t* __restrict__ leaf_of, const fl
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float2 k = anchor[leaf_of[i]];
-    double e = 1. / ie[i];
+    // eps^2 = 1 / _1_eps^2 on the FP32 pipe (the record holds it in FP32; an FP64 division
+    // per vortex costs more than the rest of this kernel on GB300's narrow FP64 pipe)
+    const double iel = ie[i];
+    const float ief = (float)iel;
     float gf = (float)g[i];
-    float e2 = (float)(e * e);
-    if (ie[i] == 0.) { gf = 0.f; e2 = 1.f; }
+    float e2 = __frcp_rn(ief * ief);
+    if (iel == 0.) { gf = 0.f; e2 = 1.f; }
     src[i] = make_float4((float)(x[i] - (double)k.x), (float)(y[i] - (double)k.y), gf, e2);
     src_k[i] = k;
     src_a4[i] = make_float4(k.x, k.y, 0.f, 0.f);
