@@ -335,7 +335,7 @@ __global__ void k_eps_cand(int64_t nl, const int32_t* __restrict__ near_off, con
     for_near_leaves(near_run, r0, r1, s_runs[wq], [&](int32_t q, bool ok) {
         bool hit = false;
         float e = 0.f;
-        if (ok && !first_round) dall = fmaxf(dall, __int_as_float(leaf_disp[q]));  // nothing merges before the first ε round
+        if (ok && !first_round) dall = fmaxf(dall, __int_as_float(leaf_disp[q]));  // nothing merges before the first epsilon round
         if (ok) {
             const float4 b = box[q];
             if (b.x <= b.z) {
