@@ -856,7 +856,8 @@ void build_frames(Ctx& c) {
 void count_near_pairs(Ctx& c) {
     cudaStream_t s = c.st();
     const int64_t nl = c.nleaves;
-    DArr<int32_t> nz, pre;
+    DArr<int32_t>& nz = c.np_nz;  // context scratch: no device allocation per pass
+    DArr<int32_t>& pre = c.np_pre;
     nz.reserve(nl + 1);
     pre.reserve(nl + 2);
     k_leaf_nz<<<grid_for(nl, 256), 256, 0, s>>>(nl, c.lf_vf.p, c.lf_vl.p, c.g.p, nz.p);

@@ -255,6 +255,7 @@ struct Ctx {
     DArr<float> src_ie;             // per vortex: (float)_1_eps
     DArr<float4> src_a4;            // per vortex: anchor of its leaf (x, y, 0, 0), 16-byte records
     DArr<int2> run_js;              // per near run: first source slot, offset in its leaf's near sequence
+    DArr<int32_t> np_nz, np_pre;    // near-pair count: non-zero vortices per leaf and their prefix
     DArr<int32_t> leaf_tot;         // per leaf: length of its near sequence
     DArr<float4> lf_dbox;           // per leaf (diffusive): box of non-zero vortices and segment centres
 
