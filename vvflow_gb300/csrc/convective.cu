@@ -832,9 +832,11 @@ void check_bodies_at_rest(Ctx& c) {
 void build_frames(Ctx& c) {
     cudaStream_t s = c.st();
     const int64_t n = c.n, nl = c.nleaves;
-    double4 root;
-    VV_CUDA(cudaMemcpyAsync(&root, c.nd_geom.p, sizeof root, cudaMemcpyDeviceToHost, s));
+    double4 rootl;
+    double4* rp = pinned_at(c, 64, &rootl);
+    VV_CUDA(cudaMemcpyAsync(rp, c.nd_geom.p, sizeof rootl, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));
+    const double4 root = *rp;
     Frame fr = make_frame(std::fmax(std::fabs(root.x), std::fabs(root.y)) + std::fmax(root.z, root.w));
     c.frame_G = fr.G;
     c.lf_anchor.reserve(nl + 1);
@@ -867,10 +869,11 @@ void count_near_pairs(Ctx& c) {
     VV_CUDA(cudaMemsetAsync(out, 0, 8, s));
     k_near_pairs<<<grid_for(nl, 256), 256, 0, s>>>(nl, nz.p, pre.p, c.near_off.p, c.near_run.p, out);
     VV_LAUNCH_CHECK();
-    unsigned long long v = 0;
-    VV_CUDA(cudaMemcpyAsync(&v, out, 8, cudaMemcpyDeviceToHost, s));
+    unsigned long long vl = 0;
+    unsigned long long* v = pinned_at(c, 120, &vl);
+    VV_CUDA(cudaMemcpyAsync(v, out, 8, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));
-    c.stats.near_pairs = (int64_t)v;
+    c.stats.near_pairs = (int64_t)*v;
 }
 
 void convective(Ctx& c) {
@@ -902,10 +905,11 @@ void convective(Ctx& c) {
         if (c.conv_tile == 128) launch(k_conv32<128>, 128);
         else if (c.conv_tile == 256) launch(k_conv32<256>, 256);
         else launch(k_conv32<192>, 192);
-        unsigned long long e = 0;
-        VV_CUDA(cudaMemcpyAsync(&e, a.err, 8, cudaMemcpyDeviceToHost, s));
+        unsigned long long el = 0;
+        unsigned long long* ep = pinned_at(c, 96, &el);
+        VV_CUDA(cudaMemcpyAsync(ep, a.err, 8, cudaMemcpyDeviceToHost, s));
         VV_CUDA(cudaStreamSynchronize(s));
-        if (e) throw ApiError{VVGPU_ERR_TIMEOUT, "near-field staging wait timed out"};
+        if (*ep) throw ApiError{VVGPU_ERR_TIMEOUT, "near-field staging wait timed out"};
     } else {
         KernelTimer kt(c, VVGPU_T_CONVECTIVE);
         k_conv64<8><<<grid, CW * 32, 0, s>>>(a);

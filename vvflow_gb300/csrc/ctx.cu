@@ -202,7 +202,7 @@ int vvgpu_ctx_create(const vvgpu_cfg* cfg, vvgpu_ctx** out) {
     }
     c.stream = c.own_stream;
     // pinned host words for the small device reads of the step (counts, flags)
-    if (cudaMallocHost(&c.h_pin, 16 * sizeof(int32_t)) != cudaSuccess) {
+    if (cudaMallocHost(&c.h_pin, 512) != cudaSuccess) {
         cudaGetLastError();
         c.h_pin = nullptr;  // the reads then go through pageable memory
     }

@@ -565,7 +565,8 @@ void diffusive(Ctx& c) {
         else k_diff32<1><<<grid, DW * 32, 0, s>>>(a);
         VV_LAUNCH_CHECK();
     }
-    unsigned long long cand[2] = {0, 0};
+    unsigned long long candl[2] = {0, 0};
+    unsigned long long* cand = pinned_at(c, 104, candl);
     VV_CUDA(cudaMemcpyAsync(cand, c.counters.p + 2, 16, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));
     c.stats.diff_candidates = (int64_t)cand[0];

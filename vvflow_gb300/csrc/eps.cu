@@ -933,11 +933,13 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                c.e_og[cur].p, c.e_oie[cur].p, c.x.p, c.y.p, c.g.p, c.ie.p,
                                                c.counters.p);
     VV_LAUNCH_CHECK();
-    unsigned long long mcount = 0, nev = 0, nrec = 0;
-    VV_CUDA(cudaMemcpyAsync(&mcount, c.counters.p, 8, cudaMemcpyDeviceToHost, s));
-    VV_CUDA(cudaMemcpyAsync(&nev, c.counters.p + 14, 8, cudaMemcpyDeviceToHost, s));
-    VV_CUDA(cudaMemcpyAsync(&nrec, c.counters.p + 16, 8, cudaMemcpyDeviceToHost, s));
+    unsigned long long hl[3] = {0, 0, 0};
+    unsigned long long* h3 = pinned_at(c, 128, hl);
+    VV_CUDA(cudaMemcpyAsync(h3, c.counters.p, 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaMemcpyAsync(h3 + 1, c.counters.p + 14, 8, cudaMemcpyDeviceToHost, s));
+    VV_CUDA(cudaMemcpyAsync(h3 + 2, c.counters.p + 16, 8, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));
+    const unsigned long long mcount = h3[0], nev = h3[1], nrec = h3[2];
     c.eps_evaluations = (int64_t)nev;
     c.eps_records = (int64_t)nrec;
     if (merged) *merged = (int64_t)mcount;

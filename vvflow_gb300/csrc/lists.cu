@@ -706,9 +706,11 @@ void tree_lists(Ctx& c) {
     int32_t* err = (int32_t*)c.counters.p + 1;
     VV_CUDA(cudaMemsetAsync(err, 0, 4, s));
     // frames of every node
-    double4 root;
-    VV_CUDA(cudaMemcpyAsync(&root, c.nd_geom.p, sizeof root, cudaMemcpyDeviceToHost, s));
+    double4 rootl;
+    double4* rp = pinned_at(c, 64, &rootl);
+    VV_CUDA(cudaMemcpyAsync(rp, c.nd_geom.p, sizeof rootl, cudaMemcpyDeviceToHost, s));
     VV_CUDA(cudaStreamSynchronize(s));
+    const double4 root = *rp;
     Frame fr = make_frame(std::fmax(std::fabs(root.x), std::fabs(root.y)) + std::fmax(root.z, root.w));
     c.frame_G = fr.G;
     c.nf_geo.reserve(nn); c.nf_k.reserve(nn); c.nf_cm.reserve(nn); c.nf_g.reserve(nn);

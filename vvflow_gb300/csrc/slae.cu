@@ -726,7 +726,8 @@ void slae(Ctx& c, vvgpu_body_out* out) {
             k_sum_stage2<<<1, 256, 0, s>>>(SUM_BLOCKS, c.sum_part.p + k * SUM_BLOCKS, acc + k);
             VV_LAUNCH_CHECK();
         }
-        double h[2];
+        double hl[2];
+        double* h = pinned_at(c, 160, hl);
         VV_CUDA(cudaMemcpyAsync(h, acc, 16, cudaMemcpyDeviceToHost, s));
         VV_CUDA(cudaStreamSynchronize(s));
         if (!(h[0] > 1e-26 * h[1])) break;

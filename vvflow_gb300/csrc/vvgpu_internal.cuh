@@ -131,7 +131,7 @@ struct Ctx {
     // fixed-point rounds the epsilon/merge pass may take (vvgpu_set_eps_round_limit)
     int64_t eps_max_rounds = 4096;
     uint32_t wait_spins = STAGE_SPINS;  // polls of one shared-memory staging wait
-    int32_t* h_pin = nullptr;           // 16 pinned host words for small device reads
+    int32_t* h_pin = nullptr;           // 512 pinned host bytes for the small device reads of a step
     // kernel shapes of the FP32 pair passes (vvgpu_autotune_tiles): sources per staged tile
     // of the convective near field, targets per lane of the diffusive pass
     int conv_tile = 192, diff_targets = 1;
@@ -485,6 +485,13 @@ inline unsigned grid_for(int64_t n, int block) {
 void exclusive_scan(Ctx& c, const int32_t* in, int32_t* out, int64_t n);
 // Reads one int32 from device memory (synchronises the stream).
 int32_t read_i32(Ctx& c, const int32_t* p);
+// Host landing place of a small device read at byte `off` of the context's pinned block
+// (bytes: 0 read_i32, 16 tree counts, 64 root box, 96 staging error, 104 diffusive
+// counts, 120 near-pair count, 128 epsilon counters, 160 residual norms), or `fallback` without the block.
+template <class T>
+inline T* pinned_at(Ctx& c, size_t off, T* fallback) {
+    return c.h_pin ? reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(c.h_pin) + off) : fallback;
+}
 
 // ---- per-module entry points (throw ApiError / CudaError) ----
 void ensure_vortex_capacity(Ctx& c, int64_t n, bool keep);
