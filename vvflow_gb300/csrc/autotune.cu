@@ -1,7 +1,7 @@
 // Kernel shapes of the FP32 pair passes, chosen per context by timing them on the
 // context's own tree: the sources per staged tile of the convective near field (k_conv32:
-// 128, 192 or 256; shared memory per block 32, 48 or 64 KB) and the targets per lane of the
-// diffusive pass (k_diff32: 1 or 2).  Each variant computes the same sums (in a different
+// 128, 192 or 256; shared memory per block 32, 48 or 64 KB) and the targets per pass of the
+// diffusive pass (k_diff32: shape 1 takes up to 16, shape 2 up to 8).  Each variant computes the same sums (in a different
 // order of the FP32 partial sums), so the choice changes speed, not the method.  No
 // counterpart in the reference, whose OpenMP loops have no tile shapes.
 #include <cmath>
@@ -10,8 +10,8 @@
 
 namespace vvgpu {
 
-// ms (may be null): convective at tiles 128, 192, 256, then diffusive at 1 and 2 targets
-// per lane (device time, the best of two runs each).  Velocities and friction are left as
+// ms (may be null): convective at tiles 128, 192, 256, then diffusive at shapes 1 and 2
+// (device time, the best of two runs each).  Velocities and friction are left as
 // they were.
 void autotune_tiles(Ctx& c, double* ms) {
     c.tune_pending = false;

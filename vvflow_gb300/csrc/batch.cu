@@ -8,7 +8,7 @@
 // instance's launches on its stream, so the GPU runs many instances at once while the
 // per-level host reads of one instance's tree build overlap the kernels of the others.
 // vvgpu_batch_autotune first has every instance time its own kernel shapes in its next step
-// (sources per staged tile of the convective near field, targets per lane of the diffusive
+// (sources per staged tile of the convective near field, targets per pass of the diffusive
 // pass; vvgpu_autotune_tiles), then times the pool sizes it is given on real steps and keeps
 // the fastest.
 #include <algorithm>

@@ -10,10 +10,10 @@
 //
 // One warp per target leaf in both paths.  FP64 path (k_diff64): eight target slots times
 // four source lanes, every pair in double precision with the reference's formulas.  FP32
-// path (k_diff32): DIFF32_DT targets per lane in 8 / DIFF32_DT lane groups (one target per
-// lane, eight groups of four lanes), the lanes of a group striding over the sources of the
-// candidate leaves (staged in shared memory per batch);
-// vortex pairs in local frames (frame.cuh) with
+// path (k_diff32): only same-sign pairs contribute, so the candidate sources (staged in
+// shared memory per batch) are split by sign, and each target, one per lane group of
+// 32 / G lanes (G the power of two at or above the targets of the pass), strides over the
+// sources of its own sign only; vortex pairs in local frames (frame.cuh) with
 // FP32 exp/rsqrt; pairs whose cut-off or coincidence test falls within a rigorous bound of
 // the FP32 error of its threshold are re-evaluated in FP64, so the set of contributing
 // pairs is the reference's.  Wall segments are always FP64.  Friction goes to TAtt::fric
@@ -208,62 +208,70 @@ __global__ void __launch_bounds__(DW * 32) k_diff64(DiffArgs a) {
     if (lane == 0 && ncand) atomicAdd(a.cand, ncand);
 }
 
-// FP32 path.  Warp per target leaf, eight targets per chunk, split into 8 / DT lane groups
-// that each hold DT targets per lane in registers; the 4 DT lanes of a group stride over the
-// sources of the candidate leaves, taken as one flattened sequence per batch of up to HIT_CAP
-// candidate leaves (so every source is loaded once per group and applied to DT targets).
-// Pair arithmetic is FP32 in local frames with compensated accumulation.  Pairs whose
-// cut-off or coincidence test falls within the rigorous FP32 error bound of its threshold,
-// and the wall-segment terms, are evaluated in FP64 into per-lane accumulators that are
-// reduced in a fixed order, so results are reproducible.
-template <int DT>
+// FP32 path.  Warp per target leaf.  Only same-sign pairs contribute (vortex_influence,
+// MDiffusiveFast.cpp:97), so each staged batch of candidate sources (up to HIT_CAP candidate
+// leaves, flattened) is split by sign: positive sources from the front of the warp's
+// buffer, negative ones from the back, zero ones dropped.  A pass takes up to TMAX targets
+// of the leaf (a window of TMAX vortices), positives first; G (the power of two at or above
+// its active targets) lane groups of 32 / G lanes each hold one target and stride over the
+// sources of that target's sign only.  Pair arithmetic is FP32 in local frames with
+// compensated accumulation.  Pairs whose cut-off or coincidence test falls within the
+// rigorous FP32 error bound of its threshold, and the wall-segment terms, are evaluated in
+// FP64 into per-lane accumulators that are reduced in a fixed order, so results are
+// reproducible.
+template <int TMAX>
 __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
-    constexpr int LG = 4 * DT;  // lanes per group (source stride)
     __shared__ int2 s_runs[DW][32];
     __shared__ int4 s_hit[DW][HIT_CAP];     // flattened start, first vortex, shift x, shift y (bits)
     __shared__ float2 s_hitb[DW][HIT_CAP];  // error bound D of the leaf
-    __shared__ float4 s_src[DW][SRC_CAP];  // staged sources: x, y in L's frame, g, index (bits)
+    __shared__ float4 s_src[DW][SRC_CAP];   // x, y in L's frame, g, index (bits); + front, - back
     __shared__ int32_t s_hitq[DW][HIT_CAP]; // leaf
-    __shared__ unsigned long long s_nsrc[DW];  // candidate sources of the warp's chunks
-    // per lane FP64 accumulators (s2x, s2y, s1, s3x, s3y, s0 of its targets), touched only by
-    // band pairs and wall segments; lane-major so that lanes never share a bank row
-    __shared__ double s_d64[DW][DT * 6][32];
+    __shared__ unsigned long long s_nsrc[DW];
+    __shared__ double s_d64[DW][6][32];     // per lane FP64 s2x, s2y, s1, s3x, s3y, s0
     const int wq = threadIdx.x >> 5;
     const int64_t L = (int64_t)blockIdx.x * DW + wq;
     const int lane = threadIdx.x & 31;
     if (L >= a.nl) return;
-    const int grp = lane / LG, sub = lane % LG;
     const float2 kL = a.anchor[L];
     const int32_t v0 = a.lvf[L], v1 = a.lvl[L];
     const int32_t r0 = a.near_off[L], r1 = a.near_off[L + 1];
     const float bandc = ldexpf(64.f, -19);
-    double(&d64)[DT * 6][32] = s_d64[wq];
+    double(&d64)[6][32] = s_d64[wq];
+    const unsigned lt = (1u << lane) - 1u;
     unsigned long long ncand = 0;
     if (lane == 0) s_nsrc[wq] = 0ull;
-    for (int32_t c0 = v0; c0 < v1; c0 += 8) {
-        const int32_t tb = c0 + grp * DT;  // first target of this lane's group
-        float tx[DT], ty[DT], ief[DT], ie2[DT], b16[DT], iefl[DT];
-        unsigned act = 0, pos = 0;  // bit t: target t active / positive
-        float bx0 = INFINITY, by0 = INFINITY, bx1 = -INFINITY, by1 = -INFINITY, rmax = 0.f;
-#pragma unroll
-        for (int t = 0; t < DT; t++) {
-            const int32_t i = tb + t;
-            const unsigned long long gb = (i < v1) ? (unsigned long long)__double_as_longlong(a.g[i]) : 0ull;
-            tx[t] = ty[t] = ief[t] = ie2[t] = b16[t] = iefl[t] = 0.f;
-            if ((gb << 1) != 0ull) {  // g != 0 and its sign from the bit pattern (integer pipe)
-                act |= 1u << t;
-                if ((gb >> 63) == 0ull) pos |= 1u << t;
-                const float4 r4 = a.src32[i];
-                tx[t] = r4.x; ty[t] = r4.y;
-                ief[t] = a.src_ie[i];
-                ie2[t] = ief[t] * ief[t];
-                iefl[t] = ief[t] * 1.4426950408889634f;  // log2(e) / eps
-                b16[t] = 16.f * ief[t] * (1.f + 1e-3f);
-                bx0 = fminf(bx0, r4.x); by0 = fminf(by0, r4.y);
-                bx1 = fmaxf(bx1, r4.x); by1 = fmaxf(by1, r4.y);
-                rmax = fmaxf(rmax, (8.f / ief[t]) * (1.f + 1e-4f));
-            }
+    for (int32_t c0 = v0; c0 < v1; c0 += TMAX) {
+        // signs of the window's vortices from their bit patterns (g != 0: active)
+        const int32_t wi = c0 + lane;
+        const unsigned long long gw =
+            (lane < TMAX && wi < v1) ? (unsigned long long)__double_as_longlong(a.g[wi]) : 0ull;
+        const bool nzw = (gw << 1) != 0ull;
+        const unsigned P = __ballot_sync(0xffffffffu, nzw && (gw >> 63) == 0ull);
+        const unsigned N = __ballot_sync(0xffffffffu, nzw && (gw >> 63) != 0ull);
+        const int nP = __popc(P), na = nP + __popc(N);
+        if (na == 0) continue;  // warp-uniform
+        const int lgg = na <= 1 ? 0 : 32 - __clz(na - 1);  // log2 G
+        const int lgl = 5 - lgg;                           // log2 of the lanes per group
+        const int LG = 1 << lgl;
+        const int grp = lane >> lgl, sub = lane & (LG - 1);
+        const bool act = grp < na;
+        const bool neg = grp >= nP;
+        int32_t i = -1;
+        float tx = 0.f, ty = 0.f, ief = 0.f, ie2 = 0.f, b16 = 0.f, iefl = 0.f, reach = 0.f;
+        if (act) {
+            unsigned m = neg ? N : P;
+            for (int t = neg ? nP : 0; t < grp; t++) m &= m - 1u;
+            i = c0 + (__ffs(m) - 1);
+            const float4 r4 = a.src32[i];
+            tx = r4.x; ty = r4.y;
+            ief = a.src_ie[i];
+            ie2 = ief * ief;
+            iefl = ief * 1.4426950408889634f;  // log2(e) / eps
+            b16 = 16.f * ief * (1.f + 1e-3f);
+            reach = (8.f / ief) * (1.f + 1e-4f);
         }
+        float bx0 = act ? tx : INFINITY, by0 = act ? ty : INFINITY;
+        float bx1 = act ? tx : -INFINITY, by1 = act ? ty : -INFINITY, rmax = reach;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
@@ -272,106 +280,94 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
             by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
             rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
         }
-        if (!(bx0 <= bx1)) continue;  // no active target in this chunk (warp-uniform)
-        int nact = 0;
-#pragma unroll
-        for (int gg = 0; gg < 32 / LG; gg++) nact += __shfl_sync(0xffffffffu, __popc(act), gg * LG);
         const float pad = rmax + ldexpf(fabsf(bx0) + fabsf(bx1) + fabsf(by0) + fabsf(by1) + a.Gf, -16);
         const float tmax = fmaxf(fmaxf(fabsf(bx0), fabsf(bx1)), fmaxf(fabsf(by0), fabsf(by1)));
-        float p2x[DT], p2y[DT], p1[DT], h2x[DT], l2x[DT], h2y[DT], l2y[DT], h1[DT], l1[DT];
-#pragma unroll
-        for (int t = 0; t < DT; t++) p2x[t] = p2y[t] = p1[t] = h2x[t] = l2x[t] = h2y[t] = l2y[t] = h1[t] = l1[t] = 0.f;
+        float p2x = 0.f, p2y = 0.f, p1 = 0.f, h2x = 0.f, l2x = 0.f, h2y = 0.f, l2y = 0.f, h1 = 0.f, l1 = 0.f;
         bool used64 = false;
-        int since = 0;
-        // candidate leaves are gathered over the near list (up to HIT_CAP) before their
-        // sources are staged and applied
+        int since = 0;  // this lane's sources in the plain partial sums
         int nh_acc = 0;
         int32_t tot_acc = 0;
         bool seg_acc = false;
+        const bool want_p = nP > 0, want_n = nP < na;
         auto flush = [&]() {
-            // band parameters of this batch: the largest error bound D of its leaves
             float Dm = 0.f;
             for (int h = 0; h < nh_acc; h++) Dm = fmaxf(Dm, s_hitb[wq][h].x);
             const float tiny = 2.f * Dm + 1e-9f, tiny2 = tiny * tiny;
-            float bndv[DT];  // each target's band half-width for this batch
-#pragma unroll
-            for (int t = 0; t < DT; t++) bndv[t] = fmaf(b16[t], Dm, bandc);
+            const float bndv = fmaf(b16, Dm, bandc);
             for (int32_t kb = 0; kb < tot_acc; kb += SRC_CAP) {
                 const int32_t nst = min(SRC_CAP, tot_acc - kb);
-                // stage the sources (shifted into L's frame) once per warp
-                for (int32_t k = lane; k < nst; k += 32) {
-                    const int32_t kk = kb + k;
-                    int lo = 0, hi = nh_acc - 1;
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (s_hit[wq][mid].x <= kk) lo = mid;
-                        else hi = mid - 1;
+                // stage the batch's sources (shifted into L's frame), split by sign
+                int np_b = 0, nn_b = 0;
+                for (int32_t k0 = 0; k0 < nst; k0 += 32) {
+                    const int32_t k = k0 + lane;
+                    bool sp = false, sn = false;
+                    float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (k < nst) {
+                        const int32_t kk = kb + k;
+                        int lo = 0, hi = nh_acc - 1;
+                        while (lo < hi) {
+                            const int mid = (lo + hi + 1) >> 1;
+                            if (s_hit[wq][mid].x <= kk) lo = mid;
+                            else hi = mid - 1;
+                        }
+                        const int4 hc = s_hit[wq][lo];
+                        const int32_t j = hc.y + (kk - hc.x);
+                        const float4 s4 = a.src32[j];
+                        rec = make_float4(s4.x + __int_as_float(hc.z), s4.y + __int_as_float(hc.w), s4.z,
+                                          __int_as_float(j));
+                        sp = want_p && s4.z > 0.f;
+                        sn = want_n && s4.z < 0.f;
                     }
-                    const int4 hc = s_hit[wq][lo];
-                    const int32_t j = hc.y + (kk - hc.x);
-                    const float4 s4 = a.src32[j];
-                    s_src[wq][k] = make_float4(s4.x + __int_as_float(hc.z), s4.y + __int_as_float(hc.w), s4.z,
-                                               __int_as_float(j));
+                    const unsigned bp = __ballot_sync(0xffffffffu, sp), bn = __ballot_sync(0xffffffffu, sn);
+                    if (sp) s_src[wq][np_b + __popc(bp & lt)] = rec;
+                    if (sn) s_src[wq][SRC_CAP - 1 - (nn_b + __popc(bn & lt))] = rec;
+                    np_b += __popc(bp);
+                    nn_b += __popc(bn);
                 }
                 __syncwarp();
-                for (int32_t k0 = sub; k0 < nst;) {
-                  // at most 32 - since sources of this lane before the next fold
-                  const int32_t cnt = min(32 - since, (nst - k0 + LG - 1) / LG);
-                  const int32_t kend = k0 + cnt * LG;
-                  for (int32_t k = k0; k < kend; k += LG) {
-                    const float4 sv = s_src[wq][k];
-                    const int32_t j = __float_as_int(sv.w);
-                    // a target's pair with itself is excluded by the reference's coincidence rule;
-                    // a source with g = 0 has no same-sign target
-                    const int32_t jr = j - tb;
-                    const unsigned self = (jr >= 0 && jr < DT) ? (1u << jr) : 0u;
-                    const unsigned sgn = sv.z > 0.f ? pos : (sv.z < 0.f ? ~pos : 0u);
-                    const unsigned same = sgn & act & ~self;
-                    unsigned pend = 0;  // targets whose pair with this source goes to FP64
-#pragma unroll
-                    for (int t = 0; t < DT; t++) {
-                        const float dx = tx[t] - sv.x, dy = ty[t] - sv.y;
+                const int nmine = act ? (neg ? nn_b : np_b) : 0;
+                const float4* base = s_src[wq] + (neg ? SRC_CAP - 1 : 0);
+                const int dir = neg ? -1 : 1;
+                for (int k0 = sub; k0 < nmine;) {
+                    // at most 32 - since sources of this lane before the next fold
+                    const int cnt = min(32 - since, (nmine - k0 + LG - 1) >> lgl);
+                    const int kend = k0 + (cnt << lgl);
+                    for (int k = k0; k < kend; k += LG) {
+                        const float4 sv = base[dir * k];
+                        const int32_t j = __float_as_int(sv.w);
+                        const float dx = tx - sv.x, dy = ty - sv.y;
                         const float r2 = dx * dx + dy * dy;
-                        const float du = r2 * ie2[t] - 64.f;  // (|dr| / eps)^2 - 64
-                        const float bnd = bndv[t];
-                        const bool sm = (same >> t) & 1u;
-                        if (sm && (fabsf(du) < bnd || r2 < tiny2)) pend |= 1u << t;
-                        const bool in = sm && du <= -bnd && r2 >= tiny2;
+                        const float du = r2 * ie2 - 64.f;  // (|dr| / eps)^2 - 64
+                        const bool in = du <= -bndv && r2 >= tiny2;
                         const float r2c = in ? r2 : 1.f;
                         const float rs = rsqrtf(r2c);
                         // exp(-|dr| / eps) as 2^(-|dr| (log2(e) / eps)), one MUFU ex2
                         float ex2v;
-                        asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex2v) : "f"(-(r2c * rs) * iefl[t]));
+                        asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex2v) : "f"(-(r2c * rs) * iefl));
                         const float tv = in ? sv.z * ex2v : 0.f;
                         const float qv = tv * rs;
-                        p2x[t] = fmaf(dx, qv, p2x[t]);
-                        p2y[t] = fmaf(dy, qv, p2y[t]);
-                        p1[t] += tv;
-                    }
-                    if (pend) {  // rare: the reference's FP64 test and term
-                        if (!used64) {
-                            for (int w = 0; w < DT * 6; w++) d64[w][lane] = 0.;
-                            used64 = true;
-                        }
-                        for (int t = 0; t < DT; t++) {
-                            if (!((pend >> t) & 1u)) continue;
-                            const int32_t i = tb + t;
-                            vortex_term64(a.x[i], a.y[i], a.g[i], a.ie[i], a.x[j], a.y[j], a.g[j], d64[6 * t][lane],
-                                          d64[6 * t + 1][lane], d64[6 * t + 2][lane]);
+                        p2x = fmaf(dx, qv, p2x);
+                        p2y = fmaf(dy, qv, p2y);
+                        p1 += tv;
+                        // the cut-off or coincidence test within the FP32 error bound: the
+                        // reference's FP64 test and term (a target's pair with itself excluded)
+                        if ((fabsf(du) < bndv || r2 < tiny2) && j != i) {
+                            if (!used64) {
+                                for (int w = 0; w < 6; w++) d64[w][lane] = 0.;
+                                used64 = true;
+                            }
+                            vortex_term64(a.x[i], a.y[i], a.g[i], a.ie[i], a.x[j], a.y[j], a.g[j], d64[0][lane],
+                                          d64[1][lane], d64[2][lane]);
                         }
                     }
-                  }
-                  k0 = kend;
-                  since += cnt;
-                  if (since == 32) {
-                      since = 0;
-#pragma unroll
-                      for (int t = 0; t < DT; t++) {
-                          acc_add(h2x[t], l2x[t], p2x[t]); p2x[t] = 0.f;
-                          acc_add(h2y[t], l2y[t], p2y[t]); p2y[t] = 0.f;
-                          acc_add(h1[t], l1[t], p1[t]); p1[t] = 0.f;
-                      }
-                  }
+                    k0 = kend;
+                    since += cnt;
+                    if (since == 32) {
+                        since = 0;
+                        acc_add(h2x, l2x, p2x); p2x = 0.f;
+                        acc_add(h2y, l2y, p2y); p2y = 0.f;
+                        acc_add(h1, l1, p1); p1 = 0.f;
+                    }
                 }
                 __syncwarp();
             }
@@ -380,29 +376,25 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
                 for (int h = 0; h < nh_acc; h++) {
                     const int32_t qq = s_hitq[wq][h];
                     const int32_t qs0 = a.lsf[qq], qs1 = a.lsl[qq];
-                    if (qs0 >= qs1) continue;
+                    if (qs0 >= qs1 || !act) continue;
                     if (!used64) {
-                        for (int w = 0; w < DT * 6; w++) d64[w][lane] = 0.;
+                        for (int w = 0; w < 6; w++) d64[w][lane] = 0.;
                         used64 = true;
                     }
-                    for (int t = 0; t < DT; t++) {
-                        if (!((act >> t) & 1u)) continue;
-                        const int32_t i = tb + t;
-                        const double xi = a.x[i], yi = a.y[i], gi = a.g[i], ie = a.ie[i];
-                        for (int32_t qs = qs0 + sub; qs < qs1; qs += LG) {
-                            const int32_t sgm = a.seg_order[qs];
-                            const double dx = xi - a.rx[sgm], dy = yi - a.ry[sgm];
-                            const double dr2 = dx * dx + dy * dy;
-                            const double dr = sqrt(dr2);
-                            const double ea = -dr * ie;
-                            if (ea < EXP_ARG_RESTRICTION) continue;
-                            const double ex = exp(ea);
-                            const double dsx = -a.dly[sgm], dsy = a.dlx[sgm];
-                            d64[6 * t + 3][lane] += dsx * ex;
-                            d64[6 * t + 4][lane] += dsy * ex;
-                            d64[6 * t + 5][lane] += (dr * ie + 1) / dr2 * (dx * dsx + dy * dsy) * ex;
-                            atomicAdd(&a.fric[sgm], ie * ie * gi * ex * sqrt(dsx * dsx + dsy * dsy));
-                        }
+                    const double xi = a.x[i], yi = a.y[i], gi = a.g[i], ie = a.ie[i];
+                    for (int32_t qs = qs0 + sub; qs < qs1; qs += LG) {
+                        const int32_t sgm = a.seg_order[qs];
+                        const double dx = xi - a.rx[sgm], dy = yi - a.ry[sgm];
+                        const double dr2 = dx * dx + dy * dy;
+                        const double dr = sqrt(dr2);
+                        const double ea = -dr * ie;
+                        if (ea < EXP_ARG_RESTRICTION) continue;
+                        const double ex = exp(ea);
+                        const double dsx = -a.dly[sgm], dsy = a.dlx[sgm];
+                        d64[3][lane] += dsx * ex;
+                        d64[4][lane] += dsy * ex;
+                        d64[5][lane] += (dr * ie + 1) / dr2 * (dx * dsx + dy * dsy) * ex;
+                        atomicAdd(&a.fric[sgm], ie * ie * gi * ex * sqrt(dsx * dsx + dsy * dsy));
                     }
                 }
             }
@@ -443,7 +435,7 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
             const bool any_seg = __any_sync(0xffffffffu, segs > 0);
             __syncwarp();
             if (hit) {
-                const int r = __popc(mask & ((1u << lane) - 1));
+                const int r = __popc(mask & lt);
                 // Bound D on the FP32 error of |dr| for any pair of this leaf: each of dx, dy
                 // carries at most 2^-24 (|t| + |s| + |s + sh| + |dx|) from the roundings of the
                 // records, the shift and the subtraction (4x slack).
@@ -457,8 +449,8 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
             }
             __syncwarp();
             if (lane == 0) {
-                ncand += (unsigned long long)nact * (unsigned long long)total;
-                s_nsrc[wq] += (unsigned long long)total;  // in shared memory: no register held
+                ncand += (unsigned long long)na * (unsigned long long)total;
+                s_nsrc[wq] += (unsigned long long)total;
             }
             nh_acc += nh;
             tot_acc += total;
@@ -466,74 +458,67 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
             if (nh_acc > HIT_CAP - 32) flush();
         });
         if (nh_acc > 0) flush();
-        // fold, then combine the LG source lanes of each group as double-float pairs
-#pragma unroll
-        for (int t = 0; t < DT; t++) {
-            acc_add(h2x[t], l2x[t], p2x[t]);
-            acc_add(h2y[t], l2y[t], p2y[t]);
-            acc_add(h1[t], l1[t], p1[t]);
-#pragma unroll
-            for (int o = LG / 2; o > 0; o >>= 1) {
-                ff_add(h2x[t], l2x[t], __shfl_xor_sync(0xffffffffu, h2x[t], o), __shfl_xor_sync(0xffffffffu, l2x[t], o));
-                ff_add(h2y[t], l2y[t], __shfl_xor_sync(0xffffffffu, h2y[t], o), __shfl_xor_sync(0xffffffffu, l2y[t], o));
-                ff_add(h1[t], l1[t], __shfl_xor_sync(0xffffffffu, h1[t], o), __shfl_xor_sync(0xffffffffu, l1[t], o));
-            }
+        // fold, then combine the LG lanes of each group as double-float pairs
+        acc_add(h2x, l2x, p2x);
+        acc_add(h2y, l2y, p2y);
+        acc_add(h1, l1, p1);
+        for (int o = LG >> 1; o > 0; o >>= 1) {
+            ff_add(h2x, l2x, __shfl_xor_sync(0xffffffffu, h2x, o), __shfl_xor_sync(0xffffffffu, l2x, o));
+            ff_add(h2y, l2y, __shfl_xor_sync(0xffffffffu, h2y, o), __shfl_xor_sync(0xffffffffu, l2y, o));
+            ff_add(h1, l1, __shfl_xor_sync(0xffffffffu, h1, o), __shfl_xor_sync(0xffffffffu, l1, o));
         }
         const bool any64 = __any_sync(0xffffffffu, used64);
         if (any64) {
             if (!used64)
-                for (int w = 0; w < DT * 6; w++) d64[w][lane] = 0.;
+                for (int w = 0; w < 6; w++) d64[w][lane] = 0.;
             __syncwarp();
             // fixed-order sum over the LG lanes of each group into the group's first slot
-            for (int w = sub; w < DT * 6; w += LG) {
+            for (int w = sub; w < 6; w += LG) {
                 double acc = 0.;
-                for (int l2 = 0; l2 < LG; l2++) acc += d64[w][grp * LG + l2];
-                d64[w][grp * LG] = acc;
+                for (int l2 = 0; l2 < LG; l2++) acc += d64[w][(grp << lgl) + l2];
+                d64[w][grp << lgl] = acc;
             }
             __syncwarp();
         }
-        // lane sub == t of each group writes target t of its group
-#pragma unroll
-        for (int t = 0; t < DT; t++) {
-            if (sub != t || !((act >> t) & 1u)) continue;
-            const int32_t i = tb + t;
+        if (act && sub == 0) {
             if (!any64) {
                 // MDiffusiveFast.cpp:41-45 with no wall term (s0 = s3 = 0), in FP32
                 const float gif = (float)a.g[i];
-                float t1 = h1[t] + l1[t];
+                float t1 = h1 + l1;
                 if (((t1 > 0.f) - (t1 < 0.f)) != ((gif > 0.f) - (gif < 0.f)) || fabsf(t1) < fabsf(0.1f * gif))
                     t1 = 0.1f * gif;
-                const float f = ief[t] / ((float)a.re * t1);
-                a.vx[i] = a.vx[i] + (double)((h2x[t] + l2x[t]) * f);
-                a.vy[i] = a.vy[i] + (double)((h2y[t] + l2y[t]) * f);
+                const float f = ief / ((float)a.re * t1);
+                a.vx[i] = a.vx[i] + (double)((h2x + l2x) * f);
+                a.vy[i] = a.vy[i] + (double)((h2y + l2y) * f);
             } else {
                 const double gi = a.g[i], ie = a.ie[i];
-                const double* dv = &d64[6 * t][grp * LG];
-                double s2x = dv[0 * 32] + ((double)h2x[t] + (double)l2x[t]);
-                double s2y = dv[1 * 32] + ((double)h2y[t] + (double)l2y[t]);
-                double s1 = dv[2 * 32] + ((double)h1[t] + (double)l1[t]);
-                double s0 = dv[5 * 32];
+                const int g0 = grp << lgl;
+                double s2x = d64[0][g0] + ((double)h2x + (double)l2x);
+                double s2y = d64[1][g0] + ((double)h2y + (double)l2y);
+                double s1 = d64[2][g0] + ((double)h1 + (double)l1);
+                double s0 = d64[5][g0];
                 if ((dsgn(s1) != dsgn(gi)) || (fabs(s1) < fabs(0.1 * gi))) s1 = 0.1 * gi;
                 double f = ie / (a.re * s1);
                 double vx = a.vx[i] + s2x * f, vy = a.vy[i] + s2y * f;
                 if (s0 > C_PI) s0 = C_PI;
                 f = ie * ie / (a.re * (C_2PI - s0));
-                vx += dv[3 * 32] * f;
-                vy += dv[4 * 32] * f;
+                vx += d64[3][g0] * f;
+                vy += d64[4][g0] * f;
                 a.vx[i] = vx;
                 a.vy[i] = vy;
             }
         }
+        __syncwarp();  // the group sums in d64 are read before the next pass clears them
     }
     ncand = warp_sum_u64(ncand);
     if (lane == 0 && ncand) atomicAdd(a.cand, ncand);
     if (lane == 0 && s_nsrc[wq]) atomicAdd(a.cand + 1, s_nsrc[wq]);
 }
 
-// Targets per lane: the context's choice (vvgpu_autotune_tiles), 1 by default: one target
-// per lane, eight lane groups of four, measured faster than two targets per lane (9.25 vs
-// 9.92 ms at 4M) and four (11.9 ms), with fewer registers and spills; k_diff32's launch
-// bound of 7 blocks per SM (9.14 ms) beats 6 (9.25) and 8 (10.07, more spills)
+// Targets per pass: the context's choice (vvgpu_autotune_tiles; shape 1: up to 16, shape
+// 2: up to 8).  Against the earlier mapping (eight targets per pass, four lanes each, every
+// candidate source applied to every target and the opposite-sign pairs zeroed): 7.16 against
+// 8.54 ms at 4M, with bit-identical epsilon and merges.
 
 }  // namespace
 
@@ -561,8 +546,8 @@ void diffusive(Ctx& c) {
     {
         KernelTimer kt(c, VVGPU_T_DIFFUSIVE);
         if (c.precision == VVGPU_FP64) k_diff64<<<grid, DW * 32, 0, s>>>(a);
-        else if (c.diff_targets == 2) k_diff32<2><<<grid, DW * 32, 0, s>>>(a);
-        else k_diff32<1><<<grid, DW * 32, 0, s>>>(a);
+        else if (c.diff_targets == 2) k_diff32<8><<<grid, DW * 32, 0, s>>>(a);
+        else k_diff32<16><<<grid, DW * 32, 0, s>>>(a);
         VV_LAUNCH_CHECK();
     }
     unsigned long long candl[2] = {0, 0};

@@ -133,7 +133,7 @@ struct Ctx {
     uint32_t wait_spins = STAGE_SPINS;  // polls of one shared-memory staging wait
     int32_t* h_pin = nullptr;           // 512 pinned host bytes for the small device reads of a step
     // kernel shapes of the FP32 pair passes (vvgpu_autotune_tiles): sources per staged tile
-    // of the convective near field, targets per lane of the diffusive pass
+    // of the convective near field, shape of the diffusive pass (1: 16 targets, 2: 8 per pass)
     int conv_tile = 192, diff_targets = 1;
     bool tune_pending = false;  // tune both at the next convective pass
 
