@@ -28,7 +28,8 @@ namespace vvgpu {
 namespace {
 
 constexpr int DW = 4;
-constexpr int SRC_CAP = 256;  // FP32 path: sources staged per warp at a time
+constexpr int SRC_CAP = 256;  // FP32 path: shared-memory source records per warp
+constexpr int SRC_BATCH = SRC_CAP - 32;  // FP32 path: sources staged per warp at a time
 // candidate leaves gathered per warp before their sources are staged (64: measured 9.86 ms
 // against 10.14 ms for one batch of 32 near leaves at a time at 4M; 96 costs occupancy)
 constexpr int HIT_CAP = 64;
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(DW * 32) k_diff64(DiffArgs a) {
 // FP64 into per-lane accumulators that are reduced in a fixed order, so results are
 // reproducible.
 template <int TMAX>
-__global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
+__global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
     __shared__ int2 s_runs[DW][32];
     __shared__ int4 s_hit[DW][HIT_CAP];     // flattened start, first vortex, shift x, shift y (bits)
     __shared__ float2 s_hitb[DW][HIT_CAP];  // error bound D of the leaf
@@ -240,6 +241,8 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
     const unsigned lt = (1u << lane) - 1u;
     unsigned long long ncand = 0;
     if (lane == 0) s_nsrc[wq] = 0ull;
+    for (int k = lane; k < SRC_CAP; k += 32) s_src[wq][k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
     for (int32_t c0 = v0; c0 < v1; c0 += TMAX) {
         // signs of the window's vortices from their bit patterns (g != 0: active)
         const int32_t wi = c0 + lane;
@@ -294,8 +297,8 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
             for (int h = 0; h < nh_acc; h++) Dm = fmaxf(Dm, s_hitb[wq][h].x);
             const float tiny = 2.f * Dm + 1e-9f, tiny2 = tiny * tiny;
             const float bndv = fmaf(b16, Dm, bandc);
-            for (int32_t kb = 0; kb < tot_acc; kb += SRC_CAP) {
-                const int32_t nst = min(SRC_CAP, tot_acc - kb);
+            for (int32_t kb = 0; kb < tot_acc; kb += SRC_BATCH) {
+                const int32_t nst = min(SRC_BATCH, tot_acc - kb);
                 // stage the batch's sources (shifted into L's frame), split by sign
                 int np_b = 0, nn_b = 0;
                 for (int32_t k0 = 0; k0 < nst; k0 += 32) {
@@ -325,20 +328,29 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
                     nn_b += __popc(bn);
                 }
                 __syncwarp();
+                // Every lane steps through max(np_b, nn_b) / LG sources (warp-uniform trip
+                // count and fold points); steps beyond the lane's own list read a finite record
+                // (the buffer is zeroed at the start and a batch fills at most SRC_BATCH <=
+                // SRC_CAP - 32 of it, so no index leaves the buffer) and add exactly zero.
                 const int nmine = act ? (neg ? nn_b : np_b) : 0;
-                const float4* base = s_src[wq] + (neg ? SRC_CAP - 1 : 0);
-                const int dir = neg ? -1 : 1;
-                for (int k0 = sub; k0 < nmine;) {
-                    // at most 32 - since sources of this lane before the next fold
-                    const int cnt = min(32 - since, (nmine - k0 + LG - 1) >> lgl);
-                    const int kend = k0 + (cnt << lgl);
-                    for (int k = k0; k < kend; k += LG) {
-                        const float4 sv = base[dir * k];
-                        const int32_t j = __float_as_int(sv.w);
+                const int steps = (max(np_b, nn_b) + LG - 1) >> lgl;
+                const int stride = neg ? -LG : LG;
+                const float4* p = s_src[wq] + (neg ? SRC_CAP - 1 - sub : sub);
+                int rem = nmine - sub;  // > 0: the lane's current source is in its list
+                for (int s0 = 0; s0 < steps;) {
+                    // at most 32 - since steps before the next fold
+                    const int cnt = min(32 - since, steps - s0);
+                    unsigned bmask = 0;  // band pairs of this window (bit: step within it)
+                    const float4* pw = p;
+                    for (int st = 0; st < cnt; st++) {
+                        const float4 sv = *p;
+                        p += stride;
+                        const bool ok = rem > 0;
+                        rem -= LG;
                         const float dx = tx - sv.x, dy = ty - sv.y;
                         const float r2 = dx * dx + dy * dy;
                         const float du = r2 * ie2 - 64.f;  // (|dr| / eps)^2 - 64
-                        const bool in = du <= -bndv && r2 >= tiny2;
+                        const bool in = ok && du <= -bndv && r2 >= tiny2;
                         const float r2c = in ? r2 : 1.f;
                         const float rs = rsqrtf(r2c);
                         // exp(-|dr| / eps) as 2^(-|dr| (log2(e) / eps)), one MUFU ex2
@@ -349,18 +361,24 @@ __global__ void __launch_bounds__(DW * 32, 7) k_diff32(DiffArgs a) {
                         p2x = fmaf(dx, qv, p2x);
                         p2y = fmaf(dy, qv, p2y);
                         p1 += tv;
-                        // the cut-off or coincidence test within the FP32 error bound: the
-                        // reference's FP64 test and term (a target's pair with itself excluded)
-                        if ((fabsf(du) < bndv || r2 < tiny2) && j != i) {
-                            if (!used64) {
-                                for (int w = 0; w < 6; w++) d64[w][lane] = 0.;
-                                used64 = true;
-                            }
-                            vortex_term64(a.x[i], a.y[i], a.g[i], a.ie[i], a.x[j], a.y[j], a.g[j], d64[0][lane],
-                                          d64[1][lane], d64[2][lane]);
-                        }
+                        // the cut-off or coincidence test within the FP32 error bound
+                        if (ok && (fabsf(du) < bndv || r2 < tiny2)) bmask |= 1u << st;
                     }
-                    k0 = kend;
+                    // the window's band pairs, in order: the reference's FP64 test and term
+                    // (a target's pair with itself excluded)
+                    while (bmask) {
+                        const int st = __ffs(bmask) - 1;
+                        bmask &= bmask - 1u;
+                        const int32_t j = __float_as_int(pw[st * stride].w);
+                        if (j == i) continue;
+                        if (!used64) {
+                            for (int w = 0; w < 6; w++) d64[w][lane] = 0.;
+                            used64 = true;
+                        }
+                        vortex_term64(a.x[i], a.y[i], a.g[i], a.ie[i], a.x[j], a.y[j], a.g[j], d64[0][lane],
+                                      d64[1][lane], d64[2][lane]);
+                    }
+                    s0 += cnt;
                     since += cnt;
                     if (since == 32) {
                         since = 0;
