@@ -10,7 +10,9 @@ timed with CUDA events on the context's stream.  The headline `value` is the FP3
 path; the plain FP64 path is timed on the same workload for the ratio the metric names,
 and both are checked against each other and against an FP64 direct sum.  `e2e` is the same
 step with host buffers: pinned host -> device copy of the inputs and device -> host copy
-of the results inside the timed region.  With N > 1 (torchrun) every rank runs an
+of the results inside the timed region (the list's positions, circulations, epsilons and
+origins are copied out beside the convective and diffusive passes, once the epsilon/merge
+pass has fixed them; the velocities after those passes).  With N > 1 (torchrun) every rank runs an
 independent replica (different seed); value = all vortices / max time over ranks.
 
 Reference arm: the reference's CPU algorithm (the C restatement in oracle/, which mirrors
@@ -231,6 +233,25 @@ def hot_path(S, wl, mn, mx):
     S.convective()
     S.diffusive()
     S.tree_destroy()
+
+
+def hot_path_host(S, wl, mn, mx, outs, oorig):
+    """hot_path with the list returned to host buffers: positions, circulations, epsilons and
+    origins are copied out beside the convective and diffusive passes (the list is final
+    after the epsilon/merge pass), the velocities after them."""
+    S.tree_build(wl.far_criteria, mn, mx)
+    S.slae()
+    S.tree_destroy()
+    S.vortex_shed()
+    S.tree_build(wl.far_criteria, mn, mx)
+    S.eps(True)
+    S.get_vortices_async(outs["x"].data_ptr(), outs["y"].data_ptr(), outs["g"].data_ptr(), outs["ie"].data_ptr(),
+                         oorig.data_ptr())
+    S.convective()
+    S.diffusive()
+    S.tree_destroy()
+    S.get_vortices_into(vx=outs["vx"].data_ptr(), vy=outs["vy"].data_ptr())
+    S.wait_vortices()
 
 
 def learned_in_step(args, make, restore, wl, mn, mx, state, idx, ux, uy, rel, ms64):
@@ -668,16 +689,14 @@ def gpu_arm(args):
     h2d = 4 * 8 * N
     for _ in range(1):
         S.set_vortices_from(N, hx.data_ptr(), hy.data_ptr(), hg.data_ptr(), hie.data_ptr())
-        hot_path(S, wl, mn, mx)
+        hot_path_host(S, wl, mn, mx, outs, oorig)
     torch.cuda.synchronize()
     barrier()
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2.record()
     for _ in range(args.steps):
         S.set_vortices_from(N, hx.data_ptr(), hy.data_ptr(), hg.data_ptr(), hie.data_ptr())
-        hot_path(S, wl, mn, mx)
-        S.get_vortices_into(outs["x"].data_ptr(), outs["y"].data_ptr(), outs["g"].data_ptr(),
-                            outs["ie"].data_ptr(), outs["vx"].data_ptr(), outs["vy"].data_ptr(), oorig.data_ptr())
+        hot_path_host(S, wl, mn, mx, outs, oorig)
     e3.record()
     torch.cuda.synchronize()
     barrier()

@@ -217,6 +217,19 @@ int64_t vvgpu_num_segments(const vvgpu_ctx* ctx);
 /* Copies the vortex list back to host memory; any pointer may be NULL. */
 int vvgpu_get_vortices(vvgpu_ctx* ctx, double* x, double* y, double* g, double* inv_eps,
                        double* vx, double* vy, int64_t* orig);
+/* Starts copying the vortex list's positions, circulations, inverse epsilons and origin
+ * indices (as vvgpu_get_vortices; any pointer may be NULL) to host memory and returns
+ * without waiting: the list is first copied on the device into a private snapshot, in
+ * order on the context's stream, then to the host on a copy stream, so that the copies run
+ * beside the context's later calls (after vvgpu_eps, the list does not change again in the
+ * step: the convective and diffusive passes write only velocities and wall friction).  The
+ * host arrays must stay valid, and must not be read, until vvgpu_wait_vortices returns;
+ * with page-locked host memory the copies overlap the kernels.  A second call first waits
+ * for the first.  The reference keeps the list in host memory (Space::VortexList); this is
+ * the drop-in's return path for it after the epsilon pass. */
+int vvgpu_get_vortices_async(vvgpu_ctx* ctx, double* x, double* y, double* g, double* inv_eps, int64_t* orig);
+/* Waits for the download vvgpu_get_vortices_async started (returns at once without one). */
+int vvgpu_wait_vortices(vvgpu_ctx* ctx);
 /* Device pointers to the resident SoA arrays (valid until the next call that resizes). */
 int vvgpu_device_arrays(vvgpu_ctx* ctx, double** x, double** y, double** g, double** inv_eps,
                         double** vx, double** vy);

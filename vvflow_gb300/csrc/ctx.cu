@@ -224,8 +224,9 @@ int vvgpu_ctx_destroy(vvgpu_ctx* h) {
     cudaSetDevice(c.device);
     cudaStreamSynchronize(c.stream);
     if (c.side) cudaStreamSynchronize(c.side);
-    cudaStream_t own = c.own_stream, side = c.side;
-    cudaEvent_t e1 = c.ev_fork, e2 = c.ev_join;
+    if (c.dl_stream) cudaStreamSynchronize(c.dl_stream);
+    cudaStream_t own = c.own_stream, side = c.side, dls = c.dl_stream;
+    cudaEvent_t e1 = c.ev_fork, e2 = c.ev_join, e3 = c.dl_ready, e4 = c.dl_done;
     for (auto& r : c.ev_rec) {
         cudaEventDestroy(r.a);
         cudaEventDestroy(r.b);
@@ -237,6 +238,9 @@ int vvgpu_ctx_destroy(vvgpu_ctx* h) {
     if (side) cudaStreamDestroy(side);
     if (e1) cudaEventDestroy(e1);
     if (e2) cudaEventDestroy(e2);
+    if (dls) cudaStreamDestroy(dls);
+    if (e3) cudaEventDestroy(e3);
+    if (e4) cudaEventDestroy(e4);
     return VVGPU_OK;
 }
 
@@ -506,6 +510,46 @@ int vvgpu_get_vortices(vvgpu_ctx* h, double* x, double* y, double* g, double* ie
     d2h(vy, c.vy.p, c.n, s);
     d2h(orig, c.orig.p, c.n, s);
     VV_CUDA(cudaStreamSynchronize(s));
+    API_END
+}
+
+int vvgpu_get_vortices_async(vvgpu_ctx* h, double* x, double* y, double* g, double* ie, int64_t* orig) {
+    API_BEGIN(h)
+    if (c.dl_pending) {
+        c.dl_pending = false;
+        VV_CUDA(cudaEventSynchronize(c.dl_done));
+    }
+    if (!c.dl_stream) {
+        VV_CUDA(cudaStreamCreateWithFlags(&c.dl_stream, cudaStreamNonBlocking));
+        VV_CUDA(cudaEventCreateWithFlags(&c.dl_ready, cudaEventDisableTiming));
+        VV_CUDA(cudaEventCreateWithFlags(&c.dl_done, cudaEventDisableTiming));
+    }
+    const int64_t n = c.n;
+    if (n > 0) {
+        cudaStream_t s = c.st();
+        c.dl_snap.reserve((size_t)5 * n);
+        double* snap = c.dl_snap.p;
+        const size_t bytes = (size_t)n * 8;
+        void* dst[5] = {x, y, g, ie, orig};
+        const void* src[5] = {c.x.p, c.y.p, c.g.p, c.ie.p, c.orig.p};
+        for (int k = 0; k < 5; k++)
+            if (dst[k]) VV_CUDA(cudaMemcpyAsync(snap + k * n, src[k], bytes, cudaMemcpyDeviceToDevice, s));
+        VV_CUDA(cudaEventRecord(c.dl_ready, s));
+        VV_CUDA(cudaStreamWaitEvent(c.dl_stream, c.dl_ready, 0));
+        for (int k = 0; k < 5; k++)
+            if (dst[k]) VV_CUDA(cudaMemcpyAsync(dst[k], snap + k * n, bytes, cudaMemcpyDeviceToHost, c.dl_stream));
+        VV_CUDA(cudaEventRecord(c.dl_done, c.dl_stream));
+        c.dl_pending = true;
+    }
+    API_END
+}
+
+int vvgpu_wait_vortices(vvgpu_ctx* h) {
+    API_BEGIN(h)
+    if (c.dl_pending) {
+        c.dl_pending = false;
+        VV_CUDA(cudaEventSynchronize(c.dl_done));
+    }
     API_END
 }
 

@@ -719,20 +719,29 @@ __global__ void k_zb_scatter(int64_t n, const int32_t* __restrict__ partner, con
                              const double* __restrict__ oy, const double* __restrict__ og,
                              const double* __restrict__ x0, const double* __restrict__ y0, int32_t* zb, float4* recO,
                              int32_t* dmax_bits, int32_t* leaf_disp) {
+    __shared__ int s_max[EB / 32];
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int32_t p = partner[i];
-    if (p >= 0) {
-        atomicMin(&zb[p], (int32_t)i);
-        float2 a = anchor[leaf_of[i]];
-        recO[i] = make_float4(rel(ox[i], a.x), rel(oy[i], a.y), (float)dsgn(og[i]), 0.f);
-        // displacement of the merged position (rounded up), for the candidate-list check
-        float d = (float)(fabs(ox[i] - x0[i]) + fabs(oy[i] - y0[i])) * (1.f + 1e-5f);
-        atomicMax(&leaf_disp[leaf_of[i]], __float_as_int(d));  // per leaf, for the list check
-        // the global maximum: one atomic per warp (all merged vortices hit one address)
-        const unsigned am = __activemask();
-        const int wmax = __reduce_max_sync(am, __float_as_int(d));
-        if ((threadIdx.x & 31) == __ffs(am) - 1) atomicMax(dmax_bits, wmax);
+    int dbits = 0;  // displacement bits (non-negative floats order as integers)
+    if (i < n) {
+        const int32_t p = partner[i];
+        if (p >= 0) {
+            atomicMin(&zb[p], (int32_t)i);
+            float2 a = anchor[leaf_of[i]];
+            recO[i] = make_float4(rel(ox[i], a.x), rel(oy[i], a.y), (float)dsgn(og[i]), 0.f);
+            // displacement of the merged position (rounded up), for the candidate-list check
+            float d = (float)(fabs(ox[i] - x0[i]) + fabs(oy[i] - y0[i])) * (1.f + 1e-5f);
+            dbits = __float_as_int(d);
+            atomicMax(&leaf_disp[leaf_of[i]], dbits);  // per leaf, for the list check
+        }
+    }
+    // the global maximum: one atomic per block (every merged vortex would hit one address)
+    dbits = __reduce_max_sync(0xffffffffu, dbits);
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = dbits;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int m = 0;
+        for (int w = 0; w < EB / 32; w++) m = max(m, s_max[w]);
+        if (m > 0) atomicMax(dmax_bits, m);
     }
 }
 

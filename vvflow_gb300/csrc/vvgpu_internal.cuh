@@ -116,6 +116,12 @@ struct Ctx {
     // (forked and joined through the two events); created on first use
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // list download beside later calls (vvgpu_get_vortices_async): device snapshot of x, y,
+    // g, ie, orig (5 n words), copy stream, snapshot-taken and copies-done events
+    DArr<double> dl_snap;
+    cudaStream_t dl_stream = nullptr;
+    cudaEvent_t dl_ready = nullptr, dl_done = nullptr;
+    bool dl_pending = false;
     std::string last_error;
 
     double re = 1.0 / 0.0, dt = 1.0, inf_vx = 0, inf_vy = 0, inf_g = 0, time = 0, grav_x = 0, grav_y = 0;

@@ -114,6 +114,8 @@ SIGNATURES = {
     "vvgpu_num_vortices": (C.c_int64, [_H]),
     "vvgpu_num_segments": (C.c_int64, [_H]),
     "vvgpu_get_vortices": (C.c_int, [_H, _D, _D, _D, _D, _D, _D, _I64]),
+    "vvgpu_get_vortices_async": (C.c_int, [_H, _D, _D, _D, _D, _I64]),
+    "vvgpu_wait_vortices": (C.c_int, [_H]),
     "vvgpu_device_arrays": (C.c_int, [_H] + [C.POINTER(C.c_void_p)] * 6),
     "vvgpu_get_segments": (C.c_int, [_H] + [_D] * 8),
     "vvgpu_get_body_geom": (C.c_int, [_H, C.c_int] + [_D] * 5),
@@ -504,6 +506,18 @@ class GpuSpace:
         f = lambda a, t=D: C.cast(C.c_void_p(a), t) if a else None
         self._ok(self.lib.vvgpu_get_vortices(self.h, f(x), f(y), f(g), f(ie), f(vx), f(vy),
                                              f(orig, C.POINTER(C.c_int64))), "get_vortices")
+
+    def get_vortices_async(self, x=0, y=0, g=0, ie=0, orig=0):
+        """Starts copying positions, circulations, inverse epsilons and origin indices into
+        caller-owned host buffers given as addresses (0 = skip) and returns at once; the
+        buffers are ready after wait_vortices()."""
+        D = C.POINTER(C.c_double)
+        f = lambda a, t=D: C.cast(C.c_void_p(a), t) if a else None
+        self._ok(self.lib.vvgpu_get_vortices_async(self.h, f(x), f(y), f(g), f(ie), f(orig, C.POINTER(C.c_int64))),
+                 "get_vortices_async")
+
+    def wait_vortices(self):
+        self._ok(self.lib.vvgpu_wait_vortices(self.h), "wait_vortices")
 
     def set_vortices_from(self, n, x, y, g, ie=0):
         """Replaces the vortex list from host buffers given as addresses (e.g. pinned memory)."""
