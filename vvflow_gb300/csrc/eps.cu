@@ -549,6 +549,84 @@ __device__ Top2 two_nearest(const EpsView& v, int32_t L, int32_t i, int32_t excl
     return best;
 }
 
+// Warp-collective two_nearest for the rounds with few targets (their time is the longest
+// single search).  The lanes split the candidate leaves (lane k takes every 32nd one, the
+// target's own leaf included) and keep their own FP32 two smallest distances, pruning with
+// their own threshold (never below the final one); the warp's two smallest give the final
+// threshold, then each lane takes the exact FP64 top-2 of its candidates within it and the
+// warp merges those in (distance, slot) order.  The two smallest FP32 distances, the final
+// threshold and the exact (distance, slot) top-2 do not depend on the order in which the
+// candidates are met, so the result is two_nearest's.  Every lane returns it.
+__device__ __forceinline__ void min2_merge(float& t1, float& t2, float a1, float a2) {
+    const float n1 = fminf(t1, a1);
+    t2 = fminf(fmaxf(t1, a1), fminf(t2, a2));
+    t1 = n1;
+}
+__device__ Top2 two_nearest_w(const EpsView& v, int32_t L, int32_t i, int32_t excl, double px, double py,
+                              bool use_list, int2* s_runs) {
+    const int lane = threadIdx.x & 31;
+    const float2 aL = v.anchor[L];
+    const float tx = (float)(px - (double)aL.x), ty = (float)(py - (double)aL.y);
+    const float ext = (use_list ? v.rn[L] : v.rnear[L]) + *v.dmax;
+    const float D = ldexpf(ext + fabsf(tx) + fabsf(ty) + v.Gf, -17);
+    float t1 = INFINITY, t2 = INFINITY, thr = INFINITY;
+    uint32_t nrec = 0;
+    Top2 best{DBL_MAX, DBL_MAX, INT_MAX, INT_MAX, INFINITY, 0};
+    const int32_t nc = use_list ? v.ncand[L] : -1;
+    const int32_t* cl = v.cand + (size_t)L * CAND_CAP;
+#pragma unroll 1
+    for (int pass = 0; pass < 2; pass++) {
+        auto visit = [&](int32_t q) {
+            const float2 sh = frame_shift(v.anchor[q], aL, v.Gf);
+            if (box_lb(v.box[q], sh, tx, ty) > thr) return;
+            if (pass == 0) nrec += (uint32_t)(v.lvl[q] - v.lvf[q]);
+            for (int32_t j = v.lvf[q]; j < v.lvl[q]; j++) {
+                Cand c = cand_state<false>(v, j, i, excl);
+                if (!c.live) continue;
+                const float dx = tx - (c.rec.x + sh.x), dy = ty - (c.rec.y + sh.y);
+                const float d = dx * dx + dy * dy;
+                if (pass == 0) {
+                    if (d < t1) { t2 = t1; t1 = d; thr = thr_of(t2, D); }
+                    else if (d < t2) { t2 = d; thr = thr_of(t2, D); }
+                } else if (d <= thr) {
+                    double xj, yj, gj;
+                    cand_exact<false>(v, j, i, xj, yj, gj);
+                    top2_push(best, dabs2(dsub(px, xj), dsub(py, yj)), j);
+                }
+            }
+        };
+        if (lane == 0) visit(L);
+        if (nc >= 0) {
+            for (int32_t k = lane; k < nc; k += 32) {
+                const int32_t q = cl[k];
+                if (q != L) visit(q);
+            }
+        } else {
+            for_near_leaves(v.near_run, v.near_off[L], v.near_off[L + 1], s_runs, [&](int32_t q, bool ok) {
+                if (ok && q != L) visit(q);
+            });
+        }
+        if (pass == 0) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                min2_merge(t1, t2, __shfl_xor_sync(0xffffffffu, t1, o), __shfl_xor_sync(0xffffffffu, t2, o));
+            thr = thr_of(t2, D);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double r1 = __shfl_xor_sync(0xffffffffu, best.r1, o), r2 = __shfl_xor_sync(0xffffffffu, best.r2, o);
+        const int32_t l1 = __shfl_xor_sync(0xffffffffu, best.l1, o), l2 = __shfl_xor_sync(0xffffffffu, best.l2, o);
+        if (l1 != INT_MAX) top2_push(best, r1, l1);
+        if (l2 != INT_MAX) top2_push(best, r2, l2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nrec += __shfl_xor_sync(0xffffffffu, nrec, o);
+    best.thr = thr;
+    best.nrec = nrec;
+    return best;
+}
+
 // Inputs of the last round's evaluation of a target, to tell whether it must run again.
 struct DirtyView {
     const int32_t* zb_prev;   // absorber table the last evaluation saw
@@ -621,7 +699,92 @@ __global__ void k_eps_compact(int64_t n, const int32_t* __restrict__ flag, const
     if (i < n && flag[i]) list[pos[i]] = (int32_t)i;
 }
 
-// Evaluates every target (FIRST: the first round) or the targets list[0 .. *count).
+// One target's evaluation: its two nearest live candidates, the merge decision
+// (MEpsilonFast.cpp:128-173) and its new epsilon.  WARP: the searches are warp-collective
+// (two_nearest_w; every lane computes the same outcome).
+struct Outcome {
+    int32_t partner;
+    double px, py, gi, ie;
+    float sr1, sr2;
+    uint32_t nrec;
+};
+template <bool FIRST, bool WARP>
+__device__ __forceinline__ Outcome eval_target(const EpsView& v, int32_t i, const int32_t* __restrict__ leaf_of,
+                                               const double* __restrict__ mcs_l, const double* __restrict__ epr_l,
+                                               const double* __restrict__ ie_in, int2* s_runs) {
+    auto search = [&](int32_t L, int32_t excl, double x, double y, bool use_list) {
+        if constexpr (WARP) return two_nearest_w(v, L, i, excl, x, y, use_list, s_runs);
+        else return two_nearest<FIRST>(v, L, i, excl, x, y, use_list);
+    };
+    const int32_t L = leaf_of[i];
+    const double gi0 = v.g0[i];
+    Outcome o{SKIPPED, v.x0[i], v.y0[i], gi0, ie_in[i], -1.f, -1.f, 0u};
+    if (gi0 != 0 && !(v.zb[i] < i)) {
+        const double mcs = mcs_l[L];
+        Top2 t = search(L, -1, o.px, o.py, true);
+        o.sr1 = t.thr;
+        o.nrec += t.nrec;
+        double e;
+        o.partner = -1;
+        if (t.l1 == INT_MAX) e = DBL_MIN;
+        else if (t.l2 == INT_MAX) e = __dsqrt_rn(t.r1);
+        else if (isnan(mcs)) e = __dsqrt_rn(t.r2);
+        else {
+            double x1, y1, g1, x2, y2, g2;
+            cand_exact<FIRST>(v, t.l1, i, x1, y1, g1);
+            cand_exact<FIRST>(v, t.l2, i, x2, y2, g2);
+            if ((t.r1 < mcs) || ((dsgn(g1) == dsgn(g2)) && (dsgn(g1) != dsgn(o.gi)))) {
+                // MergeVortexes (MEpsilonFast.cpp:111-126)
+                if (dsgn(o.gi) == dsgn(g1)) {
+                    double sx = dadd(dmul(o.px, o.gi), dmul(x1, g1));
+                    double sy = dadd(dmul(o.py, o.gi), dmul(y1, g1));
+                    double inv = ddiv(1., dadd(o.gi, g1));
+                    o.px = dmul(sx, inv);
+                    o.py = dmul(sy, inv);
+                } else if (fabs(o.gi) < fabs(g1)) {
+                    o.px = x1;
+                    o.py = y1;
+                }
+                o.gi = dadd(o.gi, g1);
+                o.partner = t.l1;
+                Top2 u = search(L, t.l1, o.px, o.py, false);
+                o.sr2 = u.thr;
+                o.nrec += u.nrec;
+                if (u.l1 == INT_MAX) e = DBL_MIN;
+                else if (u.l2 == INT_MAX) e = __dsqrt_rn(u.r1);
+                else e = __dsqrt_rn(u.r2);
+            } else {
+                e = __dsqrt_rn(t.r2);
+            }
+        }
+        o.ie = ddiv(1.0, smax(e, epr_l[L]));
+    }
+    return o;
+}
+
+// Whether an outcome differs from target i's last one; stores it and its search radii.
+__device__ __forceinline__ bool store_outcome(const EpsView& v, DirtyView& dv, int32_t i, const Outcome& o,
+                                              const double* __restrict__ oie_old, int32_t* partner_new,
+                                              double* ox_new, double* oy_new, double* og_new, double* oie_new) {
+    const bool ch = (o.partner != v.partner[i] && !(o.partner == SKIPPED && v.partner[i] == SKIPPED)) ||
+                    (__double_as_longlong(o.px) != __double_as_longlong(v.ox[i])) ||
+                    (__double_as_longlong(o.py) != __double_as_longlong(v.oy[i])) ||
+                    (__double_as_longlong(o.gi) != __double_as_longlong(v.og[i])) ||
+                    (__double_as_longlong(o.ie) != __double_as_longlong(oie_old[i]));
+    partner_new[i] = o.partner;
+    ox_new[i] = o.px; oy_new[i] = o.py; og_new[i] = o.gi; oie_new[i] = o.ie;
+    dv.sr1[i] = o.sr1;
+    dv.sr2[i] = o.sr2;
+    return ch;
+}
+
+// Rounds with at most this many targets run one warp per target (k_eps_round_w): their time
+// is the longest single search, which the warp splits 32 ways.
+constexpr int64_t EPS_WARP_MAX = 8192;
+constexpr unsigned EPS_WARP_GRID = 152u * 16u;  // blocks of EB / 32 warps: one pass at the limit
+
+// Evaluates every target (FIRST: the first round) or the targets list[0 .. *count) when
+// there are more than EPS_WARP_MAX of them, one thread per target.
 template <bool FIRST>
 __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* __restrict__ list,
                             const int32_t* __restrict__ count, const int32_t* __restrict__ leaf_of,
@@ -630,70 +793,46 @@ __global__ void k_eps_round(int64_t n, EpsView v, DirtyView dv, const int32_t* _
                             int32_t* partner_new, double* ox_new, double* oy_new, double* og_new, double* oie_new,
                             int32_t* changed, unsigned long long* evals, unsigned long long* nrec_total) {
     const int64_t cnt = FIRST ? n : (int64_t)*count;
+    if (!FIRST && cnt <= EPS_WARP_MAX) return;  // k_eps_round_w's
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(evals, (unsigned long long)cnt);
     const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t kstep = FIRST ? cnt : (int64_t)gridDim.x * blockDim.x;  // FIRST: one target per thread
     for (int64_t kk = k0; kk < cnt; kk += kstep) {
         const int32_t i = FIRST ? (int32_t)kk : list[kk];
-        const int32_t L = leaf_of[i];
-        const double gi0 = v.g0[i];
-        int32_t partner = SKIPPED;
-        double px = v.x0[i], py = v.y0[i], gi = gi0, ie = ie_in[i];
-        float sr1 = -1.f, sr2 = -1.f;
-        uint32_t nrec = 0;
-        if (gi0 != 0 && !(v.zb[i] < i)) {
-            const double mcs = mcs_l[L];
-            Top2 t = two_nearest<FIRST>(v, L, i, -1, px, py, true);
-            sr1 = t.thr;
-            nrec += t.nrec;
-            double e;
-            partner = -1;
-            if (t.l1 == INT_MAX) e = DBL_MIN;
-            else if (t.l2 == INT_MAX) e = __dsqrt_rn(t.r1);
-            else if (isnan(mcs)) e = __dsqrt_rn(t.r2);
-            else {
-                double x1, y1, g1, x2, y2, g2;
-                cand_exact<FIRST>(v, t.l1, i, x1, y1, g1);
-                cand_exact<FIRST>(v, t.l2, i, x2, y2, g2);
-                if ((t.r1 < mcs) || ((dsgn(g1) == dsgn(g2)) && (dsgn(g1) != dsgn(gi)))) {
-                    // MergeVortexes (MEpsilonFast.cpp:111-126)
-                    if (dsgn(gi) == dsgn(g1)) {
-                        double sx = dadd(dmul(px, gi), dmul(x1, g1));
-                        double sy = dadd(dmul(py, gi), dmul(y1, g1));
-                        double inv = ddiv(1., dadd(gi, g1));
-                        px = dmul(sx, inv);
-                        py = dmul(sy, inv);
-                    } else if (fabs(gi) < fabs(g1)) {
-                        px = x1;
-                        py = y1;
-                    }
-                    gi = dadd(gi, g1);
-                    partner = t.l1;
-                    Top2 u = two_nearest<FIRST>(v, L, i, t.l1, px, py, false);
-                    sr2 = u.thr;
-                    nrec += u.nrec;
-                    if (u.l1 == INT_MAX) e = DBL_MIN;
-                    else if (u.l2 == INT_MAX) e = __dsqrt_rn(u.r1);
-                    else e = __dsqrt_rn(u.r2);
-                } else {
-                    e = __dsqrt_rn(t.r2);
-                }
-            }
-            ie = ddiv(1.0, smax(e, epr_l[L]));
-        }
-        bool ch = (partner != v.partner[i] && !(partner == SKIPPED && v.partner[i] == SKIPPED)) ||
-                  (__double_as_longlong(px) != __double_as_longlong(v.ox[i])) ||
-                  (__double_as_longlong(py) != __double_as_longlong(v.oy[i])) ||
-                  (__double_as_longlong(gi) != __double_as_longlong(v.og[i])) ||
-                  (__double_as_longlong(ie) != __double_as_longlong(oie_old[i]));
-        partner_new[i] = partner;
-        ox_new[i] = px; oy_new[i] = py; og_new[i] = gi; oie_new[i] = ie;
-        dv.sr1[i] = sr1;
-        dv.sr2[i] = sr2;
+        const Outcome o = eval_target<FIRST, false>(v, i, leaf_of, mcs_l, epr_l, ie_in, nullptr);
+        const bool ch = store_outcome(v, dv, i, o, oie_old, partner_new, ox_new, oy_new, og_new, oie_new);
         const unsigned am = __activemask();  // one store per warp to the shared flag
         if (__any_sync(am, ch) && (threadIdx.x & 31) == __ffs(am) - 1) *changed = 1;
-        const unsigned wrec = __reduce_add_sync(am, nrec);
+        const unsigned wrec = __reduce_add_sync(am, o.nrec);
         if ((threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(nrec_total, (unsigned long long)wrec);
+    }
+}
+
+// The targets list[0 .. *count) of a round after the first when there are at most
+// EPS_WARP_MAX of them: one warp per target, same outcomes as k_eps_round.
+__global__ void __launch_bounds__(EB) k_eps_round_w(EpsView v, DirtyView dv, const int32_t* __restrict__ list,
+                                                    const int32_t* __restrict__ count,
+                                                    const int32_t* __restrict__ leaf_of,
+                                                    const double* __restrict__ mcs_l,
+                                                    const double* __restrict__ epr_l,
+                                                    const double* __restrict__ ie_in,
+                                                    const double* __restrict__ oie_old, int32_t* partner_new,
+                                                    double* ox_new, double* oy_new, double* og_new,
+                                                    double* oie_new, int32_t* changed, unsigned long long* evals,
+                                                    unsigned long long* nrec_total) {
+    __shared__ int2 s_runs[EB / 32][32];
+    const int64_t cnt = *count;
+    if (cnt > EPS_WARP_MAX) return;  // k_eps_round's
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(evals, (unsigned long long)cnt);
+    const int wq = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t kk = (int64_t)blockIdx.x * (EB / 32) + wq; kk < cnt; kk += (int64_t)gridDim.x * (EB / 32)) {
+        const int32_t i = list[kk];
+        const Outcome o = eval_target<false, true>(v, i, leaf_of, mcs_l, epr_l, ie_in, s_runs[wq]);
+        if (lane == 0) {
+            if (store_outcome(v, dv, i, o, oie_old, partner_new, ox_new, oy_new, og_new, oie_new)) *changed = 1;
+            atomicAdd(nrec_total, (unsigned long long)o.nrec);
+        }
+        __syncwarp();
     }
 }
 
@@ -909,11 +1048,19 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                     n, v, dv, nullptr, nullptr, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
                     c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
                     c.counters.p + 14, c.counters.p + 16);
-            else
+            else {
+                // the round's target count is on the device: each kernel returns at once
+                // unless the count is its own
                 k_eps_round<false><<<std::min<unsigned>(grid_for(n, EB), 152u * 32u), EB, 0, s>>>(
                     n, v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
                     c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
                     c.counters.p + 14, c.counters.p + 16);
+                VV_LAUNCH_CHECK();
+                k_eps_round_w<<<EPS_WARP_GRID, EB, 0, s>>>(
+                    v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
+                    c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
+                    c.counters.p + 14, c.counters.p + 16);
+            }
             VV_LAUNCH_CHECK();
         }
         // new absorber table and merged records; leaves whose members changed
