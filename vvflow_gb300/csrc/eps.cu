@@ -433,6 +433,9 @@ __device__ __forceinline__ void cand_exact(const EpsView& v, int32_t j, int32_t 
     gj = moved ? v.og[j] : v.g0[j];
 }
 
+// FP32 squared distance of a candidate, formed the same way by every search kernel
+__device__ __forceinline__ float cand_d2(float dx, float dy) { return __fmaf_rn(dx, dx, __fmul_rn(dy, dy)); }
+
 __device__ __forceinline__ float thr_of(float t2, float D) {
     if (!(t2 < INFINITY)) return INFINITY;
     float r = sqrtf(t2) * (1.f + 1e-5f) + 2.f * D;
@@ -480,7 +483,7 @@ __device__ __forceinline__ void scan_leaf(const EpsView& v, int32_t q, float2 aL
         Cand c = cand_state<FIRST>(v, j, i, excl);
         if (!c.live) continue;
         float dx = tx - (c.rec.x + sh.x), dy = ty - (c.rec.y + sh.y);
-        float d = dx * dx + dy * dy;
+        float d = cand_d2(dx, dy);
         if (PASS == 0) {
             if (d < t1) { t2 = t1; t1 = d; thr = thr_of(t2, D); }
             else if (d < t2) { t2 = d; thr = thr_of(t2, D); }
@@ -574,6 +577,22 @@ __device__ Top2 two_nearest_w(const EpsView& v, int32_t L, int32_t i, int32_t ex
     Top2 best{DBL_MAX, DBL_MAX, INT_MAX, INT_MAX, INFINITY, 0};
     const int32_t nc = use_list ? v.ncand[L] : -1;
     const int32_t* cl = v.cand + (size_t)L * CAND_CAP;
+    {
+        // starting threshold for the lanes' pruning: the warp's two smallest distances over
+        // L's own members (not below the final threshold, which takes every candidate)
+        float s1 = INFINITY, s2 = INFINITY;
+        for (int32_t j = v.lvf[L] + lane; j < v.lvl[L]; j += 32) {
+            Cand c = cand_state<false>(v, j, i, excl);
+            if (!c.live) continue;
+            const float d = cand_d2(tx - c.rec.x, ty - c.rec.y);
+            if (d < s1) { s2 = s1; s1 = d; }
+            else if (d < s2) s2 = d;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            min2_merge(s1, s2, __shfl_xor_sync(0xffffffffu, s1, o), __shfl_xor_sync(0xffffffffu, s2, o));
+        thr = thr_of(s2, D);
+    }
 #pragma unroll 1
     for (int pass = 0; pass < 2; pass++) {
         auto visit = [&](int32_t q) {
@@ -584,10 +603,10 @@ __device__ Top2 two_nearest_w(const EpsView& v, int32_t L, int32_t i, int32_t ex
                 Cand c = cand_state<false>(v, j, i, excl);
                 if (!c.live) continue;
                 const float dx = tx - (c.rec.x + sh.x), dy = ty - (c.rec.y + sh.y);
-                const float d = dx * dx + dy * dy;
+                const float d = cand_d2(dx, dy);
                 if (pass == 0) {
-                    if (d < t1) { t2 = t1; t1 = d; thr = thr_of(t2, D); }
-                    else if (d < t2) { t2 = d; thr = thr_of(t2, D); }
+                    if (d < t1) { t2 = t1; t1 = d; thr = fminf(thr, thr_of(t2, D)); }
+                    else if (d < t2) { t2 = d; thr = fminf(thr, thr_of(t2, D)); }
                 } else if (d <= thr) {
                     double xj, yj, gj;
                     cand_exact<false>(v, j, i, xj, yj, gj);
