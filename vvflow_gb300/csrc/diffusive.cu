@@ -215,10 +215,12 @@ __global__ void __launch_bounds__(DW * 32) k_diff64(DiffArgs a) {
 // buffer, negative ones from the back, zero ones dropped.  A pass takes up to TMAX targets
 // of the leaf (a window of TMAX vortices), positives first; G (the power of two at or above
 // its active targets) lane groups of 32 / G lanes each hold one target and stride over the
-// sources of that target's sign only.  Pair arithmetic is FP32 in local frames with
-// compensated accumulation.  Pairs whose cut-off or coincidence test falls within the
-// rigorous FP32 error bound of its threshold, and the wall-segment terms, are evaluated in
-// FP64 into per-lane accumulators that are reduced in a fixed order, so results are
+// sources of that target's sign only, all lanes stepping the same count (the longer
+// list's) so that the loop and the compensated folds every 32 steps are warp-uniform.
+// Pair arithmetic is FP32 in local frames.  Pairs whose cut-off or coincidence test falls
+// within the rigorous FP32 error bound of its threshold are marked in a per-window mask and
+// evaluated in FP64 after the window, outside the arithmetic loop; they and the wall-segment
+// terms go to per-lane accumulators that are reduced in a fixed order, so results are
 // reproducible.
 template <int TMAX>
 __global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
