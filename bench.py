@@ -11,8 +11,8 @@ path; the plain FP64 path is timed on the same workload for the ratio the metric
 and both are checked against each other and against an FP64 direct sum.  `e2e` is the same
 step with host buffers: pinned host -> device copy of the inputs and device -> host copy
 of the results inside the timed region (the list's positions, circulations, epsilons and
-origins are copied out beside the convective and diffusive passes, once the epsilon/merge
-pass has fixed them; the velocities after those passes).  With N > 1 (torchrun) every rank runs an
+origins are copied out beside the diffusive pass, the epsilon/merge pass having fixed them;
+the velocities after it).  With N > 1 (torchrun) every rank runs an
 independent replica (different seed); value = all vortices / max time over ranks.
 
 Reference arm: the reference's CPU algorithm (the C restatement in oracle/, which mirrors
@@ -237,17 +237,18 @@ def hot_path(S, wl, mn, mx):
 
 def hot_path_host(S, wl, mn, mx, outs, oorig):
     """hot_path with the list returned to host buffers: positions, circulations, epsilons and
-    origins are copied out beside the convective and diffusive passes (the list is final
-    after the epsilon/merge pass), the velocities after them."""
+    origins are copied out beside the diffusive pass (the list is final after the
+    epsilon/merge pass; started after the convective pass, whose small device reads would
+    otherwise queue behind the copies on the copy engine), the velocities after it."""
     S.tree_build(wl.far_criteria, mn, mx)
     S.slae()
     S.tree_destroy()
     S.vortex_shed()
     S.tree_build(wl.far_criteria, mn, mx)
     S.eps(True)
+    S.convective()
     S.get_vortices_async(outs["x"].data_ptr(), outs["y"].data_ptr(), outs["g"].data_ptr(), outs["ie"].data_ptr(),
                          oorig.data_ptr())
-    S.convective()
     S.diffusive()
     S.tree_destroy()
     S.get_vortices_into(vx=outs["vx"].data_ptr(), vy=outs["vy"].data_ptr())

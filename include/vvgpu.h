@@ -224,8 +224,10 @@ int vvgpu_get_vortices(vvgpu_ctx* ctx, double* x, double* y, double* g, double* 
  * beside the context's later calls (after vvgpu_eps, the list does not change again in the
  * step: the convective and diffusive passes write only velocities and wall friction).  The
  * host arrays must stay valid, and must not be read, until vvgpu_wait_vortices returns;
- * with page-locked host memory the copies overlap the kernels.  A second call first waits
- * for the first.  The reference keeps the list in host memory (Space::VortexList); this is
+ * with page-locked host memory the copies overlap the kernels.  The context's own small
+ * device reads (counts, flags) share the copy engine and queue behind these copies, so a
+ * caller starts them after vvgpu_convective (the diffusive pass reads only at its end).  A
+ * second call first waits for the first.  The reference keeps the list in host memory (Space::VortexList); this is
  * the drop-in's return path for it after the epsilon pass. */
 int vvgpu_get_vortices_async(vvgpu_ctx* ctx, double* x, double* y, double* g, double* inv_eps, int64_t* orig);
 /* Waits for the download vvgpu_get_vortices_async started (returns at once without one). */

@@ -102,6 +102,22 @@ __global__ void k_iota64(int64_t* out, int64_t n, int64_t base) {
 
 // orig = 0..n-1, and *bad = 1 if a position or circulation is not finite or an inverse
 // epsilon is NaN or negative (+inf is a valid _1_eps: coincident vortices have epsilon 0)
+// Device snapshot of the list for the download beside later calls: the five arrays side by
+// side (orig as its 64-bit pattern), each only when its host pointer was given (bit k of
+// want).  One kernel instead of five device-to-device copies, which the copy engine runs
+// at a fraction of the SMs' copy rate.
+__global__ void k_snapshot(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
+                           const double* __restrict__ g, const double* __restrict__ ie,
+                           const int64_t* __restrict__ orig, unsigned want, double* __restrict__ snap) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (want & 1u) snap[i] = x[i];
+    if (want & 2u) snap[n + i] = y[i];
+    if (want & 4u) snap[2 * n + i] = g[i];
+    if (want & 8u) snap[3 * n + i] = ie[i];
+    if (want & 16u) snap[4 * n + i] = __longlong_as_double((long long)orig[i]);
+}
+
 __global__ void k_set_orig_check(int64_t n, int64_t* __restrict__ orig, const double* __restrict__ x,
                                  const double* __restrict__ y, const double* __restrict__ g,
                                  const double* __restrict__ ie, int32_t* bad) {
@@ -531,9 +547,11 @@ int vvgpu_get_vortices_async(vvgpu_ctx* h, double* x, double* y, double* g, doub
         double* snap = c.dl_snap.p;
         const size_t bytes = (size_t)n * 8;
         void* dst[5] = {x, y, g, ie, orig};
-        const void* src[5] = {c.x.p, c.y.p, c.g.p, c.ie.p, c.orig.p};
+        unsigned want = 0;
         for (int k = 0; k < 5; k++)
-            if (dst[k]) VV_CUDA(cudaMemcpyAsync(snap + k * n, src[k], bytes, cudaMemcpyDeviceToDevice, s));
+            if (dst[k]) want |= 1u << k;
+        k_snapshot<<<grid_for(n, 256), 256, 0, s>>>(n, c.x.p, c.y.p, c.g.p, c.ie.p, c.orig.p, want, snap);
+        VV_LAUNCH_CHECK();
         VV_CUDA(cudaEventRecord(c.dl_ready, s));
         VV_CUDA(cudaStreamWaitEvent(c.dl_stream, c.dl_ready, 0));
         for (int k = 0; k < 5; k++)
