@@ -1025,12 +1025,12 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
     VV_CUDA(cudaMemsetAsync(dmax_bits, 0, 4, s));
     VV_CUDA(cudaMemsetAsync(c.counters.p + 14, 0, 8, s));
     VV_CUDA(cudaMemsetAsync(c.counters.p + 16, 0, 8, s));
-    for (;;) {
-        rounds++;
+    // One round: evaluations from the current guesses (buffer cr) into the other buffer.
+    auto enqueue_round = [&](bool first, int cr) {
         // boxes and candidate leaves from the current guesses
-        k_eps_box<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.lf_vf.p, c.lf_vl.p, c.e_rec0.p, c.e_recO[cur].p,
-                                                  c.e_partner[cur].p, c.e_zb.p, c.lf_box32.p, c.e_box_prev.p,
-                                                  c.e_live.p, c.e_sr1.p, c.e_sr2.p, c.e_rreg.p, rounds == 1,
+        k_eps_box<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.lf_vf.p, c.lf_vl.p, c.e_rec0.p, c.e_recO[cr].p,
+                                                  c.e_partner[cr].p, c.e_zb.p, c.lf_box32.p, c.e_box_prev.p,
+                                                  c.e_live.p, c.e_sr1.p, c.e_sr2.p, c.e_rreg.p, first,
                                                   c.e_changed.p);
         VV_LAUNCH_CHECK();
         {
@@ -1039,19 +1039,19 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                            c.lf_box32.p, c.e_live.p, fr.Gf, c.e_cand.p, c.e_ncand.p,
                                                            c.lf_rn.p, c.e_rlist.p, c.e_rnear.p, c.e_lchanged.p,
                                                            c.e_dirty.p, c.e_chg.p, c.e_nchg.p, c.e_box_prev.p,
-                                                           c.e_rreg.p, c.e_lchg_pre.p, rounds == 1, c.e_ldisp.p,
+                                                           c.e_rreg.p, c.e_lchg_pre.p, first, c.e_ldisp.p,
                                                            c.e_chglist.p, c.e_dloc.p);
             VV_LAUNCH_CHECK();
         }
         EpsView v{c.lf_vf.p, c.lf_vl.p, c.lf_anchor.p, c.lf_box32.p, c.lf_rn.p, c.e_rnear.p,
                   (const float*)dmax_bits, c.near_off.p, c.near_run.p,
-                  c.e_cand.p, c.e_ncand.p, c.e_rec0.p, c.e_recO[cur].p, c.e_x0.p, c.e_y0.p, c.e_g0.p,
-                  c.e_partner[cur].p, c.e_zb.p, c.e_ox[cur].p, c.e_oy[cur].p, c.e_og[cur].p, fr.G, fr.Gf};
-        const int nx = cur ^ 1;
+                  c.e_cand.p, c.e_ncand.p, c.e_rec0.p, c.e_recO[cr].p, c.e_x0.p, c.e_y0.p, c.e_g0.p,
+                  c.e_partner[cr].p, c.e_zb.p, c.e_ox[cr].p, c.e_oy[cr].p, c.e_og[cr].p, fr.G, fr.Gf};
+        const int nx = cr ^ 1;
         DirtyView dv{c.e_zb_prev.p, c.e_vch.p, c.e_chg.p, c.e_nchg.p, c.e_recO[nx].p, c.e_sr1.p, c.e_sr2.p};
         const int32_t* list = nullptr;
-        if (rounds > 1) {
-            k_eps_mark<<<grid_for(n, EB), EB, 0, s>>>(n, v, dv, c.leaf_of.p, c.e_dirty.p, c.e_oie[cur].p,
+        if (!first) {
+            k_eps_mark<<<grid_for(n, EB), EB, 0, s>>>(n, v, dv, c.leaf_of.p, c.e_dirty.p, c.e_oie[cr].p,
                                                       c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p,
                                                       c.e_oie[nx].p, c.e_flag.p);
             VV_LAUNCH_CHECK();
@@ -1062,21 +1062,21 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
         }
         {
             KernelTimer kt(c, VVGPU_T_EPS_ROUND);
-            if (rounds == 1)
+            if (first)
                 k_eps_round<true><<<grid_for(n, EB), EB, 0, s>>>(
-                    n, v, dv, nullptr, nullptr, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
+                    n, v, dv, nullptr, nullptr, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cr].p,
                     c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
                     c.counters.p + 14, c.counters.p + 16);
             else {
                 // the round's target count is on the device: each kernel returns at once
                 // unless the count is its own
                 k_eps_round<false><<<std::min<unsigned>(grid_for(n, EB), 152u * 32u), EB, 0, s>>>(
-                    n, v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
+                    n, v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cr].p,
                     c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
                     c.counters.p + 14, c.counters.p + 16);
                 VV_LAUNCH_CHECK();
                 k_eps_round_w<<<EPS_WARP_GRID, EB, 0, s>>>(
-                    v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cur].p,
+                    v, dv, list, c.e_pos.p + n, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cr].p,
                     c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
                     c.counters.p + 14, c.counters.p + 16);
             }
@@ -1090,18 +1090,30 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
                                                     c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_x0.p, c.e_y0.p,
                                                     c.e_zb.p, c.e_recO[nx].p, dmax_bits, c.e_ldisp.p);
         VV_LAUNCH_CHECK();
-        k_leaf_changed<<<grid_for(n, EB), EB, 0, s>>>(n, c.leaf_of.p, c.e_partner[cur].p, c.e_partner[nx].p,
-                                                      c.e_ox[cur].p, c.e_ox[nx].p, c.e_oy[cur].p, c.e_oy[nx].p,
-                                                      c.e_og[cur].p, c.e_og[nx].p, c.e_zb_prev.p, c.e_zb.p,
+        k_leaf_changed<<<grid_for(n, EB), EB, 0, s>>>(n, c.leaf_of.p, c.e_partner[cr].p, c.e_partner[nx].p,
+                                                      c.e_ox[cr].p, c.e_ox[nx].p, c.e_oy[cr].p, c.e_oy[nx].p,
+                                                      c.e_og[cr].p, c.e_og[nx].p, c.e_zb_prev.p, c.e_zb.p,
                                                       c.e_lchanged.p, c.e_vch.p);
         VV_LAUNCH_CHECK();
         exclusive_scan(c, c.e_lchanged.p, c.e_lchg_pre.p, nl);
         k_chg_list<<<grid_for(nl, EB), EB, 0, s>>>(nl, c.e_lchanged.p, c.e_lchg_pre.p, c.e_chglist.p);
         VV_LAUNCH_CHECK();
-        cur = nx;
-        int32_t changed = read_i32(c, c.e_changed.p);
-        if (!changed) break;
-        if (rounds >= max_rounds) throw ApiError{VVGPU_ERR_TIMEOUT, "epsilon/merge rounds did not converge"};
+    };
+    const auto timeout = [] { return ApiError{VVGPU_ERR_TIMEOUT, "epsilon/merge rounds did not converge"}; };
+    rounds = 1;
+    enqueue_round(true, 0);
+    cur = 1;
+    int32_t changed = read_i32(c, c.e_changed.p);
+    if (changed && rounds >= max_rounds) throw timeout();
+    if (changed) {
+        for (;;) {
+            rounds++;
+            enqueue_round(false, cur);
+            cur ^= 1;
+            changed = read_i32(c, c.e_changed.p);
+            if (!changed) break;
+            if (rounds >= max_rounds) throw timeout();
+        }
     }
     VV_CUDA(cudaMemsetAsync(c.counters.p, 0, 8, s));
     k_eps_final<<<grid_for(n, EB), EB, 0, s>>>(n, c.e_partner[cur].p, c.e_zb.p, c.e_ox[cur].p, c.e_oy[cur].p,

@@ -493,7 +493,8 @@ void exclusive_scan(Ctx& c, const int32_t* in, int32_t* out, int64_t n);
 int32_t read_i32(Ctx& c, const int32_t* p);
 // Host landing place of a small device read at byte `off` of the context's pinned block
 // (bytes: 0 read_i32, 16 tree counts, 64 root box, 96 staging error, 104 diffusive
-// counts, 120 near-pair count, 128 epsilon counters, 160 residual norms), or `fallback` without the block.
+// counts, 120 near-pair count, 128 epsilon counters, 160 residual norms), or `fallback`
+// without the block.
 template <class T>
 inline T* pinned_at(Ctx& c, size_t off, T* fallback) {
     return c.h_pin ? reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(c.h_pin) + off) : fallback;
