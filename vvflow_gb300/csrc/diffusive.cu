@@ -28,10 +28,12 @@ namespace vvgpu {
 namespace {
 
 constexpr int DW = 4;
-constexpr int SRC_CAP = 256;  // FP32 path: shared-memory source records per warp
-constexpr int SRC_BATCH = SRC_CAP - 32;  // FP32 path: sources staged per warp at a time
-// candidate leaves gathered per warp before their sources are staged (64: measured 9.86 ms
-// against 10.14 ms for one batch of 32 near leaves at a time at 4M; 96 costs occupancy)
+// FP32 path: shared-memory source records per warp (256: 5.74 ms at 4M against 5.85 ms for
+// 320) and sources staged per warp at a time
+constexpr int SRC_CAP = 256;
+constexpr int SRC_BATCH = SRC_CAP - 32;
+// candidate leaves gathered per warp before their sources are staged (64: 5.74 ms at 4M
+// against 5.80 ms for 48 and 5.86 ms for 96)
 constexpr int HIT_CAP = 64;
 
 // Box of non-zero vortices and segment centres of each leaf, FP32 in the leaf's own frame.
