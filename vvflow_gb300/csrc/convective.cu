@@ -259,20 +259,24 @@ __global__ void __launch_bounds__(CW * 32) k_conv64(ConvArgs a) {
 // of its sources and then folds them into a TwoSum-compensated pair.
 constexpr int TC32 = 8;
 // CT: sources per staged tile (128, 192 or 256; the context's choice, vvgpu_autotune_tiles)
+// Warps per block of k_conv32: one (16 blocks per SM), so that an SM takes a new leaf as
+// soon as any warp's leaf is done (6.81 ms at 4M against 7.32 ms for two warps per block
+// and 7.63 ms for four, where a block waited for its slowest leaf)
+constexpr int CW32 = 1;
 constexpr size_t conv32_smem(int ct) {
-    return (size_t)CW * 2 * ct * 2 * sizeof(float4) + (size_t)CW * 2 * sizeof(uint64_t);
+    return (size_t)CW32 * 2 * ct * 2 * sizeof(float4) + (size_t)CW32 * 2 * sizeof(uint64_t);
 }
 
 template <int CT>
-__global__ void __launch_bounds__(CW * 32, 4) k_conv32(ConvArgs a) {
+__global__ void __launch_bounds__(CW32 * 32, 16) k_conv32(ConvArgs a) {
     extern __shared__ __align__(128) unsigned char conv_smem[];
     const int wq = threadIdx.x >> 5;
-    const int64_t L = (int64_t)blockIdx.x * CW + wq;
+    const int64_t L = (int64_t)blockIdx.x * CW32 + wq;
     const int lane = threadIdx.x & 31;
     if (L >= a.nl) return;
     float4* const t_rec = reinterpret_cast<float4*>(conv_smem) + (size_t)wq * 2 * CT;           // [2][CT]
-    float4* const t_anc = reinterpret_cast<float4*>(conv_smem) + (size_t)(CW + wq) * 2 * CT;    // [2][CT]
-    uint64_t* const bar = reinterpret_cast<uint64_t*>(reinterpret_cast<float4*>(conv_smem) + (size_t)CW * 4 * CT) +
+    float4* const t_anc = reinterpret_cast<float4*>(conv_smem) + (size_t)(CW32 + wq) * 2 * CT;    // [2][CT]
+    uint64_t* const bar = reinterpret_cast<uint64_t*>(reinterpret_cast<float4*>(conv_smem) + (size_t)CW32 * 4 * CT) +
                           2 * wq;
     if (lane == 0) {
         stage_bar_init(&bar[0]);
@@ -899,7 +903,7 @@ void convective(Ctx& c) {
         auto launch = [&](auto kern, int ct) {
             VV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)conv32_smem(ct)));
             KernelTimer kt(c, VVGPU_T_CONVECTIVE);
-            kern<<<grid, CW * 32, conv32_smem(ct), s>>>(a);
+            kern<<<grid_for(c.nleaves, CW32), CW32 * 32, conv32_smem(ct), s>>>(a);
             VV_LAUNCH_CHECK();
         };
         if (c.conv_tile == 128) launch(k_conv32<128>, 128);
