@@ -1063,7 +1063,9 @@ void eps_pass(Ctx& c, int merge, int64_t* merged) {
         {
             KernelTimer kt(c, VVGPU_T_EPS_ROUND);
             if (first)
-                k_eps_round<true><<<grid_for(n, EB), EB, 0, s>>>(
+                // one-warp blocks: a block holds no warp waiting for a slower one (5.49
+                // against 5.54 ms for the rounds at 4M with four-warp blocks)
+                k_eps_round<true><<<grid_for(n, 32), 32, 0, s>>>(
                     n, v, dv, nullptr, nullptr, c.leaf_of.p, c.lf_mcs.p, c.lf_epr.p, c.ie.p, c.e_oie[cr].p,
                     c.e_partner[nx].p, c.e_ox[nx].p, c.e_oy[nx].p, c.e_og[nx].p, c.e_oie[nx].p, c.e_changed.p,
                     c.counters.p + 14, c.counters.p + 16);
