@@ -164,7 +164,7 @@ int vvgpu_set_eps_round_limit(vvgpu_ctx* ctx, int64_t max_rounds);
  * (0 polls: every wait runs out).  No counterpart in the reference (it has no GPU). */
 int vvgpu_set_wait_limit(vvgpu_ctx* ctx, uint32_t spins);
 /* Kernel shapes of the FP32 pair passes: sources per shared-memory tile of the convective
- * near field (128, 192 or 256; default 192) and the shape of the diffusive pass (1: up to
+ * near field (128, 192 or 256; default 256) and the shape of the diffusive pass (1: up to
  * 16 targets of a leaf per pass, 2: up to 8; default 1).  The variants compute the same sums in a different order of their FP32
  * partial sums.  vvgpu_autotune_tiles times every shape on the context's current tree
  * (built; after vvgpu_eps, where the pass would run) and keeps the fastest of each; the

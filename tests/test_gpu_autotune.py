@@ -73,7 +73,7 @@ def test_autotune_fp64_has_one_shape_and_bad_shapes_are_rejected():
     from vvflow_gb300.vvgpu import VVGpuError
     S = _prepared(0)
     tile, dt, ms = S.autotune_tiles()
-    assert (tile, dt) == (192, 1) and np.all(ms == -1)
+    assert (tile, dt) == (256, 1) and np.all(ms == -1)
     for shape in ((64, 1), (192, 3), (100, 2)):
         with pytest.raises(VVGpuError) as ei:
             S.set_tiles(*shape)

@@ -1,8 +1,9 @@
 // Kernel shapes of the FP32 pair passes, chosen per context by timing them on the
 // context's own tree: the sources per staged tile of the convective near field (k_conv32:
-// 128, 192 or 256; shared memory per block 32, 48 or 64 KB) and the targets per pass of the
-// diffusive pass (k_diff32: shape 1 takes up to 16, shape 2 up to 8).  Each variant computes the same sums (in a different
-// order of the FP32 partial sums), so the choice changes speed, not the method.  No
+// 128, 192 or 256; shared memory per one-warp block 8, 12 or 16 KB) and the targets per pass
+// of the diffusive pass (k_diff32: shape 1 takes up to 16, shape 2 up to 8).  Each variant
+// computes the same sums (in a different order of the FP32 partial sums), so the choice
+// changes speed, not the method.  No
 // counterpart in the reference, whose OpenMP loops have no tile shapes.
 #include <cmath>
 

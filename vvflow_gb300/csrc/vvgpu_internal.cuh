@@ -139,8 +139,9 @@ struct Ctx {
     uint32_t wait_spins = STAGE_SPINS;  // polls of one shared-memory staging wait
     int32_t* h_pin = nullptr;           // 512 pinned host bytes for the small device reads of a step
     // kernel shapes of the FP32 pair passes (vvgpu_autotune_tiles): sources per staged tile
-    // of the convective near field, shape of the diffusive pass (1: 16 targets, 2: 8 per pass)
-    int conv_tile = 192, diff_targets = 1;
+    // of the convective near field (256 by default), shape of the diffusive pass (1: 16
+    // targets, 2: 8 per pass)
+    int conv_tile = 256, diff_targets = 1;
     bool tune_pending = false;  // tune both at the next convective pass
 
     // segments (host copies of geometry are kept for body bookkeeping)

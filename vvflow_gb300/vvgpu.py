@@ -284,7 +284,7 @@ class GpuSpace:
                  "autotune_tiles")
         return int(t[0]), int(d[0]), ms
 
-    def set_tiles(self, conv_tile: int = 192, diff_targets: int = 1):
+    def set_tiles(self, conv_tile: int = 256, diff_targets: int = 1):
         self._ok(self.lib.vvgpu_set_tiles(self.h, int(conv_tile), int(diff_targets)), "set_tiles")
 
     def tiles(self):
