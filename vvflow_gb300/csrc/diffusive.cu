@@ -27,7 +27,9 @@ namespace vvgpu {
 
 namespace {
 
-constexpr int DW = 4;
+// warps per block: two (12 blocks per SM in the FP32 pass): 5.52 ms at 4M against 5.74 ms for
+// four and 6.33 ms for one
+constexpr int DW = 2;
 // FP32 path: shared-memory source records per warp (256: 5.74 ms at 4M against 5.85 ms for
 // 320) and sources staged per warp at a time
 constexpr int SRC_CAP = 256;
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__(DW * 32) k_diff64(DiffArgs a) {
 // terms go to per-lane accumulators that are reduced in a fixed order, so results are
 // reproducible.
 template <int TMAX>
-__global__ void __launch_bounds__(DW * 32, 6) k_diff32(DiffArgs a) {
+__global__ void __launch_bounds__(DW * 32, 12) k_diff32(DiffArgs a) {
     __shared__ int2 s_runs[DW][32];
     __shared__ int4 s_hit[DW][HIT_CAP];     // flattened start, first vortex, shift x, shift y (bits)
     __shared__ float2 s_hitb[DW][HIT_CAP];  // error bound D of the leaf
