@@ -107,6 +107,8 @@ __global__ void k_leaf_params(int64_t nl, const double4* __restrict__ lgeom, con
             const float pxg = (float)(px - A.x), pyg = (float)(py - A.y);
             const float R = brad[b] + fabsf(pxg) + fabsf(pyg);
             const float E = ldexpf(R * R, -19);
+            // the decision bounds, formed when resf or E changes rather than per segment
+            float lo = resf - (E + eres), hi = resf + (E + eres);
             for (int64_t k = 0; k < cnt; k++) {
                 const int64_t s = f + k;
                 const float2 sp = seg32[s];
@@ -114,8 +116,8 @@ __global__ void k_leaf_params(int64_t nl, const double4* __restrict__ lgeom, con
                 const float df = dx * dx + dy * dy;
                 bool less, exact = false;
                 if (att < 0) less = true;  // res = DBL_MAX: any finite distance is smaller
-                else if (df < resf - (E + eres)) less = true;
-                else if (df > resf + (E + eres)) less = false;
+                else if (df < lo) less = true;
+                else if (df > hi) less = false;
                 else {
                     if (!rese_ok) { res = dabs2(dsub(px, rx[att]), dsub(py, ry[att])); rese_ok = true; }
                     const double d = dabs2(dsub(px, rx[s]), dsub(py, ry[s]));
@@ -123,8 +125,13 @@ __global__ void k_leaf_params(int64_t nl, const double4* __restrict__ lgeom, con
                     if (less) res = d;
                     exact = true;
                 }
-                if (less) { resf = df; eres = E; att = s; rese_ok = exact; }
-                else k += 9;  // MEpsilonFast.cpp:248
+                if (less) {
+                    resf = df; eres = E; att = s; rese_ok = exact;
+                    lo = resf - (E + eres);
+                    hi = resf + (E + eres);
+                } else {
+                    k += 9;  // MEpsilonFast.cpp:248
+                }
             }
         }
     }
